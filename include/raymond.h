@@ -1,0 +1,186 @@
+/*
+ * raymond.h — the C ABI of libraymond_cuda.so, the GB300 (sm_103a) backend
+ * for Raymond's GPU render path.
+ *
+ * These entry points replace what src/Renderer.mjs does through WebGPU. The
+ * packed buffers they take are byte-for-byte the ones Scene.pack() makes
+ * (src/Scene.mjs:15-60): 64-byte primitives, 32-byte BVH nodes
+ * (src/BVH.mjs:1-16), 96-byte materials, 16-float triangle attribute blocks
+ * and the u32 lights/volumes/CDF list (src/Renderer.mjs:598-607). The
+ * 208-byte uniform block is Params (src/shaders.mjs:9-30) as
+ * Renderer.#writeParams fills it (src/Renderer.mjs:925-991).
+ *
+ * Conventions: every call returns RAYMOND_OK (0) or a negative status; the
+ * message is kept per handle (raymond_last_error). Host pointers are only
+ * read during the call. A handle is used from one host thread at a time and
+ * all its device work runs in order on the handle's CUDA stream.
+ */
+#ifndef RAYMOND_H
+#define RAYMOND_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RAYMOND_OK 0
+#define RAYMOND_EINVAL -1    /* bad argument or malformed packed data */
+#define RAYMOND_ENOMEM -2    /* a device or host allocation failed */
+#define RAYMOND_ECUDA -3     /* a CUDA call or kernel failed */
+#define RAYMOND_ESTATE -4    /* call out of order (e.g. read before render) */
+#define RAYMOND_ETIMEOUT -5  /* a device-side wait hit its iteration limit */
+#define RAYMOND_ECAPACITY -6 /* a request exceeds a fixed capacity */
+
+/* Optional trace-shader features (src/shaders.mjs:55-58; src/Renderer.mjs:434-439). */
+#define RAYMOND_FEATURE_VOLUMES 1u
+#define RAYMOND_FEATURE_TEXTURES 2u
+#define RAYMOND_FEATURE_ENVIRONMENT 4u
+#define RAYMOND_FEATURE_DISPERSION 8u
+
+/* raymond_render flags. */
+#define RAYMOND_FLAG_CAUSTICS 1u /* run light tracing + photon mapping this frame */
+#define RAYMOND_FLAG_DENOISE 2u  /* run the à-trous passes this frame */
+#define RAYMOND_FLAG_MEGAKERNEL 4u /* force the one-kernel path (else the tuned choice) */
+#define RAYMOND_FLAG_WAVEFRONT 8u  /* force the wavefront path */
+
+#define RAYMOND_PARAMS_BYTES 208
+#define RAYMOND_IMAGE_KEY_BYTES 168
+
+typedef struct raymond raymond_t;
+
+typedef struct raymond_config {
+    int device;              /* CUDA ordinal */
+    uint32_t seed;           /* XORed into the sample hashes; 0 reproduces the reference streams */
+    uint64_t path_capacity;  /* wavefront paths in flight; 0 = sized from free memory */
+    uint32_t reserved[4];
+} raymond_config;
+
+/* Renderer.create (src/Renderer.mjs:247-279): picks the device, makes the stream. */
+int raymond_create(raymond_t** out, const raymond_config* cfg);
+
+/* Renderer.dispose (src/Renderer.mjs:531-547). */
+void raymond_destroy(raymond_t* h);
+
+/* The message of the handle's last failure ("" if none). h may be NULL for create errors. */
+const char* raymond_last_error(raymond_t* h);
+
+/*
+ * Renderer.#upload (src/Renderer.mjs:550-626). prims: prim_slots 64-byte
+ * records, the first bvh_prim_count in BVH leaf order, then the volumes.
+ * nodes: node_count 32-byte records. materials: mat_count 96-byte records.
+ * attributes: attr_vec4s vec4s. lights: words u32 = light_count light
+ * primitive indices, volume_count volume primitive indices, light_count CDF
+ * entries as f32 bits. Validates every index before anything is uploaded;
+ * restarts the average.
+ */
+int raymond_upload_scene(raymond_t* h, const void* prims, uint32_t prim_slots, uint32_t bvh_prim_count,
+                         const void* nodes, uint32_t node_count, const void* materials, uint32_t mat_count,
+                         const float* attributes, uint32_t attr_vec4s, const uint32_t* lights, uint32_t words,
+                         uint32_t light_count, uint32_t volume_count);
+
+/*
+ * Renderer.#uploadTextures (src/Renderer.mjs:637-661). which: 0 = colour
+ * textures (sRGB bytes, decoded on sampling), 1 = normal maps (plain bytes).
+ * rgba: layers × h × w × 4 bytes, every layer already resized to w × h.
+ */
+int raymond_upload_textures(raymond_t* h, int which, const uint8_t* rgba, uint32_t w, uint32_t hgt,
+                            uint32_t layers);
+
+/*
+ * Renderer.#uploadEnvironment (src/Renderer.mjs:723-760). rgba16f: w × h
+ * half floats × 4; table: cw × (ch + 1) f32 as EnvironmentMap.importance()
+ * lays it out (src/EnvironmentMap.mjs:202-247).
+ */
+int raymond_upload_environment(raymond_t* h, const uint16_t* rgba16f, uint32_t w, uint32_t hgt,
+                               const float* table, uint32_t cw, uint32_t ch_plus_1);
+
+/* Renderer.#writeEmitters' buffer (src/Renderer.mjs:670-717): vec4_count vec4s. */
+int raymond_set_emitters(raymond_t* h, const float* data, uint32_t vec4_count);
+
+/* Renderer.#resize (src/Renderer.mjs:766-799): keeps buffers that are big enough. */
+int raymond_resize(raymond_t* h, uint32_t w, uint32_t hgt);
+
+/*
+ * Renderer.render's GPU work (src/Renderer.mjs:441-490): the trace, then
+ * with RAYMOND_FLAG_CAUSTICS light tracing, splat resolve and photon gather,
+ * then with RAYMOND_FLAG_DENOISE prepare, 5 à-trous passes and compose,
+ * then the tone map into the headless display buffer. Enqueued only.
+ */
+int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint32_t flags);
+
+/* Waits for the handle's stream: backs device.queue.onSubmittedWorkDone(). */
+int raymond_sync(raymond_t* h);
+
+/*
+ * Renderer.readPixels (src/Renderer.mjs:502-528): w × h × 4 floats, the
+ * average (every float divided by samples) or, with denoised, the denoised
+ * result as is. Synchronous.
+ */
+int raymond_read_pixels(raymond_t* h, float* out_rgba, uint64_t bytes, int denoised, uint32_t samples);
+
+/*
+ * The raw per-pixel sums behind readPixels: accum (rgb, luminance² in w),
+ * guide albedo and guide normal (w: distance), w × h × 4 floats each, not
+ * divided by the sample count. Any output may be NULL. Synchronous.
+ */
+int raymond_read_guides(raymond_t* h, float* accum, float* guide_albedo, float* guide_normal, uint64_t bytes_each);
+
+/* The display pass's output (src/shaders.mjs:2124-2152) as w × h RGBA8. */
+int raymond_read_display(raymond_t* h, uint8_t* out_rgba8, uint64_t bytes);
+
+/*
+ * Primary-ray closest hits on the uploaded scene: rays are 6 floats each
+ * (origin, direction); out prim is the leaf-order primitive index
+ * (0xffffffff for a miss), the index space of the shader's Hit.prim
+ * (src/shaders.mjs:380-447) and of Scene.raycast's best (src/Scene.mjs:250).
+ * Host pointers; copies in and out inside the call.
+ */
+int raymond_trace_primary(raymond_t* h, const float* rays, uint32_t n, uint32_t* prim, float* t);
+
+/* The same on device pointers, enqueued on the handle's stream (no copies, no sync). */
+int raymond_trace_primary_device(raymond_t* h, const float* d_rays, uint32_t n, uint32_t* d_prim,
+                                 float* d_t);
+
+/*
+ * Standalone BVH builder producing BVH.build's exact output (src/BVH.mjs:
+ * 57-234): mins/maxs 3 doubles per primitive; nodes_out room for
+ * max(1, 2*count - 1) 32-byte nodes; order_out count u32. Host only, no
+ * handle. Returns the node count, or 0 on a bad argument.
+ */
+uint32_t raymond_bvh_build(const double* mins, const double* maxs, uint32_t count, uint32_t max_leaf,
+                           void* nodes_out, uint32_t* order_out, int threads);
+
+/* Device-side pointers of the handle's per-pixel buffers, for zero-copy callers (bench, tests). */
+typedef struct raymond_buffers {
+    float* accum;         /* w*h float4 */
+    float* guide_albedo;  /* w*h float4 */
+    float* guide_normal;  /* w*h float4 */
+    float* denoised;      /* w*h float4 */
+    uint8_t* display;     /* w*h RGBA8 */
+    uint32_t width, height;
+} raymond_buffers;
+int raymond_get_buffers(raymond_t* h, raymond_buffers* out);
+
+/* The handle's CUDA stream (a cudaStream_t), for callers that time or order work around it. */
+void* raymond_get_stream(raymond_t* h);
+
+/*
+ * Counters of the last frame: kernel launches, paths, and the device time of
+ * each stage from CUDA events recorded on the handle's stream around it
+ * (valid once the frame has finished, e.g. after raymond_sync).
+ */
+typedef struct raymond_stats {
+    uint64_t launches;
+    uint64_t rays_primary, rays_extension, rays_shadow, rays_photon;
+    uint64_t paths;
+    float ms_trace, ms_caustics, ms_denoise, ms_display;
+} raymond_stats;
+int raymond_get_stats(raymond_t* h, raymond_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAYMOND_H */

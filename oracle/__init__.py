@@ -1,0 +1,148 @@
+"""CPU oracle of Raymond's render path — TEST INFRASTRUCTURE ONLY.
+
+A restatement of the reference's algorithms (BVH.build, Scene.raycast,
+the trace shader's traversal and, in oracle/pathtrace.cpp, its path
+tracer and denoiser) used only as the checker by tests/,
+__graft_entry__.smoke() and the cpu_baseline leg of bench.py. Nothing in
+raymond_gb300 imports it. Parity status: pinned against the known answers
+of the reference's own unit tests; not against executed reference output
+(no JavaScript engine exists on either machine)."""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .build import LIB, build
+
+_lib = None
+NONE = 0xFFFFFFFF
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(LIB)
+        P, U32, I, D, F = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_double, ctypes.c_float
+        _lib.ro_bvh_build.restype = U32
+        _lib.ro_bvh_build.argtypes = [P, P, U32, U32, P, P]
+        _lib.ro_raycast_batch.restype = None
+        _lib.ro_raycast_batch.argtypes = [P, U32, P, P, P, U32, D, P, P, P, P, P, I]
+        _lib.ro_intersect_double.restype = I
+        _lib.ro_intersect_double.argtypes = [P, U32, P, P, D, P]
+        _lib.ro_trace32_batch.restype = None
+        _lib.ro_trace32_batch.argtypes = [P, P, P, U32, F, I, P, P, P, P, I]
+        _lib.ro_render.restype = None
+        _lib.ro_render.argtypes = [P, P, P, P, P, P, U32, U32, U32, U32, U32, P, P, P, P, I]
+        _lib.ro_denoise.restype = None
+        _lib.ro_denoise.argtypes = [P, P, P, U32, U32, U32, P, I]
+        _lib.ro_display.restype = None
+        _lib.ro_display.argtypes = [P, P, P, P]
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data if a is not None else None
+
+
+def threads() -> int:
+    return os.cpu_count() or 1
+
+
+def bvh_build(mins, maxs, max_leaf=4):
+    """BVH.build (src/BVH.mjs:57-234): returns (nodes u32 (n*8,), order u32)."""
+    mins = np.ascontiguousarray(mins, dtype=np.float64).reshape(-1)
+    maxs = np.ascontiguousarray(maxs, dtype=np.float64).reshape(-1)
+    count = mins.size // 3
+    nodes = np.zeros(max(1, 2 * count - 1) * 8, dtype=np.uint32)
+    order = np.zeros(count, dtype=np.uint32)
+    n = lib().ro_bvh_build(_p(mins), _p(maxs), count, max_leaf, _p(nodes), _p(order))
+    return nodes[: n * 8].copy(), order
+
+
+def raycast(packed, rays, t_max=np.inf, nthreads=None):
+    """Scene.raycast in double on the packed scene: dict of prim, t, uv, normal, front."""
+    rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+    n = len(rays)
+    prim = np.empty(n, dtype=np.uint32)
+    t = np.empty(n, dtype=np.float64)
+    uv = np.empty(2 * n, dtype=np.float64)
+    normal = np.empty(3 * n, dtype=np.float64)
+    front = np.empty(n, dtype=np.uint8)
+    attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
+    lib().ro_raycast_batch(_p(packed.primitives), packed.primitiveCount, _p(packed.nodes), _p(attrs), _p(rays), n,
+                           float(t_max), _p(prim), _p(t), _p(uv), _p(normal), _p(front), nthreads or threads())
+    return {"prim": prim, "t": t, "uv": uv.reshape(-1, 2), "normal": normal.reshape(-1, 3), "front": front}
+
+
+def intersect_double(packed, p, o, d, t_max=np.inf):
+    o = np.ascontiguousarray(o, dtype=np.float64)
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    out = np.zeros(3, dtype=np.float64)
+    hit = lib().ro_intersect_double(_p(packed.primitives), int(p), _p(o), _p(d), float(t_max), _p(out))
+    return out if hit else None
+
+
+def trace32(packed, rays, t_max=1e30, any_hit=False, nthreads=None):
+    """The trace shader's traversal in f32, with counters: dict prim, t, inner, tested."""
+    rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+    n = len(rays)
+    prim = np.empty(n, dtype=np.uint32)
+    t = np.empty(n, dtype=np.float32)
+    inner = np.empty(n, dtype=np.uint32)
+    tested = np.empty(n, dtype=np.uint32)
+    lib().ro_trace32_batch(_p(packed.primitives), _p(packed.nodes), _p(rays), n, float(t_max), 1 if any_hit else 0,
+                           _p(prim), _p(t), _p(inner), _p(tested), nthreads or threads())
+    return {"prim": prim, "t": t, "inner": inner, "tested": tested}
+
+
+def bytes_per_ray(inner: np.ndarray, tested: np.ndarray) -> np.ndarray:
+    """Algorithmic bytes of one traversal: the root box, both child boxes of
+    every inner node visited, and every primitive record tested:
+    32·(1 + 2·inner) + 64·tested."""
+    return 32 * (1 + 2 * inner.astype(np.int64)) + 64 * tested.astype(np.int64)
+
+
+def render(packed, lights_words, params: bytes, region=None, seed_hash=0, nthreads=None):
+    """One frame of the trace shader's main() restated in f32 over a region
+    (x0, y0, w, h) of the image: dict accum/albedo/normal (h×w×4 sums) and
+    counters (algorithmic bytes, rays, surface hits, paths)."""
+    import struct
+    width, height = struct.unpack_from("<2I", params, 160)
+    x0, y0, rw, rh = region if region else (0, 0, width, height)
+    accum = np.zeros(rw * rh * 4, dtype=np.float32)
+    alb = np.zeros(rw * rh * 4, dtype=np.float32)
+    nrm = np.zeros(rw * rh * 4, dtype=np.float32)
+    counters = np.zeros(4, dtype=np.uint64)
+    pbuf = np.frombuffer(bytes(params), dtype=np.uint8).copy()
+    words = np.ascontiguousarray(lights_words, dtype=np.uint32)
+    attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
+    lib().ro_render(_p(packed.primitives), _p(packed.nodes), _p(packed.materials), _p(attrs), _p(words), _p(pbuf),
+                    seed_hash, x0, y0, rw, rh, _p(accum), _p(alb), _p(nrm), _p(counters), nthreads or threads())
+    return {"accum": accum.reshape(rh, rw, 4), "albedo": alb.reshape(rh, rw, 4), "normal": nrm.reshape(rh, rw, 4),
+            "bytes": int(counters[0]), "rays": int(counters[1]), "hits": int(counters[2]), "paths": int(counters[3])}
+
+
+def denoise(accum, guide_albedo, guide_normal, width, height, total_samples, nthreads=None):
+    """prepare, five à-trous passes and compose (src/shaders.mjs:1974-2097): h×w×4."""
+    out = np.zeros(width * height * 4, dtype=np.float32)
+    a = np.ascontiguousarray(accum, dtype=np.float32)
+    g = np.ascontiguousarray(guide_albedo, dtype=np.float32)
+    n = np.ascontiguousarray(guide_normal, dtype=np.float32)
+    lib().ro_denoise(_p(a), _p(g), _p(n), width, height, total_samples, _p(out), nthreads or threads())
+    return out.reshape(height, width, 4)
+
+
+def display(accum, denoised, params: bytes):
+    """The display pass (src/shaders.mjs:2124-2152) into RGBA8."""
+    import struct
+    width, height = struct.unpack_from("<2I", params, 160)
+    out = np.zeros(width * height * 4, dtype=np.uint8)
+    a = np.ascontiguousarray(accum, dtype=np.float32)
+    d = np.ascontiguousarray(denoised if denoised is not None else accum, dtype=np.float32)
+    pbuf = np.frombuffer(bytes(params), dtype=np.uint8).copy()
+    lib().ro_display(_p(a), _p(d), _p(pbuf), _p(out))
+    return out.reshape(height, width, 4)

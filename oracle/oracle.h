@@ -1,0 +1,82 @@
+// Raymond CPU oracle — TEST INFRASTRUCTURE ONLY.
+//
+// A plain CPU restatement of the reference renderer's algorithms (Raymond,
+// JavaScript + WGSL), used by tests/, __graft_entry__.smoke() and the
+// cpu_baseline leg of bench.py as the checker. The product library
+// (libraymond_cuda.so) never links, loads or calls anything here.
+//
+// Parity status: the reference is JavaScript/WGSL and no JS engine exists on
+// either machine, so no executed reference output is available. The oracle is
+// pinned instead against every known answer the reference's own unit tests
+// hold for this path (tests/unit/bvh.test.mjs, scene.test.mjs,
+// camera.test.mjs, shaders.test.mjs), restated in tests/test_oracle_*.py.
+// Byte-level parity of the BVH build with BVH.mjs is therefore pinned by
+// those invariants only ("parity unpinned" against executed reference code).
+//
+// Every function names the reference file:line it restates.
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RO_NONE 0xffffffffu
+
+// ---- BVH.build (src/BVH.mjs:57-234) ----
+// mins/maxs: 3 doubles per primitive. nodes_out must hold max(1, 2*count-1)
+// 32-byte nodes; order_out `count` u32. Returns the node count.
+uint32_t ro_bvh_build(const double* mins, const double* maxs, uint32_t count, uint32_t max_leaf,
+                      void* nodes_out, uint32_t* order_out);
+
+// ---- Scene.raycast (src/Scene.mjs:202-283, 549-674), in double ----
+// Packed buffers exactly as Scene.#pack lays them out. rays: 6 floats per
+// ray (origin xyz, direction xyz), read as doubles. Outputs per ray: the
+// leaf-order primitive index (RO_NONE for a miss), t, u, v, and the facing
+// shading normal and front flag of Scene.raycast's Hit (normal maps are
+// not applied here).
+void ro_raycast_batch(const void* prims, uint32_t prim_count, const void* nodes,
+                      const float* attributes, const float* rays, uint32_t n, double t_max,
+                      uint32_t* prim_out, double* t_out, double* uv_out, double* normal_out,
+                      uint8_t* front_out, int threads);
+
+// Intersection of one primitive in double (Scene.#intersect, src/Scene.mjs:579-674).
+// Returns 1 and writes t,u,v on a hit nearer than t_max.
+int ro_intersect_double(const void* prims, uint32_t p, const double* o, const double* d,
+                        double t_max, double* tuv);
+
+// ---- trace() of the trace shader (src/shaders.mjs:363-447), in f32 ----
+// The GPU's own traversal order and arithmetic, restated on the CPU, with
+// counters for the algorithmic byte figure: inner nodes whose two children
+// were tested, and primitives tested. any_hit as the shader's shadow rays.
+void ro_trace32_batch(const void* prims, const void* nodes, const float* rays, uint32_t n,
+                      float t_max, int any_hit, uint32_t* prim_out, float* t_out,
+                      uint32_t* inner_out, uint32_t* tested_out, int threads);
+
+// One ray of the above, returning (t, u, v) too.
+void ro_trace32_one(const void* prims, const void* nodes, const float* o, const float* d, float t_max, int any_hit,
+                    uint32_t* prim_out, float* tuv_out, uint32_t* inner_out, uint32_t* tested_out);
+
+// ---- the trace shader's path tracer (src/shaders.mjs:131-1899), in f32 ----
+// Renders params.samples_per_frame samples for every pixel of the region
+// [x0, x0+rw) × [y0, y0+rh) of the params' image, as main() does, and
+// writes the region's per-pixel sums (accum rgb+lum², guide albedo, guide
+// normal), 4 floats each, row-major over the region. seed_hash is XORed into
+// the sample hashes (0: the reference's streams). counters (optional, 4
+// u64): algorithmic bytes, rays traced, surface hits, paths.
+void ro_render(const void* prims, const void* nodes, const void* materials, const float* attributes,
+               const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0, uint32_t y0,
+               uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out,
+               uint64_t* counters, int threads);
+
+// ---- the denoiser (src/shaders.mjs:1916-2098) and display (2114-2152) ----
+// Full-image à-trous from the accumulated buffers: prepare, steps 1..16,
+// compose. out: w*h*4 floats.
+void ro_denoise(const float* accum, const float* guide_albedo, const float* guide_normal, uint32_t w, uint32_t h,
+                uint32_t total_samples, float* out, int threads);
+// The display pass into RGBA8.
+void ro_display(const float* accum, const float* denoised, const void* params208, uint8_t* out);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,1056 @@
+// The trace shader's path tracer (src/shaders.mjs:131-1899), the denoiser
+// (src/shaders.mjs:1916-2098) and the display math (src/shaders.mjs:
+// 2114-2152), restated as scalar f32 C++ on the CPU — TEST INFRASTRUCTURE
+// ONLY. The integer sample hashes are bit-exact; the f32 arithmetic follows
+// the WGSL expression by expression (compiled without contraction), with
+// the math library's sqrt/sin/cos/exp/log/pow/atan2/acos called, never
+// re-implemented. Textured materials and environment maps are not
+// restated here (they read like the sky gradient's absence: the oracle
+// scenes use neither).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "oracle.h"
+
+namespace {
+
+const float PI = 3.14159265358979f;
+const uint32_t NONE = 0xffffffffu;
+const float INF = 1e30f;
+
+struct V {
+    float x, y, z;
+};
+inline V v3(float x, float y, float z) { return {x, y, z}; }
+inline V vs(float s) { return {s, s, s}; }
+inline V vf(const float* p) { return {p[0], p[1], p[2]}; }
+inline V operator+(V a, V b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V operator-(V a, V b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V operator-(V a) { return {-a.x, -a.y, -a.z}; }
+inline V operator*(V a, V b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+inline V operator*(V a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+inline V operator/(V a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+inline float dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V cross(V a, V b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline float len(V a) { return std::sqrt(dot(a, a)); }
+inline V norm(V a) { return a / std::sqrt(dot(a, a)); }
+inline float wmin(float a, float b) { return b < a ? b : a; }  // WGSL min(e1, e2)
+inline float wmax(float a, float b) { return b > a ? b : a; }
+inline float clampf(float x, float lo, float hi) { return wmin(wmax(x, lo), hi); }
+inline float sgn(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+inline uint32_t fbits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return u;
+}
+inline float bitsf(uint32_t u) {
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+inline bool finite3(V v) {
+    return (fbits(v.x) & 0x7f800000u) != 0x7f800000u && (fbits(v.y) & 0x7f800000u) != 0x7f800000u &&
+           (fbits(v.z) & 0x7f800000u) != 0x7f800000u;
+}
+inline float lum(V c) { return dot(c, v3(0.2126f, 0.7152f, 0.0722f)); }
+
+// ---- uniform block (src/shaders.mjs:9-24) ----
+struct Params {
+    float cam_pos[3], lens_radius, cam_right[3], tan_half_fov, cam_up[3], focus_distance, cam_forward[3], aspect;
+    float sky_zenith[3], sun_omc, sky_horizon[3];
+    uint32_t sun_on;
+    float sky_ground[3], firefly_clamp, sun_dir[3];
+    uint32_t light_count;
+    float sun_radiance[3];
+    uint32_t max_bounces, view, volume_count;
+    float env_strength, env_rotation;
+    uint32_t width, height, sample_offset, samples_per_frame, total_samples;
+    float exposure;
+    uint32_t denoise, caustics;
+    float photon_radius, photon_cell;
+    uint32_t pad5, pad6;
+};
+static_assert(sizeof(Params) == 208, "208-byte uniforms");
+
+// ---- sample hashes (src/shaders.mjs:135-212) ----
+inline uint32_t pcg(uint32_t v) {
+    const uint32_t state = v * 747796405u + 2891336453u;
+    const uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+inline float unit(uint32_t x) { return float(x >> 8u) * (1.0f / 16777216.0f); }
+inline uint32_t reverse_bits(uint32_t x) {
+    uint32_t r = 0;
+    for (int i = 0; i < 32; ++i) {
+        r = (r << 1) | (x & 1u);
+        x >>= 1;
+    }
+    return r;
+}
+inline uint32_t owen(uint32_t x, uint32_t seed) {
+    uint32_t v = reverse_bits(x);
+    v ^= v * 0x3d20adeau;
+    v += seed;
+    v *= (seed >> 16u) | 1u;
+    v ^= v * 0x05526c56u;
+    v ^= v * 0x53a22864u;
+    return reverse_bits(v);
+}
+inline uint32_t sobol2(uint32_t i) {
+    uint32_t r = 0u, v = 0x80000000u, j = i;
+    while (j != 0u) {
+        if ((j & 1u) != 0u) r ^= v;
+        j >>= 1u;
+        v ^= v >> 1u;
+    }
+    return r;
+}
+
+struct Sampler {
+    uint32_t rng_state = 0;
+    bool qmc_on = false;
+    uint32_t qmc_seed = 0, qmc_index = 0, qmc_dim = 0;
+
+    void qmc_next(uint32_t& key, uint32_t& idx) {
+        key = pcg(qmc_seed ^ pcg(qmc_dim));
+        qmc_dim++;
+        idx = owen(qmc_index, key);
+    }
+    float rand() {
+        if (qmc_on) {
+            uint32_t k, y;
+            qmc_next(k, y);
+            return unit(owen(reverse_bits(y), pcg(k)));
+        }
+        rng_state = pcg(rng_state);
+        return unit(rng_state);
+    }
+    void rand2(float& a, float& b) {
+        if (qmc_on) {
+            uint32_t k, y;
+            qmc_next(k, y);
+            a = unit(owen(reverse_bits(y), pcg(k)));
+            b = unit(owen(sobol2(y), pcg(k + 1u)));
+            return;
+        }
+        a = rand();
+        b = rand();
+    }
+};
+
+// frame (src/shaders.mjs:217-225): columns c0, c1, n.
+inline V in_frame(V n, V l) {
+    const float s = n.z >= 0.0f ? 1.0f : -1.0f;
+    const float a = -1.0f / (s + n.z);
+    const float b = n.x * n.y * a;
+    const V c0 = v3(1.0f + s * n.x * n.x * a, s * b, -s * n.x);
+    const V c1 = v3(b, s + n.y * n.y * a, -n.y);
+    return c0 * l.x + c1 * l.y + n * l.z;
+}
+
+struct Ctx {
+    const uint8_t* prims;
+    const uint8_t* nodes;
+    const float* mats;
+    const float* attrs;
+    const uint32_t* lights;
+    Params P;
+    // counters
+    uint64_t bytes = 0, rays = 0, hits = 0;
+
+    const float* pf(uint32_t i) const { return reinterpret_cast<const float*>(prims + size_t(i) * 64); }
+    const uint32_t* pu(uint32_t i) const { return reinterpret_cast<const uint32_t*>(prims + size_t(i) * 64); }
+    const float* mf(uint32_t i) const { return mats + size_t(i) * 24; }
+    uint32_t mu(uint32_t i, int k) const { return fbits(mats[size_t(i) * 24 + k]); }
+};
+
+struct HitR {
+    float t;
+    uint32_t prim;
+    float u, v;
+};
+
+HitR trace(Ctx& c, V o, V d, float t_max, bool any_hit) {
+    const float of[3] = {o.x, o.y, o.z}, df[3] = {d.x, d.y, d.z};
+    uint32_t prim, inner, tested;
+    float tuv[3];
+    ro_trace32_one(c.prims, c.nodes, of, df, t_max, any_hit ? 1 : 0, &prim, tuv, &inner, &tested);
+    c.rays++;
+    c.bytes += 32ull * (1 + 2ull * inner) + 64ull * tested;
+    return {tuv[0], prim, tuv[1], tuv[2]};
+}
+
+struct Surf {
+    V p, n, ng;
+    bool front;
+    uint32_t material, light, kind;
+    float u, v;
+};
+
+// sphere_uv (src/shaders.mjs:573-577).
+void sphere_uv(V n, const float* p, float& u, float& v) {
+    const V x = vf(p + 8), north = vf(p + 12);
+    const V z = cross(x, north);
+    const float uu = std::atan2(-dot(n, z), dot(n, x)) / (2.0f * PI);
+    u = uu - std::floor(uu);
+    v = std::acos(clampf(dot(n, north), -1.0f, 1.0f)) / PI;
+}
+
+// surface (src/shaders.mjs:460-569), without normal maps.
+Surf surface(Ctx& c, V o, V d, const HitR& hit) {
+    const float* p = c.pf(hit.prim);
+    const uint32_t* pu = c.pu(hit.prim);
+    const V point = o + d * hit.t;
+    V ng, ns;
+    float u = 0, v = 0;
+    c.hits++;
+    c.bytes += 64 + 96;  // the primitive record and its material
+    switch (pu[0]) {
+        case 0:
+            ng = norm(point - vf(p + 4));
+            ns = ng;
+            sphere_uv(ng, p, u, v);
+            break;
+        case 1:
+            ng = norm(cross(vf(p + 8), vf(p + 12)));
+            ns = ng;
+            u = hit.u;
+            v = 1.0f - hit.v;
+            break;
+        case 2: {
+            const V r0 = vf(p + 4), r1 = vf(p + 8), r2 = vf(p + 12);
+            const V lp = v3(dot(r0, point) + p[7], dot(r1, point) + p[11], dot(r2, point) + p[15]);
+            const V a = v3(std::fabs(lp.x), std::fabs(lp.y), std::fabs(lp.z));
+            const V half = v3(1.0f / len(r0), 1.0f / len(r1), 1.0f / len(r2));
+            if (a.x >= a.y && a.x >= a.z) {
+                ng = r0 * sgn(lp.x);
+                u = (1.0f - sgn(lp.x) * lp.z) * half.z;
+                v = (1.0f - lp.y) * half.y;
+            } else if (a.y >= a.z) {
+                ng = r1 * sgn(lp.y);
+                u = (1.0f + lp.x) * half.x;
+                v = (1.0f + sgn(lp.y) * lp.z) * half.z;
+            } else {
+                ng = r2 * sgn(lp.z);
+                u = (1.0f + sgn(lp.z) * lp.x) * half.x;
+                v = (1.0f - lp.y) * half.y;
+            }
+            ng = norm(ng);
+            ns = ng;
+            break;
+        }
+        default: {
+            const V e1 = vf(p + 8) - vf(p + 4), e2 = vf(p + 12) - vf(p + 4);
+            ng = norm(cross(e1, e2));
+            ns = ng;
+            u = hit.u;
+            v = hit.v;
+            if (pu[3] != NONE) {
+                c.bytes += 64;  // the attribute block
+                const float* A = c.attrs + size_t(pu[3]) * 4;
+                const float w = 1.0f - hit.u - hit.v;
+                const uint32_t flags = uint32_t(A[15]);
+                if (flags & 1u) {
+                    ns = norm(vf(A) * w + vf(A + 4) * hit.u + vf(A + 8) * hit.v);
+                    if (dot(ns, ng) < 0.0f) ns = -ns;
+                }
+                if (flags & 2u) {
+                    u = A[3] * w + A[7] * hit.u + A[11] * hit.v;
+                    v = A[12] * w + A[13] * hit.u + A[14] * hit.v;
+                }
+            }
+        }
+    }
+    const bool front = dot(ng, d) < 0.0f;
+    const float flip = front ? 1.0f : -1.0f;
+    return {point, ns * flip, ng * flip, front, pu[1], pu[2], pu[0], u, v};
+}
+
+V offset(const Surf& s, V wi) {
+    const float eps = 1e-4f * wmax(1.0f, wmax(std::fabs(s.p.x), wmax(std::fabs(s.p.y), std::fabs(s.p.z))));
+    return s.p + s.ng * (dot(wi, s.ng) > 0.0f ? eps : -eps);
+}
+
+V sky(const Params& P, V d) {
+    const V hz = vf(P.sky_horizon), zn = vf(P.sky_zenith), gr = vf(P.sky_ground);
+    if (d.y >= 0.0f) {
+        const float t = std::sqrt(wmin(d.y, 1.0f));
+        return hz * (1.0f - t) + zn * t;
+    }
+    const float t = std::sqrt(wmin(-d.y, 1.0f));
+    return hz * (1.0f - t) + gr * t;
+}
+bool in_sun(const Params& P, V d) { return P.sun_on != 0u && dot(d, vf(P.sun_dir)) >= 1.0f - P.sun_omc; }
+
+// ---- materials (src/shaders.mjs:693-871) ----
+struct Mat {
+    V color;
+    uint32_t kind;
+    V emission;
+    float roughness;
+    V checker;
+    float checker_size, ior, dispersion, density, anisotropy;
+};
+Mat material(const Ctx& c, uint32_t i) {
+    const float* m = c.mf(i);
+    return {vf(m), c.mu(i, 3), vf(m + 4), m[7], vf(m + 8), m[11], m[12], m[19], m[20], m[21]};
+}
+V albedo(const Mat& m, V p) {
+    V col = m.color;
+    if (m.checker_size > 0.0f) {
+        const float cx = std::floor(p.x / m.checker_size + 1e-3f), cy = std::floor(p.y / m.checker_size + 1e-3f),
+                    cz = std::floor(p.z / m.checker_size + 1e-3f);
+        const int odd = (int(cx) + int(cy) + int(cz)) & 1;
+        col = odd != 0 ? m.checker : m.color;
+    }
+    return col;
+}
+bool is_delta(const Mat& m) { return m.kind == 3 || (m.kind == 1 && m.roughness < 0.01f); }
+float ggx_alpha2(float r) {
+    const float a = wmax(r * r, 0.002f);
+    return a * a;
+}
+float ggx_d(float nh, float a2) {
+    const float k = nh * nh * (a2 - 1.0f) + 1.0f;
+    return a2 / (PI * k * k);
+}
+float smith_g1(float nv, float a2) { return 2.0f * nv / (nv + std::sqrt(a2 + (1.0f - a2) * nv * nv)); }
+float schlick_s(float f0, float c) { return f0 + (1.0f - f0) * std::pow(1.0f - clampf(c, 0.0f, 1.0f), 5.0f); }
+V schlick_v(V f0, float c) {
+    const float k = std::pow(1.0f - clampf(c, 0.0f, 1.0f), 5.0f);
+    return f0 + (vs(1.0f) - f0) * k;
+}
+float dielectric_f0(float ior) {
+    const float r = (ior - 1.0f) / (ior + 1.0f);
+    return r * r;
+}
+float fresnel(float cos_i, float eta) {
+    const float sin2_t = (1.0f - cos_i * cos_i) / (eta * eta);
+    if (sin2_t >= 1.0f) return 1.0f;
+    const float cos_t = std::sqrt(1.0f - sin2_t);
+    const float rs = (cos_i - eta * cos_t) / (cos_i + eta * cos_t);
+    const float rp = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+    return 0.5f * (rs * rs + rp * rp);
+}
+float spec_chance(const Mat& m, float nv) { return clampf(schlick_s(dielectric_f0(m.ior), nv) * 4.0f + 0.1f, 0.1f, 0.9f); }
+
+void eval_bsdf(const Mat& m, V base, V n, V wo, V wi, V& f, float& pdf) {
+    const float nl = dot(n, wi), nv = dot(n, wo);
+    f = vs(0.0f);
+    pdf = 0.0f;
+    if (nl <= 0.0f || nv <= 0.0f) return;
+    if (m.kind == 0) {
+        f = base * (nl / PI);
+        pdf = nl / PI;
+        return;
+    }
+    const float a2 = ggx_alpha2(m.roughness);
+    const V h = norm(wo + wi);
+    const float nh = wmax(dot(n, h), 0.0f), vh = wmax(dot(wo, h), 1e-6f);
+    const float d = ggx_d(nh, a2);
+    const float g = smith_g1(nv, a2) * smith_g1(nl, a2);
+    const float spec_pdf = d * nh / (4.0f * vh);
+    if (m.kind == 1) {
+        f = schlick_v(base, vh) * (d * g / (4.0f * nv));
+        pdf = spec_pdf;
+        return;
+    }
+    const float f0 = dielectric_f0(m.ior);
+    const float coat = schlick_s(f0, vh) * d * g / (4.0f * nv);
+    const float through = (1.0f - schlick_s(f0, nl)) * (1.0f - schlick_s(f0, nv));
+    const V diffuse = base * (through * nl / PI);
+    const float chance = spec_chance(m, nv);
+    f = vs(coat) + diffuse;
+    pdf = chance * spec_pdf + (1.0f - chance) * nl / PI;
+}
+
+V cosine_hemisphere(V n, Sampler& s) {
+    float a, b;
+    s.rand2(a, b);
+    const float r = std::sqrt(a), phi = 2.0f * PI * b;
+    return norm(in_frame(n, v3(r * std::cos(phi), r * std::sin(phi), std::sqrt(wmax(0.0f, 1.0f - r * r)))));
+}
+V sample_cone(V axis, float omc, Sampler& s) {
+    float a, b;
+    s.rand2(a, b);
+    const float cos_t = 1.0f - a * omc;
+    const float sin_t = std::sqrt(wmax(0.0f, 1.0f - cos_t * cos_t));
+    const float phi = 2.0f * PI * b;
+    return norm(in_frame(axis, v3(sin_t * std::cos(phi), sin_t * std::sin(phi), cos_t)));
+}
+V reflect(V i, V n) { return i - n * (2.0f * dot(n, i)); }
+V refract(V i, V n, float eta) {
+    const float ni = dot(n, i);
+    const float k = 1.0f - eta * eta * (1.0f - ni * ni);
+    if (k < 0.0f) return vs(0.0f);
+    return i * eta - n * (eta * ni + std::sqrt(k));
+}
+
+struct Bs {
+    V wi, weight;
+    float pdf;
+    bool delta, ok;
+};
+Bs sample_bsdf(const Mat& m, V base, const Surf& sf, V wo, Sampler& s) {
+    const V n = sf.n;
+    const float nv = dot(n, wo);
+    if (m.kind == 3) {
+        const float eta = sf.front ? m.ior : 1.0f / m.ior;
+        const float f = fresnel(clampf(nv, 0.0f, 1.0f), eta);
+        if (s.rand() < f) return {reflect(-wo, n), vs(1.0f), 0.0f, true, true};
+        const V wi = refract(-wo, n, 1.0f / eta);
+        if (dot(wi, wi) == 0.0f) return {reflect(-wo, n), vs(1.0f), 0.0f, true, true};
+        return {norm(wi), sf.front ? base : vs(1.0f), 0.0f, true, true};
+    }
+    if (m.kind == 1 && m.roughness < 0.01f) return {reflect(-wo, n), schlick_v(base, nv), 0.0f, true, true};
+    V wi;
+    if (m.kind == 0) {
+        wi = cosine_hemisphere(n, s);
+    } else if (m.kind == 1 || s.rand() < spec_chance(m, nv)) {
+        const float a2 = ggx_alpha2(m.roughness);
+        float a, b;
+        s.rand2(a, b);
+        const float cos_t = std::sqrt((1.0f - a) / (1.0f + (a2 - 1.0f) * a));
+        const float sin_t = std::sqrt(wmax(0.0f, 1.0f - cos_t * cos_t));
+        const float phi = 2.0f * PI * b;
+        const V h = norm(in_frame(n, v3(sin_t * std::cos(phi), sin_t * std::sin(phi), cos_t)));
+        wi = reflect(-wo, h);
+    } else {
+        wi = cosine_hemisphere(n, s);
+    }
+    if (dot(wi, sf.ng) <= 0.0f) return {vs(0), vs(0), 0.0f, false, false};
+    V f;
+    float pdf;
+    eval_bsdf(m, base, n, wo, wi, f, pdf);
+    if (pdf <= 0.0f) return {vs(0), vs(0), 0.0f, false, false};
+    return {wi, f / pdf, pdf, false, true};
+}
+
+// ---- lights (src/shaders.mjs:877-1018); no environment map ----
+uint32_t choices(const Params& P) { return P.light_count + (P.sun_on != 0u ? 1u : 0u); }
+float light_cdf(const Ctx& c, uint32_t l) { return bitsf(c.lights[c.P.light_count + c.P.volume_count + l]); }
+float light_chance(const Ctx& c, uint32_t l) {
+    const float below = l > 0u ? light_cdf(c, l - 1u) : 0.0f;
+    return (light_cdf(c, l) - below) * float(c.P.light_count) / float(choices(c.P));
+}
+float sphere_omc(float r, float d2) {
+    const float x = wmin(r * r / d2, 1.0f);
+    return x / (1.0f + std::sqrt(1.0f - x));
+}
+float power_heuristic(float a, float b) {
+    const float a2 = a * a, b2 = b * b;
+    if (a2 + b2 <= 0.0f) return 0.0f;
+    return a2 / (a2 + b2);
+}
+struct Ls {
+    V wi;
+    float dist;
+    V radiance;
+    float pdf;
+};
+Ls sample_light(Ctx& c, V p, Sampler& s) {
+    const Params& P = c.P;
+    const uint32_t ch = choices(P);
+    const float x = s.rand() * float(ch);
+    uint32_t pick = std::min(uint32_t(x), ch - 1u);
+    float chance = 1.0f / float(ch);
+    if (P.sun_on != 0u && pick == P.light_count) {
+        const V wi = sample_cone(vf(P.sun_dir), P.sun_omc, s);
+        return {wi, INF, vf(P.sun_radiance), chance / (2.0f * PI * P.sun_omc)};
+    }
+    // pick_light: the first CDF entry above u.
+    const float u = x / float(P.light_count);
+    uint32_t lo = 0u, hi = P.light_count - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) / 2u;
+        if (light_cdf(c, mid) > u) hi = mid;
+        else lo = mid + 1u;
+    }
+    pick = lo;
+    chance = light_chance(c, pick);
+    const uint32_t pi = c.lights[pick];
+    const float* pr = c.pf(pi);
+    const Mat m = material(c, c.pu(pi)[1]);
+    c.bytes += 64 + 96;
+    if (c.pu(pi)[0] == 1) {
+        float a, b;
+        s.rand2(a, b);
+        const V q = vf(pr + 4) + vf(pr + 8) * a + vf(pr + 12) * b;
+        const V to = q - p;
+        const float d2 = dot(to, to);
+        const float dist = std::sqrt(d2);
+        const V wi = to / dist;
+        const V cr = cross(vf(pr + 8), vf(pr + 12));
+        const float area = len(cr);
+        const float cos_l = -dot(wi, cr / area);
+        if (cos_l <= 0.0f) return {vs(0), 0.0f, vs(0), 0.0f};
+        return {wi, dist, m.emission, chance * d2 / (cos_l * area)};
+    }
+    const V to = vf(pr + 4) - p;
+    const float d2 = dot(to, to);
+    const float r = pr[7];
+    if (d2 <= r * r) return {vs(0), 0.0f, vs(0), 0.0f};
+    const float omc = sphere_omc(r, d2);
+    const V wi = sample_cone(to / std::sqrt(d2), omc, s);
+    return {wi, dot(to, wi) - std::sqrt(wmax(dot(to, wi) * dot(to, wi) - (d2 - r * r), 0.0f)), m.emission,
+            chance / (2.0f * PI * omc)};
+}
+float light_pdf(const Ctx& c, uint32_t prim, V p, V wi, float t) {
+    const float* pr = c.pf(prim);
+    const float chance = light_chance(c, c.pu(prim)[2]);
+    if (c.pu(prim)[0] == 1) {
+        const V cr = cross(vf(pr + 8), vf(pr + 12));
+        const float area = len(cr);
+        const float cos_l = std::fabs(dot(wi, cr / area));
+        return chance * t * t / wmax(cos_l * area, 1e-12f);
+    }
+    const V to = vf(pr + 4) - p;
+    return chance / (2.0f * PI * sphere_omc(pr[7], dot(to, to)));
+}
+
+// ---- media (src/shaders.mjs:1024-1123) ----
+inline float safe1(float d) { return std::fabs(d) < 1e-20f ? (d >= 0.0f ? 1e-20f : -1e-20f) : d; }
+void volume_span(const Ctx& c, uint32_t i, V o, V d, float& x, float& y) {
+    const float* p = c.pf(i);
+    if (c.pu(i)[0] == 0) {
+        const V oc = o - vf(p + 4);
+        const float a = dot(d, d), hb = dot(oc, d);
+        const float disc = hb * hb - a * (dot(oc, oc) - p[7] * p[7]);
+        if (disc < 0.0f) {
+            x = 1.0f;
+            y = 0.0f;
+            return;
+        }
+        const float sq = std::sqrt(disc);
+        x = wmax((-hb - sq) / a, 0.0f);
+        y = (-hb + sq) / a;
+        return;
+    }
+    float tn = -INF, tf = INF, tminv[3], tmaxv[3];
+    for (int r = 0; r < 3; ++r) {
+        const V row = vf(p + 4 + r * 4);
+        const float lo = dot(row, o) + p[7 + r * 4];
+        const float inv = 1.0f / safe1(dot(row, d));
+        const float t0 = (-1.0f - lo) * inv, t1 = (1.0f - lo) * inv;
+        tminv[r] = wmin(t0, t1);
+        tmaxv[r] = wmax(t0, t1);
+    }
+    (void)tn;
+    (void)tf;
+    x = wmax(wmax(wmax(tminv[0], tminv[1]), tminv[2]), 0.0f);
+    y = wmin(wmin(tmaxv[0], tmaxv[1]), tmaxv[2]);
+}
+float hg(float cth, float g) {
+    const float k = 1.0f + g * g - 2.0f * g * cth;
+    return (1.0f - g * g) / (4.0f * PI * k * std::sqrt(k));
+}
+float transmittance(const Ctx& c, V o, V d, float dist) {
+    float depth = 0.0f;
+    for (uint32_t k = 0; k < c.P.volume_count; ++k) {
+        const uint32_t i = c.lights[c.P.light_count + k];
+        float x, y;
+        volume_span(c, i, o, d, x, y);
+        const float end = wmin(y, dist);
+        if (x < end) depth += c.mf(c.pu(i)[1])[20] * (end - x);
+    }
+    return std::exp(-depth);
+}
+
+// ---- dispersion (src/shaders.mjs:1127-1144) ----
+float lobe(float x, float mu, float below, float above) {
+    const float t = (x - mu) / (x < mu ? below : above);
+    return std::exp(-0.5f * t * t);
+}
+V wavelength_rgb(float l) {
+    const float x = 1.056f * lobe(l, 599.8f, 37.9f, 31.0f) + 0.362f * lobe(l, 442.0f, 16.0f, 26.7f) -
+                    0.065f * lobe(l, 501.1f, 20.4f, 26.2f);
+    const float y = 0.821f * lobe(l, 568.8f, 46.9f, 40.5f) + 0.286f * lobe(l, 530.9f, 16.3f, 31.1f);
+    const float z = 1.217f * lobe(l, 437.0f, 11.8f, 36.0f) + 0.681f * lobe(l, 459.0f, 26.0f, 13.8f);
+    const V rgb = v3(3.2406f * x - 1.5372f * y - 0.4986f * z, -0.9689f * x + 1.8758f * y + 0.0415f * z,
+                     0.0557f * x - 0.2040f * y + 1.0570f * z);
+    return v3(wmax(rgb.x, 0.0f), wmax(rgb.y, 0.0f), wmax(rgb.z, 0.0f)) * v3(1.92985f, 2.94689f, 3.11081f);
+}
+
+bool roulette(V& tp, uint32_t depth, Sampler& s) {
+    if (depth < 3u) return true;
+    const float survive = wmin(wmax(tp.x, wmax(tp.y, tp.z)), 0.95f);
+    if (s.rand() >= survive) return false;
+    tp = tp / survive;
+    return true;
+}
+
+// radiance() (src/shaders.mjs:1179-1359), for the color view.
+V radiance(Ctx& c, float px, float py, Sampler& s, float spectrum_u, V& g_albedo, float g_normal[4]) {
+    const Params& P = c.P;
+    g_albedo = vs(1.0f);
+    g_normal[0] = g_normal[1] = g_normal[2] = g_normal[3] = 0.0f;
+    bool guided = false;
+    float travelled = 0.0f;
+
+    // camera_ray(px, true) (src/shaders.mjs:1148-1166)
+    const float ndcx = 2.0f * px / float(P.width) - 1.0f, ndcy = 1.0f - 2.0f * py / float(P.height);
+    const V fwd = vf(P.cam_forward), right = vf(P.cam_right), up = vf(P.cam_up), pos = vf(P.cam_pos);
+    V dir = norm(fwd + right * (ndcx * P.tan_half_fov * P.aspect) + up * (ndcy * P.tan_half_fov));
+    V o = pos, d = dir;
+    if (P.lens_radius > 0.0f) {
+        const V focus = pos + dir * (P.focus_distance / dot(dir, fwd));
+        float a, b;
+        s.rand2(a, b);
+        const float ux = 2.0f * a - 1.0f, uy = 2.0f * b - 1.0f;
+        float lx = 0.0f, ly = 0.0f;
+        if (!(ux == 0.0f && uy == 0.0f)) {
+            if (std::fabs(ux) > std::fabs(uy)) {
+                const float phi = (PI / 4.0f) * (uy / ux);
+                lx = ux * std::cos(phi);
+                ly = ux * std::sin(phi);
+            } else {
+                const float phi = PI / 2.0f - (PI / 4.0f) * (ux / uy);
+                lx = uy * std::cos(phi);
+                ly = uy * std::sin(phi);
+            }
+        }
+        o = pos + right * (lx * P.lens_radius) + up * (ly * P.lens_radius);
+        d = norm(focus - o);
+    }
+
+    V throughput = vs(1.0f), result = vs(0.0f);
+    float last_pdf = 0.0f;
+    bool last_delta = true;
+    V last_p = o;
+    const uint32_t ch = choices(P);
+    float wavelength = 0.0f;
+    bool caustic = false, diffuse_seen = false;
+
+    for (uint32_t depth = 0; depth <= P.max_bounces; ++depth) {
+        s.qmc_dim = (depth + 1u) << 16u;
+        const HitR hit = trace(c, o, d, INF, false);
+
+        if (P.volume_count > 0) {
+            float sc_t = hit.t;
+            uint32_t sc_v = NONE;
+            for (uint32_t k = 0; k < P.volume_count; ++k) {
+                const uint32_t i = c.lights[P.light_count + k];
+                float x, y;
+                volume_span(c, i, o, d, x, y);
+                const float end = wmin(y, sc_t);
+                if (x < end) {
+                    const float t = x - std::log(1.0f - s.rand()) / c.mf(c.pu(i)[1])[20];
+                    if (t < end) {
+                        sc_t = t;
+                        sc_v = i;
+                    }
+                }
+            }
+            if (sc_v != NONE) {
+                const Mat vm = material(c, c.pu(sc_v)[1]);
+                const V p = o + d * sc_t;
+                travelled += sc_t;
+                if (!guided) {
+                    guided = true;
+                    g_albedo = throughput * vm.color;
+                    g_normal[0] = -d.x;
+                    g_normal[1] = -d.y;
+                    g_normal[2] = -d.z;
+                    g_normal[3] = travelled;
+                }
+                if (depth == P.max_bounces) break;
+                throughput = throughput * vm.color;
+                if (ch > 0u) {
+                    const Ls ls = sample_light(c, p, s);
+                    if (ls.pdf > 0.0f) {
+                        const float phase = hg(dot(d, ls.wi), vm.anisotropy);
+                        const float reach = ls.dist * (1.0f - 1e-3f);
+                        if (trace(c, p, ls.wi, reach, true).prim == NONE)
+                            result = result + throughput * ls.radiance *
+                                                  (phase * transmittance(c, p, ls.wi, reach) *
+                                                   power_heuristic(ls.pdf, phase) / ls.pdf);
+                    }
+                }
+                float a, b;
+                s.rand2(a, b);
+                float cth = 1.0f - 2.0f * a;
+                const float g = vm.anisotropy;
+                if (std::fabs(g) >= 1e-3f) {
+                    const float sq = (1.0f - g * g) / (1.0f + g - 2.0f * g * a);
+                    cth = clampf((1.0f + g * g - sq * sq) / (2.0f * g), -1.0f, 1.0f);
+                }
+                const float sin_t = std::sqrt(wmax(0.0f, 1.0f - cth * cth));
+                const float phi = 2.0f * PI * b;
+                const V wi = norm(in_frame(d, v3(sin_t * std::cos(phi), sin_t * std::sin(phi), cth)));
+                last_pdf = hg(dot(d, wi), g);
+                last_delta = false;
+                last_p = p;
+                o = p;
+                d = wi;
+                caustic = false;
+                diffuse_seen = true;
+                if (!roulette(throughput, depth, s)) break;
+                continue;
+            }
+        }
+
+        if (hit.prim == NONE) {
+            if (!guided) g_albedo = throughput;
+            result = result + throughput * sky(P, d);
+            if (in_sun(P, d) && !(caustic && last_delta)) {
+                float w = 1.0f;
+                if (!last_delta) w = power_heuristic(last_pdf, 1.0f / (float(ch) * 2.0f * PI * P.sun_omc));
+                result = result + throughput * vf(P.sun_radiance) * w;
+            }
+            break;
+        }
+
+        const Surf sf = surface(c, o, d, hit);
+        const Mat m = material(c, sf.material);
+        travelled += hit.t;
+        if (!guided && (m.kind == 4 || !is_delta(m) || depth == P.max_bounces)) {
+            guided = true;
+            g_albedo = throughput * (m.kind == 4 ? vs(1.0f) : albedo(m, sf.p));
+            g_normal[0] = sf.n.x;
+            g_normal[1] = sf.n.y;
+            g_normal[2] = sf.n.z;
+            g_normal[3] = travelled;
+        }
+        if (sf.front && (m.emission.x > 0.0f || m.emission.y > 0.0f || m.emission.z > 0.0f) &&
+            !(caustic && last_delta && sf.light != NONE)) {
+            float w = 1.0f;
+            if (!last_delta && sf.light != NONE) w = power_heuristic(last_pdf, light_pdf(c, hit.prim, last_p, d, hit.t));
+            result = result + throughput * m.emission * w;
+        }
+        if (m.kind == 4) break;
+        if (!is_delta(m)) {
+            caustic = P.caustics != 0u && !diffuse_seen;
+            diffuse_seen = true;
+        }
+        if (depth == P.max_bounces) break;
+
+        const V base = albedo(m, sf.p);
+        const V wo = -d;
+        if (!is_delta(m) && ch > 0u) {
+            const Ls ls = sample_light(c, sf.p, s);
+            if (ls.pdf > 0.0f && dot(ls.wi, sf.ng) > 0.0f) {
+                V f;
+                float pdf;
+                eval_bsdf(m, base, sf.n, wo, ls.wi, f, pdf);
+                const V origin = offset(sf, ls.wi);
+                const float reach = (ls.dist - dot(origin - sf.p, ls.wi)) * (1.0f - 1e-3f);
+                if (pdf > 0.0f && trace(c, origin, ls.wi, reach, true).prim == NONE)
+                    result = result + throughput * f * ls.radiance *
+                                          (transmittance(c, origin, ls.wi, reach) * power_heuristic(ls.pdf, pdf) / ls.pdf);
+            }
+        }
+        // dispersed (src/shaders.mjs:1412-1423)
+        Mat sm = m;
+        if (m.kind == 3 && m.dispersion > 0.0f) {
+            if (wavelength == 0.0f) {
+                wavelength = 380.0f + 340.0f * spectrum_u;
+                throughput = throughput * wavelength_rgb(wavelength);
+            }
+            const float l = wavelength * 1e-3f;
+            sm.ior = m.ior + m.dispersion * (1.0f / (l * l) - 1.0f / (0.5876f * 0.5876f));
+        }
+        const Bs bs = sample_bsdf(sm, base, sf, wo, s);
+        if (!bs.ok) break;
+        throughput = throughput * bs.weight;
+        last_pdf = bs.pdf;
+        last_delta = bs.delta;
+        last_p = sf.p;
+        o = offset(sf, bs.wi);
+        d = bs.wi;
+        if (!roulette(throughput, depth, s)) break;
+    }
+    return result;
+}
+
+// inspect() (src/shaders.mjs:1377-1407).
+V inspect(Ctx& c, float px, float py) {
+    const Params& P = c.P;
+    const float ndcx = 2.0f * px / float(P.width) - 1.0f, ndcy = 1.0f - 2.0f * py / float(P.height);
+    const V d = norm(vf(P.cam_forward) + vf(P.cam_right) * (ndcx * P.tan_half_fov * P.aspect) +
+                     vf(P.cam_up) * (ndcy * P.tan_half_fov));
+    const V o = vf(P.cam_pos);
+    const HitR hit = trace(c, o, d, INF, false);
+    if (hit.prim == NONE) return P.view == 1u ? sky(P, d) : vs(0.0f);
+    const Surf sf = surface(c, o, d, hit);
+    const Mat m = material(c, sf.material);
+    if (P.view == 1u) {
+        if (m.kind == 4) return m.emission / wmax(wmax(m.emission.x, m.emission.y), wmax(m.emission.z, 1.0f));
+        return albedo(m, sf.p);
+    }
+    if (P.view == 2u) return sf.n;
+    return vs(hit.t);
+}
+
+}  // namespace
+
+extern "C" void ro_render(const void* prims, const void* nodes, const void* materials, const float* attributes,
+                          const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0, uint32_t y0,
+                          uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out,
+                          uint64_t* counters, int threads) {
+    Params P;
+    std::memcpy(&P, params208, sizeof P);
+    std::atomic<uint32_t> next{0};
+    std::atomic<uint64_t> tot_bytes{0}, tot_rays{0}, tot_hits{0};
+    const uint32_t n = rw * rh;
+    auto worker = [&] {
+        Ctx c{static_cast<const uint8_t*>(prims), static_cast<const uint8_t*>(nodes),
+              static_cast<const float*>(materials), attributes, lights, P};
+        for (;;) {
+            const uint32_t k0 = next.fetch_add(64);
+            if (k0 >= n) break;
+            for (uint32_t k = k0; k < std::min(n, k0 + 64); ++k) {
+                const uint32_t x = x0 + k % rw, y = y0 + k / rw;
+                const uint32_t index = y * P.width + x;
+                float sum[4] = {0, 0, 0, 0}, sa[3] = {0, 0, 0}, sn[4] = {0, 0, 0, 0};
+                for (uint32_t s = 0; s < P.samples_per_frame; ++s) {
+                    // main()'s seeding (src/shaders.mjs:1852-1859)
+                    Sampler sm;
+                    sm.rng_state = pcg(index ^ pcg(P.sample_offset + s)) ^ seed_hash;
+                    sm.qmc_on = true;
+                    sm.qmc_seed = pcg(index + 0x9e3779b9u) ^ seed_hash;
+                    sm.qmc_index = P.sample_offset + s;
+                    sm.qmc_dim = 0u;
+                    const float spectrum_u =
+                        float((pcg(index * 7919u + 1u) + (P.sample_offset + s) * 2654435769u) >> 8u) *
+                        (1.0f / 16777216.0f);
+                    V col, ga = vs(0.0f);
+                    float gn[4] = {0, 0, 0, 0};
+                    if (P.view == 0u) {
+                        float jx, jy;
+                        sm.rand2(jx, jy);
+                        col = radiance(c, float(x) + jx, float(y) + jy, sm, spectrum_u, ga, gn);
+                        const float peak = wmax(col.x, wmax(col.y, col.z));
+                        if (P.firefly_clamp > 0.0f && peak > P.firefly_clamp) col = col * (P.firefly_clamp / peak);
+                    } else {
+                        col = inspect(c, float(x) + 0.5f, float(y) + 0.5f);
+                    }
+                    if (finite3(col) && finite3(ga) && finite3(v3(gn[0], gn[1], gn[2])) && finite3(vs(gn[3]))) {
+                        const float l = lum(col);
+                        sum[0] += col.x;
+                        sum[1] += col.y;
+                        sum[2] += col.z;
+                        sum[3] += l * l;
+                        sa[0] += ga.x;
+                        sa[1] += ga.y;
+                        sa[2] += ga.z;
+                        for (int q = 0; q < 4; ++q) sn[q] += gn[q];
+                    }
+                }
+                for (int q = 0; q < 4; ++q) accum_out[size_t(k) * 4 + q] = sum[q];
+                if (albedo_out) {
+                    for (int q = 0; q < 3; ++q) albedo_out[size_t(k) * 4 + q] = sa[q];
+                    albedo_out[size_t(k) * 4 + 3] = 0.0f;
+                }
+                if (normal_out)
+                    for (int q = 0; q < 4; ++q) normal_out[size_t(k) * 4 + q] = sn[q];
+            }
+        }
+        tot_bytes += c.bytes;
+        tot_rays += c.rays;
+        tot_hits += c.hits;
+    };
+    const int nt = std::max(1, threads);
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto& t : pool) t.join();
+    if (counters) {
+        counters[0] = tot_bytes;
+        counters[1] = tot_rays;
+        counters[2] = tot_hits;
+        counters[3] = uint64_t(n) * P.samples_per_frame;
+    }
+}
+
+// ---- denoiser (src/shaders.mjs:1930-2097) ----
+namespace {
+struct Den {
+    const float *accum, *ga, *gn;
+    uint32_t w, h;
+    float n;
+    V albedo_at(uint32_t i) const {
+        return v3(wmax(ga[i * 4] / n, 0.01f), wmax(ga[i * 4 + 1] / n, 0.01f), wmax(ga[i * 4 + 2] / n, 0.01f));
+    }
+    void normal_at(uint32_t i, float* out) const {
+        const V g = vf(gn + size_t(i) * 4);
+        const V nn = dot(g, g) > 0.0f ? norm(g) : vs(0.0f);
+        out[0] = nn.x;
+        out[1] = nn.y;
+        out[2] = nn.z;
+        out[3] = gn[size_t(i) * 4 + 3] / n;
+    }
+    V light_at(uint32_t i) const {
+        const V a = albedo_at(i);
+        return v3(accum[i * 4] / n / a.x, accum[i * 4 + 1] / n / a.y, accum[i * 4 + 2] / n / a.z);
+    }
+};
+float similarity(const float* p, const float* q, float step) {
+    if (p[3] <= 0.0f || q[3] <= 0.0f) return (p[3] <= 0.0f && q[3] <= 0.0f) ? 1.0f : 0.0f;
+    if (p[0] * p[0] + p[1] * p[1] + p[2] * p[2] == 0.0f) return 0.0f;
+    const float wn = std::pow(wmax(p[0] * q[0] + p[1] * q[1] + p[2] * q[2], 0.0f), 64.0f);
+    const float wz = std::exp(-std::fabs(p[3] - q[3]) / (p[3] * 0.02f * step + 1e-6f));
+    return wn * wz;
+}
+const float KERNEL[3] = {0.375f, 0.25f, 0.0625f};
+
+template <typename F>
+void rows(uint32_t h, int threads, F fn) {
+    std::atomic<uint32_t> next{0};
+    auto worker = [&] {
+        for (;;) {
+            const uint32_t y = next.fetch_add(1);
+            if (y >= h) return;
+            fn(y);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < std::max(1, threads); ++t) pool.emplace_back(worker);
+    worker();
+    for (auto& t : pool) t.join();
+}
+}  // namespace
+
+extern "C" void ro_denoise(const float* accum, const float* guide_albedo, const float* guide_normal, uint32_t w,
+                           uint32_t h, uint32_t total_samples, float* out, int threads) {
+    Den D{accum, guide_albedo, guide_normal, w, h, float(std::max(total_samples, 1u))};
+    std::vector<float> a(size_t(w) * h * 4), b(size_t(w) * h * 4);
+    // prepare
+    rows(h, threads, [&](uint32_t y) {
+        for (uint32_t x = 0; x < w; ++x) {
+            const uint32_t i = y * w + x;
+            const V light = D.light_at(i);
+            float gp[4];
+            D.normal_at(i, gp);
+            const float al = lum(D.albedo_at(i));
+            float variance;
+            if (D.n >= 4.0f) {
+                const float mean = lum(vf(accum + size_t(i) * 4)) / D.n;
+                const float spread = wmax(accum[i * 4 + 3] / D.n - mean * mean, 0.0f) * D.n / (D.n - 1.0f);
+                variance = spread / D.n / (al * al);
+            } else {
+                float sum = 0, sum2 = 0, weight = 0;
+                for (int dy = -2; dy <= 2; ++dy)
+                    for (int dx = -2; dx <= 2; ++dx) {
+                        const int xx = int(x) + dx, yy = int(y) + dy;
+                        if (xx < 0 || yy < 0 || xx >= int(w) || yy >= int(h)) continue;
+                        const uint32_t j = uint32_t(yy) * w + uint32_t(xx);
+                        float gq[4];
+                        D.normal_at(j, gq);
+                        const float wt = similarity(gp, gq, 1.0f);
+                        const float l = lum(D.light_at(j));
+                        sum += wt * l;
+                        sum2 += wt * l * l;
+                        weight += wt;
+                    }
+                const float mean = sum / wmax(weight, 1e-6f);
+                variance = wmax(sum2 / wmax(weight, 1e-6f) - mean * mean, 0.0f) + 0.01f * mean * mean;
+            }
+            a[i * 4] = light.x;
+            a[i * 4 + 1] = light.y;
+            a[i * 4 + 2] = light.z;
+            a[i * 4 + 3] = variance;
+        }
+    });
+    std::vector<float>* from = &a;
+    std::vector<float>* to = &b;
+    for (int step : {1, 2, 4, 8, 16}) {
+        const std::vector<float>& in = *from;
+        std::vector<float>& o = *to;
+        rows(h, threads, [&](uint32_t y) {
+            for (uint32_t x = 0; x < w; ++x) {
+                const uint32_t i = y * w + x;
+                float gp[4];
+                D.normal_at(i, gp);
+                const float lp = lum(vf(&in[size_t(i) * 4]));
+                float variance = 0, vw = 0;
+                for (int dy = -1; dy <= 1; ++dy)
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        const int xx = int(x) + dx, yy = int(y) + dy;
+                        if (xx >= 0 && yy >= 0 && xx < int(w) && yy < int(h)) {
+                            const float wt = KERNEL[std::abs(dx)] * KERNEL[std::abs(dy)];
+                            variance += wt * in[(size_t(yy) * w + xx) * 4 + 3];
+                            vw += wt;
+                        }
+                    }
+                const float sigma = 4.0f * std::sqrt(variance / vw) + 1e-4f;
+                V sum = vs(0);
+                float sv = 0, weight = 0;
+                for (int dy = -2; dy <= 2; ++dy)
+                    for (int dx = -2; dx <= 2; ++dx) {
+                        const int xx = int(x) + dx * step, yy = int(y) + dy * step;
+                        if (xx < 0 || yy < 0 || xx >= int(w) || yy >= int(h)) continue;
+                        const uint32_t j = uint32_t(yy) * w + uint32_t(xx);
+                        const V q = vf(&in[size_t(j) * 4]);
+                        float gq[4];
+                        D.normal_at(j, gq);
+                        const float wt = KERNEL[std::abs(dx)] * KERNEL[std::abs(dy)] * similarity(gp, gq, float(step)) *
+                                         std::exp(-std::fabs(lp - lum(q)) / sigma);
+                        sum = sum + q * wt;
+                        sv += wt * wt * in[size_t(j) * 4 + 3];
+                        weight += wt;
+                    }
+                if (weight > 0.0f) {
+                    o[i * 4] = sum.x / weight;
+                    o[i * 4 + 1] = sum.y / weight;
+                    o[i * 4 + 2] = sum.z / weight;
+                    o[i * 4 + 3] = sv / (weight * weight);
+                } else {
+                    for (int q = 0; q < 4; ++q) o[i * 4 + q] = in[i * 4 + q];
+                }
+            }
+        });
+        std::swap(from, to);
+    }
+    for (uint32_t i = 0; i < w * h; ++i) {
+        const V al = D.albedo_at(i);
+        out[i * 4] = (*from)[i * 4] * al.x;
+        out[i * 4 + 1] = (*from)[i * 4 + 1] * al.y;
+        out[i * 4 + 2] = (*from)[i * 4 + 2] * al.z;
+        out[i * 4 + 3] = 0.0f;
+    }
+}
+
+extern "C" void ro_display(const float* accum, const float* denoised, const void* params208, uint8_t* out) {
+    Params P;
+    std::memcpy(&P, params208, sizeof P);
+    auto aces = [](float x) {
+        return clampf((x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f), 0.0f, 1.0f);
+    };
+    auto srgb = [](float c) {
+        const float x = clampf(c, 0.0f, 1.0f);
+        return x <= 0.0031308f ? x * 12.92f : 1.055f * std::pow(x, 1.0f / 2.4f) - 0.055f;
+    };
+    auto byte = [](float v) { return uint8_t(std::lrint(clampf(v, 0.0f, 1.0f) * 255.0f)); };
+    for (uint32_t i = 0; i < P.width * P.height; ++i) {
+        float o[3] = {0, 0, 0};
+        if (P.total_samples != 0u) {
+            const float n = float(P.total_samples);
+            const V c = v3(accum[i * 4] / n, accum[i * 4 + 1] / n, accum[i * 4 + 2] / n);
+            if (P.view == 0u) {
+                const V sh = P.denoise != 0u ? vf(denoised + size_t(i) * 4) : c;
+                o[0] = srgb(aces(sh.x * P.exposure));
+                o[1] = srgb(aces(sh.y * P.exposure));
+                o[2] = srgb(aces(sh.z * P.exposure));
+            } else if (P.view == 1u) {
+                o[0] = srgb(c.x);
+                o[1] = srgb(c.y);
+                o[2] = srgb(c.z);
+            } else if (P.view == 2u) {
+                o[0] = c.x * 0.5f + 0.5f;
+                o[1] = c.y * 0.5f + 0.5f;
+                o[2] = c.z * 0.5f + 0.5f;
+            } else {
+                const float g = c.x <= 0.0f ? 0.0f : 1.0f / (1.0f + c.x / P.focus_distance);
+                o[0] = o[1] = o[2] = g;
+            }
+        }
+        out[i * 4] = byte(o[0]);
+        out[i * 4 + 1] = byte(o[1]);
+        out[i * 4 + 2] = byte(o[2]);
+        out[i * 4 + 3] = 255;
+    }
+}

@@ -1,0 +1,353 @@
+// Native binned-SAH BVH builder producing BVH.build's exact nodes and
+// primitive order (src/BVH.mjs:57-234), so packed scenes built here and by
+// the JavaScript library are interchangeable byte for byte.
+//
+// Same decisions as the reference, organized for speed: centroids and boxes
+// in structure-of-arrays form, one pass over a node's primitives bins all
+// three axes at once, and independent subtrees are built on worker threads
+// into private node lists that are spliced into the reference's node
+// numbering afterwards (its numbering is a right-first depth-first order,
+// so a subtree's nodes form one contiguous run once its size is known).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "../../include/raymond.h"
+
+namespace {
+
+constexpr int BINS = 32;
+const double kInf = std::numeric_limits<double>::infinity();
+
+struct BuildNode {
+    double min[3], max[3];
+    uint32_t first, count;  // count 0: inner, first = left child (local index while building a subtree)
+};
+
+struct Input {
+    const double* mins;
+    const double* maxs;
+    std::vector<double> cx, cy, cz;  // centroids
+    uint32_t max_leaf;
+    uint32_t* order;
+};
+
+inline double area3(const double* mn, const double* mx) {
+    const double dx = mx[0] - mn[0];
+    const double dy = mx[1] - mn[1];
+    const double dz = mx[2] - mn[2];
+    if (!(dx >= 0.0 && dy >= 0.0 && dz >= 0.0)) return 0.0;
+    return dx * dy + dy * dz + dz * dx;
+}
+
+void bounds_of(const Input& in, uint32_t first, uint32_t n, BuildNode& node) {
+    for (int a = 0; a < 3; ++a) {
+        node.min[a] = kInf;
+        node.max[a] = -kInf;
+    }
+    for (uint32_t i = first; i < first + n; ++i) {
+        const size_t p = size_t(in.order[i]) * 3;
+        for (int a = 0; a < 3; ++a) {
+            const double lo = in.mins[p + a], hi = in.maxs[p + a];
+            if (lo < node.min[a]) node.min[a] = lo;
+            if (hi > node.max[a]) node.max[a] = hi;
+        }
+    }
+    node.first = first;
+    node.count = n;
+}
+
+// The split decision for one node: returns false for "keep as a leaf", else
+// the partition point in the order array.
+bool split_node(const Input& in, const BuildNode& node, uint32_t& mid_out) {
+    const uint32_t first = node.first, n = node.count;
+    const double* cs[3] = {in.cx.data(), in.cy.data(), in.cz.data()};
+    double cmin[3] = {kInf, kInf, kInf}, cmax[3] = {-kInf, -kInf, -kInf};
+    for (uint32_t i = first; i < first + n; ++i) {
+        const uint32_t p = in.order[i];
+        for (int a = 0; a < 3; ++a) {
+            const double c = cs[a][p];
+            if (c < cmin[a]) cmin[a] = c;
+            if (c > cmax[a]) cmax[a] = c;
+        }
+    }
+    double scale[3];
+    bool live[3];
+    for (int a = 0; a < 3; ++a) {
+        const double extent = cmax[a] - cmin[a];
+        live[a] = extent > 0.0;
+        scale[a] = live[a] ? double(BINS) / extent : 0.0;
+    }
+
+    double bmin[3][BINS][3], bmax[3][BINS][3];
+    uint32_t bcount[3][BINS];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < BINS; ++b) {
+            bcount[a][b] = 0;
+            for (int k = 0; k < 3; ++k) {
+                bmin[a][b][k] = kInf;
+                bmax[a][b][k] = -kInf;
+            }
+        }
+    // One pass bins every live axis.
+    for (uint32_t i = first; i < first + n; ++i) {
+        const uint32_t p = in.order[i];
+        const double* lo = in.mins + size_t(p) * 3;
+        const double* hi = in.maxs + size_t(p) * 3;
+        for (int a = 0; a < 3; ++a) {
+            if (!live[a]) continue;
+            const double f = std::floor((cs[a][p] - cmin[a]) * scale[a]);
+            const int b = f < double(BINS - 1) ? int(f) : BINS - 1;
+            bcount[a][b]++;
+            for (int k = 0; k < 3; ++k) {
+                if (lo[k] < bmin[a][b][k]) bmin[a][b][k] = lo[k];
+                if (hi[k] > bmax[a][b][k]) bmax[a][b][k] = hi[k];
+            }
+        }
+    }
+
+    double best_cost = kInf, best_split = 0.0;
+    int best_axis = -1;
+    for (int a = 0; a < 3; ++a) {
+        if (!live[a]) continue;
+        double right_area[BINS];
+        uint32_t right_count[BINS];
+        double rmn[3] = {kInf, kInf, kInf}, rmx[3] = {-kInf, -kInf, -kInf};
+        uint32_t total = 0;
+        for (int b = BINS - 1; b > 0; --b) {
+            if (bcount[a][b]) {
+                for (int k = 0; k < 3; ++k) {
+                    rmn[k] = std::min(rmn[k], bmin[a][b][k]);
+                    rmx[k] = std::max(rmx[k], bmax[a][b][k]);
+                }
+            }
+            total += bcount[a][b];
+            right_area[b] = area3(rmn, rmx);
+            right_count[b] = total;
+        }
+        double lmn[3] = {kInf, kInf, kInf}, lmx[3] = {-kInf, -kInf, -kInf};
+        uint32_t left_count = 0;
+        for (int b = 1; b < BINS; ++b) {
+            if (bcount[a][b - 1]) {
+                for (int k = 0; k < 3; ++k) {
+                    lmn[k] = std::min(lmn[k], bmin[a][b - 1][k]);
+                    lmx[k] = std::max(lmx[k], bmax[a][b - 1][k]);
+                }
+            }
+            left_count += bcount[a][b - 1];
+            if (left_count == 0 || right_count[b] == 0) continue;
+            const double cost = double(left_count) * area3(lmn, lmx) + double(right_count[b]) * right_area[b];
+            if (cost < best_cost) {
+                best_cost = cost;
+                best_axis = a;
+                best_split = cmin[a] + double(b) / scale[a];
+            }
+        }
+    }
+
+    const double parent_area = area3(node.min, node.max);
+    const double leaf_cost = double(n) * parent_area;
+    if (best_axis < 0) {
+        if (n <= in.max_leaf) return false;
+        mid_out = first + (n >> 1);
+        return true;
+    }
+    if (n <= in.max_leaf && best_cost + parent_area >= leaf_cost) return false;
+    const double* c = cs[best_axis];
+    int64_t i = first, j = int64_t(first) + n - 1;
+    while (i <= j) {
+        if (c[in.order[i]] < best_split) {
+            ++i;
+        } else {
+            std::swap(in.order[i], in.order[j]);
+            --j;
+        }
+    }
+    int64_t mid = i;
+    if (mid == first || mid == int64_t(first) + n) mid = int64_t(first) + (n >> 1);
+    mid_out = uint32_t(mid);
+    return true;
+}
+
+// Builds the subtree under `root` (already bounded) into a private list
+// whose entry 0 is the root; the list's numbering is the reference's
+// right-first depth-first order, relative to the root.
+void build_subtree(const Input& in, const BuildNode& root, std::vector<BuildNode>& out) {
+    out.clear();
+    out.push_back(root);
+    std::vector<uint32_t> stack;
+    if (root.count > in.max_leaf || root.count > 1) stack.push_back(0);
+    while (!stack.empty()) {
+        const uint32_t idx = stack.back();
+        stack.pop_back();
+        uint32_t mid;
+        const BuildNode node = out[idx];
+        if (!split_node(in, node, mid)) continue;
+        BuildNode l, r;
+        bounds_of(in, node.first, mid - node.first, l);
+        bounds_of(in, mid, node.first + node.count - mid, r);
+        const uint32_t li = uint32_t(out.size());
+        out.push_back(l);
+        out.push_back(r);
+        out[idx].first = li;
+        out[idx].count = 0;
+        if (l.count > 1) stack.push_back(li);
+        if (r.count > 1) stack.push_back(li + 1);
+    }
+}
+
+void write_node(uint8_t* dst, const BuildNode& n, uint32_t first, uint32_t count) {
+    float f[8];
+    for (int a = 0; a < 3; ++a) {
+        f[a] = float(n.min[a]);
+        f[4 + a] = float(n.max[a]);
+    }
+    uint32_t u[8];
+    std::memcpy(u, f, sizeof f);
+    u[3] = first;
+    u[7] = count;
+    std::memcpy(dst, u, 32);
+}
+
+}  // namespace
+
+extern "C" uint32_t raymond_bvh_build(const double* mins, const double* maxs, uint32_t count, uint32_t max_leaf,
+                                      void* nodes_out, uint32_t* order_out, int threads) {
+    if (!nodes_out || !order_out || max_leaf == 0 || (count > 0 && (!mins || !maxs))) return 0;
+    uint8_t* out = static_cast<uint8_t*>(nodes_out);
+    for (uint32_t i = 0; i < count; ++i) order_out[i] = i;
+    if (count == 0) {
+        std::memset(out, 0, 32);
+        return 1;
+    }
+    Input in;
+    in.mins = mins;
+    in.maxs = maxs;
+    in.max_leaf = max_leaf;
+    in.order = order_out;
+    in.cx.resize(count);
+    in.cy.resize(count);
+    in.cz.resize(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        in.cx[i] = (mins[size_t(i) * 3] + maxs[size_t(i) * 3]) * 0.5;
+        in.cy[i] = (mins[size_t(i) * 3 + 1] + maxs[size_t(i) * 3 + 1]) * 0.5;
+        in.cz[i] = (mins[size_t(i) * 3 + 2] + maxs[size_t(i) * 3 + 2]) * 0.5;
+    }
+
+    BuildNode root;
+    bounds_of(in, 0, count, root);
+    if (count <= max_leaf) {
+        write_node(out, root, 0, root.count);
+        return 1;
+    }
+
+    // Top levels sequentially, in the reference's order, until there are
+    // enough frontier subtrees to spread over the threads.
+    if (threads < 1) threads = 1;
+    const uint32_t want = threads > 1 ? uint32_t(threads) * 8u : 1u;
+    // The top tree: nodes whose split happened here; frontier entries are
+    // nodes left to split (with count > 1), built later as subtrees.
+    struct Top {
+        BuildNode node;
+        int32_t left;      // top index of the left child, -1 if not split here
+        int32_t frontier;  // index into frontier list, -1 if none
+    };
+    std::vector<Top> top;
+    top.push_back({root, -1, -1});
+    std::vector<uint32_t> open = {0};  // top nodes still to split (count > 1)
+    const uint32_t big_enough = count / (want * 4) + 64;
+    while (!open.empty() && top.size() < 4 * want) {
+        // Split the largest open node next (it is independent of the others).
+        auto it = std::max_element(open.begin(), open.end(),
+                                   [&](uint32_t a, uint32_t b) { return top[a].node.count < top[b].node.count; });
+        const uint32_t idx = *it;
+        if (top[idx].node.count < big_enough) break;
+        open.erase(it);
+        uint32_t mid;
+        if (!split_node(in, top[idx].node, mid)) continue;
+        BuildNode l, r;
+        bounds_of(in, top[idx].node.first, mid - top[idx].node.first, l);
+        bounds_of(in, mid, top[idx].node.first + top[idx].node.count - mid, r);
+        top[idx].left = int32_t(top.size());
+        top.push_back({l, -1, -1});
+        top.push_back({r, -1, -1});
+        if (l.count > 1) open.push_back(uint32_t(top[idx].left));
+        if (r.count > 1) open.push_back(uint32_t(top[idx].left + 1));
+    }
+    // Every top node not split here becomes a subtree root.
+    std::vector<uint32_t> frontier;
+    for (uint32_t i = 0; i < top.size(); ++i)
+        if (top[i].left < 0) {
+            top[i].frontier = int32_t(frontier.size());
+            frontier.push_back(i);
+        }
+    std::vector<std::vector<BuildNode>> subtrees(frontier.size());
+    {
+        std::atomic<uint32_t> next{0};
+        auto worker = [&] {
+            for (;;) {
+                const uint32_t k = next.fetch_add(1);
+                if (k >= frontier.size()) return;
+                build_subtree(in, top[frontier[k]].node, subtrees[k]);
+            }
+        };
+        std::vector<std::thread> pool;
+        const int nt = std::min<int>(threads, int(frontier.size()));
+        for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+        worker();
+        for (auto& t : pool) t.join();
+    }
+
+    // Total nodes under each top node (itself included).
+    std::vector<uint64_t> size(top.size(), 0);
+    for (int64_t i = int64_t(top.size()) - 1; i >= 0; --i) {
+        if (top[i].left < 0) size[i] = subtrees[top[i].frontier].size();
+        else size[i] = 1 + size[top[i].left] + size[top[i].left + 1];
+    }
+
+    // Place nodes in the reference's numbering: a split node at g has its
+    // children at c, c+1 (c = the next free index when it was split); the
+    // right child's descendants come first, then the left's.
+    uint32_t written = 0;
+    struct Item {
+        uint32_t top_index;
+        uint32_t global;
+    };
+    // Emits the subtree of a node already placed at `global`; next_free is
+    // where its descendants start.
+    std::vector<std::pair<Item, uint32_t>> work;  // (node, next_free)
+    work.push_back({{0, 0}, 1});
+    while (!work.empty()) {
+        const auto [item, next_free] = work.back();
+        work.pop_back();
+        const Top& t = top[item.top_index];
+        if (t.left < 0) {
+            // A subtree built privately: local index k maps to global via
+            // local 0 -> item.global and locals >= 1 -> next_free + k - 1.
+            const std::vector<BuildNode>& st = subtrees[t.frontier];
+            for (size_t k = 0; k < st.size(); ++k) {
+                const uint32_t g = k == 0 ? item.global : next_free + uint32_t(k) - 1;
+                const uint32_t first = st[k].count == 0 ? next_free + st[k].first - 1 : st[k].first;
+                write_node(out + size_t(g) * 32, st[k], first, st[k].count);
+                ++written;
+            }
+            continue;
+        }
+        const uint32_t c = next_free;
+        write_node(out + size_t(item.global) * 32, t.node, c, 0);
+        ++written;
+        const uint32_t li = uint32_t(t.left), ri = li + 1;
+        // Right child's descendants first (it is popped first), then the left's.
+        const uint32_t right_desc_start = c + 2;
+        const uint32_t left_desc_start = right_desc_start + uint32_t(size[ri] - 1);
+        work.push_back({{li, c}, left_desc_start});
+        work.push_back({{ri, c + 1}, right_desc_start});
+    }
+    return written;
+}

@@ -1,0 +1,210 @@
+// The à-trous denoiser (src/shaders.mjs:1916-2098) and the display tone map
+// (src/shaders.mjs:2114-2152) as sm_103a kernels on the per-pixel buffers.
+#include "kernels.cuh"
+
+namespace rmd {
+
+namespace {
+
+__device__ __forceinline__ float3 xyz4(float4 v) { return make_float3(v.x, v.y, v.z); }
+__device__ __forceinline__ float lum(float3 c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
+
+struct DenoiseView {
+    const float4* accum;
+    const float4* guide_albedo;
+    const float4* guide_normal;
+    uint32_t w, h;
+    float n;  // samples(): max(total_samples, 1)
+};
+
+__device__ __forceinline__ float3 albedo_at(const DenoiseView& v, uint32_t i) {
+    const float4 g = v.guide_albedo[i];
+    return make_float3(fmaxf(g.x / v.n, 0.01f), fmaxf(g.y / v.n, 0.01f), fmaxf(g.z / v.n, 0.01f));
+}
+__device__ __forceinline__ float4 normal_at(const DenoiseView& v, uint32_t i) {
+    const float4 g = v.guide_normal[i];
+    const float d2 = g.x * g.x + g.y * g.y + g.z * g.z;
+    float3 n = make_float3(0.0f, 0.0f, 0.0f);
+    if (d2 > 0.0f) {
+        const float l = sqrtf(d2);
+        n = make_float3(g.x / l, g.y / l, g.z / l);
+    }
+    return make_float4(n.x, n.y, n.z, g.w / v.n);
+}
+__device__ __forceinline__ float3 light_at(const DenoiseView& v, uint32_t i) {
+    const float4 a = v.accum[i];
+    const float3 al = albedo_at(v, i);
+    return make_float3(a.x / v.n / al.x, a.y / v.n / al.y, a.z / v.n / al.z);
+}
+// similarity (src/shaders.mjs:1958-1968).
+__device__ __forceinline__ float similarity(float4 p, float4 q, float step) {
+    if (p.w <= 0.0f || q.w <= 0.0f) return (p.w <= 0.0f && q.w <= 0.0f) ? 1.0f : 0.0f;
+    if (p.x * p.x + p.y * p.y + p.z * p.z == 0.0f) return 0.0f;
+    const float wn = powf(fmaxf(p.x * q.x + p.y * q.y + p.z * q.z, 0.0f), 64.0f);
+    const float wz = expf(-fabsf(p.w - q.w) / (p.w * 0.02f * step + 1e-6f));
+    return wn * wz;
+}
+
+__constant__ float c_kernel[3] = {0.375f, 0.25f, 0.0625f};
+
+// prepare (src/shaders.mjs:1974-2021).
+__global__ void k_prepare(DenoiseView v, float4* __restrict__ out) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= v.w || y >= v.h) return;
+    const uint32_t i = y * v.w + x;
+    const float n = v.n;
+    const float3 light = light_at(v, i);
+    const float4 gp = normal_at(v, i);
+    const float a = lum(albedo_at(v, i));
+    float variance;
+    if (n >= 4.0f) {
+        const float4 ac = v.accum[i];
+        const float mean = lum(xyz4(ac)) / n;
+        const float spread = fmaxf(ac.w / n - mean * mean, 0.0f) * n / (n - 1.0f);
+        variance = spread / n / (a * a);
+    } else {
+        float sum = 0.0f, sum2 = 0.0f, weight = 0.0f;
+        for (int dy = -2; dy <= 2; ++dy) {
+            for (int dx = -2; dx <= 2; ++dx) {
+                const int xx = int(x) + dx, yy = int(y) + dy;
+                if (xx < 0 || yy < 0 || xx >= int(v.w) || yy >= int(v.h)) continue;
+                const uint32_t j = uint32_t(yy) * v.w + uint32_t(xx);
+                const float w = similarity(gp, normal_at(v, j), 1.0f);
+                const float l = lum(light_at(v, j));
+                sum += w * l;
+                sum2 += w * l * l;
+                weight += w;
+            }
+        }
+        const float mean = sum / fmaxf(weight, 1e-6f);
+        variance = fmaxf(sum2 / fmaxf(weight, 1e-6f) - mean * mean, 0.0f) + 0.01f * mean * mean;
+    }
+    out[i] = make_float4(light.x, light.y, light.z, variance);
+}
+
+// atrous (src/shaders.mjs:2023-2086), one pass of the given step.
+__global__ void k_atrous(DenoiseView v, const float4* __restrict__ in, float4* __restrict__ out, int step) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= v.w || y >= v.h) return;
+    const uint32_t i = y * v.w + x;
+    const float4 centre = in[i];
+    const float4 gp = normal_at(v, i);
+    const float lp = lum(xyz4(centre));
+
+    float variance = 0.0f, variance_weight = 0.0f;
+    for (int dy = -1; dy <= 1; ++dy) {
+        for (int dx = -1; dx <= 1; ++dx) {
+            const int xx = int(x) + dx, yy = int(y) + dy;
+            if (xx >= 0 && yy >= 0 && xx < int(v.w) && yy < int(v.h)) {
+                const float w = c_kernel[dx < 0 ? -dx : dx] * c_kernel[dy < 0 ? -dy : dy];
+                variance += w * in[uint32_t(yy) * v.w + uint32_t(xx)].w;
+                variance_weight += w;
+            }
+        }
+    }
+    const float sigma = 4.0f * sqrtf(variance / variance_weight) + 1e-4f;
+
+    float3 sum = make_float3(0.0f, 0.0f, 0.0f);
+    float sum_variance = 0.0f, weight = 0.0f;
+    for (int dy = -2; dy <= 2; ++dy) {
+        for (int dx = -2; dx <= 2; ++dx) {
+            const int xx = int(x) + dx * step, yy = int(y) + dy * step;
+            if (xx < 0 || yy < 0 || xx >= int(v.w) || yy >= int(v.h)) continue;
+            const uint32_t j = uint32_t(yy) * v.w + uint32_t(xx);
+            const float4 q = in[j];
+            const float w = c_kernel[dx < 0 ? -dx : dx] * c_kernel[dy < 0 ? -dy : dy] *
+                            similarity(gp, normal_at(v, j), float(step)) * expf(-fabsf(lp - lum(xyz4(q))) / sigma);
+            sum.x += w * q.x;
+            sum.y += w * q.y;
+            sum.z += w * q.z;
+            sum_variance += w * w * q.w;
+            weight += w;
+        }
+    }
+    if (weight > 0.0f)
+        out[i] = make_float4(sum.x / weight, sum.y / weight, sum.z / weight, sum_variance / (weight * weight));
+    else
+        out[i] = centre;
+}
+
+// compose (src/shaders.mjs:2088-2097).
+__global__ void k_compose(DenoiseView v, const float4* __restrict__ in, float4* __restrict__ out) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= v.w || y >= v.h) return;
+    const uint32_t i = y * v.w + x;
+    const float3 a = albedo_at(v, i);
+    const float4 l = in[i];
+    out[i] = make_float4(l.x * a.x, l.y * a.y, l.z * a.z, 0.0f);
+}
+
+// Narkowicz's ACES fit and the sRGB OETF (src/shaders.mjs:2115-2122).
+__device__ __forceinline__ float aces1(float x) {
+    return fminf(fmaxf((x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f), 0.0f), 1.0f);
+}
+__device__ __forceinline__ float to_srgb1(float c) {
+    const float x = fminf(fmaxf(c, 0.0f), 1.0f);
+    return x <= 0.0031308f ? x * 12.92f : 1.055f * powf(x, 1.0f / 2.4f) - 0.055f;
+}
+__device__ __forceinline__ uint8_t unorm8(float v) {
+    const float c = fminf(fmaxf(v, 0.0f), 1.0f);
+    return uint8_t(__float2int_rn(c * 255.0f));
+}
+
+// fragment (src/shaders.mjs:2124-2152) into a headless RGBA8 buffer.
+__global__ void k_tonemap(Params P, const float4* __restrict__ accum, const float4* __restrict__ denoised,
+                          uchar4* __restrict__ display) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.width || y >= P.height) return;
+    const uint32_t i = y * P.width + x;
+    float3 o;
+    if (P.total_samples == 0u) {
+        o = make_float3(0.0f, 0.0f, 0.0f);
+    } else {
+        const float4 a = accum[i];
+        const float n = float(P.total_samples);
+        const float3 c = make_float3(a.x / n, a.y / n, a.z / n);
+        if (P.view == 0u) {
+            float3 shown = c;
+            if (P.denoise != 0u) shown = xyz4(denoised[i]);
+            o = make_float3(to_srgb1(aces1(shown.x * P.exposure)), to_srgb1(aces1(shown.y * P.exposure)),
+                            to_srgb1(aces1(shown.z * P.exposure)));
+        } else if (P.view == 1u) {
+            o = make_float3(to_srgb1(c.x), to_srgb1(c.y), to_srgb1(c.z));
+        } else if (P.view == 2u) {
+            o = make_float3(c.x * 0.5f + 0.5f, c.y * 0.5f + 0.5f, c.z * 0.5f + 0.5f);
+        } else {
+            const float g = c.x <= 0.0f ? 0.0f : 1.0f / (1.0f + c.x / P.focus_distance);
+            o = make_float3(g, g, g);
+        }
+    }
+    display[i] = make_uchar4(unorm8(o.x), unorm8(o.y), unorm8(o.z), 255);
+}
+
+}  // namespace
+
+int launch_denoise(const Params& P, const PixelBuffers& px, cudaStream_t st) {
+    DenoiseView v{px.accum, px.guide_albedo, px.guide_normal, P.width, P.height,
+                  float(P.total_samples > 1u ? P.total_samples : 1u)};
+    const dim3 block(16, 8), grid((P.width + 15) / 16, (P.height + 7) / 8);
+    // prepare fills light a; the passes go a→b, b→a, …; compose reads the last (src/Renderer.mjs:893-912).
+    k_prepare<<<grid, block, 0, st>>>(v, px.light_a);
+    const int steps[5] = {1, 2, 4, 8, 16};
+    float4* from = px.light_a;
+    float4* to = px.light_b;
+    for (int k = 0; k < 5; ++k) {
+        k_atrous<<<grid, block, 0, st>>>(v, from, to, steps[k]);
+        float4* t = from;
+        from = to;
+        to = t;
+    }
+    k_compose<<<grid, block, 0, st>>>(v, from, px.denoised);
+    return 7;
+}
+
+int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st) {
+    const dim3 block(16, 8), grid((P.width + 15) / 16, (P.height + 7) / 8);
+    k_tonemap<<<grid, block, 0, st>>>(P, px.accum, px.denoised, px.display);
+    return 1;
+}
+
+}  // namespace rmd

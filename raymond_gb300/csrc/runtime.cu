@@ -1,0 +1,518 @@
+// Host runtime behind include/raymond.h: device buffers in the packed
+// formats, validation of uploaded scenes, the per-handle stream, frames,
+// read-back. One handle is one renderer on one GPU.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/raymond.h"
+#include "kernels.cuh"
+
+using namespace rmd;
+
+namespace {
+
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    // Grows (never shrinks) to hold `need` bytes; contents are not kept.
+    cudaError_t reserve(size_t need) {
+        if (need <= bytes && ptr) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&ptr, need > 0 ? need : 16);
+        if (e == cudaSuccess) bytes = need > 0 ? need : 16;
+        return e;
+    }
+};
+
+}  // namespace
+
+struct raymond {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string error;
+    uint32_t seed_hash = 0;
+
+    // Scene.
+    DevBuf prims, nodes, materials, attributes, lights, emitters;
+    DevBuf textures, normal_maps, env_map, env_table;
+    uint32_t prim_slots = 0, bvh_prim_count = 0, node_count = 0, mat_count = 0, attr_vec4s = 0;
+    uint32_t light_words = 0, light_count = 0, volume_count = 0;
+    uint32_t tex_w = 1, tex_h = 1, tex_layers = 0, nrm_w = 1, nrm_h = 1, nrm_layers = 0;
+    uint32_t env_w = 1, env_h = 1, env_cw = 1, env_ch = 0;
+    uint32_t emitter_vec4s = 0;
+    bool has_scene = false;
+
+    // Per-pixel buffers.
+    DevBuf accum, guide_albedo, guide_normal, light_a, light_b, denoised, splats, display;
+    uint32_t width = 0, height = 0;
+    uint64_t capacity = 0;
+
+    // Scratch for host-pointer trace calls, and the work counter.
+    DevBuf ray_scratch, prim_scratch, t_scratch, counter;
+
+    bool rendered = false;
+    Params last_params{};
+    raymond_stats stats{};
+    // Stage boundaries of the last frame: trace, caustics, denoise, display.
+    cudaEvent_t ev[5] = {};
+    bool ev_valid = false;
+
+    int fail(int code, const char* fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        error = buf;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char* what) {
+        return fail(e == cudaErrorMemoryAllocation ? RAYMOND_ENOMEM : RAYMOND_ECUDA, "%s: %s", what,
+                    cudaGetErrorString(e));
+    }
+
+    Scene scene_view() const {
+        Scene s{};
+        s.prims = static_cast<const float4*>(prims.ptr);
+        s.nodes = static_cast<const float4*>(nodes.ptr);
+        s.materials = static_cast<const float4*>(materials.ptr);
+        s.attributes = static_cast<const float4*>(attributes.ptr);
+        s.lights = static_cast<const uint32_t*>(lights.ptr);
+        s.emitters = static_cast<const float4*>(emitters.ptr);
+        s.textures = static_cast<const uchar4*>(textures.ptr);
+        s.normal_maps = static_cast<const uchar4*>(normal_maps.ptr);
+        s.tex_w = tex_w;
+        s.tex_h = tex_h;
+        s.tex_layers = tex_layers;
+        s.nrm_w = nrm_w;
+        s.nrm_h = nrm_h;
+        s.nrm_layers = nrm_layers;
+        s.env_map = static_cast<const ushort4*>(env_map.ptr);
+        s.env_table = static_cast<const float*>(env_table.ptr);
+        s.env_w = env_w;
+        s.env_h = env_h;
+        s.env_cw = env_cw;
+        s.env_ch = env_ch;
+        s.prim_count = bvh_prim_count;
+        s.seed_hash = seed_hash;
+        return s;
+    }
+    PixelBuffers pixel_view() const {
+        PixelBuffers p{};
+        p.accum = static_cast<float4*>(accum.ptr);
+        p.guide_albedo = static_cast<float4*>(guide_albedo.ptr);
+        p.guide_normal = static_cast<float4*>(guide_normal.ptr);
+        p.light_a = static_cast<float4*>(light_a.ptr);
+        p.light_b = static_cast<float4*>(light_b.ptr);
+        p.denoised = static_cast<float4*>(denoised.ptr);
+        p.splats = static_cast<uint32_t*>(splats.ptr);
+        p.display = static_cast<uchar4*>(display.ptr);
+        return p;
+    }
+};
+
+namespace {
+
+int upload(raymond* h, DevBuf& buf, const void* src, size_t bytes, const char* what) {
+    cudaError_t e = buf.reserve(bytes);
+    if (e != cudaSuccess) return h->cuda_fail(e, what);
+    if (bytes > 0) {
+        e = cudaMemcpyAsync(buf.ptr, src, bytes, cudaMemcpyHostToDevice, h->stream);
+        if (e != cudaSuccess) return h->cuda_fail(e, what);
+    }
+    return RAYMOND_OK;
+}
+
+thread_local std::string g_create_error;
+
+}  // namespace
+
+extern "C" {
+
+int raymond_create(raymond_t** out, const raymond_config* cfg) {
+    if (!out) return RAYMOND_EINVAL;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        g_create_error = std::string("No CUDA device: ") + cudaGetErrorString(e);
+        return RAYMOND_ECUDA;
+    }
+    const int dev = cfg ? cfg->device : 0;
+    if (dev < 0 || dev >= count) {
+        g_create_error = "No such CUDA device.";
+        return RAYMOND_EINVAL;
+    }
+    e = cudaSetDevice(dev);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("cudaSetDevice: ") + cudaGetErrorString(e);
+        return RAYMOND_ECUDA;
+    }
+    raymond* h = new (std::nothrow) raymond();
+    if (!h) return RAYMOND_ENOMEM;
+    h->device = dev;
+    cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    h->seed_hash = (cfg && cfg->seed) ? pcg(cfg->seed) : 0u;
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+        delete h;
+        return RAYMOND_ECUDA;
+    }
+    for (cudaEvent_t& ev : h->ev) cudaEventCreate(&ev);
+    e = h->counter.reserve(64);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        cudaStreamDestroy(h->stream);
+        delete h;
+        return RAYMOND_ENOMEM;
+    }
+    upload_srgb_table();
+    *out = h;
+    return RAYMOND_OK;
+}
+
+void raymond_destroy(raymond_t* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    for (DevBuf* b : {&h->prims, &h->nodes, &h->materials, &h->attributes, &h->lights, &h->emitters, &h->textures,
+                      &h->normal_maps, &h->env_map, &h->env_table, &h->accum, &h->guide_albedo, &h->guide_normal,
+                      &h->light_a, &h->light_b, &h->denoised, &h->splats, &h->display, &h->ray_scratch,
+                      &h->prim_scratch, &h->t_scratch, &h->counter})
+        b->release();
+    for (cudaEvent_t ev : h->ev)
+        if (ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+const char* raymond_last_error(raymond_t* h) { return h ? h->error.c_str() : g_create_error.c_str(); }
+
+int raymond_upload_scene(raymond_t* h, const void* prims, uint32_t prim_slots, uint32_t bvh_prim_count,
+                         const void* nodes, uint32_t node_count, const void* materials, uint32_t mat_count,
+                         const float* attributes, uint32_t attr_vec4s, const uint32_t* lights, uint32_t words,
+                         uint32_t light_count, uint32_t volume_count) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!prims || !nodes || !materials || prim_slots == 0 || node_count == 0 || mat_count == 0)
+        return h->fail(RAYMOND_EINVAL, "The scene needs primitives, nodes and materials.");
+    if (bvh_prim_count > prim_slots || prim_slots - (bvh_prim_count > 0 ? bvh_prim_count : 1) < volume_count)
+        return h->fail(RAYMOND_EINVAL, "Primitive counts don't add up.");
+    if (uint64_t(light_count) * 2 + volume_count > words || (words > 0 && !lights))
+        return h->fail(RAYMOND_EINVAL, "The lights list is too short.");
+    if (attr_vec4s > 0 && !attributes) return h->fail(RAYMOND_EINVAL, "Missing attributes.");
+
+    // Validate every index the kernels follow, so no kernel reads out of
+    // bounds or loops: children come after their parent, leaves lie within
+    // the BVH's primitives.
+    const uint32_t leaf_limit = bvh_prim_count > 0 ? bvh_prim_count : 1;
+    const uint32_t* nu = static_cast<const uint32_t*>(nodes);
+    for (uint32_t i = 0; i < node_count; ++i) {
+        const uint32_t first = nu[size_t(i) * 8 + 3], count = nu[size_t(i) * 8 + 7];
+        if (count > 0) {
+            if (uint64_t(first) + count > leaf_limit)
+                return h->fail(RAYMOND_EINVAL, "Node %u's leaf runs past the primitives.", i);
+        } else if (first <= i || uint64_t(first) + 1 >= node_count) {
+            return h->fail(RAYMOND_EINVAL, "Node %u's children are out of range.", i);
+        }
+    }
+    const uint32_t* pu = static_cast<const uint32_t*>(prims);
+    for (uint32_t i = 0; i < prim_slots; ++i) {
+        const uint32_t kind = pu[size_t(i) * 16], mat = pu[size_t(i) * 16 + 1], attr = pu[size_t(i) * 16 + 3];
+        if (kind == NONE) continue;
+        if (kind > TRIANGLE) return h->fail(RAYMOND_EINVAL, "Primitive %u has an unknown kind %u.", i, kind);
+        if (mat >= mat_count) return h->fail(RAYMOND_EINVAL, "Primitive %u's material is out of range.", i);
+        if (attr != NONE && uint64_t(attr) + 4 > attr_vec4s)
+            return h->fail(RAYMOND_EINVAL, "Primitive %u's attributes are out of range.", i);
+        const uint32_t light = pu[size_t(i) * 16 + 2];
+        if (light != NONE && light >= light_count)
+            return h->fail(RAYMOND_EINVAL, "Primitive %u's light index is out of range.", i);
+    }
+    for (uint32_t k = 0; k < light_count + volume_count; ++k) {
+        if (lights[k] >= prim_slots) return h->fail(RAYMOND_EINVAL, "Light or volume %u is out of range.", k);
+        const uint32_t kind = pu[size_t(lights[k]) * 16];
+        if (kind != SPHERE && kind != QUAD && !(k >= light_count && kind == BOX))
+            return h->fail(RAYMOND_EINVAL, "Light or volume %u has the wrong kind.", k);
+    }
+
+    cudaSetDevice(h->device);
+    int rc;
+    if ((rc = upload(h, h->prims, prims, size_t(prim_slots) * 64, "primitives"))) return rc;
+    if ((rc = upload(h, h->nodes, nodes, size_t(node_count) * 32, "nodes"))) return rc;
+    if ((rc = upload(h, h->materials, materials, size_t(mat_count) * 96, "materials"))) return rc;
+    const float zero4[4] = {0, 0, 0, 0};
+    if ((rc = upload(h, h->attributes, attr_vec4s ? (const void*)attributes : (const void*)zero4,
+                     size_t(attr_vec4s ? attr_vec4s : 1) * 16, "attributes")))
+        return rc;
+    const uint32_t none = NONE;
+    if ((rc = upload(h, h->lights, words ? (const void*)lights : (const void*)&none, size_t(words ? words : 1) * 4,
+                     "lights")))
+        return rc;
+    // Stand-ins for unbound textures and environment, as the reference binds 1×1 ones.
+    if (!h->textures.ptr) {
+        const uint8_t white[4] = {255, 255, 255, 255};
+        if ((rc = upload(h, h->textures, white, 4, "textures"))) return rc;
+        if ((rc = upload(h, h->normal_maps, white, 4, "normal maps"))) return rc;
+    }
+    if (!h->env_map.ptr) {
+        const uint16_t black[4] = {0, 0, 0, 0x3c00};
+        const float t[1] = {0.0f};
+        if ((rc = upload(h, h->env_map, black, 8, "environment"))) return rc;
+        if ((rc = upload(h, h->env_table, t, 4, "environment table"))) return rc;
+    }
+    if (!h->emitters.ptr) {
+        const float e[4] = {0, 0, 0, 0};
+        if ((rc = upload(h, h->emitters, e, 16, "emitters"))) return rc;
+    }
+    h->prim_slots = prim_slots;
+    h->bvh_prim_count = bvh_prim_count;
+    h->node_count = node_count;
+    h->mat_count = mat_count;
+    h->attr_vec4s = attr_vec4s;
+    h->light_words = words;
+    h->light_count = light_count;
+    h->volume_count = volume_count;
+    h->has_scene = true;
+    h->rendered = false;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "upload");
+    return RAYMOND_OK;
+}
+
+int raymond_upload_textures(raymond_t* h, int which, const uint8_t* rgba, uint32_t w, uint32_t hgt,
+                            uint32_t layers) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!rgba || w == 0 || hgt == 0 || layers == 0 || (which != 0 && which != 1))
+        return h->fail(RAYMOND_EINVAL, "Textures need a size, layers and data.");
+    cudaSetDevice(h->device);
+    DevBuf& buf = which == 0 ? h->textures : h->normal_maps;
+    int rc = upload(h, buf, rgba, size_t(w) * hgt * layers * 4, "textures");
+    if (rc) return rc;
+    if (which == 0) {
+        h->tex_w = w;
+        h->tex_h = hgt;
+        h->tex_layers = layers;
+    } else {
+        h->nrm_w = w;
+        h->nrm_h = hgt;
+        h->nrm_layers = layers;
+    }
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "textures");
+}
+
+int raymond_upload_environment(raymond_t* h, const uint16_t* rgba16f, uint32_t w, uint32_t hgt, const float* table,
+                               uint32_t cw, uint32_t ch_plus_1) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!rgba16f || !table || w == 0 || hgt == 0 || cw == 0 || ch_plus_1 == 0)
+        return h->fail(RAYMOND_EINVAL, "The environment needs a map and a table.");
+    cudaSetDevice(h->device);
+    int rc = upload(h, h->env_map, rgba16f, size_t(w) * hgt * 8, "environment");
+    if (rc) return rc;
+    rc = upload(h, h->env_table, table, size_t(cw) * ch_plus_1 * 4, "environment table");
+    if (rc) return rc;
+    h->env_w = w;
+    h->env_h = hgt;
+    h->env_cw = cw;
+    h->env_ch = ch_plus_1 - 1;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "environment");
+}
+
+int raymond_set_emitters(raymond_t* h, const float* data, uint32_t vec4_count) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!data || vec4_count == 0) return h->fail(RAYMOND_EINVAL, "Emitters need data.");
+    cudaSetDevice(h->device);
+    int rc = upload(h, h->emitters, data, size_t(vec4_count) * 16, "emitters");
+    if (rc) return rc;
+    h->emitter_vec4s = vec4_count;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "emitters");
+}
+
+int raymond_resize(raymond_t* h, uint32_t w, uint32_t hgt) {
+    if (!h) return RAYMOND_EINVAL;
+    if (w == 0 || hgt == 0) return h->fail(RAYMOND_EINVAL, "The image needs at least one pixel.");
+    cudaSetDevice(h->device);
+    const uint64_t px = uint64_t(w) * hgt;
+    if (px > h->capacity) {
+        // Buffers kept while big enough (src/Renderer.mjs:766-778).
+        for (DevBuf* b : {&h->accum, &h->guide_albedo, &h->guide_normal, &h->light_a, &h->light_b, &h->denoised,
+                          &h->splats}) {
+            cudaError_t e = b->reserve(px * 16);
+            if (e != cudaSuccess) return h->cuda_fail(e, "pixel buffers");
+        }
+        cudaError_t e = h->display.reserve(px * 4);
+        if (e != cudaSuccess) return h->cuda_fail(e, "display buffer");
+        cudaMemsetAsync(h->splats.ptr, 0, px * 16, h->stream);
+        h->capacity = px;
+    }
+    h->width = w;
+    h->height = hgt;
+    h->rendered = false;
+    return RAYMOND_OK;
+}
+
+int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint32_t flags) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!params208) return h->fail(RAYMOND_EINVAL, "No parameters.");
+    if (!h->has_scene) return h->fail(RAYMOND_ESTATE, "No scene has been uploaded.");
+    Params P;
+    std::memcpy(&P, params208, sizeof P);
+    if (P.width != h->width || P.height != h->height || h->capacity == 0)
+        return h->fail(RAYMOND_ESTATE, "Resize to %ux%u before rendering at that size.", P.width, P.height);
+    if (P.light_count != h->light_count || P.volume_count != h->volume_count)
+        return h->fail(RAYMOND_EINVAL, "The parameters' light and volume counts don't match the scene.");
+    if (P.samples_per_frame == 0 || P.max_bounces > 64)
+        return h->fail(RAYMOND_EINVAL, "samples_per_frame must be at least 1 and max_bounces at most 64.");
+    (void)flags;
+    cudaSetDevice(h->device);
+    const Scene s = h->scene_view();
+    const PixelBuffers px = h->pixel_view();
+    int launches = 0;
+    cudaEventRecord(h->ev[0], h->stream);
+    launches += launch_megakernel(s, P, features, px, h->num_sms, h->stream);
+    cudaEventRecord(h->ev[1], h->stream);
+    cudaEventRecord(h->ev[2], h->stream);
+    if (P.denoise != 0u) launches += launch_denoise(P, px, h->stream);
+    cudaEventRecord(h->ev[3], h->stream);
+    launches += launch_tonemap(P, px, h->stream);
+    cudaEventRecord(h->ev[4], h->stream);
+    h->ev_valid = true;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return h->cuda_fail(e, "render");
+    h->last_params = P;
+    h->rendered = true;
+    h->stats = raymond_stats{};
+    h->stats.launches = uint64_t(launches);
+    h->stats.paths = uint64_t(P.width) * P.height * P.samples_per_frame;
+    return RAYMOND_OK;
+}
+
+int raymond_sync(raymond_t* h) {
+    if (!h) return RAYMOND_EINVAL;
+    cudaSetDevice(h->device);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "sync");
+}
+
+int raymond_read_pixels(raymond_t* h, float* out_rgba, uint64_t bytes, int denoised, uint32_t samples) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!h->rendered || samples == 0) return h->fail(RAYMOND_ESTATE, "Nothing has been rendered yet.");
+    if (denoised && h->last_params.denoise == 0u)
+        return h->fail(RAYMOND_ESTATE, "Only the color view is denoised, with denoise on.");
+    const uint64_t need = uint64_t(h->width) * h->height * 16;
+    if (!out_rgba || bytes < need) return h->fail(RAYMOND_EINVAL, "The output needs %llu bytes.", (unsigned long long)need);
+    cudaSetDevice(h->device);
+    cudaError_t e = cudaMemcpyAsync(out_rgba, denoised ? h->denoised.ptr : h->accum.ptr, need, cudaMemcpyDeviceToHost,
+                                    h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "read pixels");
+    if (!denoised) {
+        const float inv = float(samples);
+        const size_t n = size_t(need / 4);
+        for (size_t i = 0; i < n; ++i) out_rgba[i] /= inv;
+    }
+    return RAYMOND_OK;
+}
+
+int raymond_read_guides(raymond_t* h, float* accum, float* guide_albedo, float* guide_normal, uint64_t bytes_each) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!h->rendered) return h->fail(RAYMOND_ESTATE, "Nothing has been rendered yet.");
+    const uint64_t need = uint64_t(h->width) * h->height * 16;
+    if (bytes_each < need) return h->fail(RAYMOND_EINVAL, "Each output needs %llu bytes.", (unsigned long long)need);
+    cudaSetDevice(h->device);
+    cudaError_t e = cudaSuccess;
+    if (accum && e == cudaSuccess) e = cudaMemcpyAsync(accum, h->accum.ptr, need, cudaMemcpyDeviceToHost, h->stream);
+    if (guide_albedo && e == cudaSuccess)
+        e = cudaMemcpyAsync(guide_albedo, h->guide_albedo.ptr, need, cudaMemcpyDeviceToHost, h->stream);
+    if (guide_normal && e == cudaSuccess)
+        e = cudaMemcpyAsync(guide_normal, h->guide_normal.ptr, need, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "read guides");
+}
+
+int raymond_read_display(raymond_t* h, uint8_t* out_rgba8, uint64_t bytes) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!h->rendered) return h->fail(RAYMOND_ESTATE, "Nothing has been rendered yet.");
+    const uint64_t need = uint64_t(h->width) * h->height * 4;
+    if (!out_rgba8 || bytes < need) return h->fail(RAYMOND_EINVAL, "The output needs %llu bytes.", (unsigned long long)need);
+    cudaSetDevice(h->device);
+    cudaError_t e = cudaMemcpyAsync(out_rgba8, h->display.ptr, need, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "read display");
+}
+
+int raymond_trace_primary_device(raymond_t* h, const float* d_rays, uint32_t n, uint32_t* d_prim, float* d_t) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!h->has_scene) return h->fail(RAYMOND_ESTATE, "No scene has been uploaded.");
+    if (n == 0) return RAYMOND_OK;
+    if (!d_rays || !d_prim || !d_t) return h->fail(RAYMOND_EINVAL, "Null buffer.");
+    cudaSetDevice(h->device);
+    const int launches = launch_trace_primary(h->scene_view(), d_rays, n, d_prim, d_t,
+                                              static_cast<uint32_t*>(h->counter.ptr), h->num_sms, h->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return h->cuda_fail(e, "trace");
+    h->stats = raymond_stats{};
+    h->stats.launches = uint64_t(launches);
+    h->stats.rays_primary = n;
+    return RAYMOND_OK;
+}
+
+int raymond_trace_primary(raymond_t* h, const float* rays, uint32_t n, uint32_t* prim, float* t) {
+    if (!h) return RAYMOND_EINVAL;
+    if (n == 0) return RAYMOND_OK;
+    if (!rays || !prim || !t) return h->fail(RAYMOND_EINVAL, "Null buffer.");
+    cudaSetDevice(h->device);
+    cudaError_t e;
+    if ((e = h->ray_scratch.reserve(size_t(n) * 24)) != cudaSuccess) return h->cuda_fail(e, "ray buffer");
+    if ((e = h->prim_scratch.reserve(size_t(n) * 4)) != cudaSuccess) return h->cuda_fail(e, "hit buffer");
+    if ((e = h->t_scratch.reserve(size_t(n) * 4)) != cudaSuccess) return h->cuda_fail(e, "hit buffer");
+    e = cudaMemcpyAsync(h->ray_scratch.ptr, rays, size_t(n) * 24, cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "ray upload");
+    int rc = raymond_trace_primary_device(h, static_cast<const float*>(h->ray_scratch.ptr), n,
+                                          static_cast<uint32_t*>(h->prim_scratch.ptr),
+                                          static_cast<float*>(h->t_scratch.ptr));
+    if (rc) return rc;
+    e = cudaMemcpyAsync(prim, h->prim_scratch.ptr, size_t(n) * 4, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t, h->t_scratch.ptr, size_t(n) * 4, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "trace read-back");
+}
+
+int raymond_get_buffers(raymond_t* h, raymond_buffers* out) {
+    if (!h || !out) return RAYMOND_EINVAL;
+    out->accum = static_cast<float*>(h->accum.ptr);
+    out->guide_albedo = static_cast<float*>(h->guide_albedo.ptr);
+    out->guide_normal = static_cast<float*>(h->guide_normal.ptr);
+    out->denoised = static_cast<float*>(h->denoised.ptr);
+    out->display = static_cast<uint8_t*>(h->display.ptr);
+    out->width = h->width;
+    out->height = h->height;
+    return RAYMOND_OK;
+}
+
+void* raymond_get_stream(raymond_t* h) { return h ? static_cast<void*>(h->stream) : nullptr; }
+
+int raymond_get_stats(raymond_t* h, raymond_stats* out) {
+    if (!h || !out) return RAYMOND_EINVAL;
+    if (h->ev_valid && cudaEventQuery(h->ev[4]) == cudaSuccess) {
+        float* ms[4] = {&h->stats.ms_trace, &h->stats.ms_caustics, &h->stats.ms_denoise, &h->stats.ms_display};
+        for (int k = 0; k < 4; ++k) cudaEventElapsedTime(ms[k], h->ev[k], h->ev[k + 1]);
+    }
+    *out = h->stats;
+    return RAYMOND_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,166 @@
+"""The reference's browser-test scenes (tests/browser/fixture.mjs:35-298)
+restated, and trace(): renders one on the GPU through the Renderer and
+returns its pixels beside what the oracle's Scene.raycast sees through each
+pixel centre (fixture.mjs:311-364)."""
+
+import math
+
+import numpy as np
+
+import oracle
+from raymond_gb300 import Box, Camera, Canvas, Mat4, Material, Mesh, Quad, Renderer, Scene, Sky, Sphere, Vec3
+
+BLACK = Vec3(0, 0, 0)
+WHITE = Vec3(1, 1, 1)
+FLOOR_ALBEDO = 0.5
+
+
+def white_sky():
+    return Sky(zenith=Vec3(1, 1, 1), horizon=Vec3(1, 1, 1), ground=Vec3(1, 1, 1))
+
+
+def floor(material=None):
+    m = material or Material.diffuse(Vec3(FLOOR_ALBEDO, FLOOR_ALBEDO, FLOOR_ALBEDO))
+    return Quad(Vec3(-20, 0, 20), Vec3(40, 0, 0), Vec3(0, 0, -40), m)
+
+
+LOOK_DOWN = dict(position=Vec3(0, 4, 4), target=Vec3(0, 0, 0), fov=math.pi / 3)
+
+MATERIALS = {
+    "diffuse": Material.diffuse(Vec3(0.7, 0.7, 0.7)),
+    "plastic": Material.plastic(Vec3(0.7, 0.2, 0.2), 0.3),
+    "metal": Material.metal(Vec3(0.9, 0.8, 0.6), 0.4),
+}
+
+
+def _mixed():
+    scene = Scene(sky=Sky.black()).add(
+        floor(),
+        Sphere(Vec3(-1.2, 0.6, 0), 0.6, Material.diffuse(Vec3(1, 0, 0))),
+        Box.fromCorners(Vec3(0.2, 0, -1.4), Vec3(1.2, 1.4, -0.4), Material.metal(Vec3(1, 1, 1), 0.2), 0.6),
+        Mesh.torus(Material.plastic(Vec3(0, 0, 1)), radius=0.5, tube=0.2, segments=32, sides=16)
+        .transformed(Mat4.translate(0.9, 0.5, 1.0).multiplyMat4(Mat4.rotateX(1.2))),
+        Mesh.icosphere(Material.glass(), 1, shading="flat")
+        .transformed(Mat4.translate(-0.3, 0.4, 1.4).multiplyMat4(Mat4.scale(0.4, 0.4, 0.4))))
+    return scene, dict(position=Vec3(1.5, 3, 4.5), target=Vec3(0, 0.4, 0), fov=math.pi / 3)
+
+
+def _furnace(material):
+    scene = Scene(sky=white_sky()).add(Sphere(Vec3(0, 0, 0), 1, material))
+    return scene, dict(position=Vec3(0, 0, 3.2), target=Vec3(0, 0, 0), fov=math.pi / 3)
+
+
+SCENES = {
+    "mixed": lambda arg=None: _mixed(),
+    "furnaceDiffuse": lambda arg=None: _furnace(Material.diffuse(Vec3(0.8, 0.8, 0.8))),
+    "furnaceGlass": lambda arg=None: _furnace(Material.glass(1.5)),
+    "furnaceDispersive": lambda arg=None: _furnace(Material.glass(1.5, WHITE, 20)),
+    "furnaceFog": lambda arg=None: _furnace(Material.volume(WHITE, 2.0, 0.5)),
+    "sphereLight": lambda arg=None: (Scene(sky=Sky.black()).add(
+        floor(), Sphere(Vec3(0.5, 1.5, -1), 0.5, Material.light(Vec3(1, 1, 1), 6.0))), LOOK_DOWN),
+    "quadLight": lambda arg=None: (Scene(sky=Sky.black()).add(
+        floor(), Quad(Vec3(-0.5, 1.5, -1.5), Vec3(1.2, 0, 0), Vec3(0, 0, 0.8), Material.light(Vec3(1, 1, 1), 6.0))),
+        LOOK_DOWN),
+    "sun": lambda arg=None: (Scene(sky=Sky(zenith=BLACK, horizon=BLACK, ground=BLACK, sunStrength=2.0,
+                                           sunDirection=Vec3(0, 1, 0), sunSize=0.05)).add(floor()), LOOK_DOWN),
+    "lightAsSphere": lambda arg: (Scene(sky=Sky.black()).add(
+        floor(MATERIALS[arg]), Sphere(Vec3(0, 1.6, -0.5), 1.0, Material.light(Vec3(1, 1, 1), 2.0))), LOOK_DOWN),
+    "lightAsMesh": lambda arg: (Scene(sky=Sky.black()).add(
+        floor(MATERIALS[arg]),
+        Mesh.icosphere(Material.light(Vec3(1, 1, 1), 2.0), 5).transformed(Mat4.translate(0, 1.6, -0.5))), LOOK_DOWN),
+    "room": lambda arg=None: (Scene(sky=Sky.black()).add(
+        floor(Material.checkered(Vec3(0.8, 0.8, 0.8), Vec3(0.15, 0.15, 0.15), 0.5)),
+        Quad(Vec3(-2, 0, -2), Vec3(4, 0, 0), Vec3(0, 3, 0), Material.diffuse(Vec3(0.7, 0.3, 0.2))),
+        Sphere(Vec3(-0.6, 0.5, -0.4), 0.5, Material.diffuse(Vec3(0.3, 0.6, 0.9))),
+        Box.fromCorners(Vec3(0.2, 0, -0.8), Vec3(1.0, 0.8, 0.0), Material.plastic(Vec3(0.9, 0.9, 0.9), 0.3), 0.4),
+        Quad(Vec3(-0.6, 2.5, -0.6), Vec3(1.2, 0, 0), Vec3(0, 0, 1.2), Material.light(Vec3(1, 1, 1), 4.0))),
+        dict(position=Vec3(0.5, 2.2, 3.2), target=Vec3(0, 0.4, -0.5), fov=math.pi / 3)),
+    "blackSmoke": lambda arg=None: (Scene(sky=white_sky()).add(
+        Sphere(Vec3(-0.7, 0, 0), 0.8, Material.volume(BLACK, 1.5)),
+        Box(Mat4.translate(0.6, 0, 0).multiplyMat4(Mat4.rotateY(0.6)).multiplyMat4(Mat4.rotateX(0.4))
+            .multiplyMat4(Mat4.scale(0.6, 0.5, 0.4)), Material.volume(BLACK, 1.5))),
+        dict(position=Vec3(0, 0, 3.2), target=Vec3(0, 0, 0), fov=math.pi / 3)),
+    "lampInFog": lambda arg: (Scene(sky=Sky.black()).add(
+        floor(),
+        Box.fromCorners(Vec3(-3, 0, -3), Vec3(3, 2.5, 2), Material.volume(Vec3(0.9, 0.9, 0.9), 0.5, 0.4)),
+        Sphere(Vec3(0, 1.4, -0.5), 0.6, Material.light(WHITE, 3.0)) if arg == "light" else
+        Mesh.icosphere(Material.light(WHITE, 3.0), 5).transformed(
+            Mat4.translate(0, 1.4, -0.5).multiplyMat4(Mat4.scale(0.6, 0.6, 0.6)))), LOOK_DOWN),
+    "stripThroughGlass": lambda arg: (Scene(sky=Sky.black()).add(
+        Quad(Vec3(-0.3, -2, -3), Vec3(0.6, 0, 0), Vec3(0, 4, 0), Material.light(WHITE, 1.0)),
+        Sphere(Vec3(0, 0, 0), 1, Material.glass(1.5, WHITE, float(arg)))),
+        dict(position=Vec3(0, 0, 3.2), target=Vec3(0, 0, 0), fov=math.pi / 3)),
+}
+
+_renderer = None
+
+
+def renderer():
+    global _renderer
+    if _renderer is None:
+        _renderer = Renderer.create(Canvas(48, 48))
+    return _renderer
+
+
+def pixel_rays(camera, size):
+    rays = np.zeros((size * size, 6), dtype=np.float32)
+    for y in range(size):
+        for x in range(size):
+            r = camera.pixelRay(x, y, size, size)
+            rays[y * size + x] = [*r["origin"].tuple(), *r["direction"].tuple()]
+    return rays
+
+
+def trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoise=False, caustics=True, seed=0):
+    """Renders scene `name` and returns pixels (size²×4), denoised (or None),
+    hits (per pixel: object index, distance, normal — or None) and rays."""
+    r = renderer()
+    r.canvas.width = size
+    r.canvas.height = size
+    scene, cam_opts = SCENES[name](arg)
+    camera = Camera(**cam_opts)
+    r.scene = scene
+    r.camera = camera
+    r.view = view
+    r.maxBounces = bounces
+    r.fireflyClamp = 0
+    r.samplesPerFrame = min(spp, 16)
+    r.denoise = denoise
+    r.caustics = caustics
+    r.reset()
+    while r.samples < spp:
+        r.render()
+    r.device.queue.onSubmittedWorkDone()
+    pixels = r.readPixels()
+    den = r.readPixels(denoised=True) if denoise else None
+    rays = pixel_rays(camera, size)
+    packed = scene.pack()
+    # Scene.raycast in double on the pixel-centre rays (the rays as doubles, not f32).
+    ref = oracle.raycast(packed, rays)
+    hits = []
+    for i in range(size * size):
+        p = int(ref["prim"][i])
+        if p == oracle.NONE:
+            hits.append(None)
+        else:
+            hits.append({"object": int(packed.objectIndex[p]), "distance": float(ref["t"][i]),
+                         "normal": ref["normal"][i], "point": rays[i, :3] + rays[i, 3:] * ref["t"][i]})
+    return {"pixels": pixels, "denoised": den, "hits": hits, "rays": rays, "samples": r.samples, "scene": scene}
+
+
+def rgb(pixels, i):
+    return pixels[i * 4:i * 4 + 3].astype(np.float64)
+
+
+def interior(hits, size, obj=None):
+    """Pixels whose centre and 4 neighbours see the same object (app.test.mjs:109-124)."""
+    keep = []
+    for y in range(1, size - 1):
+        for x in range(1, size - 1):
+            i = y * size + x
+            h = hits[i]
+            if h is None or (obj is not None and h["object"] != obj):
+                continue
+            if all(hits[j] is not None and hits[j]["object"] == h["object"] for j in (i - 1, i + 1, i - size, i + size)):
+                keep.append(i)
+    return keep

@@ -1,0 +1,99 @@
+"""Per-ray hit parity of the CUDA traversal with the oracle's Scene.raycast
+(src/Scene.mjs:202-283) on identical f32 rays: the same leaf-order
+primitive index except at grazing ties (|Δt|/t ≤ 1e-5, t in double)."""
+
+import numpy as np
+import pytest
+
+import oracle
+from fixtures import interior, renderer, rgb, trace
+from parity import classify
+from raymond_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def test_cornell_primary_rays_match_raycast(gpu):
+    scene, camera, rays = scenes.cornell_primary(256, seed=1)
+    prim, t = renderer().tracePrimary(rays, scene)
+    packed = scene.pack()
+    ref = oracle.raycast(packed, rays)
+    c = classify(packed, rays, prim, t, ref)
+    assert c["wrong"] == 0, c
+    assert c["hit_miss"] + c["silhouettes"] <= 0.005 * c["n"], c
+    assert c["same"] + c["ties"] + c["silhouettes"] + c["hit_miss"] == c["n"]
+    assert c["max_t_rel"] < 1e-4, c
+    # The GPU's own traversal restated in f32 agrees exactly on this scene.
+    t32 = oracle.trace32(packed, rays)
+    assert np.array_equal(t32["prim"], prim)
+
+
+def test_sphere_field_primary_rays_match_raycast(gpu):
+    scene, camera, info = scenes.sphere_field()
+    size = 512
+    xi = scenes.mulberry32_array(7, 2 * size * size).reshape(-1, 2)
+    ys, xs = np.meshgrid(np.arange(size), np.arange(size), indexing="ij")
+    rays = scenes.camera_rays_f32(camera, size, size, xs.reshape(-1) + xi[:, 0], ys.reshape(-1) + xi[:, 1])
+    prim, t = renderer().tracePrimary(rays, scene)
+    packed = scene.pack()
+    ref = oracle.raycast(packed, rays)
+    c = classify(packed, rays, prim, t, ref)
+    assert c["wrong"] == 0, c
+    assert c["hit_miss"] + c["silhouettes"] <= 0.005 * c["n"], c
+    assert c["max_t_rel"] < 1e-3, c
+
+
+def test_empty_and_tiny_batches(gpu):
+    scene, camera, rays = scenes.cornell_primary(4, seed=3)
+    prim, t = renderer().tracePrimary(rays[:0], scene)
+    assert prim.size == 0
+    prim, t = renderer().tracePrimary(rays[:1], scene)
+    ref = oracle.raycast(scene.pack(), rays[:1])
+    assert prim[0] == ref["prim"][0]
+    # Rays along the axes (zero direction components) and rays from inside boxes.
+    odd = np.array([[0.5, 0.5, -1.0, 0, 0, 1], [0.5, 0.5, 0.5, 1, 0, 0], [0.5, 0.5, 0.5, 0, -1, 0],
+                    [0.35, 0.15, 0.65, 0, 1, 0], [2, 2, 2, 1, 1, 1], [0.5, 2.0, 0.5, 0, -1, 0]], dtype=np.float32)
+    prim, t = renderer().tracePrimary(odd, scene)
+    ref = oracle.raycast(scene.pack(), odd)
+    c = classify(scene.pack(), odd, prim, t, ref)
+    assert c["wrong"] == 0 and c["hit_miss"] == 0, c
+
+
+def test_gpu_sees_what_cpu_raycast_sees(gpu):
+    """app.test.mjs:127-156: depth within 1e-3 relative and normal dot ≥ 0.999; ≤ 0.5% disagree."""
+    size = 64
+    depth = trace("mixed", view="depth", spp=1, size=size)
+    normal = trace("mixed", view="normal", spp=1, size=size)
+    compared = wrong = 0
+    for i in range(size * size):
+        hit = depth["hits"][i]
+        g = depth["pixels"][i * 4]
+        if hit is None:
+            wrong += g != 0
+            continue
+        compared += 1
+        if abs(g - hit["distance"]) > 1e-3 * hit["distance"] or np.dot(rgb(normal["pixels"], i), hit["normal"]) < 0.999:
+            wrong += 1
+    assert compared > size * size * 0.5
+    assert wrong <= size * size * 0.005, wrong
+
+
+def test_shrinking_and_growing_keeps_pixels_in_place(gpu):
+    """app.test.mjs:158-174."""
+    for size in (56, 24, 40, 56):
+        d = trace("mixed", view="depth", spp=1, size=size)
+        wrong = 0
+        for i in range(size * size):
+            hit, g = d["hits"][i], d["pixels"][i * 4]
+            wrong += (abs(g - hit["distance"]) > 1e-3 * hit["distance"]) if hit else (g != 0)
+        assert wrong <= size * size * 0.01, (size, wrong)
+
+
+def test_albedo_view(gpu):
+    """app.test.mjs:176-186."""
+    size = 48
+    r = trace("mixed", view="albedo", spp=1, size=size)
+    for i in interior(r["hits"], size, 1):
+        assert np.allclose(np.round(rgb(r["pixels"], i), 3), [1, 0, 0])
+    for i in interior(r["hits"], size, 0):
+        assert np.allclose(np.round(rgb(r["pixels"], i), 3), [0.5, 0.5, 0.5])
