@@ -63,7 +63,8 @@ int raymond_create(raymond_t** out, const raymond_config* cfg);
 /* Renderer.dispose (src/Renderer.mjs:531-547). */
 void raymond_destroy(raymond_t* h);
 
-/* The message of the handle's last failure ("" if none). h may be NULL for create errors. */
+/* The message of the handle's last failure ("" if none). With h NULL: the last
+ * failure on this thread of a call that has no handle (create, denoise_static). */
 const char* raymond_last_error(raymond_t* h);
 
 /*
@@ -178,6 +179,28 @@ typedef struct raymond_stats {
     float ms_trace, ms_caustics, ms_denoise, ms_display;
 } raymond_stats;
 int raymond_get_stats(raymond_t* h, raymond_stats* out);
+
+/*
+ * The à-trous denoiser (prepare, five passes, compose) on caller-owned device
+ * buffers, allocating nothing. It has no counterpart in the reference: it is
+ * for callers that cannot allocate device memory once they are running — a
+ * host that hands this library a fixed memory budget up front, or a frame
+ * loop that must not take cudaMalloc's device-wide synchronization — and so
+ * cannot give a renderer its intermediate buffers. accum, guide_albedo and
+ * guide_normal are w × h float4 device arrays as a renderer accumulates them
+ * (raymond_get_buffers); out receives w × h float4; total_samples is the
+ * frame's sample count; stream is a cudaStream_t (NULL: the default stream);
+ * the kernels are only enqueued. The two intermediate light buffers live in
+ * one static device array sized for RAYMOND_DENOISE_STATIC_MAX_PIXELS pixels
+ * (8 MiB, held by every GPU that loads the library until exit); larger
+ * images return RAYMOND_ECAPACITY. The first call on a device resolves the
+ * array's address on that device (cudaGetSymbolAddress), so make it before
+ * any stream capture. Calls share the array: calls that overlap on the GPU
+ * race. Errors: raymond_last_error(NULL).
+ */
+#define RAYMOND_DENOISE_STATIC_MAX_PIXELS (512u * 512u)
+int raymond_denoise_static(const float* accum, const float* guide_albedo, const float* guide_normal, uint32_t width,
+                           uint32_t height, uint32_t total_samples, float* out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -64,6 +64,7 @@ SIGNATURES = {
     "raymond_get_buffers": (_I, [_P, ctypes.POINTER(Buffers)]),
     "raymond_get_stats": (_I, [_P, ctypes.POINTER(Stats)]),
     "raymond_get_stream": (_P, [_P]),
+    "raymond_denoise_static": (_I, [_P, _P, _P, _U32, _U32, _U32, _P, _P]),
 }
 
 _lib = None

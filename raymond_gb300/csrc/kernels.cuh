@@ -27,5 +27,7 @@ int launch_megakernel(const Scene& s, const Params& P, uint32_t features, const 
 int launch_denoise(const Params& P, const PixelBuffers& px, cudaStream_t st);
 int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st);
 void upload_srgb_table();
+// The message raymond_last_error(NULL) returns, for calls that have no handle.
+void set_handleless_error(const char* msg);
 
 }  // namespace rmd

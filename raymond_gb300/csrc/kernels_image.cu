@@ -2,6 +2,10 @@
 // (src/shaders.mjs:2114-2152) as sm_103a kernels on the per-pixel buffers.
 #include "kernels.cuh"
 
+#include <mutex>
+
+#include "../../include/raymond.h"
+
 namespace rmd {
 
 namespace {
@@ -205,6 +209,88 @@ int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st) {
     const dim3 block(16, 8), grid((P.width + 15) / 16, (P.height + 7) / 8);
     k_tonemap<<<grid, block, 0, st>>>(P, px.accum, px.denoised, px.display);
     return 1;
+}
+
+
+// ---- Denoising into a caller's buffers without allocating ----
+//
+// raymond_denoise_static runs the same prepare / à-trous / compose kernels
+// as a renderer's frame, but keeps the two intermediate light buffers in
+// this fixed file-scope device array instead of memory the renderer
+// allocates. Every GPU that loads the library holds the array until exit.
+// All calls share it: two calls whose kernels overlap on the GPU (different
+// streams, no ordering between them) race on it. Nothing in it needs to
+// start at zero: prepare writes every pixel of the first buffer and each
+// pass writes every pixel of the buffer it produces before anything reads
+// it, so the previous call's contents are never seen.
+namespace {
+
+constexpr uint32_t kStaticDenoiseMaxPixels = RAYMOND_DENOISE_STATIC_MAX_PIXELS;
+static __device__ __align__(256) float4 g_denoise_scratch[2 * kStaticDenoiseMaxPixels];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+float4* g_scratch_address[kMaxDevices] = {};
+
+}  // namespace
+
+extern "C" int raymond_denoise_static(const float* accum, const float* guide_albedo, const float* guide_normal,
+                                      uint32_t width, uint32_t height, uint32_t total_samples, float* out,
+                                      void* stream) {
+    if (!accum || !guide_albedo || !guide_normal || !out || width == 0 || height == 0) {
+        set_handleless_error("raymond_denoise_static: null buffer or empty image.");
+        return RAYMOND_EINVAL;
+    }
+    if (uint64_t(width) * height > kStaticDenoiseMaxPixels) {
+        set_handleless_error("raymond_denoise_static: the image has more pixels than the static scratch holds "
+                             "(RAYMOND_DENOISE_STATIC_MAX_PIXELS).");
+        return RAYMOND_ECAPACITY;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        set_handleless_error("raymond_denoise_static: no current CUDA device.");
+        return RAYMOND_ECUDA;
+    }
+    float4* scratch;
+    {
+        // First call on this device: resolve the array's device address
+        // (the host-side symbol is only a stand-in for it).
+        std::lock_guard<std::mutex> lock(g_scratch_mutex);
+        if (!g_scratch_address[dev]) {
+            void* addr = nullptr;
+            e = cudaGetSymbolAddress(&addr, g_denoise_scratch);
+            if (e != cudaSuccess || !addr) {
+                set_handleless_error("raymond_denoise_static: cudaGetSymbolAddress failed.");
+                return RAYMOND_ECUDA;
+            }
+            g_scratch_address[dev] = static_cast<float4*>(addr);
+        }
+        scratch = g_scratch_address[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const uint32_t pixels = width * height;
+    DenoiseView v{reinterpret_cast<const float4*>(accum), reinterpret_cast<const float4*>(guide_albedo),
+                  reinterpret_cast<const float4*>(guide_normal), width, height,
+                  float(total_samples > 1u ? total_samples : 1u)};
+    const dim3 block(16, 8), grid((width + 15) / 16, (height + 7) / 8);
+    float4* from = scratch;
+    float4* to = scratch + pixels;
+    k_prepare<<<grid, block, 0, st>>>(v, from);
+    const int steps[5] = {1, 2, 4, 8, 16};
+    for (int k = 0; k < 5; ++k) {
+        k_atrous<<<grid, block, 0, st>>>(v, from, to, steps[k]);
+        float4* t = from;
+        from = to;
+        to = t;
+    }
+    k_compose<<<grid, block, 0, st>>>(v, from, reinterpret_cast<float4*>(out));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_handleless_error("raymond_denoise_static: kernel launch failed.");
+        return RAYMOND_ECUDA;
+    }
+    return RAYMOND_OK;
 }
 
 }  // namespace rmd

@@ -138,6 +138,8 @@ thread_local std::string g_create_error;
 
 }  // namespace
 
+void rmd::set_handleless_error(const char* msg) { g_create_error = msg; }
+
 extern "C" {
 
 int raymond_create(raymond_t** out, const raymond_config* cfg) {
