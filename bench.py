@@ -181,6 +181,7 @@ def run_ours(args, rank, world, local):
     r.scene, r.camera = scene, camera
     r.maxBounces = args.bounces
     r.samplesPerFrame = args.spp
+    r.flags = {"auto": 0, "megakernel": _native.FLAG_MEGAKERNEL, "wavefront": _native.FLAG_WAVEFRONT}[args.path]
     lib = _native.lib()
     stream = torch.cuda.ExternalStream(lib.raymond_get_stream(r.handle), device=local)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -263,7 +264,7 @@ def run_ours(args, rank, world, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32 scene)",
             "config": {"workload": WORKLOAD, "width": args.size, "height": args.size, "spp": args.spp,
                        "bounces": args.bounces, "triangles": info["triangles"], "spheres": info["spheres"],
-                       "primitives": scene.pack().primitiveCount, "parallelism": f"replicas x{world}",
+                       "primitives": scene.pack().primitiveCount, "parallelism": f"replicas x{world}", "path": args.path,
                        "l2": "flushed between steps (512 MB write)"},
             "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": 208, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
@@ -289,6 +290,7 @@ def main():
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--bounces", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--path", default="auto", choices=["auto", "megakernel", "wavefront"])
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1 and args.impl == "ours":

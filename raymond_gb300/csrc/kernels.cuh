@@ -18,12 +18,33 @@ struct PixelBuffers {
 
 constexpr int TRACE_BLOCK = 128;
 
+// Wavefront path state in HBM: 8 float4 records per path (ray, throughput,
+// result, last point, guides, sample state), its last hit, two path queues,
+// the shadow-ray queue (3 float4 each) and the work counters.
+struct WavefrontState {
+    float4* s[8];
+    float4* hit;
+    uint32_t* queue[2];
+    float4* shadow;
+    uint32_t* counters;
+    uint64_t capacity;  // paths in flight
+};
+
+// Launch shape of the wavefront kernels (chosen by the tuner).
+struct WavefrontTuning {
+    int steps;                    // traversal steps between lane refills
+    int traversal_blocks_per_sm;  // persistent extend/shadow blocks per SM
+    int shade_blocks_per_sm;      // shade/generate/finalize blocks per SM
+};
+
 // Host-side launchers (kernels_*.cu). Each returns the number of kernel
 // launches it enqueued.
 int launch_trace_primary(const Scene& s, const float* rays, uint32_t n, uint32_t* prim, float* t,
                          uint32_t* work_counter, int num_sms, cudaStream_t st);
 int launch_megakernel(const Scene& s, const Params& P, uint32_t features, const PixelBuffers& px, int num_sms,
                       cudaStream_t st);
+int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,
+                     const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st);
 int launch_denoise(const Params& P, const PixelBuffers& px, cudaStream_t st);
 int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st);
 void upload_srgb_table();

@@ -1,0 +1,384 @@
+// The wavefront form of the render path: path state lives in HBM as
+// structure-of-arrays float4 records and each bounce runs as three kernels —
+// extend (closest hits), shade (one path_step per live path, pushing the
+// extension and shadow rays it makes onto queues) and shadow (any-hit
+// occlusion, adding the light of unoccluded shadow rays). Traversal kernels
+// are persistent: a warp's lanes each hold one ray, run a few traversal
+// steps, and lanes whose ray finished refill from the queue together
+// (__ballot_sync picks them, one atomicAdd claims their entries), so warps
+// stay full while rays of very different lengths drain. Queue pushes are
+// warp-aggregated the same way. Every kernel reads its work count from device
+// memory, so a frame's launches never wait on the host.
+#include "dev_shade.cuh"
+#include "kernels.cuh"
+
+namespace rmd {
+
+namespace {
+
+constexpr int WF_BLOCK = 128;
+constexpr uint32_t FULL = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t lanemask_lt() { return (1u << lane_id()) - 1u; }
+
+// Warp-aggregated push: the lanes with pred set get consecutive slots from
+// one atomicAdd on *counter. Call with every lane of the warp present.
+__device__ __forceinline__ uint32_t push_slot(uint32_t* counter, bool pred) {
+    const uint32_t mask = __ballot_sync(FULL, pred);
+    if (!mask) return 0;
+    const uint32_t leader = __ffs(mask) - 1u;
+    uint32_t base = 0;
+    if (lane_id() == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(FULL, base, leader);
+    return base + __popc(mask & lanemask_lt());
+}
+
+// ---- path state <-> SoA ----
+__device__ __forceinline__ void store_path(const WavefrontState& w, uint32_t p, const PathState& ps, uint32_t pixel) {
+    w.s[0][p] = make_float4(ps.o.x, ps.o.y, ps.o.z, ps.last_pdf);
+    w.s[1][p] = make_float4(ps.d.x, ps.d.y, ps.d.z, ps.travelled);
+    w.s[2][p] = make_float4(ps.throughput.x, ps.throughput.y, ps.throughput.z, ps.wavelength);
+    w.s[3][p] = make_float4(ps.result.x, ps.result.y, ps.result.z, ps.spectrum_u);
+    w.s[4][p] = make_float4(ps.last_p.x, ps.last_p.y, ps.last_p.z, __uint_as_float((ps.depth << 16) | ps.flags));
+    w.s[5][p] = make_float4(ps.g_albedo.x, ps.g_albedo.y, ps.g_albedo.z, __uint_as_float(ps.rng.dim));
+    w.s[6][p] = ps.g_normal;
+    reinterpret_cast<uint4*>(w.s[7])[p] = make_uint4(ps.rng.state, ps.rng.seed, ps.rng.index, pixel);
+}
+__device__ __forceinline__ uint32_t load_path(const WavefrontState& w, uint32_t p, PathState& ps) {
+    const float4 a = w.s[0][p], b = w.s[1][p], c = w.s[2][p], d = w.s[3][p], e = w.s[4][p], f = w.s[5][p];
+    ps.o = f3(a.x, a.y, a.z);
+    ps.last_pdf = a.w;
+    ps.d = f3(b.x, b.y, b.z);
+    ps.travelled = b.w;
+    ps.throughput = f3(c.x, c.y, c.z);
+    ps.wavelength = c.w;
+    ps.result = f3(d.x, d.y, d.z);
+    ps.spectrum_u = d.w;
+    ps.last_p = f3(e.x, e.y, e.z);
+    const uint32_t df = __float_as_uint(e.w);
+    ps.depth = df >> 16;
+    ps.flags = df & 0xffffu;
+    ps.g_albedo = f3(f.x, f.y, f.z);
+    ps.rng.dim = __float_as_uint(f.w);
+    ps.g_normal = w.s[6][p];
+    const uint4 r = reinterpret_cast<const uint4*>(w.s[7])[p];
+    ps.rng.state = r.x;
+    ps.rng.seed = r.y;
+    ps.rng.index = r.z;
+    ps.rng.qmc = true;
+    return r.w;
+}
+
+// Counters (u32) in w.counters: queue sizes [0], [1], shadow size [2], and
+// per-launch fetch counters [4..7] zeroed before each traversal launch.
+enum { C_QUEUE0 = 0, C_QUEUE1 = 1, C_SHADOW = 2, C_FETCH = 4 };
+
+// ---- generate: main()'s per-sample start for a batch of samples ----
+// first_sample counts from the frame's first sample (path_begin adds
+// sample_offset).
+template <uint32_t FEAT>
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_generate(Params P, WavefrontState w, uint32_t seed_hash,
+                                                          uint32_t first_sample, uint32_t n_paths) {
+    const uint32_t pixels = P.width * P.height;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_paths; p += gridDim.x * blockDim.x) {
+        const uint32_t pixel = p % pixels;
+        const uint32_t k = first_sample + p / pixels;
+        PathState ps;
+        path_begin(P, seed_hash, pixel % P.width, pixel / P.width, k, ps);
+        store_path(w, p, ps, pixel);
+        w.queue[0][p] = p;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        w.counters[C_QUEUE0] = n_paths;
+        w.counters[C_QUEUE1] = 0;
+        w.counters[C_SHADOW] = 0;
+    }
+}
+
+// ---- resumable traversal, for persistent lanes ----
+struct Traversal {
+    float3 o, d, inv;
+    float t, u, v;
+    uint32_t prim;
+    uint32_t first, count, sp;
+};
+
+// Starts a ray; returns false if it misses the root box (then it is done).
+__device__ __forceinline__ bool trav_begin(const Scene& s, Traversal& tr, float3 o, float3 d, float t_max) {
+    tr.o = o;
+    tr.d = d;
+    tr.inv = f3(1.0f / safe1(d.x), 1.0f / safe1(d.y), 1.0f / safe1(d.z));
+    tr.t = t_max;
+    tr.u = tr.v = 0.0f;
+    tr.prim = NONE;
+    tr.sp = 0;
+    const float4 mn = ldg4(s.nodes), mx = ldg4(s.nodes + 1);
+    if (slab_entry(mn, mx, o, tr.inv, t_max) >= INF) return false;
+    tr.first = __float_as_uint(mn.w);
+    tr.count = __float_as_uint(mx.w);
+    return true;
+}
+
+// One node visit; returns false when the ray is finished.
+template <bool ANY_HIT>
+__device__ __forceinline__ bool trav_step(const Scene& s, Traversal& tr, TraversalStack<STACK_SHARED>& st) {
+    bool have = false;
+    if (tr.count > 0) {
+        for (uint32_t i = tr.first; i < tr.first + tr.count; ++i) {
+            const float3 h = intersect_prim(s, i, tr.o, tr.d, tr.t);
+            if (h.x > 0.0f) {
+                tr.t = h.x;
+                tr.prim = i;
+                tr.u = h.y;
+                tr.v = h.z;
+                if (ANY_HIT) return false;
+            }
+        }
+    } else {
+        const float4* pair = s.nodes + size_t(tr.first) * 2;
+        const float4 lmn = ldg4(pair), lmx = ldg4(pair + 1), rmn = ldg4(pair + 2), rmx = ldg4(pair + 3);
+        const float tl = slab_entry(lmn, lmx, tr.o, tr.inv, tr.t);
+        const float trr = slab_entry(rmn, rmx, tr.o, tr.inv, tr.t);
+        const bool l_in = tl < INF, r_in = trr < INF;
+        if (l_in || r_in) {
+            const bool left_near = tl <= trr;
+            if (l_in && r_in && tr.sp < 64u) st.push(tr.sp++, left_near ? tr.first + 1 : tr.first);
+            const bool take_left = l_in && (left_near || !r_in);
+            tr.first = __float_as_uint(take_left ? lmn.w : rmn.w);
+            tr.count = __float_as_uint(take_left ? lmx.w : rmx.w);
+            have = true;
+        }
+    }
+    while (!have) {
+        if (tr.sp == 0) return false;
+        const uint32_t idx = st.at(--tr.sp);
+        const float4 mn = ldg4(s.nodes + size_t(idx) * 2), mx = ldg4(s.nodes + size_t(idx) * 2 + 1);
+        if (ANY_HIT || slab_entry(mn, mx, tr.o, tr.inv, tr.t) < INF) {
+            tr.first = __float_as_uint(mn.w);
+            tr.count = __float_as_uint(mx.w);
+            have = true;
+        }
+    }
+    return true;
+}
+
+// ---- extend: closest hits for every path in the queue ----
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Scene s, WavefrontState w, int q, int steps) {
+    __shared__ uint32_t stack[STACK_SHARED * WF_BLOCK];
+    TraversalStack<STACK_SHARED> st;
+    st.col = stack + threadIdx.x;
+    st.stride = WF_BLOCK;
+    const uint32_t* queue = w.queue[q];
+    const uint32_t n = w.counters[C_QUEUE0 + q];
+    uint32_t* fetch = w.counters + C_FETCH + 0;
+    Traversal tr;
+    uint32_t path = 0;
+    bool active = false, exhausted = false;
+    for (;;) {
+        // Lanes without a ray claim the next queue entries together.
+        const bool need = !active && !exhausted;
+        const uint32_t mask = __ballot_sync(FULL, need);
+        if (mask) {
+            const uint32_t leader = __ffs(mask) - 1u;
+            uint32_t base = 0;
+            if (lane_id() == leader) base = atomicAdd(fetch, __popc(mask));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                const uint32_t idx = base + __popc(mask & lanemask_lt());
+                if (idx < n) {
+                    path = queue[idx];
+                    const float4 a = w.s[0][path], b = w.s[1][path];
+                    active = trav_begin(s, tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), INF);
+                    if (!active) w.hit[path] = make_float4(INF, __uint_as_float(NONE), 0.0f, 0.0f);
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (!__any_sync(FULL, active || !exhausted)) return;
+        for (int k = 0; k < steps && active; ++k) {
+            if (!trav_step<false>(s, tr, st)) {
+                w.hit[path] = make_float4(tr.t, __uint_as_float(tr.prim), tr.u, tr.v);
+                active = false;
+            }
+        }
+    }
+}
+
+// ---- shade: one bounce of radiance() per live path ----
+template <uint32_t FEAT>
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_shade(Scene s, Params P, WavefrontState w, int q) {
+    const uint32_t n = w.counters[C_QUEUE0 + q];
+    const uint32_t* queue = w.queue[q];
+    uint32_t* out_queue = w.queue[q ^ 1];
+    uint32_t* out_count = w.counters + C_QUEUE0 + (q ^ 1);
+    uint32_t* shadow_count = w.counters + C_SHADOW;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // Whole warps iterate together so the pushes can aggregate.
+    const uint32_t rounds = (n + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t idx = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool more = false, has_shadow = false;
+        ShadowRay sh;
+        sh.valid = false;
+        uint32_t path = 0;
+        if (idx < n) {
+            path = queue[idx];
+            PathState ps;
+            const uint32_t pixel = load_path(w, path, ps);
+            const float4 hv = w.hit[path];
+            const Hit hit{hv.x, __float_as_uint(hv.y), hv.z, hv.w};
+            more = path_step<FEAT>(s, P, ps, hit, sh);
+            has_shadow = sh.valid;
+            store_path(w, path, ps, pixel);
+        }
+        const uint32_t slot = push_slot(out_count, more);
+        if (more) out_queue[slot] = path;
+        const uint32_t sslot = push_slot(shadow_count, has_shadow);
+        if (has_shadow) {
+            w.shadow[sslot * 3 + 0] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.reach);
+            w.shadow[sslot * 3 + 1] = make_float4(sh.d.x, sh.d.y, sh.d.z, __uint_as_float(path));
+            w.shadow[sslot * 3 + 2] = make_float4(sh.contribution.x, sh.contribution.y, sh.contribution.z, 0.0f);
+        }
+    }
+}
+
+// ---- shadow: any-hit occlusion; unoccluded rays add their light ----
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Scene s, WavefrontState w, int steps) {
+    __shared__ uint32_t stack[STACK_SHARED * WF_BLOCK];
+    TraversalStack<STACK_SHARED> st;
+    st.col = stack + threadIdx.x;
+    st.stride = WF_BLOCK;
+    const uint32_t n = w.counters[C_SHADOW];
+    uint32_t* fetch = w.counters + C_FETCH + 1;
+    Traversal tr;
+    uint32_t rec = 0;
+    bool active = false, exhausted = false;
+    for (;;) {
+        const bool need = !active && !exhausted;
+        const uint32_t mask = __ballot_sync(FULL, need);
+        if (mask) {
+            const uint32_t leader = __ffs(mask) - 1u;
+            uint32_t base = 0;
+            if (lane_id() == leader) base = atomicAdd(fetch, __popc(mask));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                const uint32_t idx = base + __popc(mask & lanemask_lt());
+                if (idx < n) {
+                    rec = idx;
+                    const float4 a = w.shadow[idx * 3], b = w.shadow[idx * 3 + 1];
+                    active = trav_begin(s, tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w);
+                    if (!active) {
+                        // Misses the scene's box: unoccluded.
+                        const uint32_t path = __float_as_uint(b.w);
+                        const float4 c = w.shadow[idx * 3 + 2];
+                        float4 r = w.s[3][path];
+                        w.s[3][path] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, r.w);
+                    }
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (!__any_sync(FULL, active || !exhausted)) return;
+        for (int k = 0; k < steps && active; ++k) {
+            if (!trav_step<true>(s, tr, st)) {
+                active = false;
+                if (tr.prim == NONE) {
+                    const uint32_t path = __float_as_uint(w.shadow[rec * 3 + 1].w);
+                    const float4 c = w.shadow[rec * 3 + 2];
+                    float4 r = w.s[3][path];
+                    w.s[3][path] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, r.w);
+                }
+            }
+        }
+    }
+}
+
+// ---- finalize: main()'s per-pixel sums for a batch of samples ----
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_finalize(Params P, WavefrontState w, PixelBuffers px,
+                                                          uint32_t batch_samples, bool overwrite) {
+    const uint32_t pixels = P.width * P.height;
+    for (uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x; pixel < pixels; pixel += gridDim.x * blockDim.x) {
+        float4 sum = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float3 sa = f3(0.0f);
+        float4 sn = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (uint32_t k = 0; k < batch_samples; ++k) {
+            const uint32_t p = k * pixels + pixel;
+            const float4 rr = w.s[3][p];
+            float3 c = f3(rr.x, rr.y, rr.z);
+            const float peak = maxc(c);
+            if (P.firefly_clamp > 0.0f && peak > P.firefly_clamp) c *= P.firefly_clamp / peak;
+            const float4 ga = w.s[5][p];
+            const float4 gn = w.s[6][p];
+            if (finite3(c) && finite3(f3(ga.x, ga.y, ga.z)) && finite3(f3(gn.x, gn.y, gn.z)) && finite1(gn.w)) {
+                const float l = luminance(c);
+                sum.x += c.x;
+                sum.y += c.y;
+                sum.z += c.z;
+                sum.w += l * l;
+                sa += f3(ga.x, ga.y, ga.z);
+                sn.x += gn.x;
+                sn.y += gn.y;
+                sn.z += gn.z;
+                sn.w += gn.w;
+            }
+        }
+        if (overwrite) {
+            px.accum[pixel] = sum;
+            px.guide_albedo[pixel] = make_float4(sa.x, sa.y, sa.z, 0.0f);
+            px.guide_normal[pixel] = sn;
+        } else {
+            const float4 a = px.accum[pixel], g = px.guide_albedo[pixel], nn = px.guide_normal[pixel];
+            px.accum[pixel] = make_float4(a.x + sum.x, a.y + sum.y, a.z + sum.z, a.w + sum.w);
+            px.guide_albedo[pixel] = make_float4(g.x + sa.x, g.y + sa.y, g.z + sa.z, g.w);
+            px.guide_normal[pixel] = make_float4(nn.x + sn.x, nn.y + sn.y, nn.z + sn.z, nn.w + sn.w);
+        }
+    }
+}
+
+template <uint32_t FEAT>
+int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, const PixelBuffers& px,
+                    const WavefrontTuning& tune, int num_sms, cudaStream_t st) {
+    const uint32_t pixels = P.width * P.height;
+    const uint32_t batch = uint32_t(w.capacity / pixels) > 0 ? uint32_t(w.capacity / pixels) : 1u;
+    const int grid_trav = num_sms * tune.traversal_blocks_per_sm;
+    const int grid_shade = num_sms * tune.shade_blocks_per_sm;
+    int launches = 0;
+    for (uint32_t k0 = 0; k0 < P.samples_per_frame; k0 += batch) {
+        const uint32_t nk = (P.samples_per_frame - k0) < batch ? (P.samples_per_frame - k0) : batch;
+        const uint32_t n = nk * pixels;
+        k_wf_generate<FEAT><<<grid_shade, WF_BLOCK, 0, st>>>(P, w, s.seed_hash, k0, n);
+        ++launches;
+        int q = 0;
+        for (uint32_t depth = 0; depth <= P.max_bounces; ++depth) {
+            cudaMemsetAsync(w.counters + C_FETCH, 0, 4 * sizeof(uint32_t), st);
+            k_wf_extend<<<grid_trav, WF_BLOCK, 0, st>>>(s, w, q, tune.steps);
+            // The next queue and the shadow queue start empty.
+            cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
+            cudaMemsetAsync(w.counters + C_SHADOW, 0, sizeof(uint32_t), st);
+            k_wf_shade<FEAT><<<grid_shade, WF_BLOCK, 0, st>>>(s, P, w, q);
+            k_wf_shadow<<<grid_trav, WF_BLOCK, 0, st>>>(s, w, tune.steps);
+            launches += 3;
+            q ^= 1;
+        }
+        k_wf_finalize<<<grid_shade, WF_BLOCK, 0, st>>>(P, w, px, nk, P.sample_offset == 0u && k0 == 0);
+        ++launches;
+    }
+    return launches;
+}
+
+}  // namespace
+
+int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,
+                     const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st) {
+    switch (features & 15u) {
+        case 0: return wavefront_frame<0>(s, P, w, px, tune, num_sms, st);
+        case F_VOLUMES: return wavefront_frame<F_VOLUMES>(s, P, w, px, tune, num_sms, st);
+        case F_DISPERSION: return wavefront_frame<F_DISPERSION>(s, P, w, px, tune, num_sms, st);
+        default: return wavefront_frame<15u>(s, P, w, px, tune, num_sms, st);
+    }
+}
+
+}  // namespace rmd

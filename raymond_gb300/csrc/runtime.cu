@@ -61,6 +61,12 @@ struct raymond {
     // Scratch for host-pointer trace calls, and the work counter.
     DevBuf ray_scratch, prim_scratch, t_scratch, counter;
 
+    // Wavefront path state (allocated on first wavefront frame).
+    DevBuf wf_state[8], wf_hit, wf_queue[2], wf_shadow, wf_counters;
+    uint64_t wf_capacity = 0;
+    uint64_t path_capacity_limit = 0;  // from the config; 0 = default
+    WavefrontTuning tuning{16, 8, 8};
+
     bool rendered = false;
     Params last_params{};
     raymond_stats stats{};
@@ -140,6 +146,41 @@ thread_local std::string g_create_error;
 
 void rmd::set_handleless_error(const char* msg) { g_create_error = msg; }
 
+namespace {
+
+// Paths in flight for a frame: the whole frame if it fits the limit, else
+// whole samples of it (at least one).
+int ensure_wavefront(raymond* h, const Params& P, WavefrontState& w) {
+    const uint64_t pixels = uint64_t(P.width) * P.height;
+    const uint64_t limit = h->path_capacity_limit ? h->path_capacity_limit : (8ull << 20);
+    uint64_t samples = limit / pixels;
+    if (samples < 1) samples = 1;
+    if (samples > P.samples_per_frame) samples = P.samples_per_frame;
+    const uint64_t cap = samples * pixels;
+    if (cap > h->wf_capacity) {
+        cudaError_t e = cudaSuccess;
+        for (DevBuf& b : h->wf_state)
+            if (e == cudaSuccess) e = b.reserve(cap * 16);
+        if (e == cudaSuccess) e = h->wf_hit.reserve(cap * 16);
+        if (e == cudaSuccess) e = h->wf_queue[0].reserve(cap * 4);
+        if (e == cudaSuccess) e = h->wf_queue[1].reserve(cap * 4);
+        if (e == cudaSuccess) e = h->wf_shadow.reserve(cap * 48);
+        if (e == cudaSuccess) e = h->wf_counters.reserve(64);
+        if (e != cudaSuccess) return h->cuda_fail(e, "wavefront state");
+        h->wf_capacity = cap;
+    }
+    for (int k = 0; k < 8; ++k) w.s[k] = static_cast<float4*>(h->wf_state[k].ptr);
+    w.hit = static_cast<float4*>(h->wf_hit.ptr);
+    w.queue[0] = static_cast<uint32_t*>(h->wf_queue[0].ptr);
+    w.queue[1] = static_cast<uint32_t*>(h->wf_queue[1].ptr);
+    w.shadow = static_cast<float4*>(h->wf_shadow.ptr);
+    w.counters = static_cast<uint32_t*>(h->wf_counters.ptr);
+    w.capacity = cap;
+    return RAYMOND_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int raymond_create(raymond_t** out, const raymond_config* cfg) {
@@ -166,6 +207,7 @@ int raymond_create(raymond_t** out, const raymond_config* cfg) {
     h->device = dev;
     cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
     h->seed_hash = (cfg && cfg->seed) ? pcg(cfg->seed) : 0u;
+    h->path_capacity_limit = cfg ? cfg->path_capacity : 0;
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
@@ -192,8 +234,10 @@ void raymond_destroy(raymond_t* h) {
     for (DevBuf* b : {&h->prims, &h->nodes, &h->materials, &h->attributes, &h->lights, &h->emitters, &h->textures,
                       &h->normal_maps, &h->env_map, &h->env_table, &h->accum, &h->guide_albedo, &h->guide_normal,
                       &h->light_a, &h->light_b, &h->denoised, &h->splats, &h->display, &h->ray_scratch,
-                      &h->prim_scratch, &h->t_scratch, &h->counter})
+                      &h->prim_scratch, &h->t_scratch, &h->counter, &h->wf_hit, &h->wf_queue[0], &h->wf_queue[1],
+                      &h->wf_shadow, &h->wf_counters})
         b->release();
+    for (DevBuf& b : h->wf_state) b.release();
     for (cudaEvent_t ev : h->ev)
         if (ev) cudaEventDestroy(ev);
     cudaStreamDestroy(h->stream);
@@ -378,13 +422,23 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
         return h->fail(RAYMOND_EINVAL, "The parameters' light and volume counts don't match the scene.");
     if (P.samples_per_frame == 0 || P.max_bounces > 64)
         return h->fail(RAYMOND_EINVAL, "samples_per_frame must be at least 1 and max_bounces at most 64.");
-    (void)flags;
     cudaSetDevice(h->device);
     const Scene s = h->scene_view();
     const PixelBuffers px = h->pixel_view();
+    // The wavefront runs colour frames when asked; inspection views always
+    // take the one-kernel path.
+    const bool wavefront = P.view == VIEW_COLOR && (flags & RAYMOND_FLAG_WAVEFRONT) && !(flags & RAYMOND_FLAG_MEGAKERNEL);
+    WavefrontState w{};
+    if (wavefront) {
+        const int rc = ensure_wavefront(h, P, w);
+        if (rc) return rc;
+    }
     int launches = 0;
     cudaEventRecord(h->ev[0], h->stream);
-    launches += launch_megakernel(s, P, features, px, h->num_sms, h->stream);
+    if (wavefront)
+        launches += launch_wavefront(s, P, features, w, px, h->tuning, h->num_sms, h->stream);
+    else
+        launches += launch_megakernel(s, P, features, px, h->num_sms, h->stream);
     cudaEventRecord(h->ev[1], h->stream);
     cudaEventRecord(h->ev[2], h->stream);
     if (P.denoise != 0u) launches += launch_denoise(P, px, h->stream);

@@ -270,9 +270,11 @@ class Renderer:
         self.flags = 0  # extra raymond_render flags (path choice)
 
     @staticmethod
-    def create(canvas, powerPreference="high-performance", device=0, seed=0) -> "Renderer":
-        """Renderer.create (src/Renderer.mjs:247-279); raises RuntimeError if no GPU can be used."""
-        cfg = _native.Config(device=device, seed=seed, path_capacity=0)
+    def create(canvas, powerPreference="high-performance", device=0, seed=0, pathCapacity=0) -> "Renderer":
+        """Renderer.create (src/Renderer.mjs:247-279); raises RuntimeError if no GPU can be used.
+        seed: XORed into the sample hashes (0 keeps the reference's streams);
+        pathCapacity: wavefront paths in flight (0: sized automatically)."""
+        cfg = _native.Config(device=device, seed=seed, path_capacity=pathCapacity)
         h = ctypes.c_void_p()
         rc = lib().raymond_create(ctypes.byref(h), ctypes.byref(cfg))
         if rc != _native.OK:

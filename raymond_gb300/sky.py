@@ -37,6 +37,12 @@ class Sky:
         return self.sunColor.scale(self.sunStrength / solid_angle)
 
     def radiance(self, d: Vec3) -> Vec3:
+        """What the sky shows along unit direction d (src/Sky.mjs:144-154)."""
+        if self.environment is not None:
+            from .texture import EnvironmentMap
+            u, v = EnvironmentMap.uv(d)
+            turned = EnvironmentMap.direction(u - self.environmentRotation / (2.0 * math.pi), v)
+            return self.environment.sample(turned).scale(self.environmentStrength)
         t = math.sqrt(min(abs(d.y), 1.0))
         return self.horizon.lerp(self.zenith, t) if d.y >= 0.0 else self.horizon.lerp(self.ground, t)
 
