@@ -186,6 +186,9 @@ def run_ours(args, rank, world, local):
     stream = torch.cuda.ExternalStream(lib.raymond_get_stream(r.handle), device=local)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
+    tuning = None
+    if args.path == "auto":
+        tuning = r.autotune(trials=2, cache=os.path.join(ROOT, "gpurun_out", "tuning.json"))
     for _ in range(args.warmup):
         r.render()
     r.device.queue.onSubmittedWorkDone()
@@ -264,7 +267,7 @@ def run_ours(args, rank, world, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32 scene)",
             "config": {"workload": WORKLOAD, "width": args.size, "height": args.size, "spp": args.spp,
                        "bounces": args.bounces, "triangles": info["triangles"], "spheres": info["spheres"],
-                       "primitives": scene.pack().primitiveCount, "parallelism": f"replicas x{world}", "path": args.path,
+                       "primitives": scene.pack().primitiveCount, "parallelism": f"replicas x{world}", "path": args.path, "tuning": tuning,
                        "l2": "flushed between steps (512 MB write)"},
             "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": 208, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,

@@ -100,6 +100,17 @@ int raymond_upload_environment(raymond_t* h, const uint16_t* rgba16f, uint32_t w
 /* Renderer.#writeEmitters' buffer (src/Renderer.mjs:670-717): vec4_count vec4s. */
 int raymond_set_emitters(raymond_t* h, const float* data, uint32_t vec4_count);
 
+/*
+ * Light tracing and photon mapping beyond the reference's fixed sizes
+ * (src/Renderer.mjs:37-39; src/shaders.mjs:1495-1510). photons_per_frame:
+ * light paths traced per frame (0: min(w·h·spp, capacity), as the
+ * reference). capacity: photons the map holds per frame (0: 524,288).
+ * radius: a fixed gathering radius (0: the params' shrinking radius; the
+ * grid cell is twice the radius either way). The hash table grows to at
+ * least twice the capacity (power of two, at least 2^20).
+ */
+int raymond_set_photons(raymond_t* h, uint32_t photons_per_frame, uint32_t capacity, float radius);
+
 /* Renderer.#resize (src/Renderer.mjs:766-799): keeps buffers that are big enough. */
 int raymond_resize(raymond_t* h, uint32_t w, uint32_t hgt);
 
@@ -166,6 +177,31 @@ int raymond_get_buffers(raymond_t* h, raymond_buffers* out);
 
 /* The handle's CUDA stream (a cudaStream_t), for callers that time or order work around it. */
 void* raymond_get_stream(raymond_t* h);
+
+/*
+ * How frames are launched: the one-kernel path or the wavefront, and the
+ * wavefront's launch shape. raymond_autotune picks it by timing; flags on a
+ * raymond_render call can still force either path.
+ */
+#define RAYMOND_PATH_MEGAKERNEL 1u
+#define RAYMOND_PATH_WAVEFRONT 2u
+typedef struct raymond_tuning {
+    uint32_t path;                    /* RAYMOND_PATH_* */
+    uint32_t steps;                   /* traversal steps between lane refills, 1..256 */
+    uint32_t traversal_blocks_per_sm; /* persistent extend/shadow blocks of 128 threads per SM, 1..16 */
+    uint32_t shade_blocks_per_sm;     /* shade/generate/finalize blocks per SM, 1..64 */
+} raymond_tuning;
+int raymond_set_tuning(raymond_t* h, const raymond_tuning* t);
+int raymond_get_tuning(raymond_t* h, raymond_tuning* out);
+
+/*
+ * Times candidate tunings on whole frames of the uploaded scene with these
+ * parameters and keeps the fastest (also written to best if not NULL). The
+ * trial frames overwrite the accumulation, so call it before the first
+ * frame of an image (the renderer does, when asked to tune). trials: frames
+ * timed per candidate (>= 1).
+ */
+int raymond_autotune(raymond_t* h, const void* params208, uint32_t features, uint32_t trials, raymond_tuning* best);
 
 /*
  * Counters of the last frame: kernel launches, paths, and the device time of

@@ -39,6 +39,14 @@ class Stats(ctypes.Structure):
                 ("ms_caustics", ctypes.c_float), ("ms_denoise", ctypes.c_float), ("ms_display", ctypes.c_float)]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("path", ctypes.c_uint32), ("steps", ctypes.c_uint32), ("traversal_blocks_per_sm", ctypes.c_uint32),
+                ("shade_blocks_per_sm", ctypes.c_uint32)]
+
+
+PATH_MEGAKERNEL, PATH_WAVEFRONT = 1, 2
+
+
 # Every symbol include/raymond.h declares, with its ctypes signature.
 _P = ctypes.c_void_p
 _U32 = ctypes.c_uint32
@@ -65,6 +73,10 @@ SIGNATURES = {
     "raymond_get_stats": (_I, [_P, ctypes.POINTER(Stats)]),
     "raymond_get_stream": (_P, [_P]),
     "raymond_denoise_static": (_I, [_P, _P, _P, _U32, _U32, _U32, _P, _P]),
+    "raymond_set_tuning": (_I, [_P, ctypes.POINTER(Tuning)]),
+    "raymond_set_photons": (_I, [_P, _U32, _U32, ctypes.c_float]),
+    "raymond_get_tuning": (_I, [_P, ctypes.POINTER(Tuning)]),
+    "raymond_autotune": (_I, [_P, _P, _U32, _U32, ctypes.POINTER(Tuning)]),
 }
 
 _lib = None

@@ -30,6 +30,17 @@ struct WavefrontState {
     uint64_t capacity;  // paths in flight
 };
 
+// Light tracing's splats (4 u32 per pixel, 1/65536 fixed point) and the
+// photon map: a hash table of grid cells (`table` heads, then the photon
+// count) with lists linked through the photons (3 float4 each: position and
+// next, power, incoming direction).
+struct CausticBuffers {
+    uint32_t* splats;
+    uint32_t* heads;
+    float4* photons;
+    uint32_t table, capacity, photons_per_frame;
+};
+
 // Launch shape of the wavefront kernels (chosen by the tuner).
 struct WavefrontTuning {
     int steps;                    // traversal steps between lane refills
@@ -45,6 +56,8 @@ int launch_megakernel(const Scene& s, const Params& P, uint32_t features, const 
                       cudaStream_t st);
 int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,
                      const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st);
+int launch_caustics(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb,
+                    const PixelBuffers& px, int num_sms, cudaStream_t st);
 int launch_denoise(const Params& P, const PixelBuffers& px, cudaStream_t st);
 int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st);
 void upload_srgb_table();

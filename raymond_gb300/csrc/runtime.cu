@@ -67,6 +67,13 @@ struct raymond {
     uint64_t path_capacity_limit = 0;  // from the config; 0 = default
     WavefrontTuning tuning{16, 8, 8};
 
+    // Photon map (allocated when caustics first run) and its sizing.
+    DevBuf photon_heads, photons;
+    uint32_t photon_table = 0, photon_capacity_alloc = 0;
+    uint32_t photons_override = 0, photon_capacity = 524288;
+    float photon_radius_override = 0.0f;
+    uint32_t path_choice = RAYMOND_PATH_WAVEFRONT;
+
     bool rendered = false;
     Params last_params{};
     raymond_stats stats{};
@@ -235,7 +242,7 @@ void raymond_destroy(raymond_t* h) {
                       &h->normal_maps, &h->env_map, &h->env_table, &h->accum, &h->guide_albedo, &h->guide_normal,
                       &h->light_a, &h->light_b, &h->denoised, &h->splats, &h->display, &h->ray_scratch,
                       &h->prim_scratch, &h->t_scratch, &h->counter, &h->wf_hit, &h->wf_queue[0], &h->wf_queue[1],
-                      &h->wf_shadow, &h->wf_counters})
+                      &h->wf_shadow, &h->wf_counters, &h->photon_heads, &h->photons})
         b->release();
     for (DevBuf& b : h->wf_state) b.release();
     for (cudaEvent_t ev : h->ev)
@@ -427,11 +434,38 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
     const PixelBuffers px = h->pixel_view();
     // The wavefront runs colour frames when asked; inspection views always
     // take the one-kernel path.
-    const bool wavefront = P.view == VIEW_COLOR && (flags & RAYMOND_FLAG_WAVEFRONT) && !(flags & RAYMOND_FLAG_MEGAKERNEL);
+    const bool want_wf = (flags & RAYMOND_FLAG_WAVEFRONT) ||
+                         (!(flags & RAYMOND_FLAG_MEGAKERNEL) && h->path_choice == RAYMOND_PATH_WAVEFRONT);
+    const bool wavefront = P.view == VIEW_COLOR && want_wf;
     WavefrontState w{};
     if (wavefront) {
         const int rc = ensure_wavefront(h, P, w);
         if (rc) return rc;
+    }
+    CausticBuffers cb{};
+    if (P.caustics != 0u) {
+        if (h->emitter_vec4s == 0) return h->fail(RAYMOND_ESTATE, "Caustics need raymond_set_emitters first.");
+        uint32_t table = 1u << 20;
+        while (table < 2ull * h->photon_capacity) table <<= 1;
+        if (table != h->photon_table || h->photon_capacity != h->photon_capacity_alloc) {
+            cudaError_t e = h->photon_heads.reserve((size_t(table) + 1) * 4);
+            if (e == cudaSuccess) e = h->photons.reserve(size_t(h->photon_capacity) * 48);
+            if (e != cudaSuccess) return h->cuda_fail(e, "photon map");
+            h->photon_table = table;
+            h->photon_capacity_alloc = h->photon_capacity;
+        }
+        cb.splats = static_cast<uint32_t*>(h->splats.ptr);
+        cb.heads = static_cast<uint32_t*>(h->photon_heads.ptr);
+        cb.photons = static_cast<float4*>(h->photons.ptr);
+        cb.table = h->photon_table;
+        cb.capacity = h->photon_capacity;
+        const uint64_t frame = uint64_t(P.width) * P.height * P.samples_per_frame;
+        cb.photons_per_frame = h->photons_override ? h->photons_override
+                                                   : uint32_t(frame < h->photon_capacity ? frame : h->photon_capacity);
+        if (h->photon_radius_override > 0.0f) {
+            P.photon_radius = h->photon_radius_override;
+            P.photon_cell = 2.0f * h->photon_radius_override;
+        }
     }
     int launches = 0;
     cudaEventRecord(h->ev[0], h->stream);
@@ -440,6 +474,7 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
     else
         launches += launch_megakernel(s, P, features, px, h->num_sms, h->stream);
     cudaEventRecord(h->ev[1], h->stream);
+    if (P.caustics != 0u) launches += launch_caustics(s, P, features, cb, px, h->num_sms, h->stream);
     cudaEventRecord(h->ev[2], h->stream);
     if (P.denoise != 0u) launches += launch_denoise(P, px, h->stream);
     cudaEventRecord(h->ev[3], h->stream);
@@ -557,6 +592,82 @@ int raymond_get_buffers(raymond_t* h, raymond_buffers* out) {
     out->width = h->width;
     out->height = h->height;
     return RAYMOND_OK;
+}
+
+int raymond_set_photons(raymond_t* h, uint32_t photons_per_frame, uint32_t capacity, float radius) {
+    if (!h) return RAYMOND_EINVAL;
+    if (capacity > (1u << 28) || !(radius >= 0.0f))
+        return h->fail(RAYMOND_EINVAL, "Photon capacity above 2^28 or a negative radius.");
+    h->photons_override = photons_per_frame;
+    h->photon_capacity = capacity ? capacity : 524288u;
+    h->photon_radius_override = radius;
+    return RAYMOND_OK;
+}
+
+int raymond_set_tuning(raymond_t* h, const raymond_tuning* t) {
+    if (!h || !t) return RAYMOND_EINVAL;
+    if ((t->path != RAYMOND_PATH_MEGAKERNEL && t->path != RAYMOND_PATH_WAVEFRONT) || t->steps < 1 || t->steps > 256 ||
+        t->traversal_blocks_per_sm < 1 || t->traversal_blocks_per_sm > 16 || t->shade_blocks_per_sm < 1 ||
+        t->shade_blocks_per_sm > 64)
+        return h->fail(RAYMOND_EINVAL, "Tuning out of range.");
+    h->path_choice = t->path;
+    h->tuning = WavefrontTuning{int(t->steps), int(t->traversal_blocks_per_sm), int(t->shade_blocks_per_sm)};
+    return RAYMOND_OK;
+}
+
+int raymond_get_tuning(raymond_t* h, raymond_tuning* out) {
+    if (!h || !out) return RAYMOND_EINVAL;
+    out->path = h->path_choice;
+    out->steps = uint32_t(h->tuning.steps);
+    out->traversal_blocks_per_sm = uint32_t(h->tuning.traversal_blocks_per_sm);
+    out->shade_blocks_per_sm = uint32_t(h->tuning.shade_blocks_per_sm);
+    return RAYMOND_OK;
+}
+
+int raymond_autotune(raymond_t* h, const void* params208, uint32_t features, uint32_t trials, raymond_tuning* best) {
+    if (!h || !params208) return RAYMOND_EINVAL;
+    if (trials < 1) trials = 1;
+    Params P;
+    std::memcpy(&P, params208, sizeof P);
+    // Trial frames start the image over (sample_offset 0) and skip denoising.
+    P.sample_offset = 0;
+    P.total_samples = P.samples_per_frame;
+    P.denoise = 0;
+    std::vector<raymond_tuning> cands;
+    cands.push_back({RAYMOND_PATH_MEGAKERNEL, 16, 8, 8});
+    for (uint32_t steps : {8u, 16u, 32u})
+        for (uint32_t blocks : {4u, 8u, 16u}) cands.push_back({RAYMOND_PATH_WAVEFRONT, steps, blocks, 8});
+    raymond_tuning keep{};
+    raymond_get_tuning(h, &keep);
+    float best_ms = 1e30f;
+    raymond_tuning chosen = keep;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    for (const raymond_tuning& c : cands) {
+        int rc = raymond_set_tuning(h, &c);
+        if (rc) break;
+        // One untimed frame warms caches and allocates the wavefront state.
+        rc = raymond_render(h, &P, features, 0);
+        if (rc) break;
+        cudaEventRecord(a, h->stream);
+        for (uint32_t k = 0; k < trials && rc == 0; ++k) rc = raymond_render(h, &P, features, 0);
+        cudaEventRecord(b, h->stream);
+        if (rc) break;
+        if (cudaEventSynchronize(b) != cudaSuccess) break;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best_ms) {
+            best_ms = ms;
+            chosen = c;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    raymond_set_tuning(h, &chosen);
+    h->rendered = false;
+    if (best) *best = chosen;
+    return best_ms < 1e30f ? RAYMOND_OK : h->fail(RAYMOND_ECUDA, "Autotuning found no working candidate.");
 }
 
 void* raymond_get_stream(raymond_t* h) { return h ? static_cast<void*>(h->stream) : nullptr; }

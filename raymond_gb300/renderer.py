@@ -123,6 +123,15 @@ def delta_objects(scene: Scene):
     return {"centre": allb["centre"], "radius": allb["radius"], "reach": reach, "targets": targets}
 
 
+def _gpu_name() -> str:
+    try:
+        import torch
+
+        return torch.cuda.get_device_name(0)
+    except Exception:
+        return "gpu"
+
+
 def light_table(packed):
     """The lights buffer of Renderer.#upload (src/Renderer.mjs:571-607): the
     light primitives, the volumes, then each light's running total chance
@@ -373,11 +382,10 @@ class Renderer:
         self._samples = 0
 
     # ---- frames ----
-    def render(self):
-        """Adds samplesPerFrame paths per pixel (src/Renderer.mjs:406-491)."""
+    def _prepare(self):
+        """Everything render() does before launching: uploads, resize,
+        caustics gate, uniforms. Returns the feature bits."""
         scene, camera = self._scene, self._camera
-        if scene is None or camera is None:
-            return
         width = max(1, int(self._canvas.width))
         height = max(1, int(self._canvas.height))
         if scene is not self._uploaded_scene or scene.version != self._uploaded_version:
@@ -387,26 +395,114 @@ class Renderer:
             self._upload_environment(env)
         if not self._resized or width != self._width or height != self._height:
             self._resize(width, height)
-        caustics = False  # light tracing and photon mapping: see _caustics_enabled
+        caustics = False
         if self._caustics and camera.aperture == 0 and self._view == "color" and self._volume_count == 0:
             caustics = self._caustics_enabled(scene)
         if caustics != self._caustics_active:
             self._caustics_active = caustics
             self._samples = 0
         self._write_params(scene, camera, width, height)
-        features = ((_native.FEATURE_VOLUMES if self._volume_count > 0 else 0)
-                    | (_native.FEATURE_TEXTURES if self._textured else 0)
-                    | (_native.FEATURE_ENVIRONMENT if env is not None else 0)
-                    | (_native.FEATURE_DISPERSION if self._dispersive else 0))
+        return ((_native.FEATURE_VOLUMES if self._volume_count > 0 else 0)
+                | (_native.FEATURE_TEXTURES if self._textured else 0)
+                | (_native.FEATURE_ENVIRONMENT if env is not None else 0)
+                | (_native.FEATURE_DISPERSION if self._dispersive else 0))
+
+    def render(self):
+        """Adds samplesPerFrame paths per pixel (src/Renderer.mjs:406-491)."""
+        if self._scene is None or self._camera is None:
+            return
+        features = self._prepare()
         buf = (ctypes.c_char * PARAMS_BYTES).from_buffer(self._params)
         check(lib().raymond_render(self._h, ctypes.addressof(buf), features, self.flags), self._h)
         self._samples += self._spp
 
+    def autotune(self, trials: int = 2, cache: str | None = None):
+        """Picks the launch shape for this scene and image by timing
+        candidates (the one-kernel path; wavefront traversal steps and
+        blocks per SM) and keeps the fastest; remembered in a JSON cache
+        keyed by GPU, features, scene-size bucket, resolution, samples per
+        frame and bounces. Starts the image over. Returns the tuning."""
+        import json
+        import os
+
+        if self._scene is None or self._camera is None:
+            raise RuntimeError("Set a scene and camera before tuning.")
+        features = self._prepare()
+        packed = self._scene.pack()
+        key = "|".join(str(x) for x in (
+            _gpu_name(), features, int(math.log2(max(packed.primitiveCount, 1))), self._width, self._height,
+            self._spp, self._max_bounces))
+        path = cache or os.path.join(os.path.expanduser("~"), ".cache", "raymond_gb300", "tuning.json")
+        table = {}
+        try:
+            with open(path) as f:
+                table = json.load(f)
+        except (OSError, ValueError):
+            table = {}
+        t = _native.Tuning()
+        if key in table:
+            for k, v in table[key].items():
+                setattr(t, k, v)
+            check(lib().raymond_set_tuning(self._h, ctypes.byref(t)), self._h)
+        else:
+            buf = (ctypes.c_char * PARAMS_BYTES).from_buffer(self._params)
+            check(lib().raymond_autotune(self._h, ctypes.addressof(buf), features, trials, ctypes.byref(t)), self._h)
+            table[key] = {f: getattr(t, f) for f, _ in _native.Tuning._fields_}
+            try:
+                os.makedirs(os.path.dirname(path), exist_ok=True)
+                with open(path, "w") as f:
+                    json.dump(table, f, indent=1)
+            except OSError:
+                pass
+        self._samples = 0
+        return {f: getattr(t, f) for f, _ in _native.Tuning._fields_}
+
+    @property
+    def tuning(self):
+        t = _native.Tuning()
+        check(lib().raymond_get_tuning(self._h, ctypes.byref(t)), self._h)
+        return {f: getattr(t, f) for f, _ in _native.Tuning._fields_}
+
     def _caustics_enabled(self, scene) -> bool:
-        # Light tracing is not wired into this backend's frame yet: with it
-        # off, the path tracer keeps every caustic path itself (its
-        # `caustic` split is off), so images converge to the same answer.
-        return False
+        """Renderer.#writeEmitters (src/Renderer.mjs:670-717): the lights
+        light tracing starts from, chosen by power (the sun's is what falls
+        on the targets' circles), then the targets. False if there is
+        nothing for light tracing to do."""
+        delta, sky = self._deltas, scene.sky
+        if not delta:
+            return False
+        circles = sum(math.pi * t["radius"] ** 2 for t in delta["targets"])
+        sources = list(self._light_powers)
+        if sky.sunStrength > 0:
+            omc = 2.0 * math.sin(sky.sunSize / 2.0) ** 2
+            r = sky.sunRadiance
+            lum = 0.2126 * r.x + 0.7152 * r.y + 0.0722 * r.z
+            sources.append({"prim": NONE, "power": lum * 2 * math.pi * omc * circles})
+        total = sum(src["power"] for src in sources)
+        if not (total > 0):
+            return False
+        data = np.zeros((2 + self._light_count + MAX_TARGETS) * 4, dtype=np.float32)
+        u = data.view(np.uint32)
+        u[0] = len(sources)
+        u[1] = len(delta["targets"])
+        data[2] = delta["reach"]
+        data[3] = circles
+        running = 0.0
+        for k, src in enumerate(sources):
+            running += src["power"] / total
+            data[4 + k * 4] = 1.0 if k == len(sources) - 1 else running
+            u[4 + k * 4 + 1] = src["prim"]
+            data[4 + k * 4 + 2] = src["power"] / total
+        for j, t in enumerate(delta["targets"]):
+            c = t["centre"]
+            data[4 + (len(sources) + j) * 4: 8 + (len(sources) + j) * 4] = [c.x, c.y, c.z, t["radius"]]
+        check(lib().raymond_set_emitters(self._h, ptr(data), data.size // 4), self._h)
+        return True
+
+    def setPhotons(self, photonsPerFrame=0, capacity=0, radius=0.0):
+        """Light paths per frame, photon-map capacity and a fixed gathering
+        radius beyond the reference's sizes (0: the reference's)."""
+        check(lib().raymond_set_photons(self._h, int(photonsPerFrame), int(capacity), float(radius)), self._h)
 
     def readPixels(self, denoised=False) -> np.ndarray:
         """The average so far, w×h×4 float32 from the top left (src/Renderer.mjs:502-528)."""

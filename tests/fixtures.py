@@ -92,6 +92,40 @@ SCENES = {
         dict(position=Vec3(0, 0, 3.2), target=Vec3(0, 0, 0), fov=math.pi / 3)),
 }
 
+def _dark_sun(strength, direction, size):
+    return Sky(zenith=BLACK, horizon=BLACK, ground=BLACK, sunStrength=strength, sunDirection=direction, sunSize=size)
+
+
+CAUSTIC_SCENES = {
+    "causticLamp": lambda arg=None: (Scene(sky=Sky.black()).add(
+        floor(), Sphere(Vec3(0, 0.9, 0), 0.5, Material.glass(1.5)),
+        Sphere(Vec3(0.3, 2.6, -0.2), 0.15, Material.light(WHITE, 60.0))), LOOK_DOWN),
+    "causticSun": lambda arg=None: (Scene(sky=_dark_sun(2.0, Vec3(0.3, 1, 0.1), 0.03)).add(
+        floor(), Sphere(Vec3(0, 0.9, 0), 0.5, Material.glass(1.5))), LOOK_DOWN),
+    "causticMirror": lambda arg=None: (Scene(sky=Sky.black()).add(
+        floor(), Quad(Vec3(-1, 0.2, -1.6), Vec3(2, 0, 0), Vec3(0, 1.2, 0.5), Material.metal(Vec3(0.9, 0.9, 0.9), 0)),
+        Quad(Vec3(0.25, 1.4, 1.4), Vec3(-0.5, 0, 0), Vec3(0, 0.5, 0.2), Material.light(WHITE, 30.0))), LOOK_DOWN),
+    "causticLampMany": lambda arg=None: (Scene(sky=Sky.black()).add(
+        floor(), Sphere(Vec3(0, 0.6, 0), 0.4, Material.glass(1.5)),
+        Box.fromCorners(Vec3(-0.5, 1.5, -0.5), Vec3(0.5, 1.52, 0.5), Material.glass(1.5)),
+        Sphere(Vec3(1.0, 0.35, 0.4), 0.35, Material.glass(1.5)),
+        Sphere(Vec3(0.05, 2.6, 0), 0.3, Material.light(WHITE, 15.0))), LOOK_DOWN),
+    "causticSunMany": lambda arg=None: (Scene(sky=_dark_sun(1.0, Vec3(0.2, 1, 0.1), 0.2)).add(
+        floor(),
+        *[Quad(Vec3(x0, 1.6, z0), Vec3(x1 - x0, 0, 0), Vec3(0, 0, z1 - z0), Material.diffuse(BLACK))
+          for x0, x1, z0, z1 in ((-20, -1, -20, 20), (1.1, 20, -20, 20), (-1, 1.1, -20, -0.5), (-1, 1.1, 0.5, 20))],
+        Box.fromCorners(Vec3(-1, 1.59, -0.5), Vec3(0.05, 1.61, 0.5), Material.glass(1.5)),
+        Box.fromCorners(Vec3(0.05, 1.59, -0.5), Vec3(1.1, 1.61, 0.5), Material.glass(1.5)),
+        Sphere(Vec3(0.2, 0.5, 0), 0.35, Material.glass(1.5))),
+        dict(position=Vec3(0, 1.4, 2.0), target=Vec3(0.1, 0, -0.2), fov=math.pi / 2.5)),
+    "causticThroughGlass": lambda arg=None: (Scene(sky=Sky.black()).add(
+        floor(), Sphere(Vec3(0, 0.9, 0), 0.5, Material.glass(1.5)),
+        Sphere(Vec3(0.3, 2.6, -0.2), 0.3, Material.light(WHITE, 20.0)),
+        Box.fromCorners(Vec3(-3, 0, 1.6), Vec3(3, 3.5, 1.62), Material.glass(1.5))),
+        dict(position=Vec3(0, 2.4, 2.4), target=Vec3(0, 0, 0), fov=math.pi / 4)),
+}
+SCENES.update(CAUSTIC_SCENES)
+
 _renderer = None
 
 

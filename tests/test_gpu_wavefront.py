@@ -59,3 +59,24 @@ def test_wavefront_sphere_field(gpu):
     mk = frame(scene, camera, 128, 2, _native.FLAG_MEGAKERNEL)
     wf = frame(scene, camera, 128, 2, _native.FLAG_WAVEFRONT)
     np.testing.assert_allclose(wf[0], mk[0], rtol=1e-4, atol=1e-5)
+
+
+def test_autotune_picks_a_working_shape(gpu, tmp_path):
+    scene, camera = scenes.cornell_scene()
+    r = Renderer.create(Canvas(64, 64))
+    r.scene, r.camera = scene, camera
+    r.samplesPerFrame = 2
+    t = r.autotune(trials=1, cache=str(tmp_path / "t.json"))
+    assert t["path"] in (_native.PATH_MEGAKERNEL, _native.PATH_WAVEFRONT)
+    assert r.samples == 0
+    r.render()
+    r.render()
+    r.device.queue.onSubmittedWorkDone()
+    px = r.readPixels()
+    assert np.isfinite(px).all() and px[0::4].mean() > 0
+    # The cached answer is reused without timing again.
+    r2 = Renderer.create(Canvas(64, 64))
+    r2.scene, r2.camera, r2.samplesPerFrame = scene, camera, 2
+    assert r2.autotune(trials=1, cache=str(tmp_path / "t.json")) == t
+    r.dispose()
+    r2.dispose()
