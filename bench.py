@@ -108,23 +108,29 @@ def build_workload(size, spp, bounces):
     return scene, camera, info
 
 
-def oracle_sample(scene, params: bytes, size, rows_per_strip, strips, threads):
+def oracle_sample(scene, params: bytes, size, rows_per_strip, strips, threads, detail=False):
     """The oracle's f32 path tracer on `strips` bands spread down the image:
-    returns (paths, seconds, algorithmic bytes per path, rays per path)."""
+    returns (paths, seconds, algorithmic bytes per path, rays per path), and
+    with detail the per-path closest-hit and shadow traversal bytes too."""
     import oracle
     from raymond_gb300.renderer import light_table
 
     packed = scene.pack()
     words, _ = light_table(packed)
-    paths = nbytes = rays = 0
+    tot = {"paths": 0, "bytes": 0, "rays": 0, "trav_closest": 0, "trav_shadow": 0, "rays_closest": 0,
+           "rays_shadow": 0}
     t0 = time.perf_counter()
     for k in range(strips):
         y0 = (k * size) // strips
         r = oracle.render(packed, words, params, region=(0, y0, size, rows_per_strip), nthreads=threads)
-        paths += r["paths"]
-        nbytes += r["bytes"]
-        rays += r["rays"]
-    return paths, time.perf_counter() - t0, nbytes / max(paths, 1), rays / max(paths, 1)
+        for key in tot:
+            tot[key] += r[key]
+    secs = time.perf_counter() - t0
+    p = max(tot["paths"], 1)
+    out = (tot["paths"], secs, tot["bytes"] / p, tot["rays"] / p)
+    if detail:
+        return out + ({k: tot[k] / p for k in ("trav_closest", "trav_shadow", "rays_closest", "rays_shadow")},)
+    return out
 
 
 def params_for(scene, camera, size, spp, bounces):
@@ -199,6 +205,7 @@ def run_ours(args, rank, world, local):
 
     stats = _native.Stats()
     step_ms, trace_ms, launches = [], [], 0
+    ext_ms, ext_launches, shade_ms, shadow_ms = [], [], [], []
     clocks = ClockSampler(local)
     barrier()
     torch.cuda.synchronize()
@@ -216,6 +223,10 @@ def run_ours(args, rank, world, local):
         lib.raymond_get_stats(r.handle, stats)
         trace_ms.append(stats.ms_trace)
         launches += int(stats.launches)
+        ext_ms.append(stats.ms_extend)
+        ext_launches.append(stats.launches_extend)
+        shade_ms.append(stats.ms_shade)
+        shadow_ms.append(stats.ms_shadow)
     torch.cuda.synchronize()
     barrier()
     clock_info = clocks.stop()
@@ -247,12 +258,25 @@ def run_ours(args, rank, world, local):
         # Algorithmic bytes per path from the oracle's instrumented f32 path
         # tracer on 1/64 of the frame (16 bands of 1 row), scaled to a launch.
         params = params_for(scene, camera, args.size, args.spp, args.bounces)
-        paths_s, secs_s, bytes_per_path, rays_per_path = oracle_sample(scene, params, args.size, 1, 16, threads)
+        paths_s, secs_s, bytes_per_path, rays_per_path, split = oracle_sample(scene, params, args.size, 1, 16, threads,
+                                                                              detail=True)
         # CPU baseline: the same port, a bounded sample (16 bands of 2 rows).
         cpu_paths, cpu_s, _, _ = oracle_sample(scene, params, args.size, 2, 16, threads)
         peak, peak_kind = measured_peak_hbm()
-        avg_trace_s = statistics.mean(trace_ms) / 1e3
-        achieved = bytes_per_path * paths_per_step / avg_trace_s / 1e9
+        wavefront = sum(ext_launches) > 0
+        if wavefront:
+            # Dominant kernel: k_wf_extend (closest-hit traversal). Algorithmic
+            # bytes per launch = the frame's closest-hit traversal bytes over
+            # its extend launches; duration = the mean event-timed launch.
+            kernel = "k_wf_extend"
+            launches_per_step = statistics.mean(ext_launches)
+            bytes_per_launch = split["trav_closest"] * paths_per_step / launches_per_step
+            launch_s = statistics.mean(ext_ms) / launches_per_step / 1e3
+        else:
+            kernel = "k_megakernel"
+            bytes_per_launch = bytes_per_path * paths_per_step
+            launch_s = statistics.mean(trace_ms) / 1e3
+        achieved = bytes_per_launch / launch_s / 1e9
         traffic = None
         prof = os.path.join(ROOT, "profiles", "traffic.json")
         if os.path.exists(prof):
@@ -271,11 +295,15 @@ def run_ours(args, rank, world, local):
                        "l2": "flushed between steps (512 MB write)"},
             "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": 208, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
-            "stages_ms": {"trace": statistics.mean(trace_ms), "step": statistics.mean(step_ms)},
+            "stages_ms": {"trace": statistics.mean(trace_ms), "step": statistics.mean(step_ms),
+                          "extend": statistics.mean(ext_ms), "shade": statistics.mean(shade_ms),
+                          "shadow": statistics.mean(shadow_ms)},
+            "mrays_per_s": rays_per_path * paths_per_step * args.steps * world / total_s / 1e6,
             "rays_per_path": rays_per_path,
-            "roofline": {"bound": "hbm", "kernel": "k_megakernel", "achieved": achieved, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                         "bytes_per_path": bytes_per_path},
+                         "bytes_per_launch": bytes_per_launch, "bytes_per_path": bytes_per_path,
+                         "traversal_bytes_per_path": split},
             "cpu_baseline": {"value": cpu_paths / cpu_s / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
                              "sample": f"16 bands of 2 rows x {args.size} px at {args.spp} spp (1/32 of a frame)"},
             "clocks": clock_info,

@@ -213,6 +213,9 @@ typedef struct raymond_stats {
     uint64_t rays_primary, rays_extension, rays_shadow, rays_photon;
     uint64_t paths;
     float ms_trace, ms_caustics, ms_denoise, ms_display;
+    /* wavefront frames: summed device time and launches of each stage kernel */
+    float ms_extend, ms_shade, ms_shadow;
+    uint32_t launches_extend, launches_shade, launches_shadow;
 } raymond_stats;
 int raymond_get_stats(raymond_t* h, raymond_stats* out);
 

@@ -116,14 +116,16 @@ def render(packed, lights_words, params: bytes, region=None, seed_hash=0, nthrea
     accum = np.zeros(rw * rh * 4, dtype=np.float32)
     alb = np.zeros(rw * rh * 4, dtype=np.float32)
     nrm = np.zeros(rw * rh * 4, dtype=np.float32)
-    counters = np.zeros(4, dtype=np.uint64)
+    counters = np.zeros(8, dtype=np.uint64)
     pbuf = np.frombuffer(bytes(params), dtype=np.uint8).copy()
     words = np.ascontiguousarray(lights_words, dtype=np.uint32)
     attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
     lib().ro_render(_p(packed.primitives), _p(packed.nodes), _p(packed.materials), _p(attrs), _p(words), _p(pbuf),
                     seed_hash, x0, y0, rw, rh, _p(accum), _p(alb), _p(nrm), _p(counters), nthreads or threads())
     return {"accum": accum.reshape(rh, rw, 4), "albedo": alb.reshape(rh, rw, 4), "normal": nrm.reshape(rh, rw, 4),
-            "bytes": int(counters[0]), "rays": int(counters[1]), "hits": int(counters[2]), "paths": int(counters[3])}
+            "bytes": int(counters[0]), "rays": int(counters[1]), "hits": int(counters[2]), "paths": int(counters[3]),
+            "trav_closest": int(counters[4]), "trav_shadow": int(counters[5]), "rays_closest": int(counters[6]),
+            "rays_shadow": int(counters[7])}
 
 
 def denoise(accum, guide_albedo, guide_normal, width, height, total_samples, nthreads=None):

@@ -62,8 +62,9 @@ void ro_trace32_one(const void* prims, const void* nodes, const float* o, const 
 // [x0, x0+rw) × [y0, y0+rh) of the params' image, as main() does, and
 // writes the region's per-pixel sums (accum rgb+lum², guide albedo, guide
 // normal), 4 floats each, row-major over the region. seed_hash is XORed into
-// the sample hashes (0: the reference's streams). counters (optional, 4
-// u64): algorithmic bytes, rays traced, surface hits, paths.
+// the sample hashes (0: the reference's streams). counters (optional, 8
+// u64): algorithmic bytes, rays traced, surface hits, paths; traversal bytes
+// of closest-hit traces, of shadow traces; closest-hit rays, shadow rays.
 void ro_render(const void* prims, const void* nodes, const void* materials, const float* attributes,
                const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0, uint32_t y0,
                uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out,

@@ -159,8 +159,10 @@ struct Ctx {
     const float* attrs;
     const uint32_t* lights;
     Params P;
-    // counters
+    // counters: all algorithmic bytes, rays, surface hits; traversal bytes
+    // and rays of closest-hit and of shadow (any-hit) traces apart
     uint64_t bytes = 0, rays = 0, hits = 0;
+    uint64_t trav_closest = 0, trav_shadow = 0, rays_closest = 0, rays_shadow = 0;
 
     const float* pf(uint32_t i) const { return reinterpret_cast<const float*>(prims + size_t(i) * 64); }
     const uint32_t* pu(uint32_t i) const { return reinterpret_cast<const uint32_t*>(prims + size_t(i) * 64); }
@@ -180,7 +182,15 @@ HitR trace(Ctx& c, V o, V d, float t_max, bool any_hit) {
     float tuv[3];
     ro_trace32_one(c.prims, c.nodes, of, df, t_max, any_hit ? 1 : 0, &prim, tuv, &inner, &tested);
     c.rays++;
-    c.bytes += 32ull * (1 + 2ull * inner) + 64ull * tested;
+    const uint64_t tb = 32ull * (1 + 2ull * inner) + 64ull * tested;
+    c.bytes += tb;
+    if (any_hit) {
+        c.trav_shadow += tb;
+        c.rays_shadow++;
+    } else {
+        c.trav_closest += tb;
+        c.rays_closest++;
+    }
     return {tuv[0], prim, tuv[1], tuv[2]};
 }
 
@@ -794,7 +804,7 @@ extern "C" void ro_render(const void* prims, const void* nodes, const void* mate
     Params P;
     std::memcpy(&P, params208, sizeof P);
     std::atomic<uint32_t> next{0};
-    std::atomic<uint64_t> tot_bytes{0}, tot_rays{0}, tot_hits{0};
+    std::atomic<uint64_t> tot_bytes{0}, tot_rays{0}, tot_hits{0}, tot_tc{0}, tot_ts{0}, tot_rc{0}, tot_rs{0};
     const uint32_t n = rw * rh;
     auto worker = [&] {
         Ctx c{static_cast<const uint8_t*>(prims), static_cast<const uint8_t*>(nodes),
@@ -852,6 +862,10 @@ extern "C" void ro_render(const void* prims, const void* nodes, const void* mate
         tot_bytes += c.bytes;
         tot_rays += c.rays;
         tot_hits += c.hits;
+        tot_tc += c.trav_closest;
+        tot_ts += c.trav_shadow;
+        tot_rc += c.rays_closest;
+        tot_rs += c.rays_shadow;
     };
     const int nt = std::max(1, threads);
     std::vector<std::thread> pool;
@@ -863,6 +877,10 @@ extern "C" void ro_render(const void* prims, const void* nodes, const void* mate
         counters[1] = tot_rays;
         counters[2] = tot_hits;
         counters[3] = uint64_t(n) * P.samples_per_frame;
+        counters[4] = tot_tc;
+        counters[5] = tot_ts;
+        counters[6] = tot_rc;
+        counters[7] = tot_rs;
     }
 }
 

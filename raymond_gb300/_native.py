@@ -36,7 +36,10 @@ class Stats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_uint64), ("rays_primary", ctypes.c_uint64),
                 ("rays_extension", ctypes.c_uint64), ("rays_shadow", ctypes.c_uint64),
                 ("rays_photon", ctypes.c_uint64), ("paths", ctypes.c_uint64), ("ms_trace", ctypes.c_float),
-                ("ms_caustics", ctypes.c_float), ("ms_denoise", ctypes.c_float), ("ms_display", ctypes.c_float)]
+                ("ms_caustics", ctypes.c_float), ("ms_denoise", ctypes.c_float), ("ms_display", ctypes.c_float),
+                ("ms_extend", ctypes.c_float), ("ms_shade", ctypes.c_float), ("ms_shadow", ctypes.c_float),
+                ("launches_extend", ctypes.c_uint32), ("launches_shade", ctypes.c_uint32),
+                ("launches_shadow", ctypes.c_uint32)]
 
 
 class Tuning(ctypes.Structure):

@@ -41,6 +41,16 @@ struct CausticBuffers {
     uint32_t table, capacity, photons_per_frame;
 };
 
+// CUDA events around each wavefront stage launch (kind 0 extend, 1 shade,
+// 2 shadow), recorded on the launching stream; count stops at capacity.
+struct StageEvents {
+    cudaEvent_t* begin;
+    cudaEvent_t* end;
+    int* kind;
+    int capacity;
+    int count;
+};
+
 // Launch shape of the wavefront kernels (chosen by the tuner).
 struct WavefrontTuning {
     int steps;                    // traversal steps between lane refills
@@ -55,7 +65,8 @@ int launch_trace_primary(const Scene& s, const float* rays, uint32_t n, uint32_t
 int launch_megakernel(const Scene& s, const Params& P, uint32_t features, const PixelBuffers& px, int num_sms,
                       cudaStream_t st);
 int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,
-                     const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st);
+                     const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st,
+                     StageEvents* events);
 int launch_caustics(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb,
                     const PixelBuffers& px, int num_sms, cudaStream_t st);
 int launch_denoise(const Params& P, const PixelBuffers& px, cudaStream_t st);

@@ -338,9 +338,26 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_finalize(Params P, WavefrontSta
     }
 }
 
+struct StageTimer {
+    StageEvents* ev;
+    cudaStream_t st;
+    int slot = -1;
+    void begin(int kind) {
+        slot = -1;
+        if (!ev || ev->count >= ev->capacity) return;
+        slot = ev->count++;
+        ev->kind[slot] = kind;
+        cudaEventRecord(ev->begin[slot], st);
+    }
+    void end() {
+        if (slot >= 0) cudaEventRecord(ev->end[slot], st);
+    }
+};
+
 template <uint32_t FEAT>
 int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, const PixelBuffers& px,
-                    const WavefrontTuning& tune, int num_sms, cudaStream_t st) {
+                    const WavefrontTuning& tune, int num_sms, cudaStream_t st, StageEvents* events) {
+    StageTimer timer{events, st};
     const uint32_t pixels = P.width * P.height;
     const uint32_t batch = uint32_t(w.capacity / pixels) > 0 ? uint32_t(w.capacity / pixels) : 1u;
     const int grid_trav = num_sms * tune.traversal_blocks_per_sm;
@@ -354,12 +371,18 @@ int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, co
         int q = 0;
         for (uint32_t depth = 0; depth <= P.max_bounces; ++depth) {
             cudaMemsetAsync(w.counters + C_FETCH, 0, 4 * sizeof(uint32_t), st);
+            timer.begin(0);
             k_wf_extend<<<grid_trav, WF_BLOCK, 0, st>>>(s, w, q, tune.steps);
+            timer.end();
             // The next queue and the shadow queue start empty.
             cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
             cudaMemsetAsync(w.counters + C_SHADOW, 0, sizeof(uint32_t), st);
+            timer.begin(1);
             k_wf_shade<FEAT><<<grid_shade, WF_BLOCK, 0, st>>>(s, P, w, q);
+            timer.end();
+            timer.begin(2);
             k_wf_shadow<<<grid_trav, WF_BLOCK, 0, st>>>(s, w, tune.steps);
+            timer.end();
             launches += 3;
             q ^= 1;
         }
@@ -372,12 +395,13 @@ int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, co
 }  // namespace
 
 int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,
-                     const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st) {
+                     const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st,
+                     StageEvents* events) {
     switch (features & 15u) {
-        case 0: return wavefront_frame<0>(s, P, w, px, tune, num_sms, st);
-        case F_VOLUMES: return wavefront_frame<F_VOLUMES>(s, P, w, px, tune, num_sms, st);
-        case F_DISPERSION: return wavefront_frame<F_DISPERSION>(s, P, w, px, tune, num_sms, st);
-        default: return wavefront_frame<15u>(s, P, w, px, tune, num_sms, st);
+        case 0: return wavefront_frame<0>(s, P, w, px, tune, num_sms, st, events);
+        case F_VOLUMES: return wavefront_frame<F_VOLUMES>(s, P, w, px, tune, num_sms, st, events);
+        case F_DISPERSION: return wavefront_frame<F_DISPERSION>(s, P, w, px, tune, num_sms, st, events);
+        default: return wavefront_frame<15u>(s, P, w, px, tune, num_sms, st, events);
     }
 }
 

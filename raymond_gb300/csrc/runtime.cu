@@ -14,6 +14,8 @@
 
 using namespace rmd;
 
+static constexpr int raymond_stage_events = 1024;
+
 namespace {
 
 struct DevBuf {
@@ -80,6 +82,10 @@ struct raymond {
     // Stage boundaries of the last frame: trace, caustics, denoise, display.
     cudaEvent_t ev[5] = {};
     bool ev_valid = false;
+    // Per-launch events of the wavefront stages of the last frame.
+    std::vector<cudaEvent_t> stage_begin, stage_end;
+    std::vector<int> stage_kind;
+    StageEvents stage{};
 
     int fail(int code, const char* fmt, ...) {
         char buf[512];
@@ -222,6 +228,14 @@ int raymond_create(raymond_t** out, const raymond_config* cfg) {
         return RAYMOND_ECUDA;
     }
     for (cudaEvent_t& ev : h->ev) cudaEventCreate(&ev);
+    h->stage_begin.resize(raymond_stage_events);
+    h->stage_end.resize(raymond_stage_events);
+    h->stage_kind.resize(raymond_stage_events);
+    for (int k = 0; k < raymond_stage_events; ++k) {
+        cudaEventCreate(&h->stage_begin[k]);
+        cudaEventCreate(&h->stage_end[k]);
+    }
+    h->stage = StageEvents{h->stage_begin.data(), h->stage_end.data(), h->stage_kind.data(), raymond_stage_events, 0};
     e = h->counter.reserve(64);
     if (e != cudaSuccess) {
         g_create_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
@@ -247,6 +261,8 @@ void raymond_destroy(raymond_t* h) {
     for (DevBuf& b : h->wf_state) b.release();
     for (cudaEvent_t ev : h->ev)
         if (ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : h->stage_begin) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : h->stage_end) cudaEventDestroy(ev);
     cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -469,8 +485,9 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
     }
     int launches = 0;
     cudaEventRecord(h->ev[0], h->stream);
+    h->stage.count = 0;
     if (wavefront)
-        launches += launch_wavefront(s, P, features, w, px, h->tuning, h->num_sms, h->stream);
+        launches += launch_wavefront(s, P, features, w, px, h->tuning, h->num_sms, h->stream, &h->stage);
     else
         launches += launch_megakernel(s, P, features, px, h->num_sms, h->stream);
     cudaEventRecord(h->ev[1], h->stream);
@@ -677,6 +694,21 @@ int raymond_get_stats(raymond_t* h, raymond_stats* out) {
     if (h->ev_valid && cudaEventQuery(h->ev[4]) == cudaSuccess) {
         float* ms[4] = {&h->stats.ms_trace, &h->stats.ms_caustics, &h->stats.ms_denoise, &h->stats.ms_display};
         for (int k = 0; k < 4; ++k) cudaEventElapsedTime(ms[k], h->ev[k], h->ev[k + 1]);
+        float sums[3] = {0, 0, 0};
+        uint32_t counts[3] = {0, 0, 0};
+        for (int k = 0; k < h->stage.count; ++k) {
+            float t = 0.0f;
+            if (cudaEventElapsedTime(&t, h->stage.begin[k], h->stage.end[k]) == cudaSuccess) {
+                sums[h->stage.kind[k]] += t;
+                counts[h->stage.kind[k]]++;
+            }
+        }
+        h->stats.ms_extend = sums[0];
+        h->stats.ms_shade = sums[1];
+        h->stats.ms_shadow = sums[2];
+        h->stats.launches_extend = counts[0];
+        h->stats.launches_shade = counts[1];
+        h->stats.launches_shadow = counts[2];
     }
     *out = h->stats;
     return RAYMOND_OK;
