@@ -187,6 +187,7 @@ def run_ours(args, rank, world, local):
     r.scene, r.camera = scene, camera
     r.maxBounces = args.bounces
     r.samplesPerFrame = args.spp
+    r.caustics = False  # plain path tracing: light tracing and photon mapping are the caustics workload's
     r.flags = {"auto": 0, "megakernel": _native.FLAG_MEGAKERNEL, "wavefront": _native.FLAG_WAVEFRONT}[args.path]
     lib = _native.lib()
     stream = torch.cuda.ExternalStream(lib.raymond_get_stream(r.handle), device=local)

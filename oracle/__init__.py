@@ -35,6 +35,8 @@ def lib():
         _lib.ro_intersect_double.argtypes = [P, U32, P, P, D, P]
         _lib.ro_trace32_batch.restype = None
         _lib.ro_trace32_batch.argtypes = [P, P, P, U32, F, I, P, P, P, P, I]
+        _lib.ro_surface_double.restype = None
+        _lib.ro_surface_double.argtypes = [P, P, U32, P, P, D, D, D, P]
         _lib.ro_render.restype = None
         _lib.ro_render.argtypes = [P, P, P, P, P, P, U32, U32, U32, U32, U32, P, P, P, P, I]
         _lib.ro_denoise.restype = None
@@ -148,3 +150,14 @@ def display(accum, denoised, params: bytes):
     pbuf = np.frombuffer(bytes(params), dtype=np.uint8).copy()
     lib().ro_display(_p(a), _p(d), _p(pbuf), _p(out))
     return out.reshape(height, width, 4)
+
+
+def surface_double(packed, p, o, d, t, u, v):
+    """Scene.raycast's surface frame at a hit: dict geometric, shading (unflipped), uv, tangent, up."""
+    out = np.zeros(14)
+    o = np.ascontiguousarray(o, dtype=np.float64)
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
+    lib().ro_surface_double(_p(packed.primitives), _p(attrs), int(p), _p(o), _p(d), float(t), float(u), float(v),
+                            _p(out))
+    return {"geometric": out[0:3], "shading": out[3:6], "uv": out[6:8], "tangent": out[8:11], "up": out[11:14]}

@@ -45,6 +45,12 @@ void ro_raycast_batch(const void* prims, uint32_t prim_count, const void* nodes,
 int ro_intersect_double(const void* prims, uint32_t p, const double* o, const double* d,
                         double t_max, double* tuv);
 
+// The surface frame of a hit as Scene.raycast builds it, in double
+// (src/Scene.mjs:687-879): geometric and shading normal (unflipped), uv,
+// tangent and up — 14 doubles.
+void ro_surface_double(const void* prims, const float* attributes, uint32_t p, const double* o, const double* d,
+                       double t, double bu, double bv, double* out);
+
 // ---- trace() of the trace shader (src/shaders.mjs:363-447), in f32 ----
 // The GPU's own traversal order and arithmetic, restated on the CPU, with
 // counters for the algorithmic byte figure: inner nodes whose two children

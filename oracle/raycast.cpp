@@ -533,3 +533,90 @@ extern "C" void ro_trace32_one(const void* prims, const void* nodes, const float
     if (inner_out) *inner_out = inner;
     if (tested_out) *tested_out = tested;
 }
+
+// The hit's surface frame as Scene.raycast builds it, in double
+// (src/Scene.mjs:687-879): out[0..2] geometric normal, [3..5] shading
+// normal (both unflipped), [6..7] uv (Scene.#uv, before the texture scale),
+// [8..10] tangent, [11..13] up (Scene.#tangents).
+extern "C" void ro_surface_double(const void* prims, const float* attributes, uint32_t p, const double* o,
+                                  const double* d, double t, double bu, double bv, double* out) {
+    const PrimView pv = prim(prims, p);
+    const float* f = pv.f;
+    const uint32_t kind = pv.u[0];
+    const D3 O = {o[0], o[1], o[2]}, Dd = {d[0], d[1], d[2]};
+    const D3 point = add(O, scale(Dd, t));
+    D3 g, sh;
+    normals_double(prims, attributes, p, point, bu, bv, &g, &sh);
+    double u = 0, v = 0;
+    D3 tangent{1, 0, 0}, up{0, 1, 0};
+    auto sgn = [](double x) { return x > 0 ? 1.0 : (x < 0 ? -1.0 : 0.0); };
+    if (kind == SPHERE) {
+        const D3 n = normalized(sub(point, d3(f + 4)));
+        const D3 x = d3(f + 8), north = d3(f + 12);
+        const D3 z = cross(x, north);
+        const double uu = std::atan2(-dot(n, z), dot(n, x)) / (2.0 * M_PI);
+        u = uu - std::floor(uu);
+        v = std::acos(std::min(std::max(dot(n, north), -1.0), 1.0)) / M_PI;
+        tangent = cross(north, n);
+        if (length(tangent) < 1e-6) tangent = x;
+        up = cross(n, tangent);
+    } else if (kind == QUAD) {
+        u = bu;
+        v = 1.0 - bv;
+        tangent = d3(f + 8);
+        up = d3(f + 12);
+    } else if (kind == BOX) {
+        double lp[3], half[3];
+        for (int r = 0; r < 3; ++r) {
+            lp[r] = double(f[4 + r * 4]) * point.x + double(f[5 + r * 4]) * point.y + double(f[6 + r * 4]) * point.z +
+                    double(f[7 + r * 4]);
+            half[r] = 1.0 / std::sqrt(double(f[4 + r * 4]) * f[4 + r * 4] + double(f[5 + r * 4]) * f[5 + r * 4] +
+                                      double(f[6 + r * 4]) * f[6 + r * 4]);
+        }
+        const double ax = std::fabs(lp[0]), ay = std::fabs(lp[1]), az = std::fabs(lp[2]);
+        const D3 r0 = d3(f + 4), r1 = d3(f + 8), r2 = d3(f + 12);
+        if (ax >= ay && ax >= az) {
+            u = (1.0 - sgn(lp[0]) * lp[2]) * half[2];
+            v = (1.0 - lp[1]) * half[1];
+            tangent = scale(r2, -sgn(lp[0]));
+            up = r1;
+        } else if (ay >= az) {
+            u = (1.0 + lp[0]) * half[0];
+            v = (1.0 + sgn(lp[1]) * lp[2]) * half[2];
+            tangent = r0;
+            up = scale(r2, -sgn(lp[1]));
+        } else {
+            u = (1.0 + sgn(lp[2]) * lp[0]) * half[0];
+            v = (1.0 - lp[1]) * half[1];
+            tangent = scale(r0, sgn(lp[2]));
+            up = r1;
+        }
+    } else if (kind == TRIANGLE) {
+        const uint32_t ai = pv.u[3];
+        const bool textured = ai != RO_NONE && (int(attributes[(size_t(ai) + 3) * 4 + 3]) & 2);
+        const D3 v0 = d3(f + 4);
+        const D3 e1 = sub(d3(f + 8), v0), e2 = sub(d3(f + 12), v0);
+        double du1[2] = {1, 0}, du2[2] = {0, 1};
+        if (textured) {
+            const float* A = attributes + size_t(ai) * 4;
+            const double w = 1.0 - bu - bv;
+            u = A[3] * w + A[7] * bu + A[11] * bv;
+            v = A[12] * w + A[13] * bu + A[14] * bv;
+            const double t1[2] = {double(A[7]) - A[3], double(A[13]) - A[12]};
+            const double t2[2] = {double(A[11]) - A[3], double(A[14]) - A[12]};
+            if (std::fabs(t1[0] * t2[1] - t2[0] * t1[1]) > 1e-12) {
+                du1[0] = t1[0]; du1[1] = t1[1];
+                du2[0] = t2[0]; du2[1] = t2[1];
+            }
+        } else {
+            u = bu;
+            v = bv;
+        }
+        const double det = du1[0] * du2[1] - du2[0] * du1[1];
+        tangent = scale(sub(scale(e1, du2[1]), scale(e2, du1[1])), 1.0 / det);
+        const D3 dpdv = scale(sub(scale(e2, du1[0]), scale(e1, du2[0])), 1.0 / det);
+        up = scale(dpdv, -1.0);
+    }
+    const double vals[14] = {g.x, g.y, g.z, sh.x, sh.y, sh.z, u, v, tangent.x, tangent.y, tangent.z, up.x, up.y, up.z};
+    for (int k = 0; k < 14; ++k) out[k] = vals[k];
+}

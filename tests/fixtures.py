@@ -8,7 +8,8 @@ import math
 import numpy as np
 
 import oracle
-from raymond_gb300 import Box, Camera, Canvas, Mat4, Material, Mesh, Quad, Renderer, Scene, Sky, Sphere, Vec3
+from raymond_gb300 import (Box, Camera, Canvas, EnvironmentMap, Mat4, Material, Mesh, Quad, Renderer, Scene, Sky, Sphere,
+                           Texture, Vec2, Vec3)
 
 BLACK = Vec3(0, 0, 0)
 WHITE = Vec3(1, 1, 1)
@@ -126,6 +127,76 @@ CAUSTIC_SCENES = {
 }
 SCENES.update(CAUSTIC_SCENES)
 
+# Textures and the environment of tests/browser/fixture.mjs:13-25 and environment.mjs:7-17.
+GRADIENT = Texture.procedural(64, 64, lambda u, v: Vec3(u, v, 0.5 + 0.5 * math.sin(u * 6.28)))
+GRID = Texture.procedural(64, 64, lambda u, v: Vec3((math.floor(u * 4) + 1) / 4, (math.floor(v * 4) + 1) / 4,
+                                                   ((math.floor(u * 4) + math.floor(v * 4)) % 2) * 0.8 + 0.1))
+BUMPS = Texture.normalMap(64, 64, lambda u, v: 0.03 * math.sin(u * math.pi * 4) * math.cos(v * math.pi * 6))
+PATTERN = Texture.procedural(64, 64, lambda u, v: Vec3(1 - 0.9 * u, 0.3 + 0.4 * v, 0.1 + 0.9 * u * v))
+ENV_SUN = Vec3(0.45, 0.6, -0.66).normalized()
+
+
+def _env_radiance(d):
+    near = d.dot(ENV_SUN)
+    c18 = math.cos(0.18)
+    sun = 40 * (near - c18) / (1 - c18) + 10 if near > c18 else 0
+    sky = 0.2 + 0.6 * max(d.y, 0)
+    return Vec3(sky * 0.6 + sun, sky * 0.8 + sun * 0.9, sky + sun * 0.7)
+
+
+ENVIRONMENT = EnvironmentMap.procedural(128, 64, _env_radiance)
+ENV_STRENGTH, ENV_ROTATION = 1.5, 0.7
+TEX_CAMERA = dict(position=Vec3(0.8, 2.6, 3.8), target=Vec3(0, 0.4, 0), fov=math.pi / 3)
+
+TEXTURE_SCENES = {
+    "textured": lambda arg=None: (Scene(sky=Sky.black()).add(
+        Quad(Vec3(-10, 0, 10), Vec3(20, 0, 0), Vec3(0, 0, -20), Material.diffuse(Vec3(1, 1, 1)).withTexture(GRID, 6)),
+        Sphere(Vec3(-1.0, 0.7, 0), 0.7, Material.diffuse(Vec3(1, 1, 1)).withTexture(GRADIENT),
+               rotation=Mat4.rotateZ(0.4).multiplyMat4(Mat4.rotateY(1.0))),
+        Box.fromCorners(Vec3(0.3, 0, -0.9), Vec3(1.3, 1.0, 0.1),
+                        Material.plastic(Vec3(1, 0.8, 0.8)).withTexture(GRID, Vec2(1, 2), Vec3(1, 0.8, 0.8)), 0.5),
+        Mesh.torus(Material.diffuse(Vec3(1, 1, 1)).withTexture(GRADIENT, 3), radius=0.4, tube=0.18, segments=32,
+                   sides=16).transformed(Mat4.translate(0.6, 0.35, 1.0).multiplyMat4(Mat4.rotateX(1.1)))), TEX_CAMERA),
+    "bumpy": lambda arg=None: (Scene(sky=Sky.black()).add(
+        Quad(Vec3(-10, 0, 10), Vec3(20, 0, 0), Vec3(0, 0, -20),
+             Material.diffuse(WHITE).withTexture(GRID, 6).withNormalMap(BUMPS, 1.5)),
+        Sphere(Vec3(-1.0, 0.7, 0), 0.7, Material.diffuse(WHITE).withNormalMap(BUMPS, 2),
+               rotation=Mat4.rotateZ(0.4).multiplyMat4(Mat4.rotateY(1.0))),
+        Box.fromCorners(Vec3(0.3, 0, -0.9), Vec3(1.3, 1.0, 0.1),
+                        Material.plastic(WHITE).withTexture(GRID, Vec2(1, 2)).withNormalMap(BUMPS, 2), 0.5),
+        Mesh.torus(Material.diffuse(WHITE).withTexture(GRADIENT, 3).withNormalMap(BUMPS, 2), radius=0.4, tube=0.18,
+                   segments=32, sides=16).transformed(Mat4.translate(0.6, 0.35, 1.0).multiplyMat4(Mat4.rotateX(1.1)))),
+        TEX_CAMERA),
+    "patternedLamps": lambda arg=None: (Scene(sky=Sky.black()).add(
+        Quad(Vec3(-1.5, -1, 0), Vec3(1.4, 0, 0), Vec3(0, 2, 0), Material.light(WHITE).withEmission(WHITE, 1, PATTERN)),
+        Sphere(Vec3(0.8, 0, 0), 0.8, Material.light(WHITE).withEmission(WHITE, 1, PATTERN), rotation=Mat4.rotateY(0.7))),
+        dict(position=Vec3(0, 0, 2.6), target=Vec3(0, 0, 0), fov=math.pi / 3)),
+    "patternedLamp": lambda arg: (Scene(sky=Sky.black()).add(
+        floor(), Quad(Vec3(-1.0, 1.2, -1.5), Vec3(2.0, 0, 0), Vec3(0, 0, 1.4),
+                      (Material.light(WHITE) if arg == "light" else Material.diffuse(BLACK)).withEmission(WHITE, 4, PATTERN))),
+        LOOK_DOWN),
+    "environmentSky": lambda arg=None: (Scene(sky=Sky.environment_sky(ENVIRONMENT, ENV_STRENGTH, ENV_ROTATION)),
+                                        dict(position=Vec3(0, 0, 0), target=Vec3(0.3, 0.25, -1), fov=2.2)),
+    "environmentFloor": lambda arg=None: (Scene(sky=Sky.environment_sky(ENVIRONMENT, ENV_STRENGTH, ENV_ROTATION)).add(
+        floor()), LOOK_DOWN),
+}
+SCENES.update(TEXTURE_SCENES)
+
+
+def bump(n, ng, tangent, up, t, strength):
+    """Scene.mjs bump(): the shading normal tilted by a normal-map texel."""
+    right = tangent - n * (n @ tangent)
+    if np.linalg.norm(right) < 1e-9:
+        return n
+    right = right / np.linalg.norm(right)
+    above = np.cross(n, right)
+    if above @ up < 0.0:
+        above = -above
+    tilted = right * ((t[0] * 2 - 1) * strength) + above * ((t[1] * 2 - 1) * strength) + n * (t[2] * 2 - 1)
+    tilted = tilted / np.linalg.norm(tilted)
+    return tilted if tilted @ ng > 0.0 else n
+
+
 _renderer = None
 
 
@@ -176,9 +247,28 @@ def trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoise=Fals
         p = int(ref["prim"][i])
         if p == oracle.NONE:
             hits.append(None)
-        else:
-            hits.append({"object": int(packed.objectIndex[p]), "distance": float(ref["t"][i]),
-                         "normal": ref["normal"][i], "point": rays[i, :3] + rays[i, 3:] * ref["t"][i]})
+            continue
+        m = packed.materialList[int(packed.primitives[p * 16 + 1])]
+        normal = ref["normal"][i]
+        albedo_ = None
+        if m.texture is not None or m.normalMap is not None or m.emissionTexture is not None:
+            o, d = rays[i, :3].astype(np.float64), rays[i, 3:].astype(np.float64)
+            sf = oracle.surface_double(packed, p, o, d, ref["t"][i], ref["uv"][i, 0], ref["uv"][i, 1])
+            su, sv = sf["uv"][0] * m.textureScale.x, sf["uv"][1] * m.textureScale.y
+            if m.normalMap is not None:
+                t = m.normalMap.sample_many(np.array([su]), np.array([sv]), srgb=False)[0]
+                shading = bump(sf["shading"], sf["geometric"], sf["tangent"], sf["up"], t, m.normalScale)
+                normal = shading if sf["geometric"] @ d < 0 else -shading
+            if m.type == "light":
+                e = np.array(m.emission.tuple())
+                albedo_ = e * (m.emissionTexture.sample_many(np.array([su]), np.array([sv]))[0]
+                               if m.emissionTexture is not None else 1.0)
+            elif m.texture is not None:
+                albedo_ = np.array(m.color.tuple()) * m.texture.sample_many(np.array([su]), np.array([sv]))[0]
+        if albedo_ is None:
+            albedo_ = np.array((m.emission if m.type == "light" else m.color).tuple())
+        hits.append({"object": int(packed.objectIndex[p]), "distance": float(ref["t"][i]), "normal": normal,
+                     "albedo": albedo_, "point": rays[i, :3] + rays[i, 3:] * ref["t"][i]})
     return {"pixels": pixels, "denoised": den, "hits": hits, "rays": rays, "samples": r.samples, "scene": scene}
 
 
