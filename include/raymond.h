@@ -122,6 +122,28 @@ int raymond_resize(raymond_t* h, uint32_t w, uint32_t hgt);
  */
 int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint32_t flags);
 
+/*
+ * One frame of many renderers in one pass (the batched workload): every
+ * job's paths share the executor's wavefront path pool — generate, then per
+ * bounce extend / shade / shadow over all jobs' paths at once, then finalize,
+ * the à-trous passes and the tone map over all jobs' images — so small and
+ * large images fill the GPU together. With RAYMOND_BATCH_GRAPH the frame's
+ * launches are captured once as a CUDA graph and replayed while the jobs'
+ * sizes, sample counts and bounces stay the same; each frame's uniforms
+ * reach it through a device job table copied before the launch. Colour
+ * frames only; light tracing does not run in a batch (each job's caustics
+ * flag is taken as off). Work runs on the executor's stream: sync the
+ * executor before reading the jobs' images. Limits: ≤ 2048 jobs, ≤ 2^21
+ * pixels per job.
+ */
+typedef struct raymond_job {
+    raymond_t* renderer;   /* the job's scene, image buffers and state */
+    const void* params208; /* this frame's uniform block for it */
+    uint32_t features;     /* RAYMOND_FEATURE_* of its scene */
+} raymond_job;
+#define RAYMOND_BATCH_GRAPH 1u
+int raymond_render_batch(raymond_t* executor, const raymond_job* jobs, uint32_t n, uint32_t flags);
+
 /* Waits for the handle's stream: backs device.queue.onSubmittedWorkDone(). */
 int raymond_sync(raymond_t* h);
 

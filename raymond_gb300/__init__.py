@@ -11,10 +11,10 @@ from .material import MATERIAL_TYPES, Material
 from .geometry import Box, Mesh, Quad, Sphere
 from .sky import Camera, Sky
 from .scene import BVH, NONE, PRIMITIVE_KINDS, PackedScene, Scene
-from .renderer import Canvas, Renderer
+from .renderer import BatchRenderer, Canvas, Renderer
 from .texture import EnvironmentMap, Texture
 
 __all__ = [
-    "BVH", "Box", "Camera", "Canvas", "MATERIAL_TYPES", "Mat4", "Material", "Mesh", "NONE", "PRIMITIVE_KINDS",
+    "BatchRenderer", "BVH", "Box", "Camera", "Canvas", "MATERIAL_TYPES", "Mat4", "Material", "Mesh", "NONE", "PRIMITIVE_KINDS",
     "PackedScene", "Quad", "Renderer", "Scene", "Sky", "Sphere", "Vec2", "Vec3", "Texture", "EnvironmentMap",
 ]

@@ -48,6 +48,11 @@ class Tuning(ctypes.Structure):
 
 
 PATH_MEGAKERNEL, PATH_WAVEFRONT = 1, 2
+BATCH_GRAPH = 1
+
+
+class Job(ctypes.Structure):
+    _fields_ = [("renderer", ctypes.c_void_p), ("params208", ctypes.c_void_p), ("features", ctypes.c_uint32)]
 
 
 # Every symbol include/raymond.h declares, with its ctypes signature.
@@ -78,6 +83,7 @@ SIGNATURES = {
     "raymond_denoise_static": (_I, [_P, _P, _P, _U32, _U32, _U32, _P, _P]),
     "raymond_set_tuning": (_I, [_P, ctypes.POINTER(Tuning)]),
     "raymond_set_photons": (_I, [_P, _U32, _U32, ctypes.c_float]),
+    "raymond_render_batch": (_I, [_P, ctypes.POINTER(Job), _U32, _U32]),
     "raymond_get_tuning": (_I, [_P, ctypes.POINTER(Tuning)]),
     "raymond_autotune": (_I, [_P, _P, _U32, _U32, ctypes.POINTER(Tuning)]),
 }

@@ -51,6 +51,32 @@ struct StageEvents {
     int count;
 };
 
+// One renderer's part of a batched frame: its scene, this frame's uniforms
+// and its per-pixel buffers.
+struct JobDesc {
+    Scene scene;
+    Params params;
+    PixelBuffers px;
+};
+
+// A run of a job's samples inside one wave of the path pool: samples
+// [k0, k0 + nk) of job `job` (pixels each) occupy wave paths
+// [path_offset, path_offset + nk·pixels); its pixels are wave pixels
+// [pixel_offset, pixel_offset + pixels) for the finalize pass.
+struct WaveSegment {
+    uint32_t job, k0, nk, pixels;
+    uint32_t path_offset, pixel_offset;
+};
+// A job's pixels inside a batched image pass: batch pixels
+// [pixel_offset, pixel_offset + w·h) belong to job `job`.
+struct JobPixels {
+    uint32_t job, pixel_offset;
+};
+struct WavePlan {
+    uint32_t first_segment, segments;  // into the segment array
+    uint32_t paths, pixels;            // wave totals
+};
+
 // Launch shape of the wavefront kernels (chosen by the tuner).
 struct WavefrontTuning {
     int steps;                    // traversal steps between lane refills
@@ -67,6 +93,11 @@ int launch_megakernel(const Scene& s, const Params& P, uint32_t features, const 
 int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,
                      const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st,
                      StageEvents* events);
+int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments, const WavePlan* waves,
+                           uint32_t n_waves, uint32_t max_bounces, const WavefrontState& w,
+                           const WavefrontTuning& tune, int num_sms, cudaStream_t st);
+int launch_image_batch(const JobDesc* d_jobs, const JobPixels* d_pix, uint32_t n_jobs, uint32_t total_pixels,
+                       int num_sms, cudaStream_t st);
 int launch_caustics(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb,
                     const PixelBuffers& px, int num_sms, cudaStream_t st);
 int launch_denoise(const Params& P, const PixelBuffers& px, cudaStream_t st);

@@ -52,9 +52,7 @@ __device__ __forceinline__ float similarity(float4 p, float4 q, float step) {
 __constant__ float c_kernel[3] = {0.375f, 0.25f, 0.0625f};
 
 // prepare (src/shaders.mjs:1974-2021).
-__global__ void k_prepare(DenoiseView v, float4* __restrict__ out) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= v.w || y >= v.h) return;
+__device__ void prepare_at(const DenoiseView& v, uint32_t x, uint32_t y, float4* __restrict__ out) {
     const uint32_t i = y * v.w + x;
     const float n = v.n;
     const float3 light = light_at(v, i);
@@ -85,11 +83,15 @@ __global__ void k_prepare(DenoiseView v, float4* __restrict__ out) {
     }
     out[i] = make_float4(light.x, light.y, light.z, variance);
 }
-
-// atrous (src/shaders.mjs:2023-2086), one pass of the given step.
-__global__ void k_atrous(DenoiseView v, const float4* __restrict__ in, float4* __restrict__ out, int step) {
+__global__ void k_prepare(DenoiseView v, float4* __restrict__ out) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= v.w || y >= v.h) return;
+    prepare_at(v, x, y, out);
+}
+
+// atrous (src/shaders.mjs:2023-2086), one pass of the given step.
+__device__ void atrous_at(const DenoiseView& v, const float4* __restrict__ in, float4* __restrict__ out, int step,
+                          uint32_t x, uint32_t y) {
     const uint32_t i = y * v.w + x;
     const float4 centre = in[i];
     const float4 gp = normal_at(v, i);
@@ -130,15 +132,24 @@ __global__ void k_atrous(DenoiseView v, const float4* __restrict__ in, float4* _
     else
         out[i] = centre;
 }
-
-// compose (src/shaders.mjs:2088-2097).
-__global__ void k_compose(DenoiseView v, const float4* __restrict__ in, float4* __restrict__ out) {
+__global__ void k_atrous(DenoiseView v, const float4* __restrict__ in, float4* __restrict__ out, int step) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= v.w || y >= v.h) return;
+    atrous_at(v, in, out, step, x, y);
+}
+
+// compose (src/shaders.mjs:2088-2097).
+__device__ void compose_at(const DenoiseView& v, const float4* __restrict__ in, float4* __restrict__ out, uint32_t x,
+                           uint32_t y) {
     const uint32_t i = y * v.w + x;
     const float3 a = albedo_at(v, i);
     const float4 l = in[i];
     out[i] = make_float4(l.x * a.x, l.y * a.y, l.z * a.z, 0.0f);
+}
+__global__ void k_compose(DenoiseView v, const float4* __restrict__ in, float4* __restrict__ out) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= v.w || y >= v.h) return;
+    compose_at(v, in, out, x, y);
 }
 
 // Narkowicz's ACES fit and the sRGB OETF (src/shaders.mjs:2115-2122).
@@ -155,10 +166,8 @@ __device__ __forceinline__ uint8_t unorm8(float v) {
 }
 
 // fragment (src/shaders.mjs:2124-2152) into a headless RGBA8 buffer.
-__global__ void k_tonemap(Params P, const float4* __restrict__ accum, const float4* __restrict__ denoised,
-                          uchar4* __restrict__ display) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= P.width || y >= P.height) return;
+__device__ void tonemap_at(const Params& P, const float4* __restrict__ accum, const float4* __restrict__ denoised,
+                           uchar4* __restrict__ display, uint32_t x, uint32_t y) {
     const uint32_t i = y * P.width + x;
     float3 o;
     if (P.total_samples == 0u) {
@@ -182,6 +191,12 @@ __global__ void k_tonemap(Params P, const float4* __restrict__ accum, const floa
         }
     }
     display[i] = make_uchar4(unorm8(o.x), unorm8(o.y), unorm8(o.z), 255);
+}
+__global__ void k_tonemap(Params P, const float4* __restrict__ accum, const float4* __restrict__ denoised,
+                          uchar4* __restrict__ display) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.width || y >= P.height) return;
+    tonemap_at(P, accum, denoised, display, x, y);
 }
 
 }  // namespace
@@ -211,6 +226,69 @@ int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st) {
     return 1;
 }
 
+
+// ---- batched frames: the same passes over many jobs' images in one launch ----
+namespace {
+
+// The job whose pixels hold batch pixel t (segments in pixel order).
+__device__ __forceinline__ uint32_t find_job(const JobPixels* seg, uint32_t n, uint32_t t) {
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) / 2;
+        if (seg[mid].pixel_offset <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ DenoiseView job_view(const JobDesc& jd) {
+    const Params& P = jd.params;
+    return DenoiseView{jd.px.accum, jd.px.guide_albedo, jd.px.guide_normal, P.width, P.height,
+                       float(P.total_samples > 1u ? P.total_samples : 1u)};
+}
+
+// pass: 0 prepare, 1..5 à-trous steps 1..16, 6 compose.
+__global__ void k_denoise_batch(const JobDesc* __restrict__ jobs, const JobPixels* __restrict__ seg, uint32_t n_seg,
+                                uint32_t total, int pass) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const JobPixels g = seg[find_job(seg, n_seg, t)];
+        const JobDesc& jd = jobs[g.job];
+        if (jd.params.denoise == 0u) continue;
+        const DenoiseView v = job_view(jd);
+        const uint32_t i = t - g.pixel_offset;
+        const uint32_t x = i % v.w, y = i / v.w;
+        // prepare fills light a; passes go a→b, b→a, …; compose reads light b (after 5 passes).
+        if (pass == 0) {
+            prepare_at(v, x, y, jd.px.light_a);
+        } else if (pass <= 5) {
+            const bool even = (pass - 1) % 2 == 0;
+            atrous_at(v, even ? jd.px.light_a : jd.px.light_b, even ? jd.px.light_b : jd.px.light_a,
+                      1 << (pass - 1), x, y);
+        } else {
+            compose_at(v, jd.px.light_b, jd.px.denoised, x, y);
+        }
+    }
+}
+
+__global__ void k_tonemap_batch(const JobDesc* __restrict__ jobs, const JobPixels* __restrict__ seg, uint32_t n_seg,
+                                uint32_t total) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const JobPixels g = seg[find_job(seg, n_seg, t)];
+        const JobDesc& jd = jobs[g.job];
+        const uint32_t i = t - g.pixel_offset;
+        tonemap_at(jd.params, jd.px.accum, jd.px.denoised, jd.px.display, i % jd.params.width, i / jd.params.width);
+    }
+}
+
+}  // namespace
+
+int launch_image_batch(const JobDesc* d_jobs, const JobPixels* d_pix, uint32_t n_jobs, uint32_t total_pixels,
+                       int num_sms, cudaStream_t st) {
+    const int grid = num_sms * 8;
+    for (int pass = 0; pass <= 6; ++pass) k_denoise_batch<<<grid, 256, 0, st>>>(d_jobs, d_pix, n_jobs, total_pixels, pass);
+    k_tonemap_batch<<<grid, 256, 0, st>>>(d_jobs, d_pix, n_jobs, total_pixels);
+    return 8;
+}
 
 // ---- Denoising into a caller's buffers without allocating ----
 //

@@ -74,6 +74,29 @@ __device__ __forceinline__ uint32_t load_path(const WavefrontState& w, uint32_t 
 // per-launch fetch counters [4..7] zeroed before each traversal launch.
 enum { C_QUEUE0 = 0, C_QUEUE1 = 1, C_SHADOW = 2, C_FETCH = 4 };
 
+// Where a path's scene and uniforms come from. A single frame has one of
+// each (kernel parameters); a batch looks them up in the job table by the
+// job number kept in the top 11 bits of the path's pixel word.
+struct SingleCtx {
+    Scene s;
+    Params P;
+    __device__ __forceinline__ uint32_t job_of(uint32_t) const { return 0; }
+    __device__ __forceinline__ uint32_t pixel_of(uint32_t word) const { return word; }
+    __device__ __forceinline__ const Scene& scene(uint32_t) const { return s; }
+    __device__ __forceinline__ const Params& params(uint32_t) const { return P; }
+    __device__ __forceinline__ uint32_t job_of_path(const WavefrontState&, uint32_t) const { return 0; }
+};
+struct BatchCtx {
+    const JobDesc* jobs;
+    __device__ __forceinline__ uint32_t job_of(uint32_t word) const { return word >> 21; }
+    __device__ __forceinline__ uint32_t pixel_of(uint32_t word) const { return word & 0x1fffffu; }
+    __device__ __forceinline__ const Scene& scene(uint32_t j) const { return jobs[j].scene; }
+    __device__ __forceinline__ const Params& params(uint32_t j) const { return jobs[j].params; }
+    __device__ __forceinline__ uint32_t job_of_path(const WavefrontState& w, uint32_t path) const {
+        return reinterpret_cast<const uint4*>(w.s[7])[path].w >> 21;
+    }
+};
+
 // ---- generate: main()'s per-sample start for a batch of samples ----
 // first_sample counts from the frame's first sample (path_begin adds
 // sample_offset).
@@ -164,7 +187,8 @@ __device__ __forceinline__ bool trav_step(const Scene& s, Traversal& tr, Travers
 }
 
 // ---- extend: closest hits for every path in the queue ----
-__global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Scene s, WavefrontState w, int q, int steps) {
+template <typename Ctx>
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Ctx ctx, WavefrontState w, int q, int steps) {
     __shared__ uint32_t stack[STACK_SHARED * WF_BLOCK];
     TraversalStack<STACK_SHARED> st;
     st.col = stack + threadIdx.x;
@@ -173,7 +197,7 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Scene s, WavefrontState 
     const uint32_t n = w.counters[C_QUEUE0 + q];
     uint32_t* fetch = w.counters + C_FETCH + 0;
     Traversal tr;
-    uint32_t path = 0;
+    uint32_t path = 0, job = 0;
     bool active = false, exhausted = false;
     for (;;) {
         // Lanes without a ray claim the next queue entries together.
@@ -188,8 +212,9 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Scene s, WavefrontState 
                 const uint32_t idx = base + __popc(mask & lanemask_lt());
                 if (idx < n) {
                     path = queue[idx];
+                    job = ctx.job_of_path(w, path);
                     const float4 a = w.s[0][path], b = w.s[1][path];
-                    active = trav_begin(s, tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), INF);
+                    active = trav_begin(ctx.scene(job), tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), INF);
                     if (!active) w.hit[path] = make_float4(INF, __uint_as_float(NONE), 0.0f, 0.0f);
                 } else {
                     exhausted = true;
@@ -197,18 +222,21 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Scene s, WavefrontState 
             }
         }
         if (!__any_sync(FULL, active || !exhausted)) return;
-        for (int k = 0; k < steps && active; ++k) {
-            if (!trav_step<false>(s, tr, st)) {
-                w.hit[path] = make_float4(tr.t, __uint_as_float(tr.prim), tr.u, tr.v);
-                active = false;
+        if (active) {
+            const Scene& sc = ctx.scene(job);
+            for (int k = 0; k < steps && active; ++k) {
+                if (!trav_step<false>(sc, tr, st)) {
+                    w.hit[path] = make_float4(tr.t, __uint_as_float(tr.prim), tr.u, tr.v);
+                    active = false;
+                }
             }
         }
     }
 }
 
 // ---- shade: one bounce of radiance() per live path ----
-template <uint32_t FEAT>
-__global__ void __launch_bounds__(WF_BLOCK) k_wf_shade(Scene s, Params P, WavefrontState w, int q) {
+template <uint32_t FEAT, typename Ctx>
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_shade(Ctx ctx, WavefrontState w, int q) {
     const uint32_t n = w.counters[C_QUEUE0 + q];
     const uint32_t* queue = w.queue[q];
     uint32_t* out_queue = w.queue[q ^ 1];
@@ -222,16 +250,17 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shade(Scene s, Params P, Wavefr
         bool more = false, has_shadow = false;
         ShadowRay sh;
         sh.valid = false;
-        uint32_t path = 0;
+        uint32_t path = 0, job = 0;
         if (idx < n) {
             path = queue[idx];
             PathState ps;
-            const uint32_t pixel = load_path(w, path, ps);
+            const uint32_t word = load_path(w, path, ps);
+            job = ctx.job_of(word);
             const float4 hv = w.hit[path];
             const Hit hit{hv.x, __float_as_uint(hv.y), hv.z, hv.w};
-            more = path_step<FEAT>(s, P, ps, hit, sh);
+            more = path_step<FEAT>(ctx.scene(job), ctx.params(job), ps, hit, sh);
             has_shadow = sh.valid;
-            store_path(w, path, ps, pixel);
+            store_path(w, path, ps, word);
         }
         const uint32_t slot = push_slot(out_count, more);
         if (more) out_queue[slot] = path;
@@ -239,13 +268,15 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shade(Scene s, Params P, Wavefr
         if (has_shadow) {
             w.shadow[sslot * 3 + 0] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.reach);
             w.shadow[sslot * 3 + 1] = make_float4(sh.d.x, sh.d.y, sh.d.z, __uint_as_float(path));
-            w.shadow[sslot * 3 + 2] = make_float4(sh.contribution.x, sh.contribution.y, sh.contribution.z, 0.0f);
+            w.shadow[sslot * 3 + 2] =
+                make_float4(sh.contribution.x, sh.contribution.y, sh.contribution.z, __uint_as_float(job));
         }
     }
 }
 
 // ---- shadow: any-hit occlusion; unoccluded rays add their light ----
-__global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Scene s, WavefrontState w, int steps) {
+template <typename Ctx>
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState w, int steps) {
     __shared__ uint32_t stack[STACK_SHARED * WF_BLOCK];
     TraversalStack<STACK_SHARED> st;
     st.col = stack + threadIdx.x;
@@ -253,7 +284,7 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Scene s, WavefrontState 
     const uint32_t n = w.counters[C_SHADOW];
     uint32_t* fetch = w.counters + C_FETCH + 1;
     Traversal tr;
-    uint32_t rec = 0;
+    uint32_t rec = 0, job = 0;
     bool active = false, exhausted = false;
     for (;;) {
         const bool need = !active && !exhausted;
@@ -268,7 +299,8 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Scene s, WavefrontState 
                 if (idx < n) {
                     rec = idx;
                     const float4 a = w.shadow[idx * 3], b = w.shadow[idx * 3 + 1];
-                    active = trav_begin(s, tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w);
+                    job = __float_as_uint(w.shadow[idx * 3 + 2].w);
+                    active = trav_begin(ctx.scene(job), tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w);
                     if (!active) {
                         // Misses the scene's box: unoccluded.
                         const uint32_t path = __float_as_uint(b.w);
@@ -282,14 +314,17 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Scene s, WavefrontState 
             }
         }
         if (!__any_sync(FULL, active || !exhausted)) return;
-        for (int k = 0; k < steps && active; ++k) {
-            if (!trav_step<true>(s, tr, st)) {
-                active = false;
-                if (tr.prim == NONE) {
-                    const uint32_t path = __float_as_uint(w.shadow[rec * 3 + 1].w);
-                    const float4 c = w.shadow[rec * 3 + 2];
-                    float4 r = w.s[3][path];
-                    w.s[3][path] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, r.w);
+        if (active) {
+            const Scene& sc = ctx.scene(job);
+            for (int k = 0; k < steps && active; ++k) {
+                if (!trav_step<true>(sc, tr, st)) {
+                    active = false;
+                    if (tr.prim == NONE) {
+                        const uint32_t path = __float_as_uint(w.shadow[rec * 3 + 1].w);
+                        const float4 c = w.shadow[rec * 3 + 2];
+                        float4 r = w.s[3][path];
+                        w.s[3][path] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, r.w);
+                    }
                 }
             }
         }
@@ -358,6 +393,7 @@ template <uint32_t FEAT>
 int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, const PixelBuffers& px,
                     const WavefrontTuning& tune, int num_sms, cudaStream_t st, StageEvents* events) {
     StageTimer timer{events, st};
+    const SingleCtx ctx{s, P};
     const uint32_t pixels = P.width * P.height;
     const uint32_t batch = uint32_t(w.capacity / pixels) > 0 ? uint32_t(w.capacity / pixels) : 1u;
     const int grid_trav = num_sms * tune.traversal_blocks_per_sm;
@@ -372,16 +408,16 @@ int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, co
         for (uint32_t depth = 0; depth <= P.max_bounces; ++depth) {
             cudaMemsetAsync(w.counters + C_FETCH, 0, 4 * sizeof(uint32_t), st);
             timer.begin(0);
-            k_wf_extend<<<grid_trav, WF_BLOCK, 0, st>>>(s, w, q, tune.steps);
+            k_wf_extend<SingleCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
             timer.end();
             // The next queue and the shadow queue start empty.
             cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
             cudaMemsetAsync(w.counters + C_SHADOW, 0, sizeof(uint32_t), st);
             timer.begin(1);
-            k_wf_shade<FEAT><<<grid_shade, WF_BLOCK, 0, st>>>(s, P, w, q);
+            k_wf_shade<FEAT, SingleCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q);
             timer.end();
             timer.begin(2);
-            k_wf_shadow<<<grid_trav, WF_BLOCK, 0, st>>>(s, w, tune.steps);
+            k_wf_shadow<SingleCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, tune.steps);
             timer.end();
             launches += 3;
             q ^= 1;
@@ -392,6 +428,120 @@ int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, co
     return launches;
 }
 
+
+// ---- batched frames: many renderers' jobs through one path pool ----
+
+// The segment holding wave path p (segments are in path order).
+__device__ __forceinline__ uint32_t find_segment(const WaveSegment* seg, uint32_t n_seg, uint32_t p, bool by_pixel) {
+    uint32_t lo = 0, hi = n_seg - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) / 2;
+        const uint32_t start = by_pixel ? seg[mid].pixel_offset : seg[mid].path_offset;
+        if (start <= p) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(WF_BLOCK) k_wfb_generate(const JobDesc* __restrict__ jobs,
+                                                           const WaveSegment* __restrict__ seg, uint32_t n_seg,
+                                                           WavefrontState w, uint32_t n_paths) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_paths; p += gridDim.x * blockDim.x) {
+        const WaveSegment g = seg[find_segment(seg, n_seg, p, false)];
+        const JobDesc& jd = jobs[g.job];
+        const uint32_t local = p - g.path_offset;
+        const uint32_t pixel = local % g.pixels;
+        const uint32_t k = g.k0 + local / g.pixels;
+        PathState ps;
+        path_begin(jd.params, jd.scene.seed_hash, pixel % jd.params.width, pixel / jd.params.width, k, ps);
+        store_path(w, p, ps, (g.job << 21) | pixel);
+        w.queue[0][p] = p;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        w.counters[C_QUEUE0] = n_paths;
+        w.counters[C_QUEUE1] = 0;
+        w.counters[C_SHADOW] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(WF_BLOCK) k_wfb_finalize(const JobDesc* __restrict__ jobs,
+                                                           const WaveSegment* __restrict__ seg, uint32_t n_seg,
+                                                           WavefrontState w, uint32_t n_pixels) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_pixels; t += gridDim.x * blockDim.x) {
+        const WaveSegment g = seg[find_segment(seg, n_seg, t, true)];
+        const JobDesc& jd = jobs[g.job];
+        const Params& P = jd.params;
+        const uint32_t pixel = t - g.pixel_offset;
+        float4 sum = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float3 sa = f3(0.0f);
+        float4 sn = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (uint32_t k = 0; k < g.nk; ++k) {
+            const uint32_t p = g.path_offset + k * g.pixels + pixel;
+            const float4 rr = w.s[3][p];
+            float3 c = f3(rr.x, rr.y, rr.z);
+            const float peak = maxc(c);
+            if (P.firefly_clamp > 0.0f && peak > P.firefly_clamp) c *= P.firefly_clamp / peak;
+            const float4 ga = w.s[5][p];
+            const float4 gn = w.s[6][p];
+            if (finite3(c) && finite3(f3(ga.x, ga.y, ga.z)) && finite3(f3(gn.x, gn.y, gn.z)) && finite1(gn.w)) {
+                const float l = luminance(c);
+                sum.x += c.x;
+                sum.y += c.y;
+                sum.z += c.z;
+                sum.w += l * l;
+                sa += f3(ga.x, ga.y, ga.z);
+                sn.x += gn.x;
+                sn.y += gn.y;
+                sn.z += gn.z;
+                sn.w += gn.w;
+            }
+        }
+        const PixelBuffers& px = jd.px;
+        if (P.sample_offset == 0u && g.k0 == 0u) {
+            px.accum[pixel] = sum;
+            px.guide_albedo[pixel] = make_float4(sa.x, sa.y, sa.z, 0.0f);
+            px.guide_normal[pixel] = sn;
+        } else {
+            const float4 a = px.accum[pixel], ga2 = px.guide_albedo[pixel], nn = px.guide_normal[pixel];
+            px.accum[pixel] = make_float4(a.x + sum.x, a.y + sum.y, a.z + sum.z, a.w + sum.w);
+            px.guide_albedo[pixel] = make_float4(ga2.x + sa.x, ga2.y + sa.y, ga2.z + sa.z, ga2.w);
+            px.guide_normal[pixel] = make_float4(nn.x + sn.x, nn.y + sn.y, nn.z + sn.z, nn.w + sn.w);
+        }
+    }
+}
+
+}  // namespace
+
+int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments, const WavePlan* waves,
+                           uint32_t n_waves, uint32_t max_bounces, const WavefrontState& w,
+                           const WavefrontTuning& tune, int num_sms, cudaStream_t st) {
+    const BatchCtx ctx{d_jobs};
+    const int grid_trav = num_sms * tune.traversal_blocks_per_sm;
+    const int grid_shade = num_sms * tune.shade_blocks_per_sm;
+    int launches = 0;
+    for (uint32_t v = 0; v < n_waves; ++v) {
+        const WavePlan& wp = waves[v];
+        const WaveSegment* seg = d_segments + wp.first_segment;
+        k_wfb_generate<<<grid_shade, WF_BLOCK, 0, st>>>(d_jobs, seg, wp.segments, w, wp.paths);
+        ++launches;
+        int q = 0;
+        for (uint32_t depth = 0; depth <= max_bounces; ++depth) {
+            cudaMemsetAsync(w.counters + C_FETCH, 0, 4 * sizeof(uint32_t), st);
+            k_wf_extend<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
+            cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
+            cudaMemsetAsync(w.counters + C_SHADOW, 0, sizeof(uint32_t), st);
+            k_wf_shade<15u, BatchCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q);
+            k_wf_shadow<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, tune.steps);
+            launches += 3;
+            q ^= 1;
+        }
+        k_wfb_finalize<<<grid_shade, WF_BLOCK, 0, st>>>(d_jobs, seg, wp.segments, w, wp.pixels);
+        ++launches;
+    }
+    return launches;
+}
+
+namespace {
 }  // namespace
 
 int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,

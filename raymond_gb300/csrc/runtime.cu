@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <algorithm>
 #include <vector>
 
 #include "../../include/raymond.h"
@@ -74,6 +75,19 @@ struct raymond {
     uint32_t photon_table = 0, photon_capacity_alloc = 0;
     uint32_t photons_override = 0, photon_capacity = 524288;
     float photon_radius_override = 0.0f;
+
+    // Batched frames (this handle as executor): job table, wave plan, graph.
+    DevBuf b_jobs, b_segments, b_jobpix;
+    JobDesc* b_staging = nullptr;  // pinned host copy of the job table
+    uint32_t b_staging_cap = 0;
+    cudaEvent_t b_copy_done = nullptr;
+    bool b_copy_pending = false;
+    std::vector<WavePlan> b_waves;
+    std::vector<uint64_t> b_signature;
+    uint32_t b_max_bounces = 0, b_total_pixels = 0, b_n = 0;
+    uint64_t b_paths = 0;
+    cudaGraphExec_t b_graph = nullptr;
+    int b_graph_launches = 0;  // kernels in the captured frame
     uint32_t path_choice = RAYMOND_PATH_WAVEFRONT;
 
     bool rendered = false;
@@ -261,6 +275,10 @@ void raymond_destroy(raymond_t* h) {
     for (DevBuf& b : h->wf_state) b.release();
     for (cudaEvent_t ev : h->ev)
         if (ev) cudaEventDestroy(ev);
+    if (h->b_graph) cudaGraphExecDestroy(h->b_graph);
+    if (h->b_copy_done) cudaEventDestroy(h->b_copy_done);
+    if (h->b_staging) cudaFreeHost(h->b_staging);
+    for (DevBuf* b : {&h->b_jobs, &h->b_segments, &h->b_jobpix}) b->release();
     for (cudaEvent_t ev : h->stage_begin) cudaEventDestroy(ev);
     for (cudaEvent_t ev : h->stage_end) cudaEventDestroy(ev);
     cudaStreamDestroy(h->stream);
@@ -505,6 +523,191 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
     h->stats = raymond_stats{};
     h->stats.launches = uint64_t(launches);
     h->stats.paths = uint64_t(P.width) * P.height * P.samples_per_frame;
+    return RAYMOND_OK;
+}
+
+int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint32_t flags) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!jobs || n == 0 || n > 2048) return h->fail(RAYMOND_EINVAL, "A batch needs 1 to 2048 jobs.");
+    cudaSetDevice(h->device);
+    std::vector<JobDesc> desc(n);
+    std::vector<uint64_t> sig;
+    sig.reserve(4 * size_t(n) + 2);
+    sig.push_back(n);
+    uint64_t total_paths = 0, total_pixels = 0, max_pixels = 0;
+    uint32_t max_bounces = 0;
+    for (uint32_t j = 0; j < n; ++j) {
+        raymond* r = jobs[j].renderer;
+        if (!r || !jobs[j].params208) return h->fail(RAYMOND_EINVAL, "Job %u has no renderer or parameters.", j);
+        if (r->device != h->device) return h->fail(RAYMOND_EINVAL, "Job %u is on another device.", j);
+        if (!r->has_scene || r->capacity == 0) return h->fail(RAYMOND_ESTATE, "Job %u has no scene or image.", j);
+        Params P;
+        std::memcpy(&P, jobs[j].params208, sizeof P);
+        if (P.width != r->width || P.height != r->height)
+            return h->fail(RAYMOND_ESTATE, "Job %u's parameters don't match its image size.", j);
+        if (P.light_count != r->light_count || P.volume_count != r->volume_count)
+            return h->fail(RAYMOND_EINVAL, "Job %u's light or volume counts don't match its scene.", j);
+        if (P.samples_per_frame == 0 || P.max_bounces > 64 || P.view != VIEW_COLOR)
+            return h->fail(RAYMOND_EINVAL, "Job %u: batches render colour frames of 1+ samples, 64 bounces at most.", j);
+        const uint64_t pixels = uint64_t(P.width) * P.height;
+        if (pixels >= (1u << 21)) return h->fail(RAYMOND_ECAPACITY, "Job %u has more than 2^21 pixels.", j);
+        P.caustics = 0;  // no light tracing in a batch: the path tracer keeps every path
+        desc[j].scene = r->scene_view();
+        desc[j].params = P;
+        desc[j].px = r->pixel_view();
+        total_paths += pixels * P.samples_per_frame;
+        total_pixels += pixels;
+        if (pixels > max_pixels) max_pixels = pixels;
+        if (P.max_bounces > max_bounces) max_bounces = P.max_bounces;
+        sig.push_back(reinterpret_cast<uintptr_t>(r));
+        sig.push_back(pixels);
+        sig.push_back(P.samples_per_frame);
+        sig.push_back(P.max_bounces | (uint64_t(P.width) << 32));
+    }
+    if (total_pixels > 0xffffffffull) return h->fail(RAYMOND_ECAPACITY, "The batch has too many pixels.");
+
+    // Path pool: the whole frame if memory allows, else waves of whole samples.
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const uint64_t per_path = 8 * 16 + 16 + 8 + 48;
+    uint64_t cap = uint64_t(double(free_b) * 0.5) / per_path;
+    if (h->path_capacity_limit) cap = std::min<uint64_t>(cap, h->path_capacity_limit);
+    cap = std::min<uint64_t>(cap, total_paths);
+    cap = std::min<uint64_t>(cap, 0x7fffffffull);
+    if (cap < max_pixels) cap = max_pixels;
+    sig.push_back(cap);
+
+    if (sig != h->b_signature) {
+        if (h->b_graph) {
+            cudaGraphExecDestroy(h->b_graph);
+            h->b_graph = nullptr;
+        }
+        // Plan: each job's samples in order, packed into waves of `cap` paths.
+        std::vector<WaveSegment> segs;
+        std::vector<WavePlan> waves;
+        WavePlan cur{0, 0, 0, 0};
+        for (uint32_t j = 0; j < n; ++j) {
+            const uint32_t pixels = desc[j].params.width * desc[j].params.height;
+            uint32_t k = 0;
+            while (k < desc[j].params.samples_per_frame) {
+                const uint64_t room = (cap - cur.paths) / pixels;
+                if (room == 0) {
+                    waves.push_back(cur);
+                    cur = WavePlan{uint32_t(segs.size()), 0, 0, 0};
+                    continue;
+                }
+                const uint32_t nk = uint32_t(std::min<uint64_t>(desc[j].params.samples_per_frame - k, room));
+                segs.push_back(WaveSegment{j, k, nk, pixels, cur.paths, cur.pixels});
+                cur.segments++;
+                cur.paths += nk * pixels;
+                cur.pixels += pixels;
+                k += nk;
+            }
+        }
+        if (cur.segments) waves.push_back(cur);
+        std::vector<JobPixels> jp(n);
+        uint32_t off = 0;
+        for (uint32_t j = 0; j < n; ++j) {
+            jp[j] = JobPixels{j, off};
+            off += desc[j].params.width * desc[j].params.height;
+        }
+        cudaError_t e = h->b_segments.reserve(segs.size() * sizeof(WaveSegment));
+        if (e == cudaSuccess) e = h->b_jobpix.reserve(n * sizeof(JobPixels));
+        if (e == cudaSuccess) e = h->b_jobs.reserve(n * sizeof(JobDesc));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(h->b_segments.ptr, segs.data(), segs.size() * sizeof(WaveSegment), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(h->b_jobpix.ptr, jp.data(), n * sizeof(JobPixels), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return h->cuda_fail(e, "batch plan");
+        // The pool, as for a single frame of `cap` paths.
+        if (cap > h->wf_capacity) {
+            for (DevBuf& b : h->wf_state)
+                if (e == cudaSuccess) e = b.reserve(cap * 16);
+            if (e == cudaSuccess) e = h->wf_hit.reserve(cap * 16);
+            if (e == cudaSuccess) e = h->wf_queue[0].reserve(cap * 4);
+            if (e == cudaSuccess) e = h->wf_queue[1].reserve(cap * 4);
+            if (e == cudaSuccess) e = h->wf_shadow.reserve(cap * 48);
+            if (e == cudaSuccess) e = h->wf_counters.reserve(64);
+            if (e != cudaSuccess) return h->cuda_fail(e, "batch path pool");
+            h->wf_capacity = cap;
+        }
+        if (n > h->b_staging_cap) {
+            if (h->b_staging) cudaFreeHost(h->b_staging);
+            h->b_staging = nullptr;
+            if ((e = cudaMallocHost(&h->b_staging, n * sizeof(JobDesc))) != cudaSuccess)
+                return h->cuda_fail(e, "batch staging");
+            h->b_staging_cap = n;
+        }
+        if (!h->b_copy_done) cudaEventCreateWithFlags(&h->b_copy_done, cudaEventDisableTiming);
+        h->b_waves = waves;
+        h->b_signature = sig;
+        h->b_max_bounces = max_bounces;
+        h->b_total_pixels = uint32_t(total_pixels);
+        h->b_n = n;
+        h->b_paths = total_paths;
+    }
+
+    // This frame's job table: the previous frame's copy must have left the staging buffer.
+    if (h->b_copy_pending) cudaEventSynchronize(h->b_copy_done);
+    std::memcpy(h->b_staging, desc.data(), n * sizeof(JobDesc));
+    cudaError_t e = cudaMemcpyAsync(h->b_jobs.ptr, h->b_staging, n * sizeof(JobDesc), cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "batch job table");
+    cudaEventRecord(h->b_copy_done, h->stream);
+    h->b_copy_pending = true;
+
+    WavefrontState w{};
+    for (int k = 0; k < 8; ++k) w.s[k] = static_cast<float4*>(h->wf_state[k].ptr);
+    w.hit = static_cast<float4*>(h->wf_hit.ptr);
+    w.queue[0] = static_cast<uint32_t*>(h->wf_queue[0].ptr);
+    w.queue[1] = static_cast<uint32_t*>(h->wf_queue[1].ptr);
+    w.shadow = static_cast<float4*>(h->wf_shadow.ptr);
+    w.counters = static_cast<uint32_t*>(h->wf_counters.ptr);
+    w.capacity = h->wf_capacity;
+    const JobDesc* d_jobs = static_cast<const JobDesc*>(h->b_jobs.ptr);
+    const WaveSegment* d_segs = static_cast<const WaveSegment*>(h->b_segments.ptr);
+    const JobPixels* d_pix = static_cast<const JobPixels*>(h->b_jobpix.ptr);
+    auto enqueue = [&]() {
+        int launches = launch_wavefront_batch(d_jobs, d_segs, h->b_waves.data(), uint32_t(h->b_waves.size()),
+                                              h->b_max_bounces, w, h->tuning, h->num_sms, h->stream);
+        launches += launch_image_batch(d_jobs, d_pix, h->b_n, h->b_total_pixels, h->num_sms, h->stream);
+        return launches;
+    };
+    int launches = 0;
+    cudaEventRecord(h->ev[0], h->stream);
+    if (flags & RAYMOND_BATCH_GRAPH) {
+        if (!h->b_graph) {
+            cudaGraph_t graph = nullptr;
+            e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return h->cuda_fail(e, "batch capture");
+            h->b_graph_launches = enqueue();
+            e = cudaStreamEndCapture(h->stream, &graph);
+            if (e != cudaSuccess) return h->cuda_fail(e, "batch capture");
+            e = cudaGraphInstantiate(&h->b_graph, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                h->b_graph = nullptr;
+                return h->cuda_fail(e, "batch graph");
+            }
+        }
+        e = cudaGraphLaunch(h->b_graph, h->stream);
+        if (e != cudaSuccess) return h->cuda_fail(e, "batch graph launch");
+        launches = h->b_graph_launches;
+    } else {
+        launches = enqueue();
+    }
+    cudaEventRecord(h->ev[1], h->stream);
+    for (int k = 2; k < 5; ++k) cudaEventRecord(h->ev[k], h->stream);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return h->cuda_fail(e, "batch");
+    h->ev_valid = true;
+    h->stage.count = 0;
+    for (uint32_t j = 0; j < n; ++j) {
+        raymond* r = jobs[j].renderer;
+        r->last_params = desc[j].params;
+        r->rendered = true;
+    }
+    h->stats = raymond_stats{};
+    h->stats.launches = uint64_t(launches);
+    h->stats.paths = h->b_paths;
     return RAYMOND_OK;
 }
 

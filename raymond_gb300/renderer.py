@@ -276,6 +276,7 @@ class Renderer:
         self._height = 0
         self._resized = False
         self._disposed = False
+        self._batch = None  # the BatchRenderer that rendered its last frame, if any
         self.flags = 0  # extra raymond_render flags (path choice)
 
     @staticmethod
@@ -506,6 +507,8 @@ class Renderer:
 
     def readPixels(self, denoised=False) -> np.ndarray:
         """The average so far, w×h×4 float32 from the top left (src/Renderer.mjs:502-528)."""
+        if self._batch is not None:
+            self._batch.sync()
         if not self._resized or self._samples == 0:
             raise RuntimeError("Nothing has been rendered yet.")
         if denoised and not self._denoising():
@@ -516,6 +519,8 @@ class Renderer:
 
     def readGuides(self):
         """The raw per-pixel sums: accum, guide albedo, guide normal (each h×w×4 float32)."""
+        if self._batch is not None:
+            self._batch.sync()
         shape = (self._height, self._width, 4)
         a, g, n = (np.empty(shape, dtype=np.float32) for _ in range(3))
         check(lib().raymond_read_guides(self._h, ptr(a), ptr(g), ptr(n), a.nbytes), self._h)
@@ -633,3 +638,47 @@ class Renderer:
     @property
     def handle(self):
         return self._h
+
+
+class BatchRenderer:
+    """Renders a frame of many renderers in one pass (raymond_render_batch):
+    their paths share one wavefront pool and the frame replays as one CUDA
+    graph while the set of images, sample counts and bounces stays the same.
+    Each renderer keeps its own scene, image and progressive average."""
+
+    def __init__(self, device=0, graph=True, pathCapacity=0):
+        self._exec = Renderer.create(Canvas(1, 1), device=device, pathCapacity=pathCapacity)
+        self.graph = graph
+
+    def render(self, renderers):
+        n = len(renderers)
+        jobs = (_native.Job * n)()
+        keep = []
+        for i, r in enumerate(renderers):
+            if r.scene is None or r.camera is None:
+                raise ValueError("Every renderer in a batch needs a scene and a camera.")
+            r.caustics = False
+            features = r._prepare()
+            buf = (ctypes.c_char * PARAMS_BYTES).from_buffer(r._params)
+            keep.append(buf)
+            jobs[i] = _native.Job(r.handle, ctypes.addressof(buf), features)
+        check(lib().raymond_render_batch(self._exec.handle, jobs, n, _native.BATCH_GRAPH if self.graph else 0),
+              self._exec.handle)
+        for r in renderers:
+            r._samples += r._spp
+            r._batch = self
+
+    def sync(self):
+        check(lib().raymond_sync(self._exec.handle), self._exec.handle)
+
+    @property
+    def handle(self):
+        return self._exec.handle
+
+    def stats(self):
+        st = _native.Stats()
+        check(lib().raymond_get_stats(self._exec.handle, ctypes.byref(st)), self._exec.handle)
+        return st
+
+    def dispose(self):
+        self._exec.dispose()

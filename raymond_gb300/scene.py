@@ -14,7 +14,7 @@ from . import _native
 from .geometry import Box, Mesh, Quad, Sphere
 from .material import MATERIAL_TYPES
 from .sky import Sky
-from .vec import Vec3
+from .vec import Mat4, Vec3
 
 PRIMITIVE_KINDS = {"sphere": 0, "quad": 1, "box": 2, "triangle": 3}
 NONE = 0xFFFFFFFF
@@ -144,10 +144,40 @@ def pack_objects(objects) -> PackedScene:
 
     # Per object: records (n,16) float32 with header words, bounds (n,3)×2 in double, blocks or None.
     rec_parts, min_parts, max_parts, block_parts, has_block_parts, owner_parts = [], [], [], [], [], []
+    # Materials are numbered in object order, as the reference meets them.
+    mat_ids = [material_of(o.material) for o in objects]
+    # Unrotated spheres pack in bulk (their globe axes are x and y); records
+    # are put back in object order below.
+    identity = Mat4.identity().v
+    bulk = [oi for oi, o in enumerate(objects) if type(o) is Sphere and o.rotation.v == identity]
+    bulk_set = set(bulk)
+    if bulk:
+        n = len(bulk)
+        cr = np.array([(objects[i].center.x, objects[i].center.y, objects[i].center.z, objects[i].radius)
+                       for i in bulk], dtype=np.float64)
+        mats = np.array([mat_ids[i] for i in bulk], dtype=np.uint32)
+        rec = np.zeros((n, 16), dtype=np.float32)
+        rec[:, 4:8] = cr
+        rec[:, 8] = 1.0   # globe x axis
+        rec[:, 13] = 1.0  # north pole
+        hdr = rec.view(np.uint32)
+        hdr[:, 0] = PRIMITIVE_KINDS["sphere"]
+        hdr[:, 1] = mats
+        hdr[:, 2] = NONE
+        hdr[:, 3] = NONE
+        mn, mx = _pad_bounds(cr[:, :3] - cr[:, 3:4], cr[:, :3] + cr[:, 3:4])
+        rec_parts.append(rec)
+        min_parts.append(mn)
+        max_parts.append(mx)
+        block_parts.append(np.zeros((n, 16), dtype=np.float32))
+        has_block_parts.append(np.zeros(n, dtype=bool))
+        owner_parts.append(np.array(bulk, dtype=np.int64))
     for oi, obj in enumerate(objects):
+        if oi in bulk_set:
+            continue
         if obj.material.type == "volume" and not isinstance(obj, (Sphere, Box)):
             raise TypeError("A volume must be a Sphere or a Box.")
-        mat = material_of(obj.material)
+        mat = mat_ids[oi]
         if isinstance(obj, Mesh):
             tri = obj.indices.reshape(-1, 3).astype(np.int64)
             n = len(tri)
@@ -218,6 +248,10 @@ def pack_objects(objects) -> PackedScene:
         blocks = np.concatenate(block_parts)
         has_block = np.concatenate(has_block_parts)
         owners = np.concatenate(owner_parts)
+        if bulk:
+            order = np.argsort(owners, kind="stable")
+            records, mins_all, maxs_all = records[order], mins_all[order], maxs_all[order]
+            blocks, has_block, owners = blocks[order], has_block[order], owners[order]
     else:
         records = np.zeros((0, 16), dtype=np.float32)
         mins_all = maxs_all = np.zeros((0, 3))
