@@ -313,6 +313,68 @@ def run_ours(args, rank, world, local):
     return result
 
 
+def run_batch(args):
+    """The batched workload: 64 seeded sphere-field instances rendered as
+    one graph-replayed batched frame, against the same renderers rendering
+    one at a time. Metric: Mpaths/s over the whole batch."""
+    import torch
+
+    import raymond_gb300 as rg
+    from raymond_gb300 import scenes
+
+    t0 = time.perf_counter()
+    inst = scenes.batch_instances(args.batch, spheres=args.batch_spheres)
+    rs = []
+    for scene, camera, w, h, spp, info in inst:
+        r = rg.Renderer.create(rg.Canvas(w, h))
+        r.scene, r.camera = scene, camera
+        r.maxBounces = args.bounces
+        r.samplesPerFrame = spp
+        r.caustics = False
+        rs.append(r)
+    setup_s = time.perf_counter() - t0
+    paths = sum(w * h * spp for _, _, w, h, spp, _ in inst)
+    # One at a time (each renderer's own frame, tuned path).
+    for r in rs:
+        r.render()
+    torch.cuda.synchronize()
+    for r in rs:
+        r.device.queue.onSubmittedWorkDone()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for r in rs:
+            r.render()
+        for r in rs:
+            r.device.queue.onSubmittedWorkDone()
+    single_s = (time.perf_counter() - t0) / args.steps
+    batch = rg.BatchRenderer(graph=True)
+    for _ in range(args.warmup):
+        batch.render(rs)
+    batch.sync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batch.render(rs)
+    batch.sync()
+    batch_s = (time.perf_counter() - t0) / args.steps
+    st = batch.stats()
+    out = {
+        "metric": METRIC, "value": paths / batch_s / 1e6, "unit": "Mpaths/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": batch_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32 scenes)",
+        "config": {"workload": f"batch of {len(rs)} sphere-field instances, one graph-replayed launch per frame",
+                   "paths_per_frame": paths, "triangles": [i[5]["triangles"] for i in inst],
+                   "resolutions": [f"{i[2]}x{i[3]}" for i in inst], "spp": [i[4] for i in inst],
+                   "bounces": args.bounces, "setup_s": setup_s},
+        "one_at_a_time": {"value": paths / single_s / 1e6, "unit": "Mpaths/s", "ms_per_step": single_s * 1e3},
+        "speedup_vs_one_at_a_time": single_s / batch_s,
+        "gpu_launches": int(st.launches) * args.steps,
+    }
+    for r in rs:
+        r.dispose()
+    batch.dispose()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -323,6 +385,9 @@ def main():
     ap.add_argument("--bounces", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", default="auto", choices=["auto", "megakernel", "wavefront"])
+    ap.add_argument("--workload", default="field", choices=["field", "batch"])
+    ap.add_argument("--batch", type=int, default=64)
+    ap.add_argument("--batch-spheres", type=int, default=10000)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1 and args.impl == "ours":
@@ -331,6 +396,8 @@ def main():
         torch.distributed.init_process_group("nccl")
     if args.impl == "reference":
         out = run_reference(args, rank, world)
+    elif args.workload == "batch":
+        out = run_batch(args) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, local)
     if rank == 0 and out is not None:

@@ -12,8 +12,20 @@ namespace rmd {
 
 constexpr uint32_t F_VOLUMES = 1u, F_TEXTURES = 2u, F_ENVIRONMENT = 4u, F_DISPERSION = 8u;
 
-// sRGB-encoded byte to linear, filled once per device by the host.
-__constant__ float c_srgb_to_linear[256];
+// sRGB-encoded byte to linear. Without relocatable device code every
+// translation unit that includes this header has its own copy, so each one
+// fills its own through upload_srgb_table_here() (called by the host at
+// start-up, once per device, through that unit's exported uploader).
+static __constant__ float c_srgb_to_linear[256];
+
+static inline cudaError_t upload_srgb_table_here() {
+    float table[256];
+    for (int i = 0; i < 256; ++i) {
+        const double c = i / 255.0;
+        table[i] = float(c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4));
+    }
+    return cudaMemcpyToSymbol(c_srgb_to_linear, table, sizeof table);
+}
 
 struct Material {
     float3 color;

@@ -102,7 +102,10 @@ int launch_caustics(const Scene& s, const Params& P, uint32_t features, const Ca
                     const PixelBuffers& px, int num_sms, cudaStream_t st);
 int launch_denoise(const Params& P, const PixelBuffers& px, cudaStream_t st);
 int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st);
-void upload_srgb_table();
+// Fill each kernel unit's sRGB decode table on the current device.
+cudaError_t upload_srgb_table_trace();
+cudaError_t upload_srgb_table_wavefront();
+cudaError_t upload_srgb_table_caustics();
 // The message raymond_last_error(NULL) returns, for calls that have no handle.
 void set_handleless_error(const char* msg);
 

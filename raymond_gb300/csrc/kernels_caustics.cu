@@ -312,6 +312,8 @@ int caustics_frame(const Scene& s, const Params& P, const CausticBuffers& cb, co
 
 }  // namespace
 
+cudaError_t upload_srgb_table_caustics() { return upload_srgb_table_here(); }
+
 int launch_caustics(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb,
                     const PixelBuffers& px, int num_sms, cudaStream_t st) {
     switch (features & 15u) {

@@ -140,13 +140,6 @@ int launch_megakernel(const Scene& s, const Params& P, uint32_t features, const 
     return 1;
 }
 
-void upload_srgb_table() {
-    float table[256];
-    for (int i = 0; i < 256; ++i) {
-        const double c = i / 255.0;
-        table[i] = float(c <= 0.04045 ? c / 12.92 : std::pow((c + 0.055) / 1.055, 2.4));
-    }
-    cudaMemcpyToSymbol(c_srgb_to_linear, table, sizeof table);
-}
+cudaError_t upload_srgb_table_trace() { return upload_srgb_table_here(); }
 
 }  // namespace rmd

@@ -544,6 +544,8 @@ int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments,
 namespace {
 }  // namespace
 
+cudaError_t upload_srgb_table_wavefront() { return upload_srgb_table_here(); }
+
 int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,
                      const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st,
                      StageEvents* events) {

@@ -257,7 +257,14 @@ int raymond_create(raymond_t** out, const raymond_config* cfg) {
         delete h;
         return RAYMOND_ENOMEM;
     }
-    upload_srgb_table();
+    for (cudaError_t (*up)() : {upload_srgb_table_trace, upload_srgb_table_wavefront, upload_srgb_table_caustics}) {
+        e = up();
+        if (e != cudaSuccess) {
+            g_create_error = std::string("texture tables: ") + cudaGetErrorString(e);
+            raymond_destroy(h);
+            return RAYMOND_ECUDA;
+        }
+    }
     *out = h;
     return RAYMOND_OK;
 }

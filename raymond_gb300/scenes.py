@@ -181,7 +181,8 @@ def geodesic_sphere(frequency: int):
 
 
 def sphere_field(seed: int = 2, spheres: int = 10000, frequency: int = 158):
-    """The sphere-field scene: returns (scene, camera, info)."""
+    """The sphere-field scene: returns (scene, camera, info). The centre
+    mesh has 20·frequency² triangles (499,280 at 158)."""
     rnd = mulberry32(seed)
     scene = Scene(sky=Sky(sunStrength=3.0, sunSize=0.0047124))
     scene.add(Quad(Vec3(-20, 0, 20), Vec3(40, 0, 0), Vec3(0, 0, -40), Material.diffuse(Vec3(0.5, 0.5, 0.5))))
@@ -214,3 +215,26 @@ def sphere_field(seed: int = 2, spheres: int = 10000, frequency: int = 158):
     info = {"seed": seed, "spheres": spheres, "triangles": int(mesh.triangleCount), "materials": kinds,
             "frequency": frequency}
     return scene, camera, info
+
+
+# ---------------------------------------------------------------- C4 ----
+
+BATCH_RESOLUTIONS = ((256, 256), (512, 512), (960, 540), (1920, 1080))
+
+
+def batch_instances(count: int = 64, seed: int = 4, spheres: int = 10000):
+    """`count` seeded sphere-field instances: triangles log-uniform in
+    1k–2M (as 20·f² of a geodesic sphere), a resolution from
+    {256², 512², 960×540, 1920×1080} and 1–64 samples per frame each.
+    Returns a list of (scene, camera, width, height, spp, info)."""
+    rnd = mulberry32(seed)
+    out = []
+    for i in range(count):
+        tris = math.exp(math.log(1000) + rnd() * (math.log(2_000_000) - math.log(1000)))
+        freq = max(2, int(round(math.sqrt(tris / 20))))
+        w, h = BATCH_RESOLUTIONS[min(3, int(rnd() * 4))]
+        spp = 1 + min(63, int(rnd() * 64))
+        scene, camera, info = sphere_field(seed=1000 + i, spheres=spheres, frequency=freq)
+        info["spp"] = spp
+        out.append((scene, camera, w, h, spp, info))
+    return out

@@ -26,12 +26,13 @@ def frame(scene, camera, size, spp, flags, bounces=8, frames=1, capacity=0):
     return out
 
 
-@pytest.mark.parametrize("name", ["cornell", "furnaceFog", "stripThroughGlass", "room"])
+@pytest.mark.parametrize("name", ["cornell", "furnaceFog", "stripThroughGlass", "room", "patternedLamp", "textured"])
 def test_wavefront_matches_megakernel(gpu, name):
     if name == "cornell":
         scene, camera = scenes.cornell_scene()
     else:
-        scene, opts = SCENES[name]("15" if name == "stripThroughGlass" else None)
+        arg = {"stripThroughGlass": "15", "patternedLamp": "light"}.get(name)
+        scene, opts = SCENES[name](arg)
         camera = Camera(**opts)
     mk = frame(scene, camera, 48, 4, _native.FLAG_MEGAKERNEL, frames=2)
     wf = frame(scene, camera, 48, 4, _native.FLAG_WAVEFRONT, frames=2)
