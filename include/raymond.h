@@ -263,6 +263,107 @@ int raymond_get_stats(raymond_t* h, raymond_stats* out);
 int raymond_denoise_static(const float* accum, const float* guide_albedo, const float* guide_normal, uint32_t width,
                            uint32_t height, uint32_t total_samples, float* out, void* stream);
 
+/*
+ * The learned denoiser. It has no counterpart in the reference, whose only
+ * denoiser is the à-trous filter (src/shaders.mjs:1916-2098); it stands
+ * beside that filter and, like it, only filters the displayed image: the
+ * renderer's running sums are its inputs, never its outputs.
+ *
+ * A raymond_net is a five-level U-Net of 3×3 convolutions (widths 32, 64,
+ * 96, 128, 128; BF16 weights and activations, FP32 accumulation on the
+ * tensor cores) with its FP32 master weights and Adam state, on one GPU.
+ * Inputs are 12 channels computed from a renderer's buffers (log radiance
+ * over albedo, albedo, normal, log depth, log standard error, 1/sqrt(n));
+ * the output is the log radiance over albedo, multiplied back by albedo.
+ * Errors: raymond_net_last_error(net); a failed create sets
+ * raymond_last_error(NULL).
+ */
+typedef struct raymond_net raymond_net;
+typedef struct raymond_net_config {
+    int device;
+    uint32_t seed;  /* weight initialisation (mulberry32) */
+    uint32_t reserved[6];
+} raymond_net_config;
+
+/* n images of width × height, as device float4 arrays laid out like a
+ * renderer's buffers (sums over the samples). target holds the converged
+ * mean radiance per pixel (training only). samples: n device floats, or
+ * NULL for samples_all. */
+typedef struct raymond_net_batch {
+    const float* accum;
+    const float* albedo;
+    const float* normal;
+    const float* target;
+    const float* samples;
+    float samples_all;
+    uint32_t n, width, height;
+} raymond_net_batch;
+
+int raymond_net_create(raymond_net** out, const raymond_net_config* cfg);
+void raymond_net_destroy(raymond_net* net);
+const char* raymond_net_last_error(const raymond_net* net);
+/* Parameters are one flat FP32 vector: per layer its weights [cout][9][cin]
+ * then its biases, each part starting at a multiple of 64. */
+uint64_t raymond_net_param_count(const raymond_net* net);
+int raymond_net_layout(const raymond_net* net, uint64_t* weight_offsets, uint64_t* bias_offsets, uint32_t* cin,
+                       uint32_t* cout, uint32_t layers);
+int raymond_net_set_params(raymond_net* net, const float* params, uint64_t count); /* resets Adam */
+int raymond_net_get_params(raymond_net* net, float* params, uint64_t count);
+/* Loss (mean absolute error of the log radiance over albedo) and its
+ * gradient with respect to every parameter, without a step. Training crops
+ * are multiples of 16 pixels on each side. */
+int raymond_net_gradients(raymond_net* net, const raymond_net_batch* batch, float* grads, uint64_t count, float* loss);
+/* One Adam step (beta 0.9, 0.999; eps 1e-8) on the batch, enqueued on the
+ * network's stream; loss (host, optional) waits for it. */
+int raymond_net_train_step(raymond_net* net, const raymond_net_batch* batch, float learning_rate, float* loss);
+int raymond_net_sync(raymond_net* net);
+/* Denoised radiance (float4 per pixel, any size) into out_rgba (device),
+ * enqueued on stream (NULL: the network's stream). */
+int raymond_net_infer(raymond_net* net, const raymond_net_batch* batch, float* out_rgba, void* stream);
+void* raymond_net_get_stream(raymond_net* net);
+
+/* The renderer's current image through the network: the result replaces the
+ * denoised buffer and the display image (display only; accum untouched),
+ * as a denoised frame would. samples is the frame's total sample count;
+ * out_rgba (host, optional) receives the w × h float4 result. */
+int raymond_denoise_learned(raymond_t* h, raymond_net* net, uint32_t samples, float* out_rgba);
+
+/*
+ * The network's kernels one at a time, on caller-owned device memory (NHWC
+ * BF16 tensors, channel strides multiples of 8, channel counts multiples of
+ * 16). The input is the concatenation of src0 and src1 along channels;
+ * shift 1 reads a source at half resolution (nearest-neighbour upsampling).
+ *   forward:        out (or out_f32) = act(conv(src, weight) + bias)
+ *   backward_data:  out = conv_transpose(dy, weight) × slope(mask)   (mask optional)
+ *   backward_weight: dweight += Σ dy ⊗ src, dbias += Σ dy   (FP32, accumulated)
+ * status is a device word that a kernel whose tensor-core wait ran out sets
+ * to non-zero. Errors: raymond_last_error(NULL).
+ */
+typedef struct raymond_conv {
+    uint32_t n, height, width, cin, cout;
+    const void* src0;
+    uint32_t src0_channels, src0_stride, src0_shift;
+    const void* src1;
+    uint32_t src1_channels, src1_stride, src1_shift;
+    const void* weight;
+    const float* bias;
+    const void* dy;
+    uint32_t dy_stride;
+    void* out;
+    uint32_t out_stride;
+    float* out_f32;
+    const void* mask;
+    uint32_t mask_stride;
+    float* dweight;
+    float* dbias;
+    int32_t activation; /* leaky ReLU, slope 0.1 below zero */
+    uint32_t pixels_per_cta; /* backward_weight: 0 chooses */
+    uint32_t* status;
+} raymond_conv;
+int raymond_conv3x3_forward(const raymond_conv* c, void* stream);
+int raymond_conv3x3_backward_data(const raymond_conv* c, void* stream);
+int raymond_conv3x3_backward_weight(const raymond_conv* c, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

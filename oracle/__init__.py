@@ -43,6 +43,14 @@ def lib():
         _lib.ro_denoise.argtypes = [P, P, P, U32, U32, U32, P, I]
         _lib.ro_display.restype = None
         _lib.ro_display.argtypes = [P, P, P, P]
+        _lib.ro_net_param_count.restype = ctypes.c_uint64
+        _lib.ro_net_param_count.argtypes = []
+        _lib.ro_net_layout.restype = None
+        _lib.ro_net_layout.argtypes = [P, P, P, P]
+        _lib.ro_net_loss_grad.restype = D
+        _lib.ro_net_loss_grad.argtypes = [P, P, P, P, P, P, U32, U32, U32, I, P, P]
+        _lib.ro_conv3x3.restype = None
+        _lib.ro_conv3x3.argtypes = [I, U32, U32, U32, P, U32, U32, P, U32, U32, P, P, P, P, I, P, P, P]
     return _lib
 
 
@@ -161,3 +169,65 @@ def surface_double(packed, p, o, d, t, u, v):
     lib().ro_surface_double(_p(packed.primitives), _p(attrs), int(p), _p(o), _p(d), float(t), float(u), float(v),
                             _p(out))
     return {"geometric": out[0:3], "shading": out[3:6], "uv": out[6:8], "tangent": out[8:11], "up": out[11:14]}
+
+
+# ---- the learned denoiser's network (oracle/net.cpp) ----
+
+def net_layout():
+    """Per layer (weight offset, bias offset, cin, cout) of the flat parameter vector."""
+    L = lib()
+    wo = np.zeros(19, np.uint64)
+    bo = np.zeros(19, np.uint64)
+    ci = np.zeros(19, np.uint32)
+    co = np.zeros(19, np.uint32)
+    L.ro_net_layout(_p(wo), _p(bo), _p(ci), _p(co))
+    return int(L.ro_net_param_count()), [(int(wo[i]), int(bo[i]), int(ci[i]), int(co[i])) for i in range(19)]
+
+
+def net_loss_grad(params, accum, albedo, normal, target, samples, bf16=False, grads=True, out=False):
+    """Loss, gradients (float64, or None) and the network output ([n,h,w,16] float32, or None)
+    for n images of h×w (float4 arrays [n,h,w,4] as a renderer accumulates them)."""
+    L = lib()
+    params = np.ascontiguousarray(params, dtype=np.float64)
+    accum = np.ascontiguousarray(accum, dtype=np.float32)
+    n, h, w = accum.shape[:3]
+    albedo = np.ascontiguousarray(albedo, dtype=np.float32)
+    normal = np.ascontiguousarray(normal, dtype=np.float32)
+    target = np.ascontiguousarray(target, dtype=np.float32)
+    samples = np.ascontiguousarray(np.broadcast_to(np.asarray(samples, np.float32), (n,)))
+    g = np.zeros(params.size, np.float64) if grads else None
+    o = np.zeros((n, h, w, 16), np.float32) if out else None
+    loss = L.ro_net_loss_grad(_p(params), _p(accum), _p(albedo), _p(normal), _p(target), _p(samples), n, h, w,
+                              1 if bf16 else 0, _p(g), _p(o))
+    return loss, g, o
+
+
+def conv3x3(mode, src0, weight, bias=None, src1=None, shift0=0, dy=None, mask=None, act=0):
+    """One 3×3 convolution in double: mode 0 forward, 1 input gradient, 2 weight/bias gradient.
+    src0 [n,h0,w0,c0] (h0 = h/2 when shift0), src1 [n,h,w,c1], weight [cout,9,cin]."""
+    L = lib()
+    src0 = np.ascontiguousarray(src0, dtype=np.float32)
+    n = src0.shape[0]
+    c0 = src0.shape[3]
+    if src1 is not None:
+        src1 = np.ascontiguousarray(src1, dtype=np.float32)
+        h, w, c1 = src1.shape[1], src1.shape[2], src1.shape[3]
+    else:
+        h, w, c1 = src0.shape[1] << shift0, src0.shape[2] << shift0, 0
+    weight = np.ascontiguousarray(weight, dtype=np.float32)
+    cout = weight.shape[0]
+    cin = c0 + c1
+    bias = None if bias is None else np.ascontiguousarray(bias, dtype=np.float32)
+    dy = None if dy is None else np.ascontiguousarray(dy, dtype=np.float32)
+    mask = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+    out = dw = db = None
+    if mode == 0:
+        out = np.zeros((n, h, w, cout), np.float32)
+    elif mode == 1:
+        out = np.zeros((n, h, w, cin), np.float32)
+    else:
+        dw = np.zeros((cout, 9, cin), np.float64)
+        db = np.zeros(cout, np.float64)
+    L.ro_conv3x3(mode, n, h, w, _p(src0), c0, shift0, _p(src1), c1, cout, _p(weight), _p(bias), _p(dy), _p(mask),
+                 act, _p(out), _p(dw), _p(db))
+    return out if mode != 2 else (dw, db)

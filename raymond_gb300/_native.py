@@ -55,6 +55,30 @@ class Job(ctypes.Structure):
     _fields_ = [("renderer", ctypes.c_void_p), ("params208", ctypes.c_void_p), ("features", ctypes.c_uint32)]
 
 
+class NetConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("seed", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 6)]
+
+
+class NetBatch(ctypes.Structure):
+    _fields_ = [("accum", ctypes.c_void_p), ("albedo", ctypes.c_void_p), ("normal", ctypes.c_void_p),
+                ("target", ctypes.c_void_p), ("samples", ctypes.c_void_p), ("samples_all", ctypes.c_float),
+                ("n", ctypes.c_uint32), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32)]
+
+
+class Conv(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32), ("height", ctypes.c_uint32), ("width", ctypes.c_uint32),
+                ("cin", ctypes.c_uint32), ("cout", ctypes.c_uint32),
+                ("src0", ctypes.c_void_p), ("src0_channels", ctypes.c_uint32), ("src0_stride", ctypes.c_uint32),
+                ("src0_shift", ctypes.c_uint32),
+                ("src1", ctypes.c_void_p), ("src1_channels", ctypes.c_uint32), ("src1_stride", ctypes.c_uint32),
+                ("src1_shift", ctypes.c_uint32),
+                ("weight", ctypes.c_void_p), ("bias", ctypes.c_void_p), ("dy", ctypes.c_void_p),
+                ("dy_stride", ctypes.c_uint32), ("out", ctypes.c_void_p), ("out_stride", ctypes.c_uint32),
+                ("out_f32", ctypes.c_void_p), ("mask", ctypes.c_void_p), ("mask_stride", ctypes.c_uint32),
+                ("dweight", ctypes.c_void_p), ("dbias", ctypes.c_void_p), ("activation", ctypes.c_int32),
+                ("pixels_per_cta", ctypes.c_uint32), ("status", ctypes.c_void_p)]
+
+
 # Every symbol include/raymond.h declares, with its ctypes signature.
 _P = ctypes.c_void_p
 _U32 = ctypes.c_uint32
@@ -86,6 +110,22 @@ SIGNATURES = {
     "raymond_render_batch": (_I, [_P, ctypes.POINTER(Job), _U32, _U32]),
     "raymond_get_tuning": (_I, [_P, ctypes.POINTER(Tuning)]),
     "raymond_autotune": (_I, [_P, _P, _U32, _U32, ctypes.POINTER(Tuning)]),
+    "raymond_net_create": (_I, [ctypes.POINTER(_P), ctypes.POINTER(NetConfig)]),
+    "raymond_net_destroy": (None, [_P]),
+    "raymond_net_last_error": (ctypes.c_char_p, [_P]),
+    "raymond_net_param_count": (_U64, [_P]),
+    "raymond_net_layout": (_I, [_P, _P, _P, _P, _P, _U32]),
+    "raymond_net_set_params": (_I, [_P, _P, _U64]),
+    "raymond_net_get_params": (_I, [_P, _P, _U64]),
+    "raymond_net_gradients": (_I, [_P, ctypes.POINTER(NetBatch), _P, _U64, _P]),
+    "raymond_net_train_step": (_I, [_P, ctypes.POINTER(NetBatch), ctypes.c_float, _P]),
+    "raymond_net_sync": (_I, [_P]),
+    "raymond_net_infer": (_I, [_P, ctypes.POINTER(NetBatch), _P, _P]),
+    "raymond_net_get_stream": (_P, [_P]),
+    "raymond_denoise_learned": (_I, [_P, _P, _U32, _P]),
+    "raymond_conv3x3_forward": (_I, [ctypes.POINTER(Conv), _P]),
+    "raymond_conv3x3_backward_data": (_I, [ctypes.POINTER(Conv), _P]),
+    "raymond_conv3x3_backward_weight": (_I, [ctypes.POINTER(Conv), _P]),
 }
 
 _lib = None
@@ -112,6 +152,12 @@ def lib():
 def check(rc: int, handle=None):
     if rc != OK:
         msg = lib().raymond_last_error(handle)
+        raise RaymondError(rc, msg.decode() if msg else f"raymond error {rc}")
+
+
+def check_net(rc: int, net):
+    if rc != OK:
+        msg = lib().raymond_net_last_error(net)
         raise RaymondError(rc, msg.decode() if msg else f"raymond error {rc}")
 
 

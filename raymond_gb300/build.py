@@ -15,7 +15,15 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libraymond_cuda.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["kernels_trace.cu", "kernels_wavefront.cu", "kernels_caustics.cu", "kernels_image.cu", "runtime.cu"]
+CUDA_SOURCES = [
+    "kernels_trace.cu",
+    "kernels_wavefront.cu",
+    "kernels_caustics.cu",
+    "kernels_image.cu",
+    "kernels_net.cu",
+    "net_runtime.cu",
+    "runtime.cu",
+]
 CXX_SOURCES = ["bvh_build.cpp"]
 
 

@@ -1,0 +1,626 @@
+// The learned denoiser's kernels: 3×3 convolutions as implicit GEMMs on the
+// fifth-generation tensor cores (tcgen05.mma, BF16 operands, FP32
+// accumulators in tensor memory) for the forward pass, the input gradient
+// and the weight gradient, plus the element-wise kernels around them
+// (input features, 2×2 pooling, the gradient split at skip connections,
+// the loss, Adam and the display composite).
+//
+// Tensors are NHWC BF16 with a channel stride that is a multiple of 8, so a
+// 16-byte cp.async moves 8 channels of one pixel. Weights are [cout][9][cin]
+// (tap-major rows, cin a multiple of 16).
+//
+// GEMM views (M × N × K, tiles of 128 × N × 64 with a 3-stage pipeline):
+//   forward        M = pixels,    N = cout, K = 9·cin   A K-major  (im2col rows), B K-major  (weights)
+//   input grad     M = pixels,    N = cin,  K = 9·cout  A K-major  (flipped taps), B MN-major (weights)
+//   weight grad    M = 9·cin + 1, N = cout, K = pixels  A MN-major (shifted input), B MN-major (dy)
+// The weight gradient's extra row is all ones, so its result row is the
+// bias gradient. A kernel that waits too long on its mbarrier records
+// NET_STATUS_TIMEOUT and returns after freeing its tensor memory.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+
+#include "dev_tcgen05.cuh"
+#include "net.cuh"
+
+namespace rmd {
+namespace net {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int kThreads = 256;
+constexpr int kStages = 3;
+constexpr int kTileM = 128;
+constexpr int kChunk = 64;                       // K elements per stage
+constexpr uint32_t kABytes = kTileM * kChunk * 2;  // 16 KB
+constexpr uint32_t kLBO = 128;                   // K-direction core-matrix stride
+constexpr uint32_t kSBO = 1024;                  // M/N-direction core-matrix stride (8 k-groups)
+
+__host__ __device__ inline uint32_t tmem_cols_for(int n) { return n <= 32 ? 32u : n <= 64 ? 64u : n <= 128 ? 128u : 256u; }
+__host__ __device__ inline uint32_t stage_bytes_for(int n) { return kABytes + uint32_t(n) * 128u; }
+
+struct Pixel {
+    int img, y, x;
+    bool valid;
+};
+__device__ __forceinline__ Pixel decode(int p, int total, int h, int w) {
+    Pixel px;
+    px.valid = p < total;
+    const int hw = h * w;
+    px.img = p / hw;
+    const int r = p - px.img * hw;
+    px.y = r / w;
+    px.x = r - px.y * w;
+    return px;
+}
+
+// Address of channel c at pixel (img, yy, xx) of the level, read from the
+// concatenated sources; false outside the image.
+__device__ __forceinline__ bool source_at(const ConvArgs& a, int img, int yy, int xx, int c, const bf16*& ptr) {
+    if (yy < 0 || xx < 0 || yy >= a.h || xx >= a.w) return false;
+    const ConvSrc& s = c < a.src[0].channels ? a.src[0] : a.src[1];
+    const int cc = c < a.src[0].channels ? c : c - a.src[0].channels;
+    const int sh = s.shift, sw = a.w >> sh, shh = a.h >> sh;
+    const size_t pix = (size_t(img) * shh + (yy >> sh)) * sw + (xx >> sh);
+    ptr = s.ptr + pix * size_t(s.stride) + cc;
+    return true;
+}
+
+__device__ __forceinline__ float slope(float v) { return v > 0.0f ? 1.0f : kLeak; }
+
+__device__ __forceinline__ void unpack8(uint4 u, float* f) {
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float2 t = __bfloat1622float2(h[i]);
+        f[2 * i] = t.x;
+        f[2 * i + 1] = t.y;
+    }
+}
+__device__ __forceinline__ uint4 pack8(const float* f) {
+    uint4 u;
+    __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&u);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+    return u;
+}
+
+template <int MODE>
+__device__ __forceinline__ void load_chunk(const ConvArgs& a, int N, int K, int m0, int k0, int kend, unsigned char* sa,
+                                           unsigned char* sb, const Pixel& row_px, int total_pixels) {
+    const int tid = threadIdx.x;
+    if (MODE == FWD || MODE == BWD_DATA) {
+        // A: thread owns one pixel row, four of the eight k-groups.
+        const int r = tid & (kTileM - 1);
+        const int cdiv = MODE == FWD ? a.cin : a.cout;
+        for (int j = 0; j < 4; ++j) {
+            const int g = (tid >> 7) + 2 * j;
+            const int k = k0 + 8 * g;
+            if (k >= kend) continue;
+            const int tap = k / cdiv;
+            const int c = k - tap * cdiv;
+            const int ty = tap / 3, tx = tap - 3 * ty;
+            const bf16* src = a.wt;
+            bool ok = false;
+            if (row_px.valid) {
+                if (MODE == FWD) {
+                    ok = source_at(a, row_px.img, row_px.y + ty - 1, row_px.x + tx - 1, c, src);
+                } else {
+                    const int yy = row_px.y - (ty - 1), xx = row_px.x - (tx - 1);
+                    if (yy >= 0 && xx >= 0 && yy < a.h && xx < a.w) {
+                        src = a.dy + ((size_t(row_px.img) * a.h + yy) * a.w + xx) * size_t(a.dy_stride) + c;
+                        ok = true;
+                    }
+                }
+            }
+            tc::cp_async16(sa + tc::core_offset(r, g, 8), ok ? src : a.wt, ok ? 16u : 0u);
+        }
+        // B
+        if (MODE == FWD) {
+            for (int idx = tid; idx < N * 8; idx += kThreads) {
+                const int row = idx >> 3, g = idx & 7;
+                const int k = k0 + 8 * g;
+                if (k < kend) tc::cp_async16(sb + tc::core_offset(row, g, 8), a.wt + size_t(row) * K + k, 16u);
+            }
+        } else {
+            const int kin = 9 * a.cin;
+            for (int idx = tid; idx < (N >> 3) * kChunk; idx += kThreads) {
+                const int kl = idx & (kChunk - 1), ng = idx >> 6;
+                const int k = k0 + kl;
+                if (k >= kend) continue;
+                const int tap = k / a.cout;
+                const int co = k - tap * a.cout;
+                tc::cp_async16(sb + ng * kSBO + kl * 16, a.wt + size_t(co) * kin + tap * a.cin + 8 * ng, 16u);
+            }
+        }
+    } else {
+        // Weight gradient. A: thread owns one pixel (k) and four 8-row groups.
+        const int kl = tid & (kChunk - 1);
+        const Pixel px = decode(k0 + kl, kend, a.h, a.w);
+        const int rows = 9 * a.cin;
+        for (int j = 0; j < 4; ++j) {
+            const int mg = (tid >> 6) + 4 * j;
+            const int m = m0 + 8 * mg;
+            unsigned char* dst = sa + mg * kSBO + kl * 16;
+            if (m < rows) {
+                const int tap = m / a.cin;
+                const int ci = m - tap * a.cin;
+                const int ty = tap / 3, tx = tap - 3 * ty;
+                const bf16* src = a.wt;
+                const bool ok = px.valid && source_at(a, px.img, px.y + ty - 1, px.x + tx - 1, ci, src);
+                tc::cp_async16(dst, ok ? src : a.wt, ok ? 16u : 0u);
+            } else {
+                uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                if (m == rows && px.valid) v.x = 0x3F80u;  // bf16 1.0 in the group's first row
+                *reinterpret_cast<uint4*>(dst) = v;
+            }
+        }
+        // B: dy, 8 output channels of one pixel per piece.
+        for (int idx = tid; idx < (N >> 3) * kChunk; idx += kThreads) {
+            const int l = idx & (kChunk - 1), ng = idx >> 6;
+            const int p = k0 + l;
+            const bool ok = p < kend;
+            tc::cp_async16(sb + ng * kSBO + l * 16, ok ? a.dy + size_t(p) * a.dy_stride + 8 * ng : a.dy, ok ? 16u : 0u);
+        }
+    }
+    (void)total_pixels;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t bars[kStages];
+    __shared__ uint32_t tslot;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int pixels = a.n * a.h * a.w;
+    const int N = MODE == BWD_DATA ? a.cin : a.cout;
+    const int K = MODE == FWD ? 9 * a.cin : MODE == BWD_DATA ? 9 * a.cout : pixels;
+    const uint32_t sbytes = stage_bytes_for(N);
+    const uint32_t tcols = tmem_cols_for(N);
+    const int m0 = blockIdx.x * kTileM;
+    int kbeg = 0, kend = K;
+    if (MODE == BWD_WEIGHT) {
+        kbeg = blockIdx.y * a.pixels_per_cta;
+        kend = min(K, kbeg + a.pixels_per_cta);
+    }
+    const int nchunks = (kend - kbeg + kChunk - 1) / kChunk;
+
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) tc::mbar_init(&bars[s], 1);
+        tc::fence_barrier_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tslot, tcols);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    tc::tc_fence_after_sync();
+    const uint32_t tbase = tslot;
+
+    Pixel row_px{0, 0, 0, false};
+    if (MODE != BWD_WEIGHT) row_px = decode(m0 + (tid & (kTileM - 1)), pixels, a.h, a.w);
+
+    uint32_t idesc = tc::idesc_bf16(kTileM, N);
+    if (MODE == BWD_DATA) idesc |= 1u << 16;
+    if (MODE == BWD_WEIGHT) idesc |= (1u << 15) | (1u << 16);
+
+    for (int c = 0; c < kStages - 1; ++c) {
+        if (c < nchunks) {
+            unsigned char* st = smem + c * sbytes;
+            load_chunk<MODE>(a, N, K, m0, kbeg + c * kChunk, kend, st, st + kABytes, row_px, pixels);
+        }
+        tc::cp_async_commit();
+    }
+
+    bool failed = false;
+    for (int i = 0; i < nchunks; ++i) {
+        asm volatile("cp.async.wait_group %0;" ::"n"(kStages - 2) : "memory");
+        tc::fence_proxy_async_smem();
+        if (__syncthreads_or(failed)) {
+            failed = true;
+            break;
+        }
+        const int s = i % kStages;
+        if (tid == 0) {
+            tc::tc_fence_after_sync();
+            const uint32_t sa = tc::smem_u32(smem + s * sbytes);
+            const uint32_t sb = sa + kABytes;
+            const int kleft = kend - (kbeg + i * kChunk);
+            const int slices = min(kChunk, kleft + 15) / 16;
+            for (int j = 0; j < slices; ++j) {
+                const uint64_t ad = tc::smem_desc(sa + j * 256, kLBO, kSBO);
+                const uint64_t bd = tc::smem_desc(sb + j * 256, kLBO, kSBO);
+                tc::mma_bf16(tbase, ad, bd, idesc, (i > 0 || j > 0) ? 1u : 0u);
+            }
+            tc::mma_commit(&bars[s]);
+        }
+        const int next = i + kStages - 1;
+        if (next < nchunks) {
+            if (i >= 1) {
+                const int prev = i - 1;
+                if (!tc::mbar_wait(&bars[prev % kStages], (prev / kStages) & 1)) failed = true;
+            }
+            if (!failed) {
+                unsigned char* st = smem + (next % kStages) * sbytes;
+                load_chunk<MODE>(a, N, K, m0, kbeg + next * kChunk, kend, st, st + kABytes, row_px, pixels);
+            }
+        }
+        tc::cp_async_commit();
+    }
+    tc::cp_async_wait_all();
+
+    // Completion of the last chunk's MMAs (and so of all of them).
+    bool done = false;
+    if (!failed) {
+        const int last = nchunks - 1;
+        done = tc::mbar_wait(&bars[last % kStages], (last / kStages) & 1);
+    }
+    const bool ok = !__syncthreads_or(!done);
+    if (!ok && tid == 0) atomicOr(a.status, NET_STATUS_TIMEOUT);
+    tc::tc_fence_after_sync();
+
+    if (ok) {
+        const int quarter = warp & 3;
+        const int row = m0 + 32 * quarter + lane;
+        const uint32_t lane_addr = tbase + (uint32_t(32 * quarter) << 16);
+        for (int c = (warp >> 2) * 16; c < N; c += 32) {
+            float v[16];
+            tc::tmem_ld16(lane_addr + uint32_t(c), v);
+            if (MODE == FWD) {
+                if (row < pixels) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        float t = v[i] + a.bias[c + i];
+                        if (a.act) t = t > 0.0f ? t : kLeak * t;
+                        v[i] = t;
+                    }
+                    if (a.out_f32) {
+                        float4* o = reinterpret_cast<float4*>(a.out_f32 + size_t(row) * a.out_stride + c);
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) o[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+                    } else {
+                        uint4* o = reinterpret_cast<uint4*>(a.out + size_t(row) * a.out_stride + c);
+                        o[0] = pack8(v);
+                        o[1] = pack8(v + 8);
+                    }
+                }
+            } else if (MODE == BWD_DATA) {
+                if (row < pixels) {
+                    if (a.mask) {
+                        const uint4* mk = reinterpret_cast<const uint4*>(a.mask + size_t(row) * a.mask_stride + c);
+                        float mv[16];
+                        unpack8(mk[0], mv);
+                        unpack8(mk[1], mv + 8);
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) v[i] *= slope(mv[i]);
+                    }
+                    uint4* o = reinterpret_cast<uint4*>(a.out + size_t(row) * a.out_stride + c);
+                    o[0] = pack8(v);
+                    o[1] = pack8(v + 8);
+                }
+            } else {
+                const int rows = 9 * a.cin;
+                if (row < rows) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) atomicAdd(a.dw + size_t(c + i) * rows + row, v[i]);
+                } else if (row == rows) {
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) atomicAdd(a.db + c + i, v[i]);
+                }
+            }
+        }
+    } else {
+        // MMAs may still be in flight: give them a bounded time before the
+        // tensor memory is released.
+        if (tid == 0) {
+            for (int s = 0; s < kStages; ++s) tc::mbar_wait(&bars[s], 0);
+        }
+    }
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+        tc::tc_fence_after_sync();
+        tc::tmem_dealloc(tbase, tcols);
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+
+static int smem_for(int n) { return int(kStages * stage_bytes_for(n)); }
+
+template <int MODE>
+static cudaError_t configure(int n, int& smem) {
+    smem = smem_for(n);
+    // Tensor memory: the CTAs that fit on an SM must not ask for more than
+    // its 512 columns, or an allocation would wait for another CTA to end.
+    const int per_sm_smem = 233472;  // 228 KB per SM
+    const int cols = int(tmem_cols_for(n));
+    const int max_ctas = 512 / cols;
+    while (per_sm_smem / (smem + 2048) > max_ctas) smem += 4096;  // + static and reserved smem
+    return cudaFuncSetAttribute(k_conv<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+const char* check_conv(const ConvArgs& a, int mode) {
+    if (a.n <= 0 || a.h <= 0 || a.w <= 0) return "conv: empty geometry";
+    if (a.cin % 16 || a.cout % 16 || a.cin < 16 || a.cout < 16) return "conv: channel counts must be multiples of 16";
+    if (a.cin > 256 || a.cout > 256) return "conv: at most 256 channels";
+    for (int i = 0; i < 2 && mode != BWD_DATA; ++i) {
+        if (i == 0 && a.src[0].channels + a.src[1].channels != a.cin) return "conv: source channels do not add up to cin";
+        const ConvSrc& s = a.src[i];
+        if (s.channels == 0) continue;
+        if (s.channels % 8 || s.stride % 8 || s.stride < s.channels) return "conv: source stride must cover its channels in multiples of 8";
+        if (s.shift < 0 || s.shift > 1) return "conv: source shift must be 0 or 1";
+        if (s.shift && ((a.h & 1) || (a.w & 1))) return "conv: an upsampled source needs even sizes";
+        if (!s.ptr || !aligned16(s.ptr)) return "conv: source must be 16-byte aligned";
+    }
+    if (!a.wt || !aligned16(a.wt)) return "conv: weights must be 16-byte aligned";
+    if (!a.status) return "conv: no status word";
+    const size_t pixels = size_t(a.n) * a.h * a.w;
+    if (pixels >= (size_t(1) << 31)) return "conv: too many pixels";
+    if (mode == FWD) {
+        if (!a.bias) return "conv: forward needs a bias";
+        if (a.out_f32) {
+            if (a.out_stride < a.cout || a.out_stride % 4 || !aligned16(a.out_f32)) return "conv: bad fp32 output";
+        } else if (!a.out || a.out_stride < a.cout || a.out_stride % 8 || !aligned16(a.out)) {
+            return "conv: bad output";
+        }
+    } else {
+        if (!a.dy || a.dy_stride < a.cout || a.dy_stride % 8 || !aligned16(a.dy)) return "conv: bad output gradient";
+    }
+    if (mode == BWD_DATA) {
+        if (!a.out || a.out_stride < a.cin || a.out_stride % 8 || !aligned16(a.out)) return "conv: bad input gradient";
+        if (a.mask && (a.mask_stride < a.cin || a.mask_stride % 8 || !aligned16(a.mask))) return "conv: bad mask";
+    }
+    if (mode == BWD_WEIGHT) {
+        if (!a.dw || !a.db) return "conv: weight gradient needs dw and db";
+        if (a.pixels_per_cta <= 0 || a.pixels_per_cta % kChunk) return "conv: pixels per CTA must be a multiple of 64";
+    }
+    return nullptr;
+}
+
+cudaError_t launch_conv(ConvArgs a, int mode, int num_sms, cudaStream_t st) {
+    const int pixels = a.n * a.h * a.w;
+    int smem = 0;
+    cudaError_t e;
+    if (mode == FWD) {
+        if ((e = configure<FWD>(a.cout, smem)) != cudaSuccess) return e;
+        k_conv<FWD><<<(pixels + kTileM - 1) / kTileM, kThreads, smem, st>>>(a);
+    } else if (mode == BWD_DATA) {
+        if ((e = configure<BWD_DATA>(a.cin, smem)) != cudaSuccess) return e;
+        k_conv<BWD_DATA><<<(pixels + kTileM - 1) / kTileM, kThreads, smem, st>>>(a);
+    } else {
+        if ((e = configure<BWD_WEIGHT>(a.cout, smem)) != cudaSuccess) return e;
+        const int mtiles = (9 * a.cin + 1 + kTileM - 1) / kTileM;
+        if (a.pixels_per_cta <= 0) {
+            // About two waves of CTAs over the SMs, at least 8 chunks each.
+            const int want = std::max(1, 2 * num_sms / mtiles);
+            int per = (pixels + want - 1) / want;
+            per = std::max(per, 8 * kChunk);
+            a.pixels_per_cta = (per + kChunk - 1) / kChunk * kChunk;
+        }
+        const int ksplit = (pixels + a.pixels_per_cta - 1) / a.pixels_per_cta;
+        k_conv<BWD_WEIGHT><<<dim3(mtiles, ksplit), kThreads, smem, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- element-wise kernels
+
+__device__ __forceinline__ float lum3(float r, float g, float b) { return r * 0.2126f + g * 0.7152f + b * 0.0722f; }
+
+// Input features of one pixel from the renderer's sums over n samples:
+// log radiance over albedo (the à-trous filter's demodulation), albedo,
+// unit normal, log depth, log standard error of the mean luminance,
+// 1/sqrt(n), and four zero channels.
+__global__ void k_features(FeatureArgs f) {
+    const int total = f.n * f.h * f.w;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= total) return;
+    const int hw = f.h * f.w;
+    const int img = p / hw, r = p - img * hw, y = r / f.w, x = r - y * f.w;
+    float v[16] = {};
+    if (y < f.src_h && x < f.src_w) {
+        const size_t i = (size_t(img) * f.src_h + y) * f.src_w + x;
+        const float n = fmaxf(f.samples ? f.samples[img] : f.samples_all, 1.0f);
+        const float4 ac = f.accum[i], al = f.albedo[i], nr = f.normal[i];
+        const float ax = fmaxf(al.x / n, 0.01f), ay = fmaxf(al.y / n, 0.01f), az = fmaxf(al.z / n, 0.01f);
+        const float mr = ac.x / n, mg = ac.y / n, mb = ac.z / n;
+        v[0] = log1pf(fmaxf(mr / ax, 0.0f));
+        v[1] = log1pf(fmaxf(mg / ay, 0.0f));
+        v[2] = log1pf(fmaxf(mb / az, 0.0f));
+        v[3] = ax;
+        v[4] = ay;
+        v[5] = az;
+        const float d2 = nr.x * nr.x + nr.y * nr.y + nr.z * nr.z;
+        if (d2 > 0.0f) {
+            const float il = rsqrtf(d2);
+            v[6] = nr.x * il;
+            v[7] = nr.y * il;
+            v[8] = nr.z * il;
+        }
+        v[9] = log1pf(fmaxf(nr.w / n, 0.0f));
+        const float m = lum3(mr, mg, mb);
+        const float var = fmaxf(ac.w / n - m * m, 0.0f) / n;
+        v[10] = log1pf(sqrtf(var));
+        v[11] = rsqrtf(n);
+        if (!(isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]) && isfinite(v[9]) && isfinite(v[10]))) {
+            for (int c = 0; c < 16; ++c) v[c] = 0.0f;
+        }
+    }
+    uint4* o = reinterpret_cast<uint4*>(f.out + size_t(p) * 16);
+    o[0] = pack8(v);
+    o[1] = pack8(v + 8);
+}
+
+// 2×2 average pooling, 8 channels per thread.
+__global__ void k_pool(const bf16* __restrict__ in, bf16* __restrict__ out, int n, int h, int w, int c) {
+    const int oh = h >> 1, ow = w >> 1, groups = c >> 3;
+    const size_t total = size_t(n) * oh * ow * groups;
+    const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int g = int(t % groups);
+    const size_t op = t / groups;
+    const int x = int(op % ow), y = int((op / ow) % oh), img = int(op / (size_t(ow) * oh));
+    float s[8] = {}, f[8];
+    for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx) {
+            const size_t ip = (size_t(img) * h + 2 * y + dy) * w + 2 * x + dx;
+            unpack8(*reinterpret_cast<const uint4*>(in + ip * c + 8 * g), f);
+            for (int i = 0; i < 8; ++i) s[i] += f[i];
+        }
+    for (int i = 0; i < 8; ++i) s[i] *= 0.25f;
+    *reinterpret_cast<uint4*>(out + op * c + 8 * g) = pack8(s);
+}
+
+// Gradient of an upsampled source: the sum over each 2×2 block of the
+// concatenation gradient's first `cup` channels, times the activation slope
+// of the coarse tensor.
+__global__ void k_split_up(const bf16* __restrict__ dcat, int cat_stride, bf16* __restrict__ g_coarse,
+                           const bf16* __restrict__ coarse, int n, int h, int w, int cup) {
+    const int oh = h >> 1, ow = w >> 1, groups = cup >> 3;
+    const size_t total = size_t(n) * oh * ow * groups;
+    const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int g = int(t % groups);
+    const size_t op = t / groups;
+    const int x = int(op % ow), y = int((op / ow) % oh), img = int(op / (size_t(ow) * oh));
+    float s[8] = {}, f[8];
+    for (int dy = 0; dy < 2; ++dy)
+        for (int dx = 0; dx < 2; ++dx) {
+            const size_t ip = (size_t(img) * h + 2 * y + dy) * w + 2 * x + dx;
+            unpack8(*reinterpret_cast<const uint4*>(dcat + ip * cat_stride + 8 * g), f);
+            for (int i = 0; i < 8; ++i) s[i] += f[i];
+        }
+    unpack8(*reinterpret_cast<const uint4*>(coarse + op * cup + 8 * g), f);
+    for (int i = 0; i < 8; ++i) s[i] *= slope(f[i]);
+    *reinterpret_cast<uint4*>(g_coarse + op * cup + 8 * g) = pack8(s);
+}
+
+// Gradient of an encoder output that feeds both a skip connection and the
+// pooling below it: (skip gradient + pooled gradient / 4) × slope.
+__global__ void k_merge(const bf16* __restrict__ skip, int skip_stride, const bf16* __restrict__ g_pool,
+                        const bf16* __restrict__ act, bf16* __restrict__ out, int n, int h, int w, int c) {
+    const int groups = c >> 3;
+    const size_t total = size_t(n) * h * w * groups;
+    const size_t t = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int g = int(t % groups);
+    const size_t p = t / groups;
+    const int x = int(p % w), y = int((p / w) % h), img = int(p / (size_t(w) * h));
+    const size_t cp = (size_t(img) * (h >> 1) + (y >> 1)) * (w >> 1) + (x >> 1);
+    float s[8], q[8], f[8];
+    unpack8(*reinterpret_cast<const uint4*>(skip + p * skip_stride + 8 * g), s);
+    unpack8(*reinterpret_cast<const uint4*>(g_pool + cp * c + 8 * g), q);
+    unpack8(*reinterpret_cast<const uint4*>(act + p * c + 8 * g), f);
+    for (int i = 0; i < 8; ++i) s[i] = (s[i] + 0.25f * q[i]) * slope(f[i]);
+    *reinterpret_cast<uint4*>(out + p * c + 8 * g) = pack8(s);
+}
+
+// L1 loss between the network's log radiance and the target's, and its
+// gradient (bf16, 16 channels, zero past the third).
+__global__ void k_loss(LossArgs L) {
+    const int total = L.n * L.h * L.w;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    float part = 0.0f;
+    if (p < total) {
+        const int hw = L.h * L.w;
+        const int img = p / hw, r = p - img * hw, y = r / L.w, x = r - y * L.w;
+        float g[16] = {};
+        if (y < L.src_h && x < L.src_w) {
+            const size_t i = (size_t(img) * L.src_h + y) * L.src_w + x;
+            const float n = fmaxf(L.samples ? L.samples[img] : L.samples_all, 1.0f);
+            const float4 al = L.albedo[i], tg = L.target[i];
+            const float a[3] = {fmaxf(al.x / n, 0.01f), fmaxf(al.y / n, 0.01f), fmaxf(al.z / n, 0.01f)};
+            const float t[3] = {tg.x, tg.y, tg.z};
+            for (int c = 0; c < 3; ++c) {
+                const float want = log1pf(fmaxf(t[c] / a[c], 0.0f));
+                const float d = L.out[size_t(p) * 16 + c] - want;
+                if (isfinite(d)) {
+                    part += fabsf(d);
+                    g[c] = (d > 0.0f ? 1.0f : d < 0.0f ? -1.0f : 0.0f) * L.scale;
+                }
+            }
+        }
+        uint4* o = reinterpret_cast<uint4*>(L.grad + size_t(p) * 16);
+        o[0] = pack8(g);
+        o[1] = pack8(g + 8);
+    }
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if ((threadIdx.x & 31) == 0 && part != 0.0f) atomicAdd(L.loss, part * L.scale);
+}
+
+// Adam on the flat parameter vector; refreshes the BF16 copy of the weights.
+__global__ void k_adam(AdamArgs A) {
+    const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= A.count) return;
+    const float g = A.grad[i];
+    const float m = A.beta1 * A.m[i] + (1.0f - A.beta1) * g;
+    const float v = A.beta2 * A.v[i] + (1.0f - A.beta2) * g * g;
+    A.m[i] = m;
+    A.v[i] = v;
+    const float p = A.param[i] - A.step * m / (sqrtf(v) + A.eps_hat);
+    A.param[i] = p;
+    A.param_bf16[i] = __float2bfloat16_rn(p);
+}
+
+// Display image: exp of the predicted log radiance, times the albedo.
+__global__ void k_compose(ComposeArgs C) {
+    const int hw = C.w * C.h;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= C.n * hw) return;
+    const int img = p / hw, r = p - img * hw, y = r / C.w, x = r - y * C.w;
+    const float n = fmaxf(C.samples ? C.samples[img] : C.samples_all, 1.0f);
+    const float4 al = C.albedo[p];
+    const float* o = C.out + ((size_t(img) * C.ph + y) * C.pw + x) * 16;
+    const float cr = expm1f(fmaxf(o[0], 0.0f)) * fmaxf(al.x / n, 0.01f);
+    const float cg = expm1f(fmaxf(o[1], 0.0f)) * fmaxf(al.y / n, 0.01f);
+    const float cb = expm1f(fmaxf(o[2], 0.0f)) * fmaxf(al.z / n, 0.01f);
+    C.dst[p] = make_float4(cr, cg, cb, 1.0f);
+}
+
+static inline unsigned blocks_for(size_t n, unsigned t) { return unsigned((n + t - 1) / t); }
+
+cudaError_t launch_features(const FeatureArgs& f, cudaStream_t st) {
+    const size_t total = size_t(f.n) * f.h * f.w;
+    k_features<<<blocks_for(total, 256), 256, 0, st>>>(f);
+    return cudaGetLastError();
+}
+cudaError_t launch_pool(const bf16* in, bf16* out, int n, int h, int w, int c, cudaStream_t st) {
+    const size_t total = size_t(n) * (h / 2) * (w / 2) * (c / 8);
+    k_pool<<<blocks_for(total, 256), 256, 0, st>>>(in, out, n, h, w, c);
+    return cudaGetLastError();
+}
+cudaError_t launch_split_up(const bf16* dcat, int cat_stride, bf16* g_coarse, const bf16* coarse, int n, int h, int w,
+                            int cup, cudaStream_t st) {
+    const size_t total = size_t(n) * (h / 2) * (w / 2) * (cup / 8);
+    k_split_up<<<blocks_for(total, 256), 256, 0, st>>>(dcat, cat_stride, g_coarse, coarse, n, h, w, cup);
+    return cudaGetLastError();
+}
+cudaError_t launch_merge(const bf16* skip, int skip_stride, const bf16* g_pool, const bf16* act, bf16* out, int n,
+                         int h, int w, int c, cudaStream_t st) {
+    const size_t total = size_t(n) * h * w * (c / 8);
+    k_merge<<<blocks_for(total, 256), 256, 0, st>>>(skip, skip_stride, g_pool, act, out, n, h, w, c);
+    return cudaGetLastError();
+}
+cudaError_t launch_loss(const LossArgs& L, cudaStream_t st) {
+    const size_t total = size_t(L.n) * L.h * L.w;
+    k_loss<<<blocks_for(total, 256), 256, 0, st>>>(L);
+    return cudaGetLastError();
+}
+cudaError_t launch_adam(const AdamArgs& A, cudaStream_t st) {
+    k_adam<<<blocks_for(A.count, 256), 256, 0, st>>>(A);
+    return cudaGetLastError();
+}
+cudaError_t launch_compose(const ComposeArgs& C, cudaStream_t st) {
+    k_compose<<<blocks_for(size_t(C.n) * C.w * C.h, 256), 256, 0, st>>>(C);
+    return cudaGetLastError();
+}
+
+}  // namespace net
+}  // namespace rmd

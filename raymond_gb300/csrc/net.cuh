@@ -1,0 +1,111 @@
+// Launch-side declarations of the learned denoiser's kernels.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+namespace rmd {
+namespace net {
+
+enum ConvMode { FWD = 0, BWD_DATA = 1, BWD_WEIGHT = 2 };
+
+constexpr float kLeak = 0.1f;  // leaky ReLU slope below zero
+constexpr unsigned NET_STATUS_TIMEOUT = 1u;
+
+// One input tensor of a convolution whose input is a channel concatenation:
+// `channels` channels at `stride` per pixel; shift 1 reads it at half
+// resolution (nearest-neighbour upsampling).
+struct ConvSrc {
+    const __nv_bfloat16* ptr;
+    int channels;
+    int stride;
+    int shift;
+};
+
+struct ConvArgs {
+    int n, h, w;     // images and spatial size (of the output, and of every full-resolution input)
+    int cin, cout;   // cin = src[0].channels + src[1].channels
+    ConvSrc src[2];  // forward and weight-gradient input
+    const __nv_bfloat16* wt;  // [cout][9][cin]
+    const float* bias;        // [cout]
+    const __nv_bfloat16* dy;  // gradient at the convolution's output (before the activation)
+    int dy_stride;
+    __nv_bfloat16* out;  // forward output or input gradient
+    int out_stride;
+    float* out_f32;  // forward output in FP32 instead of `out`
+    const __nv_bfloat16* mask;  // input gradient: times the activation slope of this tensor
+    int mask_stride;
+    float* dw;  // weight gradient, accumulated: [cout][9][cin]
+    float* db;  // bias gradient, accumulated
+    int act;    // forward: apply the leaky ReLU
+    int pixels_per_cta;  // weight gradient: K split (0 picks one)
+    unsigned* status;
+};
+
+struct FeatureArgs {
+    const float4* accum;
+    const float4* albedo;
+    const float4* normal;
+    const float* samples;  // per image, device; null uses samples_all
+    float samples_all;
+    int n, h, w;          // padded size of the feature tensor
+    int src_h, src_w;     // size of the source images (≤ h, w)
+    __nv_bfloat16* out;   // [n][h][w][16]
+};
+
+struct LossArgs {
+    const float* out;  // [n][h][w][16] network output
+    const float4* albedo;
+    const float4* target;  // per-pixel mean radiance of the converged render
+    const float* samples;
+    float samples_all;
+    int n, h, w, src_h, src_w;
+    float scale;   // 1 / (3 · pixels)
+    __nv_bfloat16* grad;  // [n][h][w][16]
+    float* loss;
+};
+
+struct AdamArgs {
+    float* param;
+    __nv_bfloat16* param_bf16;
+    const float* grad;
+    float* m;
+    float* v;
+    size_t count;
+    float beta1, beta2, step, eps_hat;
+};
+
+struct ComposeArgs {
+    const float* out;  // network output [n][ph][pw][16]
+    const float4* albedo;
+    const float* samples;  // per image, device; null uses samples_all
+    float samples_all;
+    int n, w, h, pw, ph;
+    float4* dst;  // [n][h][w]
+};
+
+const char* check_conv(const ConvArgs& a, int mode);
+cudaError_t launch_conv(ConvArgs a, int mode, int num_sms, cudaStream_t st);
+cudaError_t launch_features(const FeatureArgs& f, cudaStream_t st);
+cudaError_t launch_pool(const __nv_bfloat16* in, __nv_bfloat16* out, int n, int h, int w, int c, cudaStream_t st);
+cudaError_t launch_split_up(const __nv_bfloat16* dcat, int cat_stride, __nv_bfloat16* g_coarse,
+                            const __nv_bfloat16* coarse, int n, int h, int w, int cup, cudaStream_t st);
+cudaError_t launch_merge(const __nv_bfloat16* skip, int skip_stride, const __nv_bfloat16* g_pool,
+                         const __nv_bfloat16* act, __nv_bfloat16* out, int n, int h, int w, int c, cudaStream_t st);
+cudaError_t launch_loss(const LossArgs& L, cudaStream_t st);
+cudaError_t launch_adam(const AdamArgs& A, cudaStream_t st);
+cudaError_t launch_compose(const ComposeArgs& C, cudaStream_t st);
+
+}  // namespace net
+
+void set_handleless_error(const char* msg);
+
+}  // namespace rmd
+
+// The network over one renderer's buffers (float4 per pixel), written to
+// dst on the given stream.
+int rmd_net_denoise(struct raymond_net* net, const float* accum, const float* albedo, const float* normal,
+                    float samples, uint32_t w, uint32_t h, float* dst, void* stream, std::string* err);

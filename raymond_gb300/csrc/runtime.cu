@@ -12,6 +12,7 @@
 
 #include "../../include/raymond.h"
 #include "kernels.cuh"
+#include "net.cuh"
 
 using namespace rmd;
 
@@ -91,6 +92,7 @@ struct raymond {
     uint32_t path_choice = RAYMOND_PATH_WAVEFRONT;
 
     bool rendered = false;
+    bool learned_valid = false;  // the denoised buffer holds the network's image of this frame
     Params last_params{};
     raymond_stats stats{};
     // Stage boundaries of the last frame: trace, caustics, denoise, display.
@@ -527,6 +529,7 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
     if (e != cudaSuccess) return h->cuda_fail(e, "render");
     h->last_params = P;
     h->rendered = true;
+    h->learned_valid = false;
     h->stats = raymond_stats{};
     h->stats.launches = uint64_t(launches);
     h->stats.paths = uint64_t(P.width) * P.height * P.samples_per_frame;
@@ -711,6 +714,7 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
         raymond* r = jobs[j].renderer;
         r->last_params = desc[j].params;
         r->rendered = true;
+        r->learned_valid = false;
     }
     h->stats = raymond_stats{};
     h->stats.launches = uint64_t(launches);
@@ -728,7 +732,7 @@ int raymond_sync(raymond_t* h) {
 int raymond_read_pixels(raymond_t* h, float* out_rgba, uint64_t bytes, int denoised, uint32_t samples) {
     if (!h) return RAYMOND_EINVAL;
     if (!h->rendered || samples == 0) return h->fail(RAYMOND_ESTATE, "Nothing has been rendered yet.");
-    if (denoised && h->last_params.denoise == 0u)
+    if (denoised && h->last_params.denoise == 0u && !h->learned_valid)
         return h->fail(RAYMOND_ESTATE, "Only the color view is denoised, with denoise on.");
     const uint64_t need = uint64_t(h->width) * h->height * 16;
     if (!out_rgba || bytes < need) return h->fail(RAYMOND_EINVAL, "The output needs %llu bytes.", (unsigned long long)need);
@@ -741,6 +745,35 @@ int raymond_read_pixels(raymond_t* h, float* out_rgba, uint64_t bytes, int denoi
         const float inv = float(samples);
         const size_t n = size_t(need / 4);
         for (size_t i = 0; i < n; ++i) out_rgba[i] /= inv;
+    }
+    return RAYMOND_OK;
+}
+
+int raymond_denoise_learned(raymond_t* h, raymond_net* net, uint32_t samples, float* out_rgba) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!net) return h->fail(RAYMOND_EINVAL, "No network.");
+    if (!h->rendered || samples == 0) return h->fail(RAYMOND_ESTATE, "Nothing has been rendered yet.");
+    if (h->last_params.view != VIEW_COLOR) return h->fail(RAYMOND_ESTATE, "Only the color view is denoised.");
+    cudaSetDevice(h->device);
+    std::string err;
+    const int rc = rmd_net_denoise(net, static_cast<const float*>(h->accum.ptr),
+                                   static_cast<const float*>(h->guide_albedo.ptr),
+                                   static_cast<const float*>(h->guide_normal.ptr), float(samples), h->width, h->height,
+                                   static_cast<float*>(h->denoised.ptr), h->stream, &err);
+    if (rc) return h->fail(rc, "%s", err.c_str());
+    // The display shows the network's image, tone-mapped as a denoised frame.
+    Params P = h->last_params;
+    P.denoise = 1u;
+    P.total_samples = samples;
+    launch_tonemap(P, h->pixel_view(), h->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return h->cuda_fail(e, "learned denoise");
+    h->learned_valid = true;
+    if (out_rgba) {
+        const size_t need = size_t(h->width) * h->height * 16;
+        e = cudaMemcpyAsync(out_rgba, h->denoised.ptr, need, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) return h->cuda_fail(e, "learned denoise read-back");
     }
     return RAYMOND_OK;
 }
