@@ -309,9 +309,12 @@ int raymond_net_layout(const raymond_net* net, uint64_t* weight_offsets, uint64_
                        uint32_t* cout, uint32_t layers);
 int raymond_net_set_params(raymond_net* net, const float* params, uint64_t count); /* resets Adam */
 int raymond_net_get_params(raymond_net* net, float* params, uint64_t count);
-/* Loss (mean absolute error of the log radiance over albedo) and its
- * gradient with respect to every parameter, without a step. Training crops
- * are multiples of 16 pixels on each side. */
+/* The training loss per pixel and channel: w_log · |o − log(1 + t/a)| +
+ * w_lin · (p − t)², o the network's output, t the target radiance, a the
+ * clamped albedo, p the displayed radiance; averaged. Default 1 and 0. */
+int raymond_net_set_loss(raymond_net* net, float w_log, float w_lin);
+/* Loss and its gradient with respect to every parameter, without a step.
+ * Training crops are multiples of 16 pixels on each side. */
 int raymond_net_gradients(raymond_net* net, const raymond_net_batch* batch, float* grads, uint64_t count, float* loss);
 /* One Adam step (beta 0.9, 0.999; eps 1e-8) on the batch, enqueued on the
  * network's stream; loss (host, optional) waits for it. */
@@ -321,6 +324,11 @@ int raymond_net_sync(raymond_net* net);
  * enqueued on stream (NULL: the network's stream). */
 int raymond_net_infer(raymond_net* net, const raymond_net_batch* batch, float* out_rgba, void* stream);
 void* raymond_net_get_stream(raymond_net* net);
+/* Enqueue the network's work on a caller's cudaStream_t from now on (NULL:
+ * its own stream again; pass cudaStreamLegacy for the legacy default
+ * stream), so that it is ordered with the caller's producers and consumers
+ * of the batch memory. */
+int raymond_net_set_stream(raymond_net* net, void* stream);
 
 /* The renderer's current image through the network: the result replaces the
  * denoised buffer and the display image (display only; accum untouched),

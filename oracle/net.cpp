@@ -3,9 +3,10 @@
 // A direct (no GEMM) double-precision restatement of the network that the
 // product runs on the tensor cores: 3×3 convolutions with zero padding, the
 // leaky ReLU (slope 0.1), 2×2 average pooling, nearest-neighbour upsampling
-// concatenated ahead of the skip input, the 12 input features, the L1 loss
-// on log radiance over albedo, and reverse-mode gradients over the graph in
-// plain forward order reversed. With `bf16` set, weights and every stored
+// concatenated ahead of the skip input, the 12 input features, the loss
+// (weighted L1 on log radiance over albedo plus squared error of the
+// displayed radiance), and reverse-mode gradients over the graph in plain
+// forward order reversed. With `bf16` set, weights and every stored
 // activation and output-gradient tensor are rounded to BF16 as the GPU
 // stores them, so the two can be compared closely; without it the oracle is
 // smooth enough for finite-difference checks of its own gradients.
@@ -206,7 +207,7 @@ void ro_net_layout(uint64_t* w_off, uint64_t* b_off, uint32_t* cin, uint32_t* co
 
 double ro_net_loss_grad(const double* params, const float* accum, const float* albedo, const float* normal,
                         const float* target, const float* samples, uint32_t n, uint32_t h, uint32_t w, int bf16,
-                        double* grads, float* out16) {
+                        double w_log, double w_lin, double* grads, float* out16) {
     uint64_t w_off[19], b_off[19], total = 0;
     layout(w_off, b_off, &total);
     std::vector<double> p(params, params + total);
@@ -245,7 +246,7 @@ double ro_net_loss_grad(const double* params, const float* accum, const float* a
     if (out16)
         for (size_t k = 0; k < t[OUT].v.size(); ++k) out16[k] = float(t[OUT].v[k]);
 
-    // L1 loss on log radiance over albedo.
+    // w_log · L1 on log radiance over albedo + w_lin · squared error of the displayed radiance.
     const double scale = 1.0 / (3.0 * double(n) * h * w);
     double loss = 0.0;
     T g[NT];
@@ -258,9 +259,14 @@ double ro_net_loss_grad(const double* params, const float* accum, const float* a
                 for (int c = 0; c < 3; ++c) {
                     const double a = std::fmax(albedo[4 * q + c] / s, 0.01);
                     const double want = std::log1p(std::fmax(target[4 * q + c] / a, 0.0));
-                    const double d = t[OUT].at(int(i), int(y), int(x), c) - want;
-                    loss += std::fabs(d);
-                    g[OUT].at(int(i), int(y), int(x), c) = (d > 0 ? 1.0 : d < 0 ? -1.0 : 0.0) * scale;
+                    const double o = t[OUT].at(int(i), int(y), int(x), c);
+                    const double d = o - want;
+                    const double pred = o > 0.0 ? std::expm1(o) * a : 0.0;
+                    const double e = pred - target[4 * q + c];
+                    loss += w_log * std::fabs(d) + w_lin * e * e;
+                    double gr = w_log * (d > 0 ? 1.0 : d < 0 ? -1.0 : 0.0);
+                    if (o > 0.0) gr += w_lin * 2.0 * e * (pred + a);
+                    g[OUT].at(int(i), int(y), int(x), c) = gr * scale;
                 }
             }
     loss *= scale;

@@ -91,7 +91,7 @@ uint64_t ro_net_param_count(void);
 void ro_net_layout(uint64_t* w_off, uint64_t* b_off, uint32_t* cin, uint32_t* cout);
 double ro_net_loss_grad(const double* params, const float* accum, const float* albedo, const float* normal,
                         const float* target, const float* samples, uint32_t n, uint32_t h, uint32_t w, int bf16,
-                        double* grads, float* out16);
+                        double w_log, double w_lin, double* grads, float* out16);
 void ro_conv3x3(int mode, uint32_t n, uint32_t h, uint32_t w, const float* src0, uint32_t c0, uint32_t shift0,
                 const float* src1, uint32_t c1, uint32_t cout, const float* weight, const float* bias, const float* dy,
                 const float* mask, int act, float* out, double* dw, double* db);

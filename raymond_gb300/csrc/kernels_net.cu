@@ -522,8 +522,10 @@ __global__ void k_merge(const bf16* __restrict__ skip, int skip_stride, const bf
     *reinterpret_cast<uint4*>(out + p * c + 8 * g) = pack8(s);
 }
 
-// L1 loss between the network's log radiance and the target's, and its
-// gradient (bf16, 16 channels, zero past the third).
+// Loss between the network's output o (log radiance over albedo) and the
+// target: w_log · |o − log(1 + t/a)| + w_lin · (p − t)², p = (eᵒ − 1)·a for
+// o > 0 and 0 otherwise (the displayed radiance), per channel; and its
+// gradient (bf16, 16 channels, zero past the third). dp/do = p + a.
 __global__ void k_loss(LossArgs L) {
     const int total = L.n * L.h * L.w;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -539,11 +541,17 @@ __global__ void k_loss(LossArgs L) {
             const float a[3] = {fmaxf(al.x / n, 0.01f), fmaxf(al.y / n, 0.01f), fmaxf(al.z / n, 0.01f)};
             const float t[3] = {tg.x, tg.y, tg.z};
             for (int c = 0; c < 3; ++c) {
+                const float o = L.out[size_t(p) * 16 + c];
                 const float want = log1pf(fmaxf(t[c] / a[c], 0.0f));
-                const float d = L.out[size_t(p) * 16 + c] - want;
-                if (isfinite(d)) {
-                    part += fabsf(d);
-                    g[c] = (d > 0.0f ? 1.0f : d < 0.0f ? -1.0f : 0.0f) * L.scale;
+                const float d = o - want;
+                const float pred = o > 0.0f ? expm1f(o) * a[c] : 0.0f;
+                const float e = pred - t[c];
+                const float l = L.w_log * fabsf(d) + L.w_lin * e * e;
+                float gr = L.w_log * (d > 0.0f ? 1.0f : d < 0.0f ? -1.0f : 0.0f);
+                if (o > 0.0f) gr += L.w_lin * 2.0f * e * (pred + a[c]);
+                if (isfinite(l) && isfinite(gr)) {
+                    part += l;
+                    g[c] = gr * L.scale;
                 }
             }
         }

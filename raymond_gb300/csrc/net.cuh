@@ -64,6 +64,8 @@ struct LossArgs {
     float samples_all;
     int n, h, w, src_h, src_w;
     float scale;   // 1 / (3 · pixels)
+    float w_log;   // weight of |log radiance error| (over albedo)
+    float w_lin;   // weight of the squared linear radiance error
     __nv_bfloat16* grad;  // [n][h][w][16]
     float* loss;
 };

@@ -108,7 +108,8 @@ uint32_t mix32(uint32_t& s) {  // mulberry32
 struct raymond_net {
     int device = 0;
     int num_sms = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;  // where the network's work is enqueued: its own, or the caller's
     cudaEvent_t ready = nullptr;
     std::string error;
 
@@ -116,6 +117,7 @@ struct raymond_net {
     size_t param_count = 0;
     DevBuf params, params_bf16, grads, adam_m, adam_v, status, loss;
     uint32_t adam_t = 0;
+    float w_log = 1.0f, w_lin = 0.0f;  // loss weights
 
     DevBuf work;
     int wn = 0, wh = 0, ww = 0;
@@ -331,6 +333,8 @@ static cudaError_t run_loss(raymond_net* net, const raymond_net_batch* b, cudaSt
     L.src_h = int(b->height);
     L.src_w = int(b->width);
     L.scale = 1.0f / (3.0f * float(b->n) * float(b->width) * float(b->height));
+    L.w_log = net->w_log;
+    L.w_lin = net->w_lin;
     L.grad = net->t(T_GOUT);
     L.loss = static_cast<float*>(net->loss.ptr);
     return launch_loss(L, st);
@@ -388,7 +392,8 @@ int raymond_net_create(raymond_net** out, const raymond_net_config* cfg) {
     net->device = device;
     net->num_sms = prop.multiProcessorCount;
     cudaSetDevice(device);
-    cudaError_t e = cudaStreamCreateWithFlags(&net->stream, cudaStreamNonBlocking);
+    cudaError_t e = cudaStreamCreateWithFlags(&net->own_stream, cudaStreamNonBlocking);
+    net->stream = net->own_stream;
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&net->ready, cudaEventDisableTiming);
     size_t off = 0;
     for (int l = 0; l < kLayers; ++l) {
@@ -441,7 +446,7 @@ void raymond_net_destroy(raymond_net* net) {
                       &net->loss, &net->work})
         b->release();
     if (net->ready) cudaEventDestroy(net->ready);
-    if (net->stream) cudaStreamDestroy(net->stream);
+    if (net->own_stream) cudaStreamDestroy(net->own_stream);
     delete net;
 }
 
@@ -531,6 +536,15 @@ int raymond_net_train_step(raymond_net* net, const raymond_net_batch* batch, flo
     return loss ? finish(net, loss) : RAYMOND_OK;
 }
 
+int raymond_net_set_loss(raymond_net* net, float w_log, float w_lin) {
+    if (!net) return RAYMOND_EINVAL;
+    if (!(w_log >= 0.0f) || !(w_lin >= 0.0f) || !(w_log + w_lin > 0.0f) || !std::isfinite(w_log + w_lin))
+        return net->fail(RAYMOND_EINVAL, "Loss weights must be finite, non-negative and not both zero.");
+    net->w_log = w_log;
+    net->w_lin = w_lin;
+    return RAYMOND_OK;
+}
+
 int raymond_net_sync(raymond_net* net) {
     if (!net) return RAYMOND_EINVAL;
     cudaSetDevice(net->device);
@@ -578,6 +592,19 @@ int raymond_net_infer(raymond_net* net, const raymond_net_batch* batch, float* o
 }
 
 void* raymond_net_get_stream(raymond_net* net) { return net ? static_cast<void*>(net->stream) : nullptr; }
+
+int raymond_net_set_stream(raymond_net* net, void* stream) {
+    if (!net) return RAYMOND_EINVAL;
+    cudaSetDevice(net->device);
+    cudaStream_t next = stream ? static_cast<cudaStream_t>(stream) : net->own_stream;
+    if (next != net->stream) {
+        // Work already enqueued on the old stream comes first.
+        cudaEventRecord(net->ready, net->stream);
+        cudaStreamWaitEvent(next, net->ready, 0);
+        net->stream = next;
+    }
+    return RAYMOND_OK;
+}
 
 // ---- single kernels, on caller memory
 

@@ -82,6 +82,7 @@ struct raymond {
     JobDesc* b_staging = nullptr;  // pinned host copy of the job table
     uint32_t b_staging_cap = 0;
     cudaEvent_t b_copy_done = nullptr;
+    cudaEvent_t order = nullptr;  // orders a batch frame against the job renderers' own streams
     bool b_copy_pending = false;
     std::vector<WavePlan> b_waves;
     std::vector<uint64_t> b_signature;
@@ -244,6 +245,7 @@ int raymond_create(raymond_t** out, const raymond_config* cfg) {
         return RAYMOND_ECUDA;
     }
     for (cudaEvent_t& ev : h->ev) cudaEventCreate(&ev);
+    cudaEventCreateWithFlags(&h->order, cudaEventDisableTiming);
     h->stage_begin.resize(raymond_stage_events);
     h->stage_end.resize(raymond_stage_events);
     h->stage_kind.resize(raymond_stage_events);
@@ -286,6 +288,7 @@ void raymond_destroy(raymond_t* h) {
         if (ev) cudaEventDestroy(ev);
     if (h->b_graph) cudaGraphExecDestroy(h->b_graph);
     if (h->b_copy_done) cudaEventDestroy(h->b_copy_done);
+    if (h->order) cudaEventDestroy(h->order);
     if (h->b_staging) cudaFreeHost(h->b_staging);
     for (DevBuf* b : {&h->b_jobs, &h->b_segments, &h->b_jobpix}) b->release();
     for (cudaEvent_t ev : h->stage_begin) cudaEventDestroy(ev);
@@ -656,6 +659,14 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
         h->b_paths = total_paths;
     }
 
+    // Work already enqueued on a job renderer's own stream (a learned denoise
+    // reading its sums, a read-back) comes before this frame.
+    for (uint32_t j = 0; j < n; ++j) {
+        raymond* r = jobs[j].renderer;
+        if (r == h) continue;
+        cudaEventRecord(r->order, r->stream);
+        cudaStreamWaitEvent(h->stream, r->order, 0);
+    }
     // This frame's job table: the previous frame's copy must have left the staging buffer.
     if (h->b_copy_pending) cudaEventSynchronize(h->b_copy_done);
     std::memcpy(h->b_staging, desc.data(), n * sizeof(JobDesc));
@@ -710,8 +721,11 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
     if (e != cudaSuccess) return h->cuda_fail(e, "batch");
     h->ev_valid = true;
     h->stage.count = 0;
+    // ... and work enqueued on them later comes after it.
+    cudaEventRecord(h->order, h->stream);
     for (uint32_t j = 0; j < n; ++j) {
         raymond* r = jobs[j].renderer;
+        if (r != h) cudaStreamWaitEvent(r->stream, h->order, 0);
         r->last_params = desc[j].params;
         r->rendered = true;
         r->learned_valid = false;

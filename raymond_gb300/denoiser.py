@@ -18,6 +18,7 @@ from . import _native
 
 WEIGHTS_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights")
 DEFAULT_WEIGHTS = os.path.join(WEIGHTS_DIR, "denoiser_unet.npz")
+CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy: the legacy default stream's handle
 
 
 def _addr(t):
@@ -85,6 +86,10 @@ class Denoiser:
         self.set_params(bits.view(np.float32))
 
     # ---- training
+    def set_loss(self, w_log: float = 1.0, w_lin: float = 0.0) -> None:
+        """Loss weights: w_log on |log radiance error|, w_lin on the squared linear error."""
+        self._check(_native.lib().raymond_net_set_loss(self.handle, float(w_log), float(w_lin)))
+
     def gradients(self, batch):
         """(loss, gradients) of one batch, without a step."""
         g = np.zeros(self.param_count, np.float32)
@@ -110,6 +115,15 @@ class Denoiser:
     @property
     def stream(self):
         return _native.lib().raymond_net_get_stream(self.handle)
+
+    def use_stream(self, stream) -> None:
+        """Enqueue on this cudaStream_t (an int handle, e.g. a torch stream's
+        cuda_stream), ordered with the caller's work on the batch tensors.
+        0 is the legacy default stream (torch's default), passed on as
+        cudaStreamLegacy; None returns to the network's own stream."""
+        if stream == 0:
+            stream = CUDA_STREAM_LEGACY
+        self._check(_native.lib().raymond_net_set_stream(self.handle, stream))
 
     def dispose(self) -> None:
         if self.handle:

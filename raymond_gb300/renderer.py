@@ -278,6 +278,9 @@ class Renderer:
         self._disposed = False
         self._batch = None  # the BatchRenderer that rendered its last frame, if any
         self.flags = 0  # extra raymond_render flags (path choice)
+        # A Denoiser (raymond_gb300.denoiser) to filter the displayed image
+        # instead of the à-trous filter; None keeps the à-trous filter.
+        self.learnedDenoiser = None
 
     @staticmethod
     def create(canvas, powerPreference="high-performance", device=0, seed=0, pathCapacity=0) -> "Renderer":
@@ -416,6 +419,7 @@ class Renderer:
         buf = (ctypes.c_char * PARAMS_BYTES).from_buffer(self._params)
         check(lib().raymond_render(self._h, ctypes.addressof(buf), features, self.flags), self._h)
         self._samples += self._spp
+        self._denoise_learned()
 
     def autotune(self, trials: int = 2, cache: str | None = None):
         """Picks the launch shape for this scene and image by timing
@@ -550,6 +554,15 @@ class Renderer:
     def _denoising(self):
         return self._denoise and self._view == "color"
 
+    def _atrous(self):
+        """The à-trous filter runs inside the frame unless the network replaces it."""
+        return self._denoising() and self.learnedDenoiser is None
+
+    def _denoise_learned(self):
+        """The network over this frame's sums (display only), on this renderer's stream."""
+        if self.learnedDenoiser is not None and self._denoising():
+            check(lib().raymond_denoise_learned(self._h, self.learnedDenoiser.handle, self._samples, None), self._h)
+
     # ---- uploads (src/Renderer.mjs:550-799) ----
     def _upload(self, scene: Scene):
         packed = scene.pack()
@@ -605,7 +618,7 @@ class Renderer:
         block = params_block(scene, camera, width, height, light_count=self._light_count,
                              volume_count=self._volume_count, max_bounces=self._max_bounces, view=self._view,
                              firefly_clamp=self._firefly, samples=self._samples, spp=self._spp,
-                             exposure=self._exposure, denoise=self._denoising(), caustics=self._caustics_active,
+                             exposure=self._exposure, denoise=self._atrous(), caustics=self._caustics_active,
                              deltas=self._deltas)
         key = bytes(block[:IMAGE_KEY_BYTES])
         if key != self._image_key:
@@ -614,7 +627,7 @@ class Renderer:
             block = params_block(scene, camera, width, height, light_count=self._light_count,
                                  volume_count=self._volume_count, max_bounces=self._max_bounces, view=self._view,
                                  firefly_clamp=self._firefly, samples=0, spp=self._spp, exposure=self._exposure,
-                                 denoise=self._denoising(), caustics=self._caustics_active, deltas=self._deltas)
+                                 denoise=self._atrous(), caustics=self._caustics_active, deltas=self._deltas)
         self._params[:] = block
 
     def tracePrimary(self, rays: np.ndarray, scene: Scene | None = None):
@@ -667,6 +680,7 @@ class BatchRenderer:
         for r in renderers:
             r._samples += r._spp
             r._batch = self
+            r._denoise_learned()
 
     def sync(self):
         check(lib().raymond_sync(self._exec.handle), self._exec.handle)

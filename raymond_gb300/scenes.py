@@ -238,3 +238,71 @@ def batch_instances(count: int = 64, seed: int = 4, spheres: int = 10000):
         info["spp"] = spp
         out.append((scene, camera, w, h, spp, info))
     return out
+
+
+# ---------------------------------------------------------------- C3 ----
+
+def water_caustics(seed: int = 3, segments: int = 255):
+    """The caustics scene: a 2×2 water surface (Mesh.surface with
+    segments² cells, 130,050 triangles at 255; ior 1.33) whose height is a
+    sum of 8 seeded sinusoids (wavelength U[0.2, 2], amplitude
+    U[0.002, 0.02]), a checkered diffuse floor one unit below it, a glass
+    sphere (ior 1.5, r = 0.3) on the rim, and one spherical light of
+    r = 0.1 above, under a dim sky. Returns (scene, camera, info)."""
+    rnd = mulberry32(seed)
+    waves = []
+    for _ in range(8):
+        a = 2.0 * math.pi * rnd()
+        lam = 0.2 + 1.8 * rnd()
+        amp = 0.002 + 0.018 * rnd()
+        phase = 2.0 * math.pi * rnd()
+        waves.append((math.cos(a), math.sin(a), 2.0 * math.pi / lam, amp, phase))
+
+    def height(x, z):
+        return sum(amp * math.sin(k * (dx * x + dz * z) + ph) for dx, dz, k, amp, ph in waves)
+
+    dim = Vec3(0.02, 0.025, 0.035)
+    scene = Scene(sky=Sky(zenith=dim, horizon=dim.scale(1.5), ground=dim.scale(0.5)))
+    water = Mesh.surface(lambda u, v: Vec3(-1.0 + 2.0 * u, height(-1.0 + 2.0 * u, -1.0 + 2.0 * v), -1.0 + 2.0 * v),
+                         segments, segments, Material.glass(1.33))
+    floor = Quad(Vec3(-3.0, -1.0, 3.0), Vec3(6.0, 0.0, 0.0), Vec3(0.0, 0.0, -6.0),
+                 Material.checkered(Vec3(0.8, 0.8, 0.75), Vec3(0.25, 0.3, 0.4), 0.25))
+    ball = Sphere(Vec3(1.0, 0.3, -0.2), 0.3, Material.glass(1.5))
+    lamp = Sphere(Vec3(0.4, 2.5, 0.6), 0.1, Material.light(Vec3(1.0, 0.95, 0.85), 300.0))
+    scene.add(floor, water, ball, lamp)
+    camera = Camera(position=Vec3(0.0, 2.6, 3.4), target=Vec3(0.0, -0.6, 0.0), fov=math.radians(45.0))
+    info = {"seed": seed, "triangles": int(water.triangleCount), "waves": len(waves)}
+    return scene, camera, info
+
+
+# ------------------------------------------------- denoiser training views ----
+
+def training_views(count: int, seed: int = 7):
+    """`count` seeded views for the learned denoiser, alternating small
+    sphere-field variants (C2's generator with 300–3,000 spheres and a
+    2k–60k-triangle centre mesh, seen from a random orbit) and water
+    caustics variants (C3's generator with a random camera). Returns a
+    list of (scene, camera, info)."""
+    rnd = mulberry32(seed)
+    out = []
+    for i in range(count):
+        scene_seed = int(rnd() * 2147483647.0)
+        if i % 2 == 0:
+            spheres = int(300 + 2700 * rnd())
+            freq = int(10 + 45 * rnd())
+            scene, camera, info = sphere_field(seed=scene_seed, spheres=spheres, frequency=freq)
+            az = 2.0 * math.pi * rnd()
+            dist = 6.0 + 10.0 * rnd()
+            elev = 0.5 + 5.0 * rnd()
+            tx, tz = -3.0 + 6.0 * rnd(), -3.0 + 6.0 * rnd()
+            camera = Camera(position=Vec3(tx + dist * math.sin(az), elev, tz + dist * math.cos(az)),
+                            target=Vec3(tx, 0.3 + 1.5 * rnd(), tz), fov=math.radians(30.0 + 30.0 * rnd()))
+        else:
+            scene, camera, info = water_caustics(seed=scene_seed, segments=int(40 + 60 * rnd()))
+            az = 2.0 * math.pi * rnd()
+            dist = 2.5 + 2.0 * rnd()
+            camera = Camera(position=Vec3(dist * math.sin(az), 1.2 + 2.0 * rnd(), dist * math.cos(az)),
+                            target=Vec3(0.4 * rnd() - 0.2, -0.7, 0.4 * rnd() - 0.2), fov=math.radians(40.0 + 20.0 * rnd()))
+        info["view"] = i
+        out.append((scene, camera, info))
+    return out

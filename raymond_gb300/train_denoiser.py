@@ -1,0 +1,244 @@
+"""Trains the learned denoiser on image pairs that the path tracer renders
+itself: for each seeded view (scenes.training_views), a converged target
+and noisy renders at 1 to 64 samples per pixel with an independent sample
+stream. Training runs on the GPU through the library's own
+forward, backward and Adam kernels (raymond_net_train_step); PyTorch only
+holds the device memory and cuts the random crops.
+
+    python -m raymond_gb300.train_denoiser --views 160 --steps 4000 --out weights.npz
+
+Each --loss variant (w_log,w_lin: the weights of the L1 log-radiance and
+the squared linear-radiance terms) trains from the same initial weights on
+the same data; the one with the lowest held-out RMSE at 4 spp is saved.
+The report (--report) gives, for held-out views at 1, 4 and 16 spp, the
+RMSE against the converged render of the noisy image, of the à-trous
+filter and of the network."""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import sys
+import time
+
+import numpy as np
+
+from . import _native, scenes
+from .denoiser import DEFAULT_WEIGHTS, Denoiser, make_batch
+from .renderer import Canvas, Renderer
+
+NOISY_SPP = (1, 2, 4, 8, 16, 32, 64)
+NOISE_SEED = 0x5BD1E995
+
+
+def rmse(a, b) -> float:
+    """Root mean square RGB difference (the reference's rmse)."""
+    d = np.asarray(a, np.float64)[..., :3] - np.asarray(b, np.float64)[..., :3]
+    return float(np.sqrt(np.mean(d * d)))
+
+
+def render_view(scene, camera, size, target_spp, bounces=8):
+    """(target mean radiance, [(spp, accum, albedo, normal) sums at each of NOISY_SPP])."""
+    canvas = Canvas(size, size)
+    ref = Renderer.create(canvas)
+    ref.scene, ref.camera = scene, camera
+    ref.maxBounces = bounces
+    ref.denoise = False
+    ref.caustics = False
+    per_frame = min(64, target_spp)
+    ref.samplesPerFrame = per_frame
+    for _ in range(target_spp // per_frame):
+        ref.render()
+    target = ref.readPixels().reshape(size, size, 4)
+    ref.dispose()
+
+    noisy = Renderer.create(canvas, seed=NOISE_SEED)
+    noisy.scene, noisy.camera = scene, camera
+    noisy.maxBounces = bounces
+    noisy.denoise = False
+    noisy.caustics = False
+    out = []
+    done = 0
+    for spp in NOISY_SPP:
+        noisy.samplesPerFrame = spp - done
+        noisy.render()
+        done = spp
+        a, g, n = noisy.readGuides()
+        out.append((spp, a, g, n))
+    noisy.dispose()
+    return target, out
+
+
+def build_dataset(views, size, target_spp, log=print):
+    t0 = time.time()
+    targets, inputs = [], []
+    for k, (scene, camera, info) in enumerate(views):
+        target, noisy = render_view(scene, camera, size, target_spp)
+        targets.append(target)
+        inputs.append(noisy)
+        if (k + 1) % 16 == 0:
+            log(f"  rendered {k + 1}/{len(views)} views ({time.time() - t0:.1f} s)")
+    return targets, inputs
+
+
+def atrous(accum, albedo, normal, spp, torch):
+    """The à-trous filter (raymond_denoise_static) on one noisy render."""
+    h, w = accum.shape[:2]
+    dev = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (accum, albedo, normal)]
+    out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    _native.check(_native.lib().raymond_denoise_static(dev[0].data_ptr(), dev[1].data_ptr(), dev[2].data_ptr(), w, h,
+                                                       spp, out.data_ptr(), None))
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def learned(net, accum, albedo, normal, spp, torch):
+    h, w = accum.shape[:2]
+    dev = [torch.from_numpy(np.ascontiguousarray(x)).cuda()[None] for x in (accum, albedo, normal)]
+    out = torch.empty((1, h, w, 4), dtype=torch.float32, device="cuda")
+    net.infer(make_batch(*dev, samples_all=float(spp)), out)
+    net.sync()
+    return out[0].cpu().numpy()
+
+
+def evaluate(net, targets, inputs, spp=4):
+    import torch
+
+    rows = []
+    for target, noisy in zip(targets, inputs):
+        s, a, g, n = next(x for x in noisy if x[0] == spp)
+        rows.append({"noisy": rmse(a / s, target), "atrous": rmse(atrous(a, g, n, s, torch), target),
+                     "learned": rmse(learned(net, a, g, n, s, torch), target)})
+    mean = {k: float(np.mean([r[k] for r in rows])) for k in rows[0]}
+    return mean, rows
+
+
+def parse_losses(text):
+    out = []
+    for item in text.split(";"):
+        w_log, w_lin = (float(v) for v in item.split(","))
+        out.append((w_log, w_lin))
+    return out
+
+
+def train(net, targets, inputs, steps, batch, crop, lr, seed=1, log=print):
+    import torch
+
+    rng = np.random.default_rng(seed)
+    levels = len(NOISY_SPP)
+    # The crops are cut on a torch stream and the network runs on the same
+    # one, so each step reads finished crops and torch's allocator reuses
+    # their memory only after the step.
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    net.use_stream(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        out = _train_loop(net, targets, inputs, steps, batch, crop, lr, rng, levels, log, torch)
+    net.sync()
+    net.use_stream(None)
+    return out
+
+
+def _train_loop(net, targets, inputs, steps, batch, crop, lr, rng, levels, log, torch):
+    acc = torch.from_numpy(np.stack([[x[1] for x in v] for v in inputs])).cuda()  # [V, L, H, W, 4]
+    alb = torch.from_numpy(np.stack([[x[2] for x in v] for v in inputs])).cuda()
+    nrm = torch.from_numpy(np.stack([[x[3] for x in v] for v in inputs])).cuda()
+    tgt = torch.from_numpy(np.stack(targets)).cuda()  # [V, H, W, 4]
+    spp = torch.tensor(NOISY_SPP, dtype=torch.float32, device="cuda")
+    V, size = acc.shape[0], acc.shape[2]
+    losses = []
+    t0 = time.time()
+    for step in range(steps):
+        vi = torch.from_numpy(rng.integers(0, V, batch)).cuda()
+        li = torch.from_numpy(rng.integers(0, levels, batch)).cuda()
+        y0, x0 = (int(v) for v in rng.integers(0, size - crop + 1, 2))
+        sl = (slice(y0, y0 + crop), slice(x0, x0 + crop))
+        a = acc[vi, li][:, sl[0], sl[1]]
+        g = alb[vi, li][:, sl[0], sl[1]]
+        n = nrm[vi, li][:, sl[0], sl[1]]
+        t = tgt[vi][:, sl[0], sl[1]]
+        flip = rng.integers(0, 4)
+        if flip & 1:
+            a, g, n, t = (z.flip(2) for z in (a, g, n, t))
+        if flip & 2:
+            a, g, n, t = (z.flip(1) for z in (a, g, n, t))
+        a, g, n, t = (z.contiguous() for z in (a, g, n, t))
+        s = spp[li].contiguous()
+        warm = min(1.0, (step + 1) / 100.0)
+        rate = lr * warm * (0.02 + 0.98 * 0.5 * (1.0 + math.cos(math.pi * step / steps)))
+        want = step % 100 == 0 or step == steps - 1
+        loss = net.train_step(make_batch(a, g, n, t, samples=s), rate, want_loss=want)
+        if want:
+            losses.append((step, loss))
+            log(f"  step {step:5d}  loss {loss:.4f}  lr {rate:.2e}  {time.time() - t0:.1f} s")
+    net.sync()
+    return losses, time.time() - t0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--views", type=int, default=160)
+    ap.add_argument("--holdout", type=int, default=8)
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--target-spp", type=int, default=1024)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--crop", type=int, default=128)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--loss", default="1,0;0.5,4", help="variants w_log,w_lin separated by ';'")
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--report", default=None)
+    args = ap.parse_args(argv)
+
+    def log(msg):
+        print(msg, flush=True)
+
+    t0 = time.time()
+    views = scenes.training_views(args.views + args.holdout, seed=args.seed)
+    train_views, held = views[:args.views], views[args.views:]
+    log(f"{len(train_views)} training views, {len(held)} held out; {args.size}² at {args.target_spp} spp")
+    targets, inputs = build_dataset(train_views, args.size, args.target_spp, log)
+    h_targets, h_inputs = build_dataset(held, args.size, args.target_spp, log)
+    t_data = time.time() - t0
+    variants = []
+    best = None
+    for w_log, w_lin in parse_losses(args.loss):
+        net = Denoiser(seed=args.seed)
+        net.set_loss(w_log, w_lin)
+        log(f"loss variant w_log={w_log} w_lin={w_lin}")
+        losses, t_train = train(net, targets, inputs, args.steps, args.batch, args.crop, args.lr, seed=args.seed,
+                                log=log)
+        result = {"w_log": w_log, "w_lin": w_lin, "seconds_train": t_train, "loss": losses}
+        for spp in (1, 4, 16):
+            result[f"holdout_rmse_{spp}spp"], rows = evaluate(net, h_targets, h_inputs, spp)
+            if spp == 4:
+                result["holdout_rows_4spp"] = rows
+        log(json.dumps({k: result[k] for k in ("w_log", "w_lin", "holdout_rmse_1spp", "holdout_rmse_4spp",
+                                               "holdout_rmse_16spp")}))
+        variants.append(result)
+        score = result["holdout_rmse_4spp"]["learned"]
+        if best is None or score < best[0]:
+            if best is not None:
+                best[1].dispose()
+            best = (score, net, result)
+        else:
+            net.dispose()
+    os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
+    best[1].save(args.out)
+    report = {"views": args.views, "holdout": args.holdout, "size": args.size, "target_spp": args.target_spp,
+              "noisy_spp": list(NOISY_SPP), "steps": args.steps, "batch": args.batch, "crop": args.crop,
+              "lr": args.lr, "seed": args.seed, "seconds_data": t_data, "variants": variants,
+              "chosen": {"w_log": best[2]["w_log"], "w_lin": best[2]["w_lin"]},
+              "weights": os.path.basename(args.out)}
+    if args.report:
+        with open(args.report, "w") as f:
+            json.dump(report, f, indent=1)
+    return report
+
+
+if __name__ == "__main__":
+    main()

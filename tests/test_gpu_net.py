@@ -156,9 +156,11 @@ def test_parameter_layout_matches_oracle(gpu):
     net.dispose()
 
 
-def test_network_gradients_match_oracle(gpu):
+@pytest.mark.parametrize("w_log,w_lin", [(1.0, 0.0), (0.5, 4.0)])
+def test_network_gradients_match_oracle(gpu, w_log, w_lin):
     rng = np.random.default_rng(21)
     net = Denoiser(seed=3)
+    net.set_loss(w_log, w_lin)
     count, layout = oracle.net_layout()
     params = _random_params(count, layout, rng)
     # BF16-exact weights so both sides multiply the same numbers
@@ -170,7 +172,8 @@ def test_network_gradients_match_oracle(gpu):
            dict(accum=accum, albedo=albedo, normal=normal, target=target).items()}
     batch = make_batch(dev["accum"], dev["albedo"], dev["normal"], dev["target"], samples_all=spp)
     loss, grads = net.gradients(batch)
-    want_loss, want, _ = oracle.net_loss_grad(params.astype(np.float64), accum, albedo, normal, target, spp, bf16=True)
+    want_loss, want, _ = oracle.net_loss_grad(params.astype(np.float64), accum, albedo, normal, target, spp, bf16=True,
+                                              w_log=w_log, w_lin=w_lin)
     assert abs(loss - want_loss) <= 2e-3 * want_loss
     cos_all = float(np.dot(grads, want) / (np.linalg.norm(grads) * np.linalg.norm(want)))
     assert cos_all > 0.999

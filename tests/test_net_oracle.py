@@ -68,7 +68,8 @@ def _inputs(rng, n, h, w, spp=4.0):
     return accum, albedo, normal, target
 
 
-def test_oracle_network_gradients_match_finite_differences():
+@pytest.mark.parametrize("w_log,w_lin", [(1.0, 0.0), (0.5, 4.0)])
+def test_oracle_network_gradients_match_finite_differences(w_log, w_lin):
     count, layout = oracle.net_layout()
     rng = np.random.default_rng(11)
     params = np.zeros(count, np.float64)
@@ -76,7 +77,7 @@ def test_oracle_network_gradients_match_finite_differences():
         params[wo:wo + cout * 9 * cin] = rng.uniform(-1, 1, cout * 9 * cin) * np.sqrt(6.0 / (1.01 * 9 * cin))
         params[bo:bo + cout] = rng.uniform(-0.05, 0.05, cout)
     accum, albedo, normal, target = _inputs(rng, 1, 16, 16)
-    loss, grads, _ = oracle.net_loss_grad(params, accum, albedo, normal, target, 4.0)
+    loss, grads, _ = oracle.net_loss_grad(params, accum, albedo, normal, target, 4.0, w_log=w_log, w_lin=w_lin)
     assert np.isfinite(loss) and loss > 0
     # weights and biases of the first, a middle, a skip-concatenating and the last layer
     picks = []
@@ -89,7 +90,7 @@ def test_oracle_network_gradients_match_finite_differences():
         p1[i] += eps
         p2 = params.copy()
         p2[i] -= eps
-        lp = oracle.net_loss_grad(p1, accum, albedo, normal, target, 4.0, grads=False)[0]
-        lm = oracle.net_loss_grad(p2, accum, albedo, normal, target, 4.0, grads=False)[0]
+        lp = oracle.net_loss_grad(p1, accum, albedo, normal, target, 4.0, grads=False, w_log=w_log, w_lin=w_lin)[0]
+        lm = oracle.net_loss_grad(p2, accum, albedo, normal, target, 4.0, grads=False, w_log=w_log, w_lin=w_lin)[0]
         fd = (lp - lm) / (2 * eps)
         assert abs(fd - grads[i]) <= 1e-4 * max(abs(fd), abs(grads[i])) + 1e-9, (i, fd, grads[i])
