@@ -8,6 +8,15 @@ denoiser and the tone map. Prints one JSON line (rank 0).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--spp S] [--impl ours|reference]
 
+The default line also carries "learned_denoiser": the learned denoiser's
+inference on a 1920×1080 frame of the same scene against the tensor peak.
+Other workloads (--workload):
+  batch    64 seeded sphere-field instances as one graph-replayed batched frame
+  denoise  the learned denoiser's 1080p inference as its own line
+  rmse     time to RMSE ≤ 0.01 against a 16,384-spp render: the plain
+           one-kernel path with à-trous vs the batched wavefront path with
+           the learned denoiser
+
 Under torchrun each rank renders its own copy of the frame (replicas; the
 scene does not shard across GPUs here): value = paths of all ranks ÷ the
 slowest rank's time.
@@ -141,6 +150,276 @@ def params_for(scene, camera, size, spp, bounces):
     words, powers = light_table(packed)
     return params_block(scene, camera, size, size, light_count=len(powers), volume_count=len(packed.volumes),
                         max_bounces=bounces, spp=spp)
+
+
+def device_view(torch, ptr, shape, device):
+    """A device float32 buffer of the library's (a renderer's) as a torch tensor, without a copy."""
+
+    class _View:
+        pass
+
+    v = _View()
+    v.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": "<f4", "data": (int(ptr), False), "version": 3,
+                                  "strides": None}
+    return torch.as_tensor(v, device=f"cuda:{device}")
+
+
+def measured_peak_tensor():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured (burst)"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
+def denoiser_flops(width, height):
+    """Algorithmic FLOPs of one learned-denoiser frame: Σ over the 19 convolutions
+    of 2·H_l·W_l·C_in·C_out·9, with the 12 real input and 3 real output channels."""
+    from raymond_gb300.denoiser import Denoiser  # noqa: F401  (layer table lives in the library)
+    import oracle
+
+    _, layout = oracle.net_layout()
+    levels = [0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 3, 3, 2, 2, 1, 1, 0, 0, 0]
+    total = 0.0
+    for li, (_, _, cin, cout) in enumerate(layout):
+        cin = 12 if li == 0 else cin
+        cout = 3 if li == 18 else cout
+        px = (width / 2 ** levels[li]) * (height / 2 ** levels[li])
+        total += 2.0 * px * cin * cout * 9
+    return total
+
+
+def measure_denoiser(scene, camera, local, steps, warmup, width=1920, height=1080, spp=4):
+    """The learned denoiser's inference on a width×height frame of the scene,
+    inputs resident in HBM: mean ms per frame (CUDA events on the network's
+    stream, L2 flushed between steps), TFLOP/s against the tensor peak, the
+    end-to-end time with host buffers, and the CPU oracle's rate."""
+    import numpy as np
+    import torch
+
+    import raymond_gb300 as rg
+    from raymond_gb300 import _native
+    from raymond_gb300.denoiser import DEFAULT_WEIGHTS, Denoiser, make_batch
+
+    r = rg.Renderer.create(rg.Canvas(width, height), device=local)
+    r.scene, r.camera = scene, camera
+    r.caustics = False
+    r.denoise = False
+    r.samplesPerFrame = spp
+    r.render()
+    r.device.queue.onSubmittedWorkDone()
+    bufs = _native.Buffers()
+    _native.check(_native.lib().raymond_get_buffers(r.handle, bufs), r.handle)
+    shape = (1, height, width, 4)
+    acc, alb, nrm = (device_view(torch, p, shape, local) for p in (bufs.accum, bufs.guide_albedo, bufs.guide_normal))
+    net = Denoiser(device=local, weights=DEFAULT_WEIGHTS)
+    out = torch.empty(shape, dtype=torch.float32, device=f"cuda:{local}")
+    batch = make_batch(acc, alb, nrm, samples_all=float(r.samples))
+    # The network runs on a torch-owned stream, so torch's allocators never
+    # hold on to a stream that the library destroys.
+    stream = torch.cuda.Stream(device=local)
+    torch.cuda.synchronize()
+    net.use_stream(stream.cuda_stream)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    for _ in range(max(warmup, 3)):
+        net.infer(batch, out)
+    net.sync()
+    ms = []
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        net.infer(batch, out)
+        b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    flops = denoiser_flops(width, height)
+    peak, peak_kind = measured_peak_tensor()
+    frame_s = statistics.mean(ms) / 1e3
+    achieved = flops / frame_s / 1e12
+
+    # End to end: host (pinned) buffers in, the denoised image out.
+    host = [x.cpu().pin_memory() for x in (acc, alb, nrm)]
+    dev = [torch.empty(shape, dtype=torch.float32, device=f"cuda:{local}") for _ in range(3)]
+    res = torch.empty(shape, dtype=torch.float32).pin_memory()
+    e2e_steps = max(3, steps // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        with torch.cuda.stream(stream):
+            for d, h in zip(dev, host):
+                d.copy_(h, non_blocking=True)
+        net.infer(make_batch(*dev, samples_all=float(r.samples)), out)
+        with torch.cuda.stream(stream):
+            res.copy_(out, non_blocking=True)
+        stream.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+
+    # CPU: the oracle's network forward (double, one thread) on a 32×32 crop.
+    import oracle
+
+    crop = [np.ascontiguousarray(x[0, :32, :32].cpu().numpy()) for x in (acc, alb, nrm)]
+    params = net.get_params().astype(np.float64)
+    t0 = time.perf_counter()
+    oracle.net_loss_grad(params, crop[0][None], crop[1][None], crop[2][None], crop[0][None], float(r.samples),
+                         grads=False)
+    cpu_s = (time.perf_counter() - t0) * (width * height) / (32 * 32)
+    torch.cuda.synchronize()
+    del host, dev, res, out, flush, acc, alb, nrm
+    net.use_stream(None)
+    net.dispose()
+    r.dispose()
+    return {
+        "workload": f"learned denoiser, {width}x{height} frame of the sphere field at {spp} spp",
+        "ms_per_frame": statistics.mean(ms), "frames_per_s": 1.0 / frame_s,
+        "launches_per_frame": 25,
+        "roofline": {"bound": "tensor", "kernel": "k_conv (19 launches, whole inference)", "achieved": achieved,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "flops_per_frame": flops, "traffic": None},
+        "e2e": {"value": 1.0 / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": 3 * width * height * 16,
+                "d2h_bytes_per_step": width * height * 16},
+        "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "frames/s", "cores": 1, "kind": "port",
+                         "sample": "oracle network forward on a 32x32 crop, scaled by pixels"},
+        "l2": "flushed between steps (512 MB write)",
+    }
+
+
+def run_denoise(args, local):
+    """The learned denoiser's 1080p inference as its own bench line."""
+    scene, camera, info = build_workload(args.size, args.spp, args.bounces)
+    clocks = ClockSampler(local)
+    clocks.start()
+    d = measure_denoiser(scene, camera, local, args.steps, args.warmup)
+    clock_info = clocks.stop()
+    return {
+        "metric": "learned-denoiser frames/s at 1920x1080", "value": d["frames_per_s"], "unit": "frames/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": d["ms_per_frame"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+        "data": "synthetic (seeded mulberry32 scene, rendered at 4 spp)",
+        "config": {"workload": d["workload"], "l2": d["l2"], "weights": "raymond_gb300/weights/denoiser_unet.npz"},
+        "e2e": d["e2e"], "gpu_launches": d["launches_per_frame"] * args.steps, "roofline": d["roofline"],
+        "cpu_baseline": d["cpu_baseline"], "clocks": clock_info,
+    }
+
+
+def run_rmse(args, local):
+    """Time to RMSE ≤ 0.01 against a 16,384-spp render of the sphere field:
+    the plain one-kernel path with the à-trous filter against the batched
+    wavefront path with the learned denoiser, both displaying after every
+    frame of --spp samples. Frame times are wall-clock (each frame waited
+    for); the RMSE check after a frame is not timed."""
+    import numpy as np
+    import torch
+
+    import raymond_gb300 as rg
+    from raymond_gb300 import _native
+    from raymond_gb300.denoiser import DEFAULT_WEIGHTS, Denoiser
+
+    size = args.size
+    scene, camera, info = build_workload(size, args.spp, args.bounces)
+    dev = f"cuda:{local}"
+
+    def renderer(seed, flags):
+        r = rg.Renderer.create(rg.Canvas(size, size), device=local, seed=seed)
+        r.scene, r.camera = scene, camera
+        r.maxBounces = args.bounces
+        r.caustics = False
+        r.flags = flags
+        return r
+
+    t0 = time.perf_counter()
+    ref = renderer(0x2545F491, _native.FLAG_WAVEFRONT)
+    ref.denoise = False
+    ref.samplesPerFrame = 64
+    for _ in range(args.reference_spp // 64):
+        ref.render()
+    target = torch.from_numpy(ref.readPixels().reshape(size, size, 4)).to(dev)
+    ref.dispose()
+    ref_s = time.perf_counter() - t0
+
+    def denoised_view(r):
+        b = _native.Buffers()
+        _native.check(_native.lib().raymond_get_buffers(r.handle, b), r.handle)
+        return device_view(torch, b.denoised, (size, size, 4), local)
+
+    def err(view):
+        d = view[..., :3] - target[..., :3]
+        return float(torch.sqrt(torch.mean(d * d)).item())
+
+    def accum_view(r):
+        b = _native.Buffers()
+        _native.check(_native.lib().raymond_get_buffers(r.handle, b), r.handle)
+        return device_view(torch, b.accum, (size, size, 4), local)
+
+    def run(r, frame):
+        view = None  # the renderer's buffers exist from its first frame on
+        elapsed, curve = 0.0, []
+        reached = None
+        while r.samples < args.max_spp:
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            frame()
+            elapsed += time.perf_counter() - t
+            if view is None:
+                view, raw = denoised_view(r), accum_view(r)
+            e = err(view)
+            # the running average itself, for reference (not what is displayed)
+            d = raw[..., :3] / r.samples - target[..., :3]
+            curve.append((r.samples, elapsed, e, float(torch.sqrt(torch.mean(d * d)).item())))
+            if e <= args.threshold:
+                reached = (r.samples, elapsed)
+                break
+        return reached, curve
+
+    plain = renderer(0, _native.FLAG_MEGAKERNEL)
+    plain.denoise = True
+    plain.samplesPerFrame = args.spp
+
+    def plain_frame():
+        plain.render()
+        plain.device.queue.onSubmittedWorkDone()
+
+    plain_reached, plain_curve = run(plain, plain_frame)
+    plain.dispose()
+
+    net = Denoiser(device=local, weights=DEFAULT_WEIGHTS)
+    ours = renderer(0, _native.FLAG_WAVEFRONT)
+    ours.denoise = True
+    ours.learnedDenoiser = net
+    ours.samplesPerFrame = args.spp
+    batch = rg.BatchRenderer(device=local, graph=True)
+
+    def ours_frame():
+        batch.render([ours])
+        ours._sync()
+
+    ours_reached, ours_curve = run(ours, ours_frame)
+    ours.dispose()
+    batch.dispose()
+    net.dispose()
+
+    def summary(reached, curve):
+        last = curve[-1]
+        return {"reached": reached is not None, "seconds": reached[1] if reached else None,
+                "spp": reached[0] if reached else None, "final_spp": last[0], "final_rmse": last[2],
+                "curve_spp_seconds_rmse_rawrmse": [(s, round(t, 4), round(e, 5), round(q, 5))
+                                                   for s, t, e, q in curve[:: max(1, len(curve) // 40)]]}
+
+    p = summary(plain_reached, plain_curve)
+    o = summary(ours_reached, ours_curve)
+    speedup = (p["seconds"] / o["seconds"]) if (p["reached"] and o["reached"]) else None
+    return {
+        "metric": "time-to-RMSE 0.01 (batched wavefront + learned denoiser)", "value": o["seconds"], "unit": "s",
+        "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 trace, bf16 network", "data": "synthetic (seeded mulberry32 scene)",
+        "config": {"workload": f"sphere field {size}x{size}, {args.spp} spp per displayed frame, {args.bounces} bounces",
+                   "threshold": args.threshold, "reference_spp": args.reference_spp, "reference_seconds": ref_s,
+                   "max_spp": args.max_spp},
+        "plain_atrous": p, "batched_learned": o, "speedup_vs_plain_atrous": speedup,
+    }
 
 
 def run_reference(args, rank, world):
@@ -310,6 +589,8 @@ def run_ours(args, rank, world, local):
             "clocks": clock_info,
         }
     r.dispose()
+    if rank == 0 and not args.no_denoiser:
+        result["learned_denoiser"] = measure_denoiser(scene, camera, local, 10, 3)
     return result
 
 
@@ -385,7 +666,11 @@ def main():
     ap.add_argument("--bounces", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", default="auto", choices=["auto", "megakernel", "wavefront"])
-    ap.add_argument("--workload", default="field", choices=["field", "batch"])
+    ap.add_argument("--workload", default="field", choices=["field", "batch", "denoise", "rmse"])
+    ap.add_argument("--threshold", type=float, default=0.01)
+    ap.add_argument("--reference-spp", type=int, default=16384)
+    ap.add_argument("--max-spp", type=int, default=4096)
+    ap.add_argument("--no-denoiser", action="store_true", help="skip the learned-denoiser sub-measurement")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--batch-spheres", type=int, default=10000)
     args = ap.parse_args()
@@ -398,6 +683,10 @@ def main():
         out = run_reference(args, rank, world)
     elif args.workload == "batch":
         out = run_batch(args) if rank == 0 else None
+    elif args.workload == "denoise":
+        out = run_denoise(args, local) if rank == 0 else None
+    elif args.workload == "rmse":
+        out = run_rmse(args, local) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, local)
     if rank == 0 and out is not None:

@@ -274,7 +274,12 @@ int raymond_denoise_static(const float* accum, const float* guide_albedo, const 
  * tensor cores) with its FP32 master weights and Adam state, on one GPU.
  * Inputs are 12 channels computed from a renderer's buffers (log radiance
  * over albedo, albedo, normal, log depth, log standard error, 1/sqrt(n));
- * the output is the log radiance over albedo, multiplied back by albedo.
+ * the output is a predicted log radiance over albedo (exponentiated and
+ * multiplied back by albedo) and a per-pixel weight: the display is
+ * α·prediction + (1 − α)·running average, α = sigmoid(weight)·v/(v + 0.05²)
+ * with v the running average's relative variance of the mean luminance (the
+ * factor is 1 below 4 samples), so α → 0 and the display converges with the
+ * average as samples accumulate.
  * Errors: raymond_net_last_error(net); a failed create sets
  * raymond_last_error(NULL).
  */
@@ -309,10 +314,14 @@ int raymond_net_layout(const raymond_net* net, uint64_t* weight_offsets, uint64_
                        uint32_t* cout, uint32_t layers);
 int raymond_net_set_params(raymond_net* net, const float* params, uint64_t count); /* resets Adam */
 int raymond_net_get_params(raymond_net* net, float* params, uint64_t count);
-/* The training loss per pixel and channel: w_log · |o − log(1 + t/a)| +
- * w_lin · (p − t)², o the network's output, t the target radiance, a the
- * clamped albedo, p the displayed radiance; averaged. Default 1 and 0. */
-int raymond_net_set_loss(raymond_net* net, float w_log, float w_lin);
+/* The training loss per pixel and channel is lg(f) + lg(p), f the display,
+ * p the prediction, lg(v) = w_log · |log(1 + v/a) − log(1 + t/a)| + w_rel ·
+ * (v − t)² / (v² + 0.01), t the target radiance, a the clamped albedo (the
+ * relative term's denominator held constant; the prediction's exponent
+ * clamped to ±8, its gradient passed through); averaged. Each element's
+ * gradient is clipped to ±64 before averaging, and Adam skips non-finite
+ * gradient elements. Default weights 1 and 0. */
+int raymond_net_set_loss(raymond_net* net, float w_log, float w_rel);
 /* Loss and its gradient with respect to every parameter, without a step.
  * Training crops are multiples of 16 pixels on each side. */
 int raymond_net_gradients(raymond_net* net, const raymond_net_batch* batch, float* grads, uint64_t count, float* loss);

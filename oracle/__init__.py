@@ -48,7 +48,7 @@ def lib():
         _lib.ro_net_layout.restype = None
         _lib.ro_net_layout.argtypes = [P, P, P, P]
         _lib.ro_net_loss_grad.restype = D
-        _lib.ro_net_loss_grad.argtypes = [P, P, P, P, P, P, U32, U32, U32, I, D, D, P, P]
+        _lib.ro_net_loss_grad.argtypes = [P, P, P, P, P, P, U32, U32, U32, I, D, D, D, P, P]
         _lib.ro_conv3x3.restype = None
         _lib.ro_conv3x3.argtypes = [I, U32, U32, U32, P, U32, U32, P, U32, U32, P, P, P, P, I, P, P, P]
     return _lib
@@ -185,7 +185,7 @@ def net_layout():
 
 
 def net_loss_grad(params, accum, albedo, normal, target, samples, bf16=False, grads=True, out=False, w_log=1.0,
-                  w_lin=0.0):
+                  w_rel=0.0, rel_eps=0.01):
     """Loss, gradients (float64, or None) and the network output ([n,h,w,16] float32, or None)
     for n images of h×w (float4 arrays [n,h,w,4] as a renderer accumulates them)."""
     L = lib()
@@ -199,7 +199,7 @@ def net_loss_grad(params, accum, albedo, normal, target, samples, bf16=False, gr
     g = np.zeros(params.size, np.float64) if grads else None
     o = np.zeros((n, h, w, 16), np.float32) if out else None
     loss = L.ro_net_loss_grad(_p(params), _p(accum), _p(albedo), _p(normal), _p(target), _p(samples), n, h, w,
-                              1 if bf16 else 0, float(w_log), float(w_lin), _p(g), _p(o))
+                              1 if bf16 else 0, float(w_log), float(w_rel), float(rel_eps), _p(g), _p(o))
     return loss, g, o
 
 

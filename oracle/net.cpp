@@ -3,10 +3,11 @@
 // A direct (no GEMM) double-precision restatement of the network that the
 // product runs on the tensor cores: 3×3 convolutions with zero padding, the
 // leaky ReLU (slope 0.1), 2×2 average pooling, nearest-neighbour upsampling
-// concatenated ahead of the skip input, the 12 input features, the loss
-// (weighted L1 on log radiance over albedo plus squared error of the
-// displayed radiance), and reverse-mode gradients over the graph in plain
-// forward order reversed. With `bf16` set, weights and every stored
+// concatenated ahead of the skip input, the 12 input features, the display
+// (the network's predicted radiance blended with the running average by a
+// predicted weight), the loss (weighted L1 on log radiance over albedo plus
+// relative squared error of the display), and reverse-mode gradients over the graph in
+// plain forward order reversed. With `bf16` set, weights and every stored
 // activation and output-gradient tensor are rounded to BF16 as the GPU
 // stores them, so the two can be compared closely; without it the oracle is
 // smooth enough for finite-difference checks of its own gradients.
@@ -49,6 +50,9 @@ struct T {
 };
 
 const double kLeak = 0.1;
+const double kMaxLog = 8.0;    // the prediction's exponent is clamped to ±this
+const double kMaxGrad = 64.0;  // and clips each element's gradient to ±this (before scaling)
+const double kBlendTau = 0.05;  // the blend guard's relative error scale (off below 4 samples)
 
 // Layer table: sources (tensor ids), output id, cout, activation.
 enum { IN, E0A, E0, P1, E1A, E1, P2, E2A, E2, P3, E3A, E3, P4, E4A, E4, D3A, D3, D2A, D2, D1A, D1, D0A, D0, OUT, NT };
@@ -207,7 +211,7 @@ void ro_net_layout(uint64_t* w_off, uint64_t* b_off, uint32_t* cin, uint32_t* co
 
 double ro_net_loss_grad(const double* params, const float* accum, const float* albedo, const float* normal,
                         const float* target, const float* samples, uint32_t n, uint32_t h, uint32_t w, int bf16,
-                        double w_log, double w_lin, double* grads, float* out16) {
+                        double w_log, double w_rel, double rel_eps, double* grads, float* out16) {
     uint64_t w_off[19], b_off[19], total = 0;
     layout(w_off, b_off, &total);
     std::vector<double> p(params, params + total);
@@ -246,28 +250,52 @@ double ro_net_loss_grad(const double* params, const float* accum, const float* a
     if (out16)
         for (size_t k = 0; k < t[OUT].v.size(); ++k) out16[k] = float(t[OUT].v[k]);
 
-    // w_log · L1 on log radiance over albedo + w_lin · squared error of the displayed radiance.
+    // The display f blends the prediction p = a·e^o with the running average
+    // by alpha = sigmoid(out[3]) · guard; the loss is lg(f) + lg(p), lg(v) = w_log ·
+    // |log(1 + v/a) − log(1 + t/a)| + w_rel · (v − t)² / (v² + rel_eps) with
+    // the relative term's denominator held constant.
     const double scale = 1.0 / (3.0 * double(n) * h * w);
     double loss = 0.0;
     T g[NT];
     g[OUT].init(int(n), int(h), int(w), 16);
+    auto lg = [&](double v, double tc, double a, double* l) {
+        const double d = std::log1p(v / a) - std::log1p(std::fmax(tc / a, 0.0));
+        const double e = v - tc;
+        const double den = v * v + rel_eps;
+        *l += w_log * std::fabs(d) + w_rel * e * e / den;
+        return w_log * (d > 0 ? 1.0 : d < 0 ? -1.0 : 0.0) / (a + v) + w_rel * 2.0 * e / den;
+    };
     for (uint32_t i = 0; i < n; ++i)
         for (uint32_t y = 0; y < h; ++y)
             for (uint32_t x = 0; x < w; ++x) {
                 const size_t q = (size_t(i) * h + y) * w + x;
                 const double s = std::fmax(double(samples[i]), 1.0);
+                const double z = std::fmin(std::fmax(t[OUT].at(int(i), int(y), int(x), 3), -20.0), 20.0);
+                const double gate = 1.0 / (1.0 + std::exp(-z));
+                // guard: the average's relative variance of the mean luminance v, v/(v + tau²)
+                const double mr = std::fmax(accum[4 * q] / s, 0.0), mg = std::fmax(accum[4 * q + 1] / s, 0.0),
+                             mb = std::fmax(accum[4 * q + 2] / s, 0.0);
+                const double ml = lum(mr, mg, mb);
+                const double vm = std::fmax(accum[4 * q + 3] / s - ml * ml, 0.0) / s;
+                const double v = vm / (ml * ml + 1e-4);
+                const double guard = s < 4.0 ? 1.0 : v / (v + kBlendTau * kBlendTau);
+                const double alpha = gate * guard;
+                double g_alpha = 0.0;
                 for (int c = 0; c < 3; ++c) {
                     const double a = std::fmax(albedo[4 * q + c] / s, 0.01);
-                    const double want = std::log1p(std::fmax(target[4 * q + c] / a, 0.0));
+                    const double m = std::fmax(accum[4 * q + c] / s, 0.0);
                     const double o = t[OUT].at(int(i), int(y), int(x), c);
-                    const double d = o - want;
-                    const double pred = o > 0.0 ? std::expm1(o) * a : 0.0;
-                    const double e = pred - target[4 * q + c];
-                    loss += w_log * std::fabs(d) + w_lin * e * e;
-                    double gr = w_log * (d > 0 ? 1.0 : d < 0 ? -1.0 : 0.0);
-                    if (o > 0.0) gr += w_lin * 2.0 * e * (pred + a);
-                    g[OUT].at(int(i), int(y), int(x), c) = gr * scale;
+                    const double pred = std::exp(std::fmin(std::fmax(o, -kMaxLog), kMaxLog)) * a;
+                    const double fin = alpha * pred + (1.0 - alpha) * m;
+                    const double tc = target[4 * q + c];
+                    const double gf = lg(fin, tc, a, &loss);
+                    const double gp = lg(pred, tc, a, &loss);
+                    g_alpha += gf * (pred - m);
+                    const double go = (gf * alpha + gp) * pred;  // through the clamp as if unclamped
+                    g[OUT].at(int(i), int(y), int(x), c) = std::fmin(std::fmax(go, -kMaxGrad), kMaxGrad) * scale;
                 }
+                const double ga = g_alpha * guard * gate * (1.0 - gate);
+                g[OUT].at(int(i), int(y), int(x), 3) = std::fmin(std::fmax(ga, -kMaxGrad), kMaxGrad) * scale;
             }
     loss *= scale;
     if (!grads) return loss;

@@ -86,12 +86,13 @@ void ro_display(const float* accum, const float* denoised, const void* params208
 
 /* The learned denoiser's network (net.cpp): parameter layout, loss and
  * gradients in double (bf16 != 0 rounds weights and stored tensors to BF16
- * as the GPU stores them), and single convolutions. */
+ * as the GPU stores them; rel_eps is the relative term's ε, 0.01 on the
+ * GPU), and single convolutions. */
 uint64_t ro_net_param_count(void);
 void ro_net_layout(uint64_t* w_off, uint64_t* b_off, uint32_t* cin, uint32_t* cout);
 double ro_net_loss_grad(const double* params, const float* accum, const float* albedo, const float* normal,
                         const float* target, const float* samples, uint32_t n, uint32_t h, uint32_t w, int bf16,
-                        double w_log, double w_lin, double* grads, float* out16);
+                        double w_log, double w_rel, double rel_eps, double* grads, float* out16);
 void ro_conv3x3(int mode, uint32_t n, uint32_t h, uint32_t w, const float* src0, uint32_t c0, uint32_t shift0,
                 const float* src1, uint32_t c1, uint32_t cout, const float* weight, const float* bias, const float* dy,
                 const float* mask, int act, float* out, double* dw, double* db);

@@ -414,6 +414,50 @@ cudaError_t launch_conv(ConvArgs a, int mode, int num_sms, cudaStream_t st) {
 
 __device__ __forceinline__ float lum3(float r, float g, float b) { return r * 0.2126f + g * 0.7152f + b * 0.0722f; }
 
+// The displayed radiance of one pixel from the network's output: a
+// prediction p = a·e^o (o = out[0..2] clamped to ±kMaxLog, so p > 0) blended
+// with the running average m: f = α·p + (1 − α)·m, α = sigmoid(out[3])·g.
+// The guard g = v/(v + τ²) (v the average's relative variance of the mean
+// luminance, from the Σ luminance² channel; τ = kBlendTau, about the
+// network's own relative error) goes to zero as the average converges, so
+// the display converges with it whatever the network predicts; the network
+// learns α within that bound. Below kGuardMinSamples the per-pixel variance
+// says too little and g = 1.
+struct Blend {
+    float a[3], m[3], pred[3], fin[3], alpha, gate, guard;
+};
+__device__ __forceinline__ Blend blend_at(const float* out, const float4& ac, const float4& al, float n) {
+    Blend b;
+    b.a[0] = fmaxf(al.x / n, 0.01f);
+    b.a[1] = fmaxf(al.y / n, 0.01f);
+    b.a[2] = fmaxf(al.z / n, 0.01f);
+    b.m[0] = fmaxf(ac.x / n, 0.0f);
+    b.m[1] = fmaxf(ac.y / n, 0.0f);
+    b.m[2] = fmaxf(ac.z / n, 0.0f);
+    const float ml = lum3(b.m[0], b.m[1], b.m[2]);
+    const float var_mean = fmaxf(ac.w / n - ml * ml, 0.0f) / n;
+    const float v = var_mean / (ml * ml + 1e-4f);
+    b.guard = n < kGuardMinSamples ? 1.0f : v / (v + kBlendTau * kBlendTau);
+    b.gate = 1.0f / (1.0f + expf(-fminf(fmaxf(out[3], -20.0f), 20.0f)));
+    b.alpha = b.gate * b.guard;
+    for (int c = 0; c < 3; ++c) {
+        b.pred[c] = expf(fminf(fmaxf(out[c], -kMaxLog), kMaxLog)) * b.a[c];
+        b.fin[c] = b.alpha * b.pred[c] + (1.0f - b.alpha) * b.m[c];
+    }
+    return b;
+}
+
+// d(loss)/d(value) of one channel's value v against target t:
+// w_log · |log(1 + v/a) − log(1 + t/a)| + w_rel · (v − t)² / (v̂² + ε),
+// v̂ = v held constant; adds the loss into *l.
+__device__ __forceinline__ float loss_grad(float v, float t, float a, float w_log, float w_rel, float* l) {
+    const float d = log1pf(v / a) - log1pf(fmaxf(t / a, 0.0f));
+    const float e = v - t;
+    const float den = v * v + kRelEps;
+    *l += w_log * fabsf(d) + w_rel * e * e / den;
+    return w_log * (d > 0.0f ? 1.0f : d < 0.0f ? -1.0f : 0.0f) / (a + v) + w_rel * 2.0f * e / den;
+}
+
 // Input features of one pixel from the renderer's sums over n samples:
 // log radiance over albedo (the à-trous filter's demodulation), albedo,
 // unit normal, log depth, log standard error of the mean luminance,
@@ -522,10 +566,12 @@ __global__ void k_merge(const bf16* __restrict__ skip, int skip_stride, const bf
     *reinterpret_cast<uint4*>(out + p * c + 8 * g) = pack8(s);
 }
 
-// Loss between the network's output o (log radiance over albedo) and the
-// target: w_log · |o − log(1 + t/a)| + w_lin · (p − t)², p = (eᵒ − 1)·a for
-// o > 0 and 0 otherwise (the displayed radiance), per channel; and its
-// gradient (bf16, 16 channels, zero past the third). dp/do = p + a.
+// Loss of one pixel: loss_grad of the display f (blend_at) plus loss_grad
+// of the prediction p itself, so the prediction keeps learning whatever the
+// blend weight does; and its gradient with respect to the network's output
+// (bf16, 16 channels: three predictions and the blend logit, zero past the
+// fourth; through the exponent's clamp as if unclamped). Each element is
+// clipped to ±kMaxGrad, so one bright pixel cannot swamp a step.
 __global__ void k_loss(LossArgs L) {
     const int total = L.n * L.h * L.w;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -537,22 +583,23 @@ __global__ void k_loss(LossArgs L) {
         if (y < L.src_h && x < L.src_w) {
             const size_t i = (size_t(img) * L.src_h + y) * L.src_w + x;
             const float n = fmaxf(L.samples ? L.samples[img] : L.samples_all, 1.0f);
-            const float4 al = L.albedo[i], tg = L.target[i];
-            const float a[3] = {fmaxf(al.x / n, 0.01f), fmaxf(al.y / n, 0.01f), fmaxf(al.z / n, 0.01f)};
+            const float* out = L.out + size_t(p) * 16;
+            const Blend b = blend_at(out, L.accum[i], L.albedo[i], n);
+            const float4 tg = L.target[i];
             const float t[3] = {tg.x, tg.y, tg.z};
+            float l = 0.0f, g_alpha = 0.0f, go[4];
             for (int c = 0; c < 3; ++c) {
-                const float o = L.out[size_t(p) * 16 + c];
-                const float want = log1pf(fmaxf(t[c] / a[c], 0.0f));
-                const float d = o - want;
-                const float pred = o > 0.0f ? expm1f(o) * a[c] : 0.0f;
-                const float e = pred - t[c];
-                const float l = L.w_log * fabsf(d) + L.w_lin * e * e;
-                float gr = L.w_log * (d > 0.0f ? 1.0f : d < 0.0f ? -1.0f : 0.0f);
-                if (o > 0.0f) gr += L.w_lin * 2.0f * e * (pred + a[c]);
-                if (isfinite(l) && isfinite(gr)) {
-                    part += l;
-                    g[c] = gr * L.scale;
-                }
+                const float gf = loss_grad(b.fin[c], t[c], b.a[c], L.w_log, L.w_rel, &l);
+                const float gp = loss_grad(b.pred[c], t[c], b.a[c], L.w_log, L.w_rel, &l);
+                g_alpha += gf * (b.pred[c] - b.m[c]);
+                go[c] = (gf * b.alpha + gp) * b.pred[c];
+            }
+            go[3] = g_alpha * b.guard * b.gate * (1.0f - b.gate);
+            bool ok = isfinite(l);
+            for (int c = 0; c < 4; ++c) ok = ok && isfinite(go[c]);
+            if (ok) {
+                part += l;
+                for (int c = 0; c < 4; ++c) g[c] = fminf(fmaxf(go[c], -kMaxGrad), kMaxGrad) * L.scale;
             }
         }
         uint4* o = reinterpret_cast<uint4*>(L.grad + size_t(p) * 16);
@@ -564,10 +611,12 @@ __global__ void k_loss(LossArgs L) {
 }
 
 // Adam on the flat parameter vector; refreshes the BF16 copy of the weights.
+// A non-finite gradient element leaves its parameter and moments alone.
 __global__ void k_adam(AdamArgs A) {
     const size_t i = size_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= A.count) return;
     const float g = A.grad[i];
+    if (!isfinite(g)) return;
     const float m = A.beta1 * A.m[i] + (1.0f - A.beta1) * g;
     const float v = A.beta2 * A.v[i] + (1.0f - A.beta2) * g * g;
     A.m[i] = m;
@@ -577,19 +626,19 @@ __global__ void k_adam(AdamArgs A) {
     A.param_bf16[i] = __float2bfloat16_rn(p);
 }
 
-// Display image: exp of the predicted log radiance, times the albedo.
+// Display image: the blend of the network's prediction and the running
+// average (blend_at).
 __global__ void k_compose(ComposeArgs C) {
     const int hw = C.w * C.h;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= C.n * hw) return;
     const int img = p / hw, r = p - img * hw, y = r / C.w, x = r - y * C.w;
     const float n = fmaxf(C.samples ? C.samples[img] : C.samples_all, 1.0f);
-    const float4 al = C.albedo[p];
     const float* o = C.out + ((size_t(img) * C.ph + y) * C.pw + x) * 16;
-    const float cr = expm1f(fmaxf(o[0], 0.0f)) * fmaxf(al.x / n, 0.01f);
-    const float cg = expm1f(fmaxf(o[1], 0.0f)) * fmaxf(al.y / n, 0.01f);
-    const float cb = expm1f(fmaxf(o[2], 0.0f)) * fmaxf(al.z / n, 0.01f);
-    C.dst[p] = make_float4(cr, cg, cb, 1.0f);
+    const Blend b = blend_at(o, C.accum[p], C.albedo[p], n);
+    float c[3];
+    for (int k = 0; k < 3; ++k) c[k] = isfinite(b.fin[k]) ? b.fin[k] : b.m[k];
+    C.dst[p] = make_float4(c[0], c[1], c[2], 1.0f);
 }
 
 static inline unsigned blocks_for(size_t n, unsigned t) { return unsigned((n + t - 1) / t); }

@@ -13,6 +13,11 @@ namespace net {
 enum ConvMode { FWD = 0, BWD_DATA = 1, BWD_WEIGHT = 2 };
 
 constexpr float kLeak = 0.1f;  // leaky ReLU slope below zero
+constexpr float kMaxLog = 8.0f;    // clamp of the prediction's exponent (radiance ≤ e⁸ × albedo)
+constexpr float kMaxGrad = 64.0f;  // loss: clip of each element's gradient (before the 1/(3·pixels) scale)
+constexpr float kRelEps = 0.01f;   // loss: ε of the relative squared error
+constexpr float kBlendTau = 0.05f;        // blend guard: relative error below which the average takes over
+constexpr float kGuardMinSamples = 4.0f;  // blend guard: off below this many samples
 constexpr unsigned NET_STATUS_TIMEOUT = 1u;
 
 // One input tensor of a convolution whose input is a channel concatenation:
@@ -57,7 +62,8 @@ struct FeatureArgs {
 };
 
 struct LossArgs {
-    const float* out;  // [n][h][w][16] network output
+    const float* out;  // [n][h][w][16] network output: predicted log radiance over albedo, blend logit
+    const float4* accum;
     const float4* albedo;
     const float4* target;  // per-pixel mean radiance of the converged render
     const float* samples;
@@ -65,7 +71,7 @@ struct LossArgs {
     int n, h, w, src_h, src_w;
     float scale;   // 1 / (3 · pixels)
     float w_log;   // weight of |log radiance error| (over albedo)
-    float w_lin;   // weight of the squared linear radiance error
+    float w_rel;   // weight of the relative squared radiance error
     __nv_bfloat16* grad;  // [n][h][w][16]
     float* loss;
 };
@@ -82,6 +88,7 @@ struct AdamArgs {
 
 struct ComposeArgs {
     const float* out;  // network output [n][ph][pw][16]
+    const float4* accum;
     const float4* albedo;
     const float* samples;  // per image, device; null uses samples_all
     float samples_all;

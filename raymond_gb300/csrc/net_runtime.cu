@@ -8,7 +8,8 @@
 // with a leaky ReLU per level on the way down (2×2 average pooling between
 // levels) and on the way up (nearest-neighbour upsampling concatenated with
 // the encoder's output at that level), and a last 3×3 convolution to the
-// predicted log radiance over albedo. 19 convolutions: 1,649,664 weights and
+// predicted log radiance over albedo and a blend weight: the display is the
+// prediction blended with the running average (in FP32, per pixel). 19 convolutions: 1,649,664 weights and
 // 1,696 biases.
 #include <cuda_runtime.h>
 
@@ -117,7 +118,7 @@ struct raymond_net {
     size_t param_count = 0;
     DevBuf params, params_bf16, grads, adam_m, adam_v, status, loss;
     uint32_t adam_t = 0;
-    float w_log = 1.0f, w_lin = 0.0f;  // loss weights
+    float w_log = 1.0f, w_rel = 0.0f;  // loss weights
 
     DevBuf work;
     int wn = 0, wh = 0, ww = 0;
@@ -323,6 +324,7 @@ static cudaError_t run_features(raymond_net* net, const raymond_net_batch* b, cu
 static cudaError_t run_loss(raymond_net* net, const raymond_net_batch* b, cudaStream_t st) {
     LossArgs L{};
     L.out = net->out;
+    L.accum = reinterpret_cast<const float4*>(b->accum);
     L.albedo = reinterpret_cast<const float4*>(b->albedo);
     L.target = reinterpret_cast<const float4*>(b->target);
     L.samples = b->samples;
@@ -334,7 +336,7 @@ static cudaError_t run_loss(raymond_net* net, const raymond_net_batch* b, cudaSt
     L.src_w = int(b->width);
     L.scale = 1.0f / (3.0f * float(b->n) * float(b->width) * float(b->height));
     L.w_log = net->w_log;
-    L.w_lin = net->w_lin;
+    L.w_rel = net->w_rel;
     L.grad = net->t(T_GOUT);
     L.loss = static_cast<float*>(net->loss.ptr);
     return launch_loss(L, st);
@@ -536,12 +538,12 @@ int raymond_net_train_step(raymond_net* net, const raymond_net_batch* batch, flo
     return loss ? finish(net, loss) : RAYMOND_OK;
 }
 
-int raymond_net_set_loss(raymond_net* net, float w_log, float w_lin) {
+int raymond_net_set_loss(raymond_net* net, float w_log, float w_rel) {
     if (!net) return RAYMOND_EINVAL;
-    if (!(w_log >= 0.0f) || !(w_lin >= 0.0f) || !(w_log + w_lin > 0.0f) || !std::isfinite(w_log + w_lin))
+    if (!(w_log >= 0.0f) || !(w_rel >= 0.0f) || !(w_log + w_rel > 0.0f) || !std::isfinite(w_log + w_rel))
         return net->fail(RAYMOND_EINVAL, "Loss weights must be finite, non-negative and not both zero.");
     net->w_log = w_log;
-    net->w_lin = w_lin;
+    net->w_rel = w_rel;
     return RAYMOND_OK;
 }
 
@@ -572,6 +574,7 @@ int raymond_net_infer(raymond_net* net, const raymond_net_batch* batch, float* o
     if (e == cudaSuccess) {
         ComposeArgs C{};
         C.out = net->out;
+        C.accum = reinterpret_cast<const float4*>(batch->accum);
         C.albedo = reinterpret_cast<const float4*>(batch->albedo);
         C.samples = batch->samples;
         C.samples_all = batch->samples_all;

@@ -86,9 +86,9 @@ class Denoiser:
         self.set_params(bits.view(np.float32))
 
     # ---- training
-    def set_loss(self, w_log: float = 1.0, w_lin: float = 0.0) -> None:
-        """Loss weights: w_log on |log radiance error|, w_lin on the squared linear error."""
-        self._check(_native.lib().raymond_net_set_loss(self.handle, float(w_log), float(w_lin)))
+    def set_loss(self, w_log: float = 1.0, w_rel: float = 0.0) -> None:
+        """Loss weights: w_log on |log radiance error|, w_rel on the relative squared error."""
+        self._check(_native.lib().raymond_net_set_loss(self.handle, float(w_log), float(w_rel)))
 
     def gradients(self, batch):
         """(loss, gradients) of one batch, without a step."""

@@ -1,14 +1,14 @@
 """Trains the learned denoiser on image pairs that the path tracer renders
 itself: for each seeded view (scenes.training_views), a converged target
-and noisy renders at 1 to 64 samples per pixel with an independent sample
-stream. Training runs on the GPU through the library's own
+and noisy renders at 1 to 256 samples per pixel with an independent
+sample stream. Training runs on the GPU through the library's own
 forward, backward and Adam kernels (raymond_net_train_step); PyTorch only
 holds the device memory and cuts the random crops.
 
     python -m raymond_gb300.train_denoiser --views 160 --steps 4000 --out weights.npz
 
-Each --loss variant (w_log,w_lin: the weights of the L1 log-radiance and
-the squared linear-radiance terms) trains from the same initial weights on
+Each --loss variant (w_log,w_rel: the weights of the L1 log-radiance and
+the relative squared-radiance terms) trains from the same initial weights on
 the same data; the one with the lowest held-out RMSE at 4 spp is saved.
 The report (--report) gives, for held-out views at 1, 4 and 16 spp, the
 RMSE against the converged render of the noisy image, of the à-trous
@@ -30,7 +30,7 @@ from . import _native, scenes
 from .denoiser import DEFAULT_WEIGHTS, Denoiser, make_batch
 from .renderer import Canvas, Renderer
 
-NOISY_SPP = (1, 2, 4, 8, 16, 32, 64)
+NOISY_SPP = (1, 2, 4, 8, 16, 32, 64, 128, 256)
 NOISE_SEED = 0x5BD1E995
 
 
@@ -119,8 +119,8 @@ def evaluate(net, targets, inputs, spp=4):
 def parse_losses(text):
     out = []
     for item in text.split(";"):
-        w_log, w_lin = (float(v) for v in item.split(","))
-        out.append((w_log, w_lin))
+        w_log, w_rel = (float(v) for v in item.split(","))
+        out.append((w_log, w_rel))
     return out
 
 
@@ -188,7 +188,7 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--crop", type=int, default=128)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--loss", default="1,0;0.5,4", help="variants w_log,w_lin separated by ';'")
+    ap.add_argument("--loss", default="0.5,1", help="variants w_log,w_rel separated by ';'")
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     ap.add_argument("--report", default=None)
@@ -206,18 +206,18 @@ def main(argv=None):
     t_data = time.time() - t0
     variants = []
     best = None
-    for w_log, w_lin in parse_losses(args.loss):
+    for w_log, w_rel in parse_losses(args.loss):
         net = Denoiser(seed=args.seed)
-        net.set_loss(w_log, w_lin)
-        log(f"loss variant w_log={w_log} w_lin={w_lin}")
+        net.set_loss(w_log, w_rel)
+        log(f"loss variant w_log={w_log} w_rel={w_rel}")
         losses, t_train = train(net, targets, inputs, args.steps, args.batch, args.crop, args.lr, seed=args.seed,
                                 log=log)
-        result = {"w_log": w_log, "w_lin": w_lin, "seconds_train": t_train, "loss": losses}
+        result = {"w_log": w_log, "w_rel": w_rel, "seconds_train": t_train, "loss": losses}
         for spp in (1, 4, 16):
             result[f"holdout_rmse_{spp}spp"], rows = evaluate(net, h_targets, h_inputs, spp)
             if spp == 4:
                 result["holdout_rows_4spp"] = rows
-        log(json.dumps({k: result[k] for k in ("w_log", "w_lin", "holdout_rmse_1spp", "holdout_rmse_4spp",
+        log(json.dumps({k: result[k] for k in ("w_log", "w_rel", "holdout_rmse_1spp", "holdout_rmse_4spp",
                                                "holdout_rmse_16spp")}))
         variants.append(result)
         score = result["holdout_rmse_4spp"]["learned"]
@@ -229,10 +229,11 @@ def main(argv=None):
             net.dispose()
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     best[1].save(args.out)
-    report = {"views": args.views, "holdout": args.holdout, "size": args.size, "target_spp": args.target_spp,
+    report = {"command": "python -m raymond_gb300.train_denoiser " + " ".join(argv if argv is not None else sys.argv[1:]),
+              "views": args.views, "holdout": args.holdout, "size": args.size, "target_spp": args.target_spp,
               "noisy_spp": list(NOISY_SPP), "steps": args.steps, "batch": args.batch, "crop": args.crop,
               "lr": args.lr, "seed": args.seed, "seconds_data": t_data, "variants": variants,
-              "chosen": {"w_log": best[2]["w_log"], "w_lin": best[2]["w_lin"]},
+              "chosen": {"w_log": best[2]["w_log"], "w_rel": best[2]["w_rel"]},
               "weights": os.path.basename(args.out)}
     if args.report:
         with open(args.report, "w") as f:

@@ -156,11 +156,11 @@ def test_parameter_layout_matches_oracle(gpu):
     net.dispose()
 
 
-@pytest.mark.parametrize("w_log,w_lin", [(1.0, 0.0), (0.5, 4.0)])
-def test_network_gradients_match_oracle(gpu, w_log, w_lin):
+@pytest.mark.parametrize("w_log,w_rel", [(1.0, 0.0), (0.5, 2.0)])
+def test_network_gradients_match_oracle(gpu, w_log, w_rel):
     rng = np.random.default_rng(21)
     net = Denoiser(seed=3)
-    net.set_loss(w_log, w_lin)
+    net.set_loss(w_log, w_rel)
     count, layout = oracle.net_layout()
     params = _random_params(count, layout, rng)
     # BF16-exact weights so both sides multiply the same numbers
@@ -173,7 +173,7 @@ def test_network_gradients_match_oracle(gpu, w_log, w_lin):
     batch = make_batch(dev["accum"], dev["albedo"], dev["normal"], dev["target"], samples_all=spp)
     loss, grads = net.gradients(batch)
     want_loss, want, _ = oracle.net_loss_grad(params.astype(np.float64), accum, albedo, normal, target, spp, bf16=True,
-                                              w_log=w_log, w_lin=w_lin)
+                                              w_log=w_log, w_rel=w_rel)
     assert abs(loss - want_loss) <= 2e-3 * want_loss
     cos_all = float(np.dot(grads, want) / (np.linalg.norm(grads) * np.linalg.norm(want)))
     assert cos_all > 0.999
@@ -181,9 +181,9 @@ def test_network_gradients_match_oracle(gpu, w_log, w_lin):
         g = grads[wo:wo + cout * 9 * cin]
         r = want[wo:wo + cout * 9 * cin]
         if li == 18:
-            # only the three predicted channels carry a gradient
-            g = g.reshape(cout, -1)[:3].ravel()
-            r = r.reshape(cout, -1)[:3].ravel()
+            # only the three predicted channels and the blend weight carry a gradient
+            g = g.reshape(cout, -1)[:4].ravel()
+            r = r.reshape(cout, -1)[:4].ravel()
         rel = np.linalg.norm(g - r) / np.linalg.norm(r)
         assert rel < 0.05, (li, rel)
     net.dispose()
@@ -197,9 +197,9 @@ def test_training_reduces_the_loss(gpu):
     dev = [torch.from_numpy(v).cuda() for v in (accum, albedo, normal, target)]
     batch = make_batch(*dev, samples_all=spp)
     first = net.train_step(batch, 1e-3, want_loss=True)
-    for _ in range(150):
+    for _ in range(300):
         net.train_step(batch, 1e-3)
     last = net.train_step(batch, 1e-3, want_loss=True)
     assert np.isfinite(first) and np.isfinite(last)
-    assert last < 0.5 * first, (first, last)
+    assert last < 0.7 * first, (first, last)
     net.dispose()

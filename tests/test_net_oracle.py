@@ -52,32 +52,37 @@ def test_oracle_conv_matches_torch(shift0, c0, c1, cout):
     np.testing.assert_allclose(db, b.grad.numpy(), rtol=1e-9, atol=1e-9)
 
 
-def _inputs(rng, n, h, w, spp=4.0):
+def _inputs(rng, n, h, w, spp=4.0, level=0.4):
     accum = np.zeros((n, h, w, 4), np.float32)
-    accum[..., :3] = rng.gamma(2.0, 0.4, (n, h, w, 3)) * spp
+    accum[..., :3] = rng.gamma(2.0, level, (n, h, w, 3)) * spp
     lum = accum[..., 0] * 0.2126 + accum[..., 1] * 0.7152 + accum[..., 2] * 0.0722
     accum[..., 3] = lum * lum / spp * 1.5
     albedo = np.zeros_like(accum)
-    albedo[..., :3] = rng.uniform(0.05, 0.9, (n, h, w, 3)) * spp
+    albedo[..., :3] = rng.uniform(0.05 if level > 0.2 else 0.4, 0.9, (n, h, w, 3)) * spp
     normal = np.zeros_like(accum)
     v = rng.standard_normal((n, h, w, 3))
     normal[..., :3] = v / np.linalg.norm(v, axis=-1, keepdims=True) * spp
     normal[..., 3] = rng.uniform(1.0, 5.0, (n, h, w)) * spp
     target = np.zeros_like(accum)
-    target[..., :3] = rng.gamma(2.0, 0.4, (n, h, w, 3))
+    target[..., :3] = rng.gamma(2.0, level, (n, h, w, 3))
     return accum, albedo, normal, target
 
 
-@pytest.mark.parametrize("w_log,w_lin", [(1.0, 0.0), (0.5, 4.0)])
-def test_oracle_network_gradients_match_finite_differences(w_log, w_lin):
+# The relative term holds its denominator constant (it is not differentiated),
+# so its finite-difference check uses an ε large enough that the denominator
+# barely moves; the GPU test checks the production ε against the oracle.
+@pytest.mark.parametrize("w_log,w_rel,rel_eps", [(1.0, 0.0, 0.01), (0.5, 4e6, 1e6)])
+def test_oracle_network_gradients_match_finite_differences(w_log, w_rel, rel_eps):
     count, layout = oracle.net_layout()
     rng = np.random.default_rng(11)
     params = np.zeros(count, np.float64)
     for wo, bo, cin, cout in layout:
         params[wo:wo + cout * 9 * cin] = rng.uniform(-1, 1, cout * 9 * cin) * np.sqrt(6.0 / (1.01 * 9 * cin))
         params[bo:bo + cout] = rng.uniform(-0.05, 0.05, cout)
-    accum, albedo, normal, target = _inputs(rng, 1, 16, 16)
-    loss, grads, _ = oracle.net_loss_grad(params, accum, albedo, normal, target, 4.0, w_log=w_log, w_lin=w_lin)
+    # radiance low enough that no gradient element reaches the clip
+    accum, albedo, normal, target = _inputs(rng, 1, 16, 16, level=0.4 if w_rel == 0 else 0.1)
+    loss, grads, _ = oracle.net_loss_grad(params, accum, albedo, normal, target, 4.0, w_log=w_log, w_rel=w_rel,
+                                          rel_eps=rel_eps)
     assert np.isfinite(loss) and loss > 0
     # weights and biases of the first, a middle, a skip-concatenating and the last layer
     picks = []
@@ -90,7 +95,11 @@ def test_oracle_network_gradients_match_finite_differences(w_log, w_lin):
         p1[i] += eps
         p2 = params.copy()
         p2[i] -= eps
-        lp = oracle.net_loss_grad(p1, accum, albedo, normal, target, 4.0, grads=False, w_log=w_log, w_lin=w_lin)[0]
-        lm = oracle.net_loss_grad(p2, accum, albedo, normal, target, 4.0, grads=False, w_log=w_log, w_lin=w_lin)[0]
+        lp = oracle.net_loss_grad(p1, accum, albedo, normal, target, 4.0, grads=False, w_log=w_log, w_rel=w_rel,
+                                  rel_eps=rel_eps)[0]
+        lm = oracle.net_loss_grad(p2, accum, albedo, normal, target, 4.0, grads=False, w_log=w_log, w_rel=w_rel,
+                                  rel_eps=rel_eps)[0]
         fd = (lp - lm) / (2 * eps)
-        assert abs(fd - grads[i]) <= 1e-4 * max(abs(fd), abs(grads[i])) + 1e-9, (i, fd, grads[i])
+        # absolute slack: one pixel whose L1 term changes sign within ±eps moves the
+        # central difference by about 3e-9 here
+        assert abs(fd - grads[i]) <= 1e-3 * max(abs(fd), abs(grads[i])) + 5e-9, (i, fd, grads[i])
