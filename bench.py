@@ -615,7 +615,7 @@ def run_batch(args):
         rs.append(r)
     setup_s = time.perf_counter() - t0
     paths = sum(w * h * spp for _, _, w, h, spp, _ in inst)
-    # One at a time (each renderer's own frame, tuned path).
+    # One launch at a time: each renderer's own frame, waited for before the next.
     for r in rs:
         r.render()
     torch.cuda.synchronize()
@@ -625,9 +625,16 @@ def run_batch(args):
     for _ in range(args.steps):
         for r in rs:
             r.render()
-        for r in rs:
             r.device.queue.onSubmittedWorkDone()
     single_s = (time.perf_counter() - t0) / args.steps
+    # Each renderer's own frame on its own stream, all in flight together.
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for r in rs:
+            r.render()
+        for r in rs:
+            r.device.queue.onSubmittedWorkDone()
+    streams_s = (time.perf_counter() - t0) / args.steps
     batch = rg.BatchRenderer(graph=True)
     for _ in range(args.warmup):
         batch.render(rs)
@@ -648,6 +655,8 @@ def run_batch(args):
                    "bounces": args.bounces, "setup_s": setup_s},
         "one_at_a_time": {"value": paths / single_s / 1e6, "unit": "Mpaths/s", "ms_per_step": single_s * 1e3},
         "speedup_vs_one_at_a_time": single_s / batch_s,
+        "concurrent_streams": {"value": paths / streams_s / 1e6, "unit": "Mpaths/s", "ms_per_step": streams_s * 1e3},
+        "speedup_vs_concurrent_streams": streams_s / batch_s,
         "gpu_launches": int(st.launches) * args.steps,
     }
     for r in rs:

@@ -94,7 +94,7 @@ int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const W
                      const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st,
                      StageEvents* events);
 int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments, const WavePlan* waves,
-                           uint32_t n_waves, uint32_t max_bounces, const WavefrontState& w,
+                           uint32_t n_waves, uint32_t max_bounces, uint32_t features, const WavefrontState& w,
                            const WavefrontTuning& tune, int num_sms, cudaStream_t st);
 int launch_image_batch(const JobDesc* d_jobs, const JobPixels* d_pix, uint32_t n_jobs, uint32_t total_pixels,
                        int num_sms, cudaStream_t st);

@@ -512,9 +512,10 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wfb_finalize(const JobDesc* __rest
 
 }  // namespace
 
-int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments, const WavePlan* waves,
-                           uint32_t n_waves, uint32_t max_bounces, const WavefrontState& w,
-                           const WavefrontTuning& tune, int num_sms, cudaStream_t st) {
+template <uint32_t FEAT>
+static int batch_frame(const JobDesc* d_jobs, const WaveSegment* d_segments, const WavePlan* waves, uint32_t n_waves,
+                       uint32_t max_bounces, const WavefrontState& w, const WavefrontTuning& tune, int num_sms,
+                       cudaStream_t st) {
     const BatchCtx ctx{d_jobs};
     const int grid_trav = num_sms * tune.traversal_blocks_per_sm;
     const int grid_shade = num_sms * tune.shade_blocks_per_sm;
@@ -530,7 +531,7 @@ int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments,
             k_wf_extend<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
             cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
             cudaMemsetAsync(w.counters + C_SHADOW, 0, sizeof(uint32_t), st);
-            k_wf_shade<15u, BatchCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q);
+            k_wf_shade<FEAT, BatchCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q);
             k_wf_shadow<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, tune.steps);
             launches += 3;
             q ^= 1;
@@ -539,6 +540,21 @@ int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments,
         ++launches;
     }
     return launches;
+}
+
+// The shade kernel is compiled for the union of the jobs' features, as a
+// single frame's is for its own (no features, volumes, dispersion, or all).
+int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments, const WavePlan* waves,
+                           uint32_t n_waves, uint32_t max_bounces, uint32_t features, const WavefrontState& w,
+                           const WavefrontTuning& tune, int num_sms, cudaStream_t st) {
+    switch (features & 15u) {
+        case 0: return batch_frame<0>(d_jobs, d_segments, waves, n_waves, max_bounces, w, tune, num_sms, st);
+        case F_VOLUMES:
+            return batch_frame<F_VOLUMES>(d_jobs, d_segments, waves, n_waves, max_bounces, w, tune, num_sms, st);
+        case F_DISPERSION:
+            return batch_frame<F_DISPERSION>(d_jobs, d_segments, waves, n_waves, max_bounces, w, tune, num_sms, st);
+        default: return batch_frame<15u>(d_jobs, d_segments, waves, n_waves, max_bounces, w, tune, num_sms, st);
+    }
 }
 
 namespace {

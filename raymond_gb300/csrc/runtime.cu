@@ -548,7 +548,7 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
     sig.reserve(4 * size_t(n) + 2);
     sig.push_back(n);
     uint64_t total_paths = 0, total_pixels = 0, max_pixels = 0;
-    uint32_t max_bounces = 0;
+    uint32_t max_bounces = 0, features = 0;
     for (uint32_t j = 0; j < n; ++j) {
         raymond* r = jobs[j].renderer;
         if (!r || !jobs[j].params208) return h->fail(RAYMOND_EINVAL, "Job %u has no renderer or parameters.", j);
@@ -572,12 +572,14 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
         total_pixels += pixels;
         if (pixels > max_pixels) max_pixels = pixels;
         if (P.max_bounces > max_bounces) max_bounces = P.max_bounces;
+        features |= jobs[j].features & 15u;
         sig.push_back(reinterpret_cast<uintptr_t>(r));
         sig.push_back(pixels);
         sig.push_back(P.samples_per_frame);
         sig.push_back(P.max_bounces | (uint64_t(P.width) << 32));
     }
     if (total_pixels > 0xffffffffull) return h->fail(RAYMOND_ECAPACITY, "The batch has too many pixels.");
+    sig.push_back(features);
 
     // Path pool: the whole frame if memory allows, else waves of whole samples.
     size_t free_b = 0, total_b = 0;
@@ -688,7 +690,7 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
     const JobPixels* d_pix = static_cast<const JobPixels*>(h->b_jobpix.ptr);
     auto enqueue = [&]() {
         int launches = launch_wavefront_batch(d_jobs, d_segs, h->b_waves.data(), uint32_t(h->b_waves.size()),
-                                              h->b_max_bounces, w, h->tuning, h->num_sms, h->stream);
+                                              h->b_max_bounces, features, w, h->tuning, h->num_sms, h->stream);
         launches += launch_image_batch(d_jobs, d_pix, h->b_n, h->b_total_pixels, h->num_sms, h->stream);
         return launches;
     };
