@@ -11,6 +11,8 @@ denoiser and the tone map. Prints one JSON line (rank 0).
 The default line also carries "learned_denoiser": the learned denoiser's
 inference on a 1920×1080 frame of the same scene against the tensor peak.
 Other workloads (--workload):
+  caustics the water-caustics scene at 1024² with light tracing (1M light paths
+           splatted) and photon mapping (up to 4M photons, r = 0.01) every frame
   batch    64 seeded sphere-field instances as one graph-replayed batched frame
   denoise  the learned denoiser's 1080p inference as its own line
   rmse     time to RMSE ≤ 0.01 against a 16,384-spp render: the plain
@@ -109,10 +111,19 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def build_workload(size, spp, bounces):
+CAUSTICS_WORKLOAD = ("water caustics 1024x1024 (130,050-triangle water surface, glass sphere, r=0.1 lamp), "
+                     "8 bounces, 1M light paths splatted + photon map of up to 4M photons gathered at r=0.01")
+CAUSTICS_LIGHT_PATHS = 1_000_000
+CAUSTICS_PHOTONS = 4_194_304
+CAUSTICS_RADIUS = 0.01
+
+
+def build_workload(size, spp, bounces, workload="field"):
     import raymond_gb300 as rg
     from raymond_gb300 import scenes
 
+    if workload == "caustics":
+        return scenes.water_caustics()
     scene, camera, info = scenes.sphere_field()
     return scene, camera, info
 
@@ -461,12 +472,16 @@ def run_ours(args, rank, world, local):
     from raymond_gb300 import _native
 
     torch.cuda.set_device(local)
-    scene, camera, info = build_workload(args.size, args.spp, args.bounces)
+    caustics = args.workload == "caustics"
+    scene, camera, info = build_workload(args.size, args.spp, args.bounces, args.workload)
     r = rg.Renderer.create(rg.Canvas(args.size, args.size), device=local)
     r.scene, r.camera = scene, camera
     r.maxBounces = args.bounces
     r.samplesPerFrame = args.spp
-    r.caustics = False  # plain path tracing: light tracing and photon mapping are the caustics workload's
+    # The sphere field is plain path tracing; light tracing and photon mapping are the caustics workload's.
+    r.caustics = caustics
+    if caustics:
+        r.setPhotons(CAUSTICS_LIGHT_PATHS, CAUSTICS_PHOTONS, CAUSTICS_RADIUS)
     r.flags = {"auto": 0, "megakernel": _native.FLAG_MEGAKERNEL, "wavefront": _native.FLAG_WAVEFRONT}[args.path]
     lib = _native.lib()
     stream = torch.cuda.ExternalStream(lib.raymond_get_stream(r.handle), device=local)
@@ -485,7 +500,7 @@ def run_ours(args, rank, world, local):
 
     stats = _native.Stats()
     step_ms, trace_ms, launches = [], [], 0
-    ext_ms, ext_launches, shade_ms, shadow_ms = [], [], [], []
+    ext_ms, ext_launches, shade_ms, shadow_ms, caustics_ms = [], [], [], [], []
     clocks = ClockSampler(local)
     barrier()
     torch.cuda.synchronize()
@@ -507,6 +522,7 @@ def run_ours(args, rank, world, local):
         ext_launches.append(stats.launches_extend)
         shade_ms.append(stats.ms_shade)
         shadow_ms.append(stats.ms_shadow)
+        caustics_ms.append(stats.ms_caustics)
     torch.cuda.synchronize()
     barrier()
     clock_info = clocks.stop()
@@ -557,27 +573,21 @@ def run_ours(args, rank, world, local):
             bytes_per_launch = bytes_per_path * paths_per_step
             launch_s = statistics.mean(trace_ms) / 1e3
         achieved = bytes_per_launch / launch_s / 1e9
-        traffic = None
-        prof = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(prof):
-            try:
-                with open(prof) as f:
-                    traffic = json.load(f).get("megakernel_bytes_per_launch")
-            except (OSError, ValueError):
-                traffic = None
+        traffic = None  # no full-size DRAM capture of this kernel; see the 512² profile
         result = {
             "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32 scene)",
-            "config": {"workload": WORKLOAD, "width": args.size, "height": args.size, "spp": args.spp,
-                       "bounces": args.bounces, "triangles": info["triangles"], "spheres": info["spheres"],
-                       "primitives": scene.pack().primitiveCount, "parallelism": f"replicas x{world}", "path": args.path, "tuning": tuning,
-                       "l2": "flushed between steps (512 MB write)"},
+            "config": {"workload": CAUSTICS_WORKLOAD if caustics else WORKLOAD, "width": args.size,
+                       "height": args.size, "spp": args.spp, "bounces": args.bounces,
+                       "triangles": info["triangles"], "spheres": info.get("spheres"),
+                       "primitives": scene.pack().primitiveCount, "parallelism": f"replicas x{world}",
+                       "path": args.path, "tuning": tuning, "l2": "flushed between steps (512 MB write)"},
             "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": 208, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "stages_ms": {"trace": statistics.mean(trace_ms), "step": statistics.mean(step_ms),
                           "extend": statistics.mean(ext_ms), "shade": statistics.mean(shade_ms),
-                          "shadow": statistics.mean(shadow_ms)},
+                          "shadow": statistics.mean(shadow_ms), "caustics": statistics.mean(caustics_ms)},
             "mrays_per_s": rays_per_path * paths_per_step * args.steps * world / total_s / 1e6,
             "rays_per_path": rays_per_path,
             "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak,
@@ -585,11 +595,17 @@ def run_ours(args, rank, world, local):
                          "bytes_per_launch": bytes_per_launch, "bytes_per_path": bytes_per_path,
                          "traversal_bytes_per_path": split},
             "cpu_baseline": {"value": cpu_paths / cpu_s / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
-                             "sample": f"16 bands of 2 rows x {args.size} px at {args.spp} spp (1/32 of a frame)"},
+                             "sample": f"16 bands of 2 rows x {args.size} px at {args.spp} spp (1/32 of a frame)"
+                                       + (", camera paths only (the oracle does not restate light tracing)"
+                                          if caustics else "")},
             "clocks": clock_info,
         }
+        if caustics:
+            result["mphotons_per_s"] = CAUSTICS_LIGHT_PATHS * args.steps * world / total_s / 1e6
+            result["photons"] = {"light_paths_per_frame": CAUSTICS_LIGHT_PATHS, "capacity": CAUSTICS_PHOTONS,
+                                 "radius": CAUSTICS_RADIUS}
     r.dispose()
-    if rank == 0 and not args.no_denoiser:
+    if rank == 0 and not args.no_denoiser and not caustics:
         result["learned_denoiser"] = measure_denoiser(scene, camera, local, 10, 3)
     return result
 
@@ -675,7 +691,7 @@ def main():
     ap.add_argument("--bounces", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", default="auto", choices=["auto", "megakernel", "wavefront"])
-    ap.add_argument("--workload", default="field", choices=["field", "batch", "denoise", "rmse"])
+    ap.add_argument("--workload", default="field", choices=["field", "caustics", "batch", "denoise", "rmse"])
     ap.add_argument("--threshold", type=float, default=0.01)
     ap.add_argument("--reference-spp", type=int, default=16384)
     ap.add_argument("--max-spp", type=int, default=4096)
