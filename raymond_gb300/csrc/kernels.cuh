@@ -100,7 +100,9 @@ int launch_image_batch(const JobDesc* d_jobs, const JobPixels* d_pix, uint32_t n
                        int num_sms, cudaStream_t st);
 int launch_caustics(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb,
                     const PixelBuffers& px, int num_sms, cudaStream_t st);
-int launch_denoise(const Params& P, const PixelBuffers& px, cudaStream_t st);
+// status: a device word set non-zero if a staged tile's wait runs out (null:
+// every pass reads through L2).
+int launch_denoise(const Params& P, const PixelBuffers& px, unsigned* status, cudaStream_t st);
 int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st);
 // Fill each kernel unit's sRGB decode table on the current device.
 cudaError_t upload_srgb_table_trace();

@@ -1,5 +1,9 @@
 // The à-trous denoiser (src/shaders.mjs:1916-2098) and the display tone map
 // (src/shaders.mjs:2114-2152) as sm_103a kernels on the per-pixel buffers.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "dev_tcgen05.cuh"
 #include "kernels.cuh"
 
 #include <mutex>
@@ -25,8 +29,7 @@ __device__ __forceinline__ float3 albedo_at(const DenoiseView& v, uint32_t i) {
     const float4 g = v.guide_albedo[i];
     return make_float3(fmaxf(g.x / v.n, 0.01f), fmaxf(g.y / v.n, 0.01f), fmaxf(g.z / v.n, 0.01f));
 }
-__device__ __forceinline__ float4 normal_at(const DenoiseView& v, uint32_t i) {
-    const float4 g = v.guide_normal[i];
+__device__ __forceinline__ float4 normal_of(float4 g, const DenoiseView& v) {
     const float d2 = g.x * g.x + g.y * g.y + g.z * g.z;
     float3 n = make_float3(0.0f, 0.0f, 0.0f);
     if (d2 > 0.0f) {
@@ -35,6 +38,7 @@ __device__ __forceinline__ float4 normal_at(const DenoiseView& v, uint32_t i) {
     }
     return make_float4(n.x, n.y, n.z, g.w / v.n);
 }
+__device__ __forceinline__ float4 normal_at(const DenoiseView& v, uint32_t i) { return normal_of(v.guide_normal[i], v); }
 __device__ __forceinline__ float3 light_at(const DenoiseView& v, uint32_t i) {
     const float4 a = v.accum[i];
     const float3 al = albedo_at(v, i);
@@ -138,6 +142,115 @@ __global__ void k_atrous(DenoiseView v, const float4* __restrict__ in, float4* _
     atrous_at(v, in, out, step, x, y);
 }
 
+// The same pass with its input staged in shared memory by the tensor memory
+// accelerator: a 32×16 block of outputs reads a (32 + 4·step) × (16 + 4·step)
+// tile of the light buffer and of the normal guide, two 2D box copies that
+// complete on one mbarrier (a bounded wait; a wait that runs out sets the
+// status word and the block writes nothing). Taps outside the image are
+// skipped by coordinate, as in atrous_at; the box's out-of-image part is
+// zero-filled and never read. Same arithmetic in the same order as
+// atrous_at (the two agree to float rounding: the compiler may fuse
+// multiply-adds differently).
+constexpr int ATROUS_TW = 32, ATROUS_TH = 16, ATROUS_THREADS = 256;
+
+template <int STEP>
+struct AtrousTile {
+    static constexpr int halo = 2 * STEP;
+    static constexpr int w = ATROUS_TW + 2 * halo, h = ATROUS_TH + 2 * halo;
+    static constexpr uint32_t bytes = uint32_t(w) * h * 16;
+    static constexpr uint32_t stride = (bytes + 1023u) / 1024u * 1024u;  // second tile 1 KB aligned
+    static constexpr uint32_t smem = 2 * stride;
+};
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            tc::smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(tc::smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+template <int STEP>
+__global__ void __launch_bounds__(ATROUS_THREADS) k_atrous_tma(DenoiseView v, const __grid_constant__ CUtensorMap light,
+                                                                const __grid_constant__ CUtensorMap guide,
+                                                                float4* __restrict__ out, unsigned* status) {
+    using T = AtrousTile<STEP>;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t bar;
+    const float4* s_light = reinterpret_cast<const float4*>(smem);
+    const float4* s_guide = reinterpret_cast<const float4*>(smem + T::stride);
+    const int bx = int(blockIdx.x) * ATROUS_TW, by = int(blockIdx.y) * ATROUS_TH;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        tc::fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, 2u * T::bytes);
+        // x counts floats (4 per pixel): always a multiple of 16 bytes.
+        tma_load_2d(smem, &light, 4 * (bx - T::halo), by - T::halo, &bar);
+        tma_load_2d(smem + T::stride, &guide, 4 * (bx - T::halo), by - T::halo, &bar);
+    }
+    const bool arrived = tc::mbar_wait(&bar, 0);
+    if (!__syncthreads_and(arrived)) {
+        if (threadIdx.x == 0) {
+            atomicOr(status, 1u);
+            tc::mbar_wait(&bar, 0);  // bounded: the copies must land before the block's memory goes
+        }
+        __syncthreads();
+        return;
+    }
+    const int tx = int(threadIdx.x) % ATROUS_TW;
+    for (int ty = int(threadIdx.x) / ATROUS_TW; ty < ATROUS_TH; ty += ATROUS_THREADS / ATROUS_TW) {
+        const int x = bx + tx, y = by + ty;
+        if (x >= int(v.w) || y >= int(v.h)) continue;
+        auto at = [&](const float4* t, int xx, int yy) { return t[(yy - by + T::halo) * T::w + (xx - bx + T::halo)]; };
+        const float4 centre = at(s_light, x, y);
+        const float4 gp = normal_of(at(s_guide, x, y), v);
+        const float lp = lum(xyz4(centre));
+
+        float variance = 0.0f, variance_weight = 0.0f;
+        for (int dy = -1; dy <= 1; ++dy) {
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int xx = x + dx, yy = y + dy;
+                if (xx >= 0 && yy >= 0 && xx < int(v.w) && yy < int(v.h)) {
+                    const float w = c_kernel[dx < 0 ? -dx : dx] * c_kernel[dy < 0 ? -dy : dy];
+                    variance += w * at(s_light, xx, yy).w;
+                    variance_weight += w;
+                }
+            }
+        }
+        const float sigma = 4.0f * sqrtf(variance / variance_weight) + 1e-4f;
+
+        float3 sum = make_float3(0.0f, 0.0f, 0.0f);
+        float sum_variance = 0.0f, weight = 0.0f;
+        for (int dy = -2; dy <= 2; ++dy) {
+            for (int dx = -2; dx <= 2; ++dx) {
+                const int xx = x + dx * STEP, yy = y + dy * STEP;
+                if (xx < 0 || yy < 0 || xx >= int(v.w) || yy >= int(v.h)) continue;
+                const float4 q = at(s_light, xx, yy);
+                const float w = c_kernel[dx < 0 ? -dx : dx] * c_kernel[dy < 0 ? -dy : dy] *
+                                similarity(gp, normal_of(at(s_guide, xx, yy), v), float(STEP)) *
+                                expf(-fabsf(lp - lum(xyz4(q))) / sigma);
+                sum.x += w * q.x;
+                sum.y += w * q.y;
+                sum.z += w * q.z;
+                sum_variance += w * w * q.w;
+                weight += w;
+            }
+        }
+        const uint32_t i = uint32_t(y) * v.w + uint32_t(x);
+        if (weight > 0.0f)
+            out[i] = make_float4(sum.x / weight, sum.y / weight, sum.z / weight, sum_variance / (weight * weight));
+        else
+            out[i] = centre;
+    }
+}
+
 // compose (src/shaders.mjs:2088-2097).
 __device__ void compose_at(const DenoiseView& v, const float4* __restrict__ in, float4* __restrict__ out, uint32_t x,
                            uint32_t y) {
@@ -201,7 +314,53 @@ __global__ void k_tonemap(Params P, const float4* __restrict__ accum, const floa
 
 }  // namespace
 
-int launch_denoise(const Params& P, const PixelBuffers& px, cudaStream_t st) {
+namespace {
+
+// cuTensorMapEncodeTiled, from the driver through the runtime (no -lcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// A w×h float4 image as a 2D tensor of floats (4w × h) with a box of the
+// tile for one step.
+template <int STEP>
+bool encode_tile_map(CUtensorMap* map, const float4* base, uint32_t w, uint32_t h) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {cuuint64_t(w) * 4, h};
+    const cuuint64_t strides[1] = {cuuint64_t(w) * 16};
+    const cuuint32_t box[2] = {cuuint32_t(AtrousTile<STEP>::w * 4), cuuint32_t(AtrousTile<STEP>::h)};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float4*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int STEP>
+bool launch_atrous_tma(const DenoiseView& v, const float4* in, float4* out, unsigned* status, cudaStream_t st) {
+    CUtensorMap light, guide;
+    if (!encode_tile_map<STEP>(&light, in, v.w, v.h) || !encode_tile_map<STEP>(&guide, v.guide_normal, v.w, v.h))
+        return false;
+    static const bool configured = cudaFuncSetAttribute(k_atrous_tma<STEP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        int(AtrousTile<STEP>::smem)) == cudaSuccess;
+    if (!configured) return false;
+    const dim3 grid((v.w + ATROUS_TW - 1) / ATROUS_TW, (v.h + ATROUS_TH - 1) / ATROUS_TH);
+    k_atrous_tma<STEP><<<grid, ATROUS_THREADS, AtrousTile<STEP>::smem, st>>>(v, light, guide, out, status);
+    return true;
+}
+
+}  // namespace
+
+int launch_denoise(const Params& P, const PixelBuffers& px, unsigned* status, cudaStream_t st) {
     DenoiseView v{px.accum, px.guide_albedo, px.guide_normal, P.width, P.height,
                   float(P.total_samples > 1u ? P.total_samples : 1u)};
     const dim3 block(16, 8), grid((P.width + 15) / 16, (P.height + 7) / 8);
@@ -211,7 +370,19 @@ int launch_denoise(const Params& P, const PixelBuffers& px, cudaStream_t st) {
     float4* from = px.light_a;
     float4* to = px.light_b;
     for (int k = 0; k < 5; ++k) {
-        k_atrous<<<grid, block, 0, st>>>(v, from, to, steps[k]);
+        // Steps 1-8 stage their tiles with TMA; step 16's halo (32 pixels a
+        // side) would need 200 KB of tile for 512 outputs, so it reads L2.
+        bool staged = false;
+        if (status) {
+            switch (steps[k]) {
+                case 1: staged = launch_atrous_tma<1>(v, from, to, status, st); break;
+                case 2: staged = launch_atrous_tma<2>(v, from, to, status, st); break;
+                case 4: staged = launch_atrous_tma<4>(v, from, to, status, st); break;
+                case 8: staged = launch_atrous_tma<8>(v, from, to, status, st); break;
+                default: break;
+            }
+        }
+        if (!staged) k_atrous<<<grid, block, 0, st>>>(v, from, to, steps[k]);
         float4* t = from;
         from = to;
         to = t;

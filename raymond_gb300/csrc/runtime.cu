@@ -118,6 +118,8 @@ struct raymond {
                     cudaGetErrorString(e));
     }
 
+    unsigned* status_word() const { return static_cast<unsigned*>(counter.ptr) + 8; }
+
     Scene scene_view() const {
         Scene s{};
         s.prims = static_cast<const float4*>(prims.ptr);
@@ -254,7 +256,8 @@ int raymond_create(raymond_t** out, const raymond_config* cfg) {
         cudaEventCreate(&h->stage_end[k]);
     }
     h->stage = StageEvents{h->stage_begin.data(), h->stage_end.data(), h->stage_kind.data(), raymond_stage_events, 0};
-    e = h->counter.reserve(64);
+    e = h->counter.reserve(64);  // word 0: trace work counter; word 8: status of bounded waits
+    if (e == cudaSuccess) e = cudaMemset(h->counter.ptr, 0, 64);
     if (e != cudaSuccess) {
         g_create_error = std::string("cudaMalloc: ") + cudaGetErrorString(e);
         cudaStreamDestroy(h->stream);
@@ -523,7 +526,7 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
     cudaEventRecord(h->ev[1], h->stream);
     if (P.caustics != 0u) launches += launch_caustics(s, P, features, cb, px, h->num_sms, h->stream);
     cudaEventRecord(h->ev[2], h->stream);
-    if (P.denoise != 0u) launches += launch_denoise(P, px, h->stream);
+    if (P.denoise != 0u) launches += launch_denoise(P, px, h->status_word(), h->stream);
     cudaEventRecord(h->ev[3], h->stream);
     launches += launch_tonemap(P, px, h->stream);
     cudaEventRecord(h->ev[4], h->stream);
@@ -742,7 +745,15 @@ int raymond_sync(raymond_t* h) {
     if (!h) return RAYMOND_EINVAL;
     cudaSetDevice(h->device);
     cudaError_t e = cudaStreamSynchronize(h->stream);
-    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "sync");
+    if (e != cudaSuccess) return h->cuda_fail(e, "sync");
+    unsigned status = 0;
+    e = cudaMemcpy(&status, h->status_word(), sizeof status, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return h->cuda_fail(e, "sync");
+    if (status) {
+        cudaMemset(h->status_word(), 0, sizeof status);
+        return h->fail(RAYMOND_ETIMEOUT, "A staged tile's copy did not arrive in time; that pass wrote nothing.");
+    }
+    return RAYMOND_OK;
 }
 
 int raymond_read_pixels(raymond_t* h, float* out_rgba, uint64_t bytes, int denoised, uint32_t samples) {

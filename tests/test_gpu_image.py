@@ -108,3 +108,39 @@ def test_display_matches_oracle(gpu):
     den = oracle.denoise(acc, alb, nrm, size, size, g["samples"])
     ref = oracle.display(acc, g["denoised"], g["params"])
     assert np.abs(g["display"].astype(int) - ref.astype(int)).max() <= 1
+
+
+def test_tma_staged_atrous_matches_the_unstaged_passes(gpu):
+    """A renderer's à-trous passes of steps 1-8 read TMA-staged tiles; the
+    allocation-free entry point runs the same passes reading L2 directly.
+    Same arithmetic in the same order (the compiler may fuse multiply-adds
+    differently in the two kernels): the images agree to float rounding, on a
+    size that is no multiple of the 32×16 tile and one far below step 8's
+    halo."""
+    import ctypes
+
+    import torch
+
+    from raymond_gb300 import Canvas, Renderer, _native, scenes
+
+    for w, h in ((200, 136), (37, 23)):
+        scene, camera = scenes.cornell_scene()
+        r = Renderer.create(Canvas(w, h))
+        r.scene, r.camera = scene, camera
+        r.samplesPerFrame = 3
+        r.denoise = True
+        r.render()
+        r.device.queue.onSubmittedWorkDone()
+        staged = r.readPixels(denoised=True)
+        lib = _native.lib()
+        bufs = _native.Buffers()
+        _native.check(lib.raymond_get_buffers(r.handle, ctypes.byref(bufs)), r.handle)
+        out = torch.zeros(w * h * 4, dtype=torch.float32, device="cuda:0")
+        _native.check(lib.raymond_denoise_static(bufs.accum, bufs.guide_albedo, bufs.guide_normal, w, h, r.samples,
+                                                 out.data_ptr(), lib.raymond_get_stream(r.handle)))
+        _native.check(lib.raymond_sync(r.handle), r.handle)
+        plain = out.cpu().numpy()
+        assert np.isfinite(staged).all()
+        scale = np.maximum(np.abs(plain), 1.0)
+        assert (np.abs(staged - plain) / scale).max() <= 1e-5, (w, h, np.abs(staged - plain).max())
+        r.dispose()
