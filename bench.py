@@ -490,6 +490,14 @@ def run_ours(args, rank, world, local):
     tuning = None
     if args.path == "auto":
         tuning = r.autotune(trials=2, cache=os.path.join(ROOT, "gpurun_out", "tuning.json"))
+    if args.bvh_width:
+        import ctypes
+
+        t = _native.Tuning()
+        _native.check(_native.lib().raymond_get_tuning(r.handle, ctypes.byref(t)), r.handle)
+        t.bvh_width = args.bvh_width
+        _native.check(_native.lib().raymond_set_tuning(r.handle, ctypes.byref(t)), r.handle)
+        tuning = r.tuning
     for _ in range(args.warmup):
         r.render()
     r.device.queue.onSubmittedWorkDone()
@@ -696,6 +704,8 @@ def main():
     ap.add_argument("--reference-spp", type=int, default=16384)
     ap.add_argument("--max-spp", type=int, default=4096)
     ap.add_argument("--no-denoiser", action="store_true", help="skip the learned-denoiser sub-measurement")
+    ap.add_argument("--bvh-width", type=int, default=0, choices=[0, 2, 4],
+                    help="force the binary (2) or 4-wide (4) traversal tree; 0 keeps the tuned choice")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--batch-spheres", type=int, default=10000)
     args = ap.parse_args()

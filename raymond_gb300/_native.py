@@ -44,7 +44,7 @@ class Stats(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("path", ctypes.c_uint32), ("steps", ctypes.c_uint32), ("traversal_blocks_per_sm", ctypes.c_uint32),
-                ("shade_blocks_per_sm", ctypes.c_uint32)]
+                ("shade_blocks_per_sm", ctypes.c_uint32), ("bvh_width", ctypes.c_uint32)]
 
 
 PATH_MEGAKERNEL, PATH_WAVEFRONT = 1, 2

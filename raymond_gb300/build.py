@@ -24,7 +24,7 @@ CUDA_SOURCES = [
     "net_runtime.cu",
     "runtime.cu",
 ]
-CXX_SOURCES = ["bvh_build.cpp"]
+CXX_SOURCES = ["bvh_build.cpp", "bvh_wide.cpp"]
 
 
 def _nvcc() -> str:

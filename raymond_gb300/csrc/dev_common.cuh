@@ -54,6 +54,7 @@ static_assert(sizeof(Params) == 208, "Params is 208 bytes");
 struct Scene {
     const float4* prims;       // 4 float4 per primitive: header (as u32), p0, p1, p2
     const float4* nodes;       // 2 float4 per node: min|first, max|count
+    const float4* wide;        // 8 float4 per node of the 4-wide traversal tree, or null (bvh_wide.h)
     const float4* materials;   // 6 float4 per material
     const float4* attributes;  // 4 float4 per attribute block
     const uint32_t* lights;    // lights ‖ volumes ‖ CDF bits

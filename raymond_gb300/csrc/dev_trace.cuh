@@ -2,12 +2,14 @@
 //
 // The arithmetic of each primitive test is that of the trace shader
 // (src/shaders.mjs:262-378) in f32, so hits agree with the reference GPU path
-// up to rounding. The traversal is this backend's own: one 64-byte load
-// fetches both children of an inner node (BVH.build stores them adjacent,
-// src/BVH.mjs:196-204), the nearer is entered, the farther pushed onto a
-// per-thread stack kept in shared memory (depth-major, so a warp's pushes
-// hit distinct banks) with a local-memory tail, and a popped node is
-// re-tested against the current nearest hit before it is entered.
+// up to rounding. The traversal is this backend's own. Over the reference's
+// binary nodes: one 64-byte load fetches both children of an inner node
+// (BVH.build stores them adjacent, src/BVH.mjs:196-204), the nearer is
+// entered, the farther pushed onto a per-thread stack kept in shared memory
+// (depth-major, so a warp's pushes hit distinct banks) with a local-memory
+// tail, and a popped node is re-tested against the current nearest hit
+// before it is entered. Over the 4-wide tree derived from them at upload
+// (bvh_wide.h), when there is one: see trace_wide.
 #pragma once
 #include "dev_common.cuh"
 
@@ -129,11 +131,130 @@ struct TraversalStack {
 
 constexpr int STACK_SHARED = 16;
 
+// ---- the 4-wide tree (bvh_wide.h) ----
+constexpr uint32_t WIDE_LEAF = 0x80000000u, WIDE_NONE = 0xFFFFFFFFu;
+__device__ __forceinline__ uint32_t wide_first(uint32_t ref) { return ref & 0xFFFFFFu; }
+__device__ __forceinline__ uint32_t wide_count(uint32_t ref) { return ((ref >> 24) & 127u) + 1u; }
+
+// Entry distances (slab_entry, INF for a miss or an empty slot) of a wide
+// node's four children, and their references.
+__device__ __forceinline__ void wide_children(const float4* node, float3 o, float3 inv, float t_max, float t[4],
+                                              uint32_t ref[4]) {
+    const float4 lx = ldg4(node), hx = ldg4(node + 1), ly = ldg4(node + 2), hy = ldg4(node + 3);
+    const float4 lz = ldg4(node + 4), hz = ldg4(node + 5), r = ldg4(node + 6);
+    ref[0] = __float_as_uint(r.x);
+    ref[1] = __float_as_uint(r.y);
+    ref[2] = __float_as_uint(r.z);
+    ref[3] = __float_as_uint(r.w);
+    t[0] = slab_entry(make_float4(lx.x, ly.x, lz.x, 0.0f), make_float4(hx.x, hy.x, hz.x, 0.0f), o, inv, t_max);
+    t[1] = slab_entry(make_float4(lx.y, ly.y, lz.y, 0.0f), make_float4(hx.y, hy.y, hz.y, 0.0f), o, inv, t_max);
+    t[2] = slab_entry(make_float4(lx.z, ly.z, lz.z, 0.0f), make_float4(hx.z, hy.z, hz.z, 0.0f), o, inv, t_max);
+    t[3] = slab_entry(make_float4(lx.w, ly.w, lz.w, 0.0f), make_float4(hx.w, hy.w, hz.w, 0.0f), o, inv, t_max);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (ref[k] == WIDE_NONE) t[k] = INF;
+}
+
+__device__ __forceinline__ void order2(float* t, uint32_t* r, int a, int b) {
+    if (t[b] < t[a]) {
+        const float tt = t[a];
+        t[a] = t[b];
+        t[b] = tt;
+        const uint32_t rr = r[a];
+        r[a] = r[b];
+        r[b] = rr;
+    }
+}
+// Nearest first (a five-comparison network).
+__device__ __forceinline__ void sort4(float* t, uint32_t* r) {
+    order2(t, r, 0, 1);
+    order2(t, r, 2, 3);
+    order2(t, r, 0, 2);
+    order2(t, r, 1, 3);
+    order2(t, r, 1, 2);
+}
+
+// The wide traversal's stack of (reference, entry distance): SH entries in
+// the thread's shared column (two rows each, depth-major), the rest local;
+// 64 in all, pushes beyond dropped as in the binary traversal.
+template <int SH>
+struct WideStack {
+    uint32_t* col;
+    uint32_t stride;
+    uint2 tail[64 - SH];
+    __device__ __forceinline__ void push(uint32_t sp, uint2 v) {
+        if (sp < SH) {
+            col[(2 * sp) * stride] = v.x;
+            col[(2 * sp + 1) * stride] = v.y;
+        } else {
+            tail[sp - SH] = v;
+        }
+    }
+    __device__ __forceinline__ uint2 at(uint32_t sp) const {
+        return sp < SH ? make_uint2(col[(2 * sp) * stride], col[(2 * sp + 1) * stride]) : tail[sp - SH];
+    }
+};
+constexpr int WIDE_STACK_SHARED = 8;  // the same shared bytes as the binary stack's 16 entries
+
+// The nearest (or, with ANY_HIT, any) hit through the wide tree: a node's
+// four children are tested at once; the nearest is entered and the others
+// pushed farthest first with their entry distance, so a popped entry is
+// skipped without a load once the nearest hit is closer.
+template <bool ANY_HIT>
+__device__ __forceinline__ Hit trace_wide(const Scene& s, float3 o, float3 d, float t_max, uint32_t* stack_col,
+                                          uint32_t stack_stride) {
+    Hit hit{t_max, NONE, 0.0f, 0.0f};
+    const float3 inv = f3(1.0f / safe1(d.x), 1.0f / safe1(d.y), 1.0f / safe1(d.z));
+    WideStack<WIDE_STACK_SHARED> st;
+    st.col = stack_col;
+    st.stride = stack_stride;
+    uint32_t sp = 0, cur = 0;
+    for (;;) {
+        bool have = false;
+        if (cur & WIDE_LEAF) {
+            const uint32_t first = wide_first(cur), end = first + wide_count(cur);
+            for (uint32_t i = first; i < end; ++i) {
+                const float3 h = intersect_prim(s, i, o, d, hit.t);
+                if (h.x > 0.0f) {
+                    hit = Hit{h.x, i, h.y, h.z};
+                    if (ANY_HIT) return hit;
+                }
+            }
+        } else {
+            float t[4];
+            uint32_t ref[4];
+            wide_children(s.wide + size_t(cur) * 8, o, inv, hit.t, t, ref);
+            if (!ANY_HIT) sort4(t, ref);
+            int next = -1;
+#pragma unroll
+            for (int k = 3; k >= 0; --k) {
+                if (t[k] >= INF) continue;
+                if (next >= 0 && sp < 64u) st.push(sp++, make_uint2(ref[next], __float_as_uint(t[next])));
+                next = k;
+            }
+            if (next >= 0) {
+                cur = ref[next];
+                have = true;
+            }
+        }
+        while (!have) {
+            if (sp == 0) return hit;
+            const uint2 e = st.at(--sp);
+            if (ANY_HIT || __uint_as_float(e.y) < hit.t) {
+                cur = e.x;
+                have = true;
+            }
+        }
+    }
+}
+
 // The nearest hit in (T_MIN, t_max), or with ANY_HIT the first found
-// (occlusion). prim = NONE for a miss; then t = t_max.
+// (occlusion). prim = NONE for a miss; then t = t_max. Walks the 4-wide tree
+// when the scene has one, else the reference's binary nodes.
 template <bool ANY_HIT>
 __device__ __forceinline__ Hit trace_ray(const Scene& s, float3 o, float3 d, float t_max, uint32_t* stack_col,
                                          uint32_t stack_stride, uint32_t* counters = nullptr) {
+    if (s.wide) return trace_wide<ANY_HIT>(s, o, d, t_max, stack_col, stack_stride);
     Hit hit{t_max, NONE, 0.0f, 0.0f};
     const float3 inv = f3(1.0f / safe1(d.x), 1.0f / safe1(d.y), 1.0f / safe1(d.z));
     const float4 rmn = ldg4(s.nodes), rmx = ldg4(s.nodes + 1);

@@ -128,6 +128,8 @@ struct Traversal {
 };
 
 // Starts a ray; returns false if it misses the root box (then it is done).
+// Over the wide tree, `first` holds the reference being visited (the root
+// node first; its children's boxes are tested in the first step).
 __device__ __forceinline__ bool trav_begin(const Scene& s, Traversal& tr, float3 o, float3 d, float t_max) {
     tr.o = o;
     tr.d = d;
@@ -136,6 +138,11 @@ __device__ __forceinline__ bool trav_begin(const Scene& s, Traversal& tr, float3
     tr.u = tr.v = 0.0f;
     tr.prim = NONE;
     tr.sp = 0;
+    if (s.wide) {
+        tr.first = 0;
+        tr.count = 0;
+        return true;
+    }
     const float4 mn = ldg4(s.nodes), mx = ldg4(s.nodes + 1);
     if (slab_entry(mn, mx, o, tr.inv, t_max) >= INF) return false;
     tr.first = __float_as_uint(mn.w);
@@ -143,9 +150,56 @@ __device__ __forceinline__ bool trav_begin(const Scene& s, Traversal& tr, float3
     return true;
 }
 
+// One wide-node (or leaf) visit, as trace_wide's loop body.
+template <bool ANY_HIT>
+__device__ __forceinline__ bool trav_step_wide(const Scene& s, Traversal& tr, WideStack<WIDE_STACK_SHARED>& st) {
+    bool have = false;
+    const uint32_t cur = tr.first;
+    if (cur & WIDE_LEAF) {
+        const uint32_t first = wide_first(cur), end = first + wide_count(cur);
+        for (uint32_t i = first; i < end; ++i) {
+            const float3 h = intersect_prim(s, i, tr.o, tr.d, tr.t);
+            if (h.x > 0.0f) {
+                tr.t = h.x;
+                tr.prim = i;
+                tr.u = h.y;
+                tr.v = h.z;
+                if (ANY_HIT) return false;
+            }
+        }
+    } else {
+        float t[4];
+        uint32_t ref[4];
+        wide_children(s.wide + size_t(cur) * 8, tr.o, tr.inv, tr.t, t, ref);
+        if (!ANY_HIT) sort4(t, ref);
+        int next = -1;
+#pragma unroll
+        for (int k = 3; k >= 0; --k) {
+            if (t[k] >= INF) continue;
+            if (next >= 0 && tr.sp < 64u) st.push(tr.sp++, make_uint2(ref[next], __float_as_uint(t[next])));
+            next = k;
+        }
+        if (next >= 0) {
+            tr.first = ref[next];
+            have = true;
+        }
+    }
+    while (!have) {
+        if (tr.sp == 0) return false;
+        const uint2 e = st.at(--tr.sp);
+        if (ANY_HIT || __uint_as_float(e.y) < tr.t) {
+            tr.first = e.x;
+            have = true;
+        }
+    }
+    return true;
+}
+
 // One node visit; returns false when the ray is finished.
 template <bool ANY_HIT>
-__device__ __forceinline__ bool trav_step(const Scene& s, Traversal& tr, TraversalStack<STACK_SHARED>& st) {
+__device__ __forceinline__ bool trav_step(const Scene& s, Traversal& tr, TraversalStack<STACK_SHARED>& st,
+                                          WideStack<WIDE_STACK_SHARED>& wst) {
+    if (s.wide) return trav_step_wide<ANY_HIT>(s, tr, wst);
     bool have = false;
     if (tr.count > 0) {
         for (uint32_t i = tr.first; i < tr.first + tr.count; ++i) {
@@ -193,6 +247,9 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Ctx ctx, WavefrontState 
     TraversalStack<STACK_SHARED> st;
     st.col = stack + threadIdx.x;
     st.stride = WF_BLOCK;
+    WideStack<WIDE_STACK_SHARED> wst;
+    wst.col = st.col;
+    wst.stride = WF_BLOCK;
     const uint32_t* queue = w.queue[q];
     const uint32_t n = w.counters[C_QUEUE0 + q];
     uint32_t* fetch = w.counters + C_FETCH + 0;
@@ -225,7 +282,7 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Ctx ctx, WavefrontState 
         if (active) {
             const Scene& sc = ctx.scene(job);
             for (int k = 0; k < steps && active; ++k) {
-                if (!trav_step<false>(sc, tr, st)) {
+                if (!trav_step<false>(sc, tr, st, wst)) {
                     w.hit[path] = make_float4(tr.t, __uint_as_float(tr.prim), tr.u, tr.v);
                     active = false;
                 }
@@ -281,6 +338,9 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState 
     TraversalStack<STACK_SHARED> st;
     st.col = stack + threadIdx.x;
     st.stride = WF_BLOCK;
+    WideStack<WIDE_STACK_SHARED> wst;
+    wst.col = st.col;
+    wst.stride = WF_BLOCK;
     const uint32_t n = w.counters[C_SHADOW];
     uint32_t* fetch = w.counters + C_FETCH + 1;
     Traversal tr;
@@ -317,7 +377,7 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState 
         if (active) {
             const Scene& sc = ctx.scene(job);
             for (int k = 0; k < steps && active; ++k) {
-                if (!trav_step<true>(sc, tr, st)) {
+                if (!trav_step<true>(sc, tr, st, wst)) {
                     active = false;
                     if (tr.prim == NONE) {
                         const uint32_t path = __float_as_uint(w.shadow[rec * 3 + 1].w);

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/raymond.h"
+#include "bvh_wide.h"
 #include "kernels.cuh"
 #include "net.cuh"
 
@@ -49,6 +50,9 @@ struct raymond {
 
     // Scene.
     DevBuf prims, nodes, materials, attributes, lights, emitters;
+    DevBuf wide;            // the 4-wide traversal tree derived from `nodes`
+    bool has_wide = false;
+    bool use_wide = true;   // tuning: traverse the wide tree when there is one
     DevBuf textures, normal_maps, env_map, env_table;
     uint32_t prim_slots = 0, bvh_prim_count = 0, node_count = 0, mat_count = 0, attr_vec4s = 0;
     uint32_t light_words = 0, light_count = 0, volume_count = 0;
@@ -124,6 +128,7 @@ struct raymond {
         Scene s{};
         s.prims = static_cast<const float4*>(prims.ptr);
         s.nodes = static_cast<const float4*>(nodes.ptr);
+        s.wide = has_wide && use_wide ? static_cast<const float4*>(wide.ptr) : nullptr;
         s.materials = static_cast<const float4*>(materials.ptr);
         s.attributes = static_cast<const float4*>(attributes.ptr);
         s.lights = static_cast<const uint32_t*>(lights.ptr);
@@ -352,6 +357,11 @@ int raymond_upload_scene(raymond_t* h, const void* prims, uint32_t prim_slots, u
     int rc;
     if ((rc = upload(h, h->prims, prims, size_t(prim_slots) * 64, "primitives"))) return rc;
     if ((rc = upload(h, h->nodes, nodes, size_t(node_count) * 32, "nodes"))) return rc;
+    {
+        std::vector<float> wide;
+        h->has_wide = build_wide_bvh(nu, node_count, wide);
+        if (h->has_wide && (rc = upload(h, h->wide, wide.data(), wide.size() * sizeof(float), "wide tree"))) return rc;
+    }
     if ((rc = upload(h, h->materials, materials, size_t(mat_count) * 96, "materials"))) return rc;
     const float zero4[4] = {0, 0, 0, 0};
     if ((rc = upload(h, h->attributes, attr_vec4s ? (const void*)attributes : (const void*)zero4,
@@ -895,9 +905,10 @@ int raymond_set_tuning(raymond_t* h, const raymond_tuning* t) {
     if (!h || !t) return RAYMOND_EINVAL;
     if ((t->path != RAYMOND_PATH_MEGAKERNEL && t->path != RAYMOND_PATH_WAVEFRONT) || t->steps < 1 || t->steps > 256 ||
         t->traversal_blocks_per_sm < 1 || t->traversal_blocks_per_sm > 16 || t->shade_blocks_per_sm < 1 ||
-        t->shade_blocks_per_sm > 64)
+        t->shade_blocks_per_sm > 64 || (t->bvh_width != 0 && t->bvh_width != 2 && t->bvh_width != 4))
         return h->fail(RAYMOND_EINVAL, "Tuning out of range.");
     h->path_choice = t->path;
+    h->use_wide = t->bvh_width != 2;
     h->tuning = WavefrontTuning{int(t->steps), int(t->traversal_blocks_per_sm), int(t->shade_blocks_per_sm)};
     return RAYMOND_OK;
 }
@@ -908,6 +919,7 @@ int raymond_get_tuning(raymond_t* h, raymond_tuning* out) {
     out->steps = uint32_t(h->tuning.steps);
     out->traversal_blocks_per_sm = uint32_t(h->tuning.traversal_blocks_per_sm);
     out->shade_blocks_per_sm = uint32_t(h->tuning.shade_blocks_per_sm);
+    out->bvh_width = h->use_wide ? 4u : 2u;
     return RAYMOND_OK;
 }
 
@@ -921,9 +933,12 @@ int raymond_autotune(raymond_t* h, const void* params208, uint32_t features, uin
     P.total_samples = P.samples_per_frame;
     P.denoise = 0;
     std::vector<raymond_tuning> cands;
-    cands.push_back({RAYMOND_PATH_MEGAKERNEL, 16, 8, 8});
-    for (uint32_t steps : {8u, 16u, 32u})
-        for (uint32_t blocks : {4u, 8u, 16u}) cands.push_back({RAYMOND_PATH_WAVEFRONT, steps, blocks, 8});
+    for (uint32_t width : {4u, 2u}) {
+        if (width == 4u && !h->has_wide) continue;
+        cands.push_back({RAYMOND_PATH_MEGAKERNEL, 16, 8, 8, width});
+        for (uint32_t steps : {8u, 16u, 32u})
+            for (uint32_t blocks : {4u, 8u, 16u}) cands.push_back({RAYMOND_PATH_WAVEFRONT, steps, blocks, 8, width});
+    }
     raymond_tuning keep{};
     raymond_get_tuning(h, &keep);
     float best_ms = 1e30f;

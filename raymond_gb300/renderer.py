@@ -424,7 +424,7 @@ class Renderer:
     def autotune(self, trials: int = 2, cache: str | None = None):
         """Picks the launch shape for this scene and image by timing
         candidates (the one-kernel path; wavefront traversal steps and
-        blocks per SM) and keeps the fastest; remembered in a JSON cache
+        blocks per SM; the binary or the 4-wide tree) and keeps the fastest; remembered in a JSON cache
         keyed by GPU, features, scene-size bucket, resolution, samples per
         frame and bounces. Starts the image over. Returns the tuning."""
         import json

@@ -203,3 +203,24 @@ def test_training_reduces_the_loss(gpu):
     assert np.isfinite(first) and np.isfinite(last)
     assert last < 0.7 * first, (first, last)
     net.dispose()
+
+
+def test_conv_many_tiles_per_cta_match_oracle(gpu):
+    """Forward and input gradient run as persistent CTAs over pixel tiles with
+    one pipeline across tile boundaries: an image of 1,152 tiles gives every
+    CTA several, including a partial last one."""
+    rng = np.random.default_rng(77)
+    n, h, w, c0, cout = 1, 384, 385, 16, 16
+    src0, s0 = _bf16(rng, (n, h, w, c0))
+    weight, wv = _bf16(rng, (cout, 9, c0), 1.0 / np.sqrt(9 * c0))
+    bias = torch.from_numpy(rng.standard_normal(cout).astype(np.float32)).cuda()
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    out = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
+    _run_conv(0, n, h, w, src0, c0, 0, None, 0, cout, weight, bias=bias, out=out, act=1, status=status)
+    want = oracle.conv3x3(0, s0, wv, bias.cpu().numpy(), act=1)
+    assert np.abs(out.float().cpu().numpy() - want).max() <= 8e-3 * np.abs(want).max()
+    dy, dyv = _bf16(rng, (n, h, w, cout))
+    dx = torch.empty((n, h, w, c0), dtype=torch.bfloat16, device="cuda")
+    _run_conv(1, n, h, w, src0, c0, 0, None, 0, cout, weight, dy=dy, out=dx, status=status)
+    want = oracle.conv3x3(1, s0, wv, dy=dyv)
+    assert np.abs(dx.float().cpu().numpy() - want).max() <= 8e-3 * np.abs(want).max()
