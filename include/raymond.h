@@ -212,8 +212,9 @@ typedef struct raymond_tuning {
     uint32_t steps;                   /* traversal steps between lane refills, 1..256 */
     uint32_t traversal_blocks_per_sm; /* persistent extend/shadow blocks of 128 threads per SM, 1..16 */
     uint32_t shade_blocks_per_sm;     /* shade/generate/finalize blocks per SM, 1..64 */
-    uint32_t bvh_width;               /* 2: walk the reference's binary nodes; 4 (or 0): the 4-wide tree derived
-                                         from them at upload, when it could be built */
+    uint32_t bvh_width;               /* 2: walk the reference's binary nodes; 4: the 4-wide tree derived from
+                                         them at upload (when it could be built); 0: 4 on the wavefront path,
+                                         2 on the one-kernel path */
 } raymond_tuning;
 int raymond_set_tuning(raymond_t* h, const raymond_tuning* t);
 int raymond_get_tuning(raymond_t* h, raymond_tuning* out);

@@ -52,7 +52,7 @@ struct raymond {
     DevBuf prims, nodes, materials, attributes, lights, emitters;
     DevBuf wide;            // the 4-wide traversal tree derived from `nodes`
     bool has_wide = false;
-    bool use_wide = true;   // tuning: traverse the wide tree when there is one
+    uint32_t bvh_width = 0;  // tuning: 2 binary, 4 wide, 0 wide for the wavefront and binary for the one-kernel path
     DevBuf textures, normal_maps, env_map, env_table;
     uint32_t prim_slots = 0, bvh_prim_count = 0, node_count = 0, mat_count = 0, attr_vec4s = 0;
     uint32_t light_words = 0, light_count = 0, volume_count = 0;
@@ -124,10 +124,13 @@ struct raymond {
 
     unsigned* status_word() const { return static_cast<unsigned*>(counter.ptr) + 8; }
 
-    Scene scene_view() const {
+    // The scene as the kernels see it; `one_kernel` says which path walks it
+    // (the automatic tree choice differs per path).
+    Scene scene_view(bool one_kernel = false) const {
         Scene s{};
         s.prims = static_cast<const float4*>(prims.ptr);
         s.nodes = static_cast<const float4*>(nodes.ptr);
+        const bool use_wide = bvh_width == 4 || (bvh_width == 0 && !one_kernel);
         s.wide = has_wide && use_wide ? static_cast<const float4*>(wide.ptr) : nullptr;
         s.materials = static_cast<const float4*>(materials.ptr);
         s.attributes = static_cast<const float4*>(attributes.ptr);
@@ -489,13 +492,13 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
     if (P.samples_per_frame == 0 || P.max_bounces > 64)
         return h->fail(RAYMOND_EINVAL, "samples_per_frame must be at least 1 and max_bounces at most 64.");
     cudaSetDevice(h->device);
-    const Scene s = h->scene_view();
-    const PixelBuffers px = h->pixel_view();
     // The wavefront runs colour frames when asked; inspection views always
     // take the one-kernel path.
     const bool want_wf = (flags & RAYMOND_FLAG_WAVEFRONT) ||
                          (!(flags & RAYMOND_FLAG_MEGAKERNEL) && h->path_choice == RAYMOND_PATH_WAVEFRONT);
     const bool wavefront = P.view == VIEW_COLOR && want_wf;
+    const Scene s = h->scene_view(!wavefront);
+    const PixelBuffers px = h->pixel_view();
     WavefrontState w{};
     if (wavefront) {
         const int rc = ensure_wavefront(h, P, w);
@@ -908,7 +911,7 @@ int raymond_set_tuning(raymond_t* h, const raymond_tuning* t) {
         t->shade_blocks_per_sm > 64 || (t->bvh_width != 0 && t->bvh_width != 2 && t->bvh_width != 4))
         return h->fail(RAYMOND_EINVAL, "Tuning out of range.");
     h->path_choice = t->path;
-    h->use_wide = t->bvh_width != 2;
+    h->bvh_width = t->bvh_width;
     h->tuning = WavefrontTuning{int(t->steps), int(t->traversal_blocks_per_sm), int(t->shade_blocks_per_sm)};
     return RAYMOND_OK;
 }
@@ -919,7 +922,7 @@ int raymond_get_tuning(raymond_t* h, raymond_tuning* out) {
     out->steps = uint32_t(h->tuning.steps);
     out->traversal_blocks_per_sm = uint32_t(h->tuning.traversal_blocks_per_sm);
     out->shade_blocks_per_sm = uint32_t(h->tuning.shade_blocks_per_sm);
-    out->bvh_width = h->use_wide ? 4u : 2u;
+    out->bvh_width = h->bvh_width;
     return RAYMOND_OK;
 }
 
