@@ -25,6 +25,8 @@ struct WavefrontState {
     float4* s[8];
     float4* hit;
     uint32_t* queue[2];
+    uint32_t* sorted;    // this bounce's queue ordered by shading key, for the shade kernel
+    uint32_t* sort_key;  // per path: its shading key
     float4* shadow;
     uint32_t* counters;
     uint64_t capacity;  // paths in flight

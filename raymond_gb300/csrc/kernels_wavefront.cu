@@ -70,9 +70,36 @@ __device__ __forceinline__ uint32_t load_path(const WavefrontState& w, uint32_t 
     return r.w;
 }
 
-// Counters (u32) in w.counters: queue sizes [0], [1], shadow size [2], and
-// per-launch fetch counters [4..7] zeroed before each traversal launch.
-enum { C_QUEUE0 = 0, C_QUEUE1 = 1, C_SHADOW = 2, C_FETCH = 4 };
+// Counters (u32) in w.counters: queue sizes [0], [1], shadow size [2],
+// per-launch fetch counters [4..7], the shading-key bucket sizes [8..23] and
+// the scatter's bucket cursors [24..39], all of [4..39] zeroed before each
+// extension launch.
+enum { C_QUEUE0 = 0, C_QUEUE1 = 1, C_SHADOW = 2, C_FETCH = 4, C_BUCKET = 8, C_CURSOR = 24 };
+constexpr int SORT_BUCKETS = 16;
+constexpr int C_ZEROED = 4 + 2 * SORT_BUCKETS;  // words from C_FETCH on
+
+// The shade kernel's branch key of a finished ray: 0 for a miss, else the
+// material kind and whether the primitive is a triangle (smooth normals and
+// attributes to fetch). Shading a queue ordered by it keeps a warp's lanes
+// on the same branches.
+__device__ __forceinline__ uint32_t shade_key(const Scene& s, uint32_t prim) {
+    if (prim == NONE) return 0u;
+    const float4 hdr = ldg4(s.prims + size_t(prim) * 4);
+    const uint32_t kind = __float_as_uint(hdr.x), mat = __float_as_uint(hdr.y);
+    const uint32_t mk = __float_as_uint(ldg4(s.materials + size_t(mat) * 6).w);
+    return 2u + 2u * (mk < 6u ? mk : 6u) + (kind == TRIANGLE ? 1u : 0u);
+}
+
+// Lanes that finished a ray record its key and count it into its bucket:
+// one atomic per distinct key in the warp. All lanes of the warp call it.
+__device__ __forceinline__ void bucket_count(const WavefrontState& w, bool finished, uint32_t path, uint32_t key) {
+    const uint32_t fin = __ballot_sync(FULL, finished);
+    if (!fin) return;
+    const uint32_t peers = __match_any_sync(FULL, finished ? key : 0xFFFFFFFFu) & fin;
+    if (finished && lane_id() == uint32_t(__ffs(peers) - 1))
+        atomicAdd(w.counters + C_BUCKET + key, uint32_t(__popc(peers)));
+    if (finished) w.sort_key[path] = key;
+}
 
 // Where a path's scene and uniforms come from. A single frame has one of
 // each (kernel parameters); a batch looks them up in the job table by the
@@ -255,8 +282,13 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Ctx ctx, WavefrontState 
     uint32_t* fetch = w.counters + C_FETCH + 0;
     Traversal tr;
     uint32_t path = 0, job = 0;
-    bool active = false, exhausted = false;
+    bool active = false, exhausted = false, finished = false, missed = false;
     for (;;) {
+        // Rays finished in the last steps fetch their shading keys together
+        // (one load latency for the warp) and count them into the buckets.
+        const uint32_t key = finished ? shade_key(ctx.scene(job), tr.prim) : 0u;
+        bucket_count(w, finished, path, key);
+        finished = false;
         // Lanes without a ray claim the next queue entries together.
         const bool need = !active && !exhausted;
         const uint32_t mask = __ballot_sync(FULL, need);
@@ -273,11 +305,14 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Ctx ctx, WavefrontState 
                     const float4 a = w.s[0][path], b = w.s[1][path];
                     active = trav_begin(ctx.scene(job), tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), INF);
                     if (!active) w.hit[path] = make_float4(INF, __uint_as_float(NONE), 0.0f, 0.0f);
+                    missed = !active;
                 } else {
                     exhausted = true;
                 }
             }
         }
+        bucket_count(w, missed, path, 0u);  // rays that miss the scene's box: key 0
+        missed = false;
         if (!__any_sync(FULL, active || !exhausted)) return;
         if (active) {
             const Scene& sc = ctx.scene(job);
@@ -285,49 +320,91 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Ctx ctx, WavefrontState 
                 if (!trav_step<false>(sc, tr, st, wst)) {
                     w.hit[path] = make_float4(tr.t, __uint_as_float(tr.prim), tr.u, tr.v);
                     active = false;
+                    finished = true;
                 }
             }
         }
     }
 }
 
+// ---- scatter: this bounce's queue in shading-key order ----
+// Places are taken warp by warp in queue order (one atomic per key a warp
+// holds), so within a bucket paths keep roughly their queue order and the
+// rays shading emits stay coherent.
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_scatter(WavefrontState w, int q) {
+    __shared__ uint32_t base[SORT_BUCKETS];
+    if (threadIdx.x == 0) {
+        uint32_t sum = 0;
+        for (int k = 0; k < SORT_BUCKETS; ++k) {
+            base[k] = sum;
+            sum += w.counters[C_BUCKET + k];
+        }
+    }
+    __syncthreads();
+    const uint32_t n = w.counters[C_QUEUE0 + q];
+    const uint32_t* queue = w.queue[q];
+    const uint32_t rounds = (n + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
+    for (uint32_t r = 0; r < rounds; ++r) {  // whole warps together, for the match
+        const uint32_t i = (r * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+        const bool have = i < n;
+        const uint32_t path = have ? queue[i] : 0u;
+        const uint32_t key = have ? w.sort_key[path] : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(FULL, key) & __ballot_sync(FULL, have);
+        uint32_t at = 0;
+        const uint32_t leader = have ? uint32_t(__ffs(peers) - 1) : lane_id();
+        if (have && lane_id() == leader) at = atomicAdd(w.counters + C_CURSOR + key, uint32_t(__popc(peers)));
+        at = __shfl_sync(FULL, at, int(leader));
+        if (have) w.sorted[base[key] + at + uint32_t(__popc(peers & lanemask_lt()))] = path;
+    }
+}
+
 // ---- shade: one bounce of radiance() per live path ----
+// Shading runs in key order (the scatter's `sorted` queue) but queues
+// nothing: it records per path whether it continues (bit 0) and whether it
+// has a shadow ray (bit 1, the ray stored at the path's slot), and
+// k_wf_compact builds the next queues in the previous queue's order, which
+// keeps neighbouring paths' rays together for traversal.
 template <uint32_t FEAT, typename Ctx>
 __global__ void __launch_bounds__(WF_BLOCK) k_wf_shade(Ctx ctx, WavefrontState w, int q) {
+    const uint32_t n = w.counters[C_QUEUE0 + q];
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+        const uint32_t path = w.sorted[idx];
+        ShadowRay sh;
+        sh.valid = false;
+        PathState ps;
+        const uint32_t word = load_path(w, path, ps);
+        const uint32_t job = ctx.job_of(word);
+        const float4 hv = w.hit[path];
+        const Hit hit{hv.x, __float_as_uint(hv.y), hv.z, hv.w};
+        const bool more = path_step<FEAT>(ctx.scene(job), ctx.params(job), ps, hit, sh);
+        store_path(w, path, ps, word);
+        w.sort_key[path] = (more ? 1u : 0u) | (sh.valid ? 2u : 0u);
+        if (sh.valid) {
+            w.shadow[size_t(path) * 3 + 0] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.reach);
+            w.shadow[size_t(path) * 3 + 1] = make_float4(sh.d.x, sh.d.y, sh.d.z, __uint_as_float(path));
+            w.shadow[size_t(path) * 3 + 2] =
+                make_float4(sh.contribution.x, sh.contribution.y, sh.contribution.z, __uint_as_float(job));
+        }
+    }
+}
+
+// ---- compact: the next extension queue and the shadow list, in queue order ----
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_compact(WavefrontState w, int q) {
     const uint32_t n = w.counters[C_QUEUE0 + q];
     const uint32_t* queue = w.queue[q];
     uint32_t* out_queue = w.queue[q ^ 1];
     uint32_t* out_count = w.counters + C_QUEUE0 + (q ^ 1);
     uint32_t* shadow_count = w.counters + C_SHADOW;
     const uint32_t stride = gridDim.x * blockDim.x;
-    // Whole warps iterate together so the pushes can aggregate.
     const uint32_t rounds = (n + stride - 1) / stride;
-    for (uint32_t r = 0; r < rounds; ++r) {
+    for (uint32_t r = 0; r < rounds; ++r) {  // whole warps together, so the pushes aggregate
         const uint32_t idx = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        bool more = false, has_shadow = false;
-        ShadowRay sh;
-        sh.valid = false;
-        uint32_t path = 0, job = 0;
-        if (idx < n) {
-            path = queue[idx];
-            PathState ps;
-            const uint32_t word = load_path(w, path, ps);
-            job = ctx.job_of(word);
-            const float4 hv = w.hit[path];
-            const Hit hit{hv.x, __float_as_uint(hv.y), hv.z, hv.w};
-            more = path_step<FEAT>(ctx.scene(job), ctx.params(job), ps, hit, sh);
-            has_shadow = sh.valid;
-            store_path(w, path, ps, word);
-        }
-        const uint32_t slot = push_slot(out_count, more);
-        if (more) out_queue[slot] = path;
-        const uint32_t sslot = push_slot(shadow_count, has_shadow);
-        if (has_shadow) {
-            w.shadow[sslot * 3 + 0] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.reach);
-            w.shadow[sslot * 3 + 1] = make_float4(sh.d.x, sh.d.y, sh.d.z, __uint_as_float(path));
-            w.shadow[sslot * 3 + 2] =
-                make_float4(sh.contribution.x, sh.contribution.y, sh.contribution.z, __uint_as_float(job));
-        }
+        const uint32_t path = idx < n ? queue[idx] : 0u;
+        const uint32_t f = idx < n ? w.sort_key[path] : 0u;
+        const uint32_t slot = push_slot(out_count, (f & 1u) != 0u);
+        if (f & 1u) out_queue[slot] = path;
+        const uint32_t sslot = push_slot(shadow_count, (f & 2u) != 0u);
+        if (f & 2u) w.sorted[sslot] = path;  // the shadow list (the shade order is no longer needed)
     }
 }
 
@@ -357,14 +434,14 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState 
             if (need) {
                 const uint32_t idx = base + __popc(mask & lanemask_lt());
                 if (idx < n) {
-                    rec = idx;
-                    const float4 a = w.shadow[idx * 3], b = w.shadow[idx * 3 + 1];
-                    job = __float_as_uint(w.shadow[idx * 3 + 2].w);
+                    rec = w.sorted[idx];  // the shadow list holds paths; each path's ray sits at its slot
+                    const float4 a = w.shadow[size_t(rec) * 3], b = w.shadow[size_t(rec) * 3 + 1];
+                    job = __float_as_uint(w.shadow[size_t(rec) * 3 + 2].w);
                     active = trav_begin(ctx.scene(job), tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w);
                     if (!active) {
                         // Misses the scene's box: unoccluded.
                         const uint32_t path = __float_as_uint(b.w);
-                        const float4 c = w.shadow[idx * 3 + 2];
+                        const float4 c = w.shadow[size_t(rec) * 3 + 2];
                         float4 r = w.s[3][path];
                         w.s[3][path] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, r.w);
                     }
@@ -380,8 +457,8 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState 
                 if (!trav_step<true>(sc, tr, st, wst)) {
                     active = false;
                     if (tr.prim == NONE) {
-                        const uint32_t path = __float_as_uint(w.shadow[rec * 3 + 1].w);
-                        const float4 c = w.shadow[rec * 3 + 2];
+                        const uint32_t path = __float_as_uint(w.shadow[size_t(rec) * 3 + 1].w);
+                        const float4 c = w.shadow[size_t(rec) * 3 + 2];
                         float4 r = w.s[3][path];
                         w.s[3][path] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, r.w);
                     }
@@ -466,20 +543,22 @@ int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, co
         ++launches;
         int q = 0;
         for (uint32_t depth = 0; depth <= P.max_bounces; ++depth) {
-            cudaMemsetAsync(w.counters + C_FETCH, 0, 4 * sizeof(uint32_t), st);
+            cudaMemsetAsync(w.counters + C_FETCH, 0, C_ZEROED * sizeof(uint32_t), st);
             timer.begin(0);
             k_wf_extend<SingleCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
             timer.end();
+            k_wf_scatter<<<grid_shade, WF_BLOCK, 0, st>>>(w, q);
             // The next queue and the shadow queue start empty.
             cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
             cudaMemsetAsync(w.counters + C_SHADOW, 0, sizeof(uint32_t), st);
             timer.begin(1);
             k_wf_shade<FEAT, SingleCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q);
             timer.end();
+            k_wf_compact<<<grid_shade, WF_BLOCK, 0, st>>>(w, q);
             timer.begin(2);
             k_wf_shadow<SingleCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, tune.steps);
             timer.end();
-            launches += 3;
+            launches += 5;
             q ^= 1;
         }
         k_wf_finalize<<<grid_shade, WF_BLOCK, 0, st>>>(P, w, px, nk, P.sample_offset == 0u && k0 == 0);
@@ -587,13 +666,15 @@ static int batch_frame(const JobDesc* d_jobs, const WaveSegment* d_segments, con
         ++launches;
         int q = 0;
         for (uint32_t depth = 0; depth <= max_bounces; ++depth) {
-            cudaMemsetAsync(w.counters + C_FETCH, 0, 4 * sizeof(uint32_t), st);
+            cudaMemsetAsync(w.counters + C_FETCH, 0, C_ZEROED * sizeof(uint32_t), st);
             k_wf_extend<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
+            k_wf_scatter<<<grid_shade, WF_BLOCK, 0, st>>>(w, q);
             cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
             cudaMemsetAsync(w.counters + C_SHADOW, 0, sizeof(uint32_t), st);
             k_wf_shade<FEAT, BatchCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q);
+            k_wf_compact<<<grid_shade, WF_BLOCK, 0, st>>>(w, q);
             k_wf_shadow<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, tune.steps);
-            launches += 3;
+            launches += 5;
             q ^= 1;
         }
         k_wfb_finalize<<<grid_shade, WF_BLOCK, 0, st>>>(d_jobs, seg, wp.segments, w, wp.pixels);

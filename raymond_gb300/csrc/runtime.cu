@@ -70,7 +70,7 @@ struct raymond {
     DevBuf ray_scratch, prim_scratch, t_scratch, counter;
 
     // Wavefront path state (allocated on first wavefront frame).
-    DevBuf wf_state[8], wf_hit, wf_queue[2], wf_shadow, wf_counters;
+    DevBuf wf_state[8], wf_hit, wf_queue[2], wf_sorted, wf_sort_key, wf_shadow, wf_counters;
     uint64_t wf_capacity = 0;
     uint64_t path_capacity_limit = 0;  // from the config; 0 = default
     WavefrontTuning tuning{16, 8, 8};
@@ -204,8 +204,10 @@ int ensure_wavefront(raymond* h, const Params& P, WavefrontState& w) {
         if (e == cudaSuccess) e = h->wf_hit.reserve(cap * 16);
         if (e == cudaSuccess) e = h->wf_queue[0].reserve(cap * 4);
         if (e == cudaSuccess) e = h->wf_queue[1].reserve(cap * 4);
+        if (e == cudaSuccess) e = h->wf_sorted.reserve(cap * 4);
+        if (e == cudaSuccess) e = h->wf_sort_key.reserve(cap * 4);
         if (e == cudaSuccess) e = h->wf_shadow.reserve(cap * 48);
-        if (e == cudaSuccess) e = h->wf_counters.reserve(64);
+        if (e == cudaSuccess) e = h->wf_counters.reserve(256);
         if (e != cudaSuccess) return h->cuda_fail(e, "wavefront state");
         h->wf_capacity = cap;
     }
@@ -213,6 +215,8 @@ int ensure_wavefront(raymond* h, const Params& P, WavefrontState& w) {
     w.hit = static_cast<float4*>(h->wf_hit.ptr);
     w.queue[0] = static_cast<uint32_t*>(h->wf_queue[0].ptr);
     w.queue[1] = static_cast<uint32_t*>(h->wf_queue[1].ptr);
+    w.sorted = static_cast<uint32_t*>(h->wf_sorted.ptr);
+    w.sort_key = static_cast<uint32_t*>(h->wf_sort_key.ptr);
     w.shadow = static_cast<float4*>(h->wf_shadow.ptr);
     w.counters = static_cast<uint32_t*>(h->wf_counters.ptr);
     w.capacity = cap;
@@ -292,7 +296,8 @@ void raymond_destroy(raymond_t* h) {
                       &h->normal_maps, &h->env_map, &h->env_table, &h->accum, &h->guide_albedo, &h->guide_normal,
                       &h->light_a, &h->light_b, &h->denoised, &h->splats, &h->display, &h->ray_scratch,
                       &h->prim_scratch, &h->t_scratch, &h->counter, &h->wf_hit, &h->wf_queue[0], &h->wf_queue[1],
-                      &h->wf_shadow, &h->wf_counters, &h->photon_heads, &h->photons})
+                      &h->wf_sorted, &h->wf_sort_key, &h->wf_shadow, &h->wf_counters, &h->photon_heads,
+                      &h->photons, &h->wide})
         b->release();
     for (DevBuf& b : h->wf_state) b.release();
     for (cudaEvent_t ev : h->ev)
@@ -656,8 +661,10 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
             if (e == cudaSuccess) e = h->wf_hit.reserve(cap * 16);
             if (e == cudaSuccess) e = h->wf_queue[0].reserve(cap * 4);
             if (e == cudaSuccess) e = h->wf_queue[1].reserve(cap * 4);
+            if (e == cudaSuccess) e = h->wf_sorted.reserve(cap * 4);
+            if (e == cudaSuccess) e = h->wf_sort_key.reserve(cap * 4);
             if (e == cudaSuccess) e = h->wf_shadow.reserve(cap * 48);
-            if (e == cudaSuccess) e = h->wf_counters.reserve(64);
+            if (e == cudaSuccess) e = h->wf_counters.reserve(256);
             if (e != cudaSuccess) return h->cuda_fail(e, "batch path pool");
             h->wf_capacity = cap;
         }
@@ -698,6 +705,8 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
     w.hit = static_cast<float4*>(h->wf_hit.ptr);
     w.queue[0] = static_cast<uint32_t*>(h->wf_queue[0].ptr);
     w.queue[1] = static_cast<uint32_t*>(h->wf_queue[1].ptr);
+    w.sorted = static_cast<uint32_t*>(h->wf_sorted.ptr);
+    w.sort_key = static_cast<uint32_t*>(h->wf_sort_key.ptr);
     w.shadow = static_cast<float4*>(h->wf_shadow.ptr);
     w.counters = static_cast<uint32_t*>(h->wf_counters.ptr);
     w.capacity = h->wf_capacity;
