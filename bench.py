@@ -332,6 +332,8 @@ def run_rmse(args, local):
     size = args.size
     scene, camera, info = build_workload(size, args.spp, args.bounces)
     dev = f"cuda:{local}"
+    clocks = ClockSampler(local)
+    clocks.start()
 
     def renderer(seed, flags):
         r = rg.Renderer.create(rg.Canvas(size, size), device=local, seed=seed)
@@ -419,6 +421,7 @@ def run_rmse(args, local):
                 "curve_spp_seconds_rmse_rawrmse": [(s, round(t, 4), round(e, 5), round(q, 5))
                                                    for s, t, e, q in curve[:: max(1, len(curve) // 40)]]}
 
+    clock_info = clocks.stop()
     p = summary(plain_reached, plain_curve)
     o = summary(ours_reached, ours_curve)
     speedup = (p["seconds"] / o["seconds"]) if (p["reached"] and o["reached"]) else None
@@ -429,7 +432,7 @@ def run_rmse(args, local):
         "config": {"workload": f"sphere field {size}x{size}, {args.spp} spp per displayed frame, {args.bounces} bounces",
                    "threshold": args.threshold, "reference_spp": args.reference_spp, "reference_seconds": ref_s,
                    "max_spp": args.max_spp},
-        "plain_atrous": p, "batched_learned": o, "speedup_vs_plain_atrous": speedup,
+        "plain_atrous": p, "batched_learned": o, "speedup_vs_plain_atrous": speedup, "clocks": clock_info,
     }
 
 

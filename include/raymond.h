@@ -279,7 +279,7 @@ int raymond_denoise_static(const float* accum, const float* guide_albedo, const 
  * over albedo, albedo, normal, log depth, log standard error, 1/sqrt(n));
  * the output is a predicted log radiance over albedo (exponentiated and
  * multiplied back by albedo) and a per-pixel weight: the display is
- * α·prediction + (1 − α)·running average, α = sigmoid(weight)·v/(v + 0.05²)
+ * α·prediction + (1 − α)·running average, α = sigmoid(weight)·v/(v + 0.1²)
  * with v the running average's relative variance of the mean luminance (the
  * factor is 1 below 4 samples), so α → 0 and the display converges with the
  * average as samples accumulate.

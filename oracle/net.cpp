@@ -52,7 +52,7 @@ struct T {
 const double kLeak = 0.1;
 const double kMaxLog = 8.0;    // the prediction's exponent is clamped to ±this
 const double kMaxGrad = 64.0;  // and clips each element's gradient to ±this (before scaling)
-const double kBlendTau = 0.05;  // the blend guard's relative error scale (off below 4 samples)
+const double kBlendTau = 0.1;   // the blend guard's relative error scale (off below 4 samples)
 
 // Layer table: sources (tensor ids), output id, cout, activation.
 enum { IN, E0A, E0, P1, E1A, E1, P2, E2A, E2, P3, E3A, E3, P4, E4A, E4, D3A, D3, D2A, D2, D1A, D1, D0A, D0, OUT, NT };

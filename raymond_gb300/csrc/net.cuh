@@ -16,7 +16,7 @@ constexpr float kLeak = 0.1f;  // leaky ReLU slope below zero
 constexpr float kMaxLog = 8.0f;    // clamp of the prediction's exponent (radiance ≤ e⁸ × albedo)
 constexpr float kMaxGrad = 64.0f;  // loss: clip of each element's gradient (before the 1/(3·pixels) scale)
 constexpr float kRelEps = 0.01f;   // loss: ε of the relative squared error
-constexpr float kBlendTau = 0.05f;        // blend guard: relative error below which the average takes over
+constexpr float kBlendTau = 0.1f;         // blend guard: relative error below which the average takes over
 constexpr float kGuardMinSamples = 4.0f;  // blend guard: off below this many samples
 constexpr unsigned NET_STATUS_TIMEOUT = 1u;
 
