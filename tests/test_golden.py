@@ -1,0 +1,107 @@
+"""Golden fixtures (tests/golden/, written by make_golden.py from the oracle):
+the oracle, the product's native BVH builder and packer, and the CUDA path
+are all checked against the same committed bytes, so a result that drifts on
+another machine or compiler (the GB300 machine is Arm) shows here."""
+
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from parity import classify
+from raymond_gb300 import Canvas, Renderer, scenes
+from raymond_gb300.scene import BVH
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    with np.load(os.path.join(GOLDEN, name)) as z:
+        return {k: z[k] for k in z.files}
+
+
+def test_oracle_bvh_matches_golden():
+    g = load("bvh_boxes.npz")
+    nodes, order = oracle.bvh_build(g["mins"], g["maxs"])
+    assert np.array_equal(nodes, g["nodes"])
+    assert np.array_equal(order, g["order"])
+
+
+@pytest.mark.parametrize("threads", [1, 8])
+def test_native_bvh_matches_golden(threads):
+    g = load("bvh_boxes.npz")
+    b = BVH.build(g["mins"], g["maxs"], threads=threads)
+    assert np.array_equal(b.nodes, g["nodes"])
+    assert np.array_equal(b.order, g["order"])
+
+
+def test_packed_cornell_matches_golden():
+    g = load("cornell.npz")
+    scene, camera = scenes.cornell_scene()
+    packed = scene.pack()
+    assert np.array_equal(packed.primitives, g["primitives"])
+    assert np.array_equal(packed.nodes, g["nodes"])
+    assert np.array_equal(packed.materials, g["materials"])
+
+
+def test_oracle_raycast_matches_golden():
+    g = load("cornell.npz")
+    scene, camera = scenes.cornell_scene()
+    hits = oracle.raycast(scene.pack(), g["rays"])
+    assert np.array_equal(hits["prim"], g["prim"])
+    np.testing.assert_allclose(hits["t"], g["t"], rtol=1e-12, atol=0)
+
+
+def test_oracle_path_tracer_matches_golden():
+    g = load("cornell_image.npz")
+    scene, camera = scenes.cornell_scene()
+    packed = scene.pack()
+    from raymond_gb300.renderer import light_table
+
+    words, _ = light_table(packed)
+    img = oracle.render(packed, words, g["params"].tobytes(), nthreads=1)
+    # f32 arithmetic compiled without contraction; libm may differ in the
+    # last place between machines, so compare to rounding, not bits.
+    np.testing.assert_allclose(img["accum"], g["accum"], rtol=1e-4, atol=1e-5)
+
+
+@pytest.mark.gpu
+def test_gpu_hits_match_golden(gpu):
+    g = load("cornell.npz")
+    scene, camera = scenes.cornell_scene()
+    r = Renderer.create(Canvas(1, 1))
+    prim, t = r.tracePrimary(g["rays"], scene)
+    r.dispose()
+    ref = {"prim": g["prim"], "t": g["t"]}
+    c = classify(scene.pack(), g["rays"], prim, t, ref)
+    assert c["wrong"] == 0, c
+    assert c["hit_miss"] + c["silhouettes"] <= 0.005 * c["n"], c
+
+
+@pytest.mark.gpu
+def test_gpu_image_matches_golden(gpu):
+    g = load("cornell_image.npz")
+    scene, camera = scenes.cornell_scene()
+    r = Renderer.create(Canvas(16, 16))
+    r.scene, r.camera = scene, camera
+    r.maxBounces, r.samplesPerFrame, r.fireflyClamp, r.denoise = 6, 4, 0, False
+    r.render()
+    assert r.params == g["params"].tobytes()  # the same 208-byte block
+    accum, albedo, normal = r.readGuides()
+    r.dispose()
+    # same sample streams, f32 on both sides: most pixels agree to 1e-3
+    rel = np.abs(accum[..., :3] - g["accum"][..., :3]) / np.maximum(np.abs(g["accum"][..., :3]), 1e-3)
+    assert (rel.max(axis=2) < 1e-3).mean() > 0.9
+    assert abs(accum[..., :3].mean() / g["accum"][..., :3].mean() - 1) < 0.02
+
+
+@pytest.mark.gpu
+def test_oracle_and_builder_match_golden_on_the_gpu_machine(gpu):
+    """Run with the GPU tests so the oracle and the native builder, compiled
+    on the GPU machine's own (Arm) cores, are pinned to the same bytes."""
+    test_oracle_bvh_matches_golden()
+    test_native_bvh_matches_golden(8)
+    test_packed_cornell_matches_golden()
+    test_oracle_raycast_matches_golden()
+    test_oracle_path_tracer_matches_golden()
