@@ -38,7 +38,9 @@ constexpr uint32_t kABytes = kTileM * kChunk * 2;  // 16 KB
 constexpr uint32_t kLBO = 128;                   // K-direction core-matrix stride
 constexpr uint32_t kSBO = 1024;                  // M/N-direction core-matrix stride (8 k-groups)
 
-__host__ __device__ inline uint32_t tmem_cols_for(int n) { return n <= 32 ? 32u : n <= 64 ? 64u : n <= 128 ? 128u : 256u; }
+__host__ __device__ inline uint32_t tmem_cols_for(int n) {
+    return n <= 32 ? 32u : n <= 64 ? 64u : n <= 128 ? 128u : n <= 256 ? 256u : 512u;
+}
 __host__ __device__ inline uint32_t stage_bytes_for(int n) { return kABytes + uint32_t(n) * 128u; }
 
 struct Pixel {
@@ -328,9 +330,247 @@ __global__ void __launch_bounds__(kThreads) k_conv(ConvArgs a) {
     }
 }
 
+// ---------------------------------------------------------------- warp-specialised forward / input gradient
+
+// Roles of k_conv_ws's 13 warps: 0-3 drain accumulators (warp w reads the
+// tensor-memory lanes 32·w…), 4-11 load stages, 12 issues the MMAs.
+constexpr int kWsEpilogueWarps = 4, kWsLoadWarps = 8;
+constexpr int kWsLoaders = kWsLoadWarps * 32;
+constexpr int kWsMmaWarp = kWsEpilogueWarps + kWsLoadWarps;
+constexpr int kWsThreads = (kWsMmaWarp + 1) * 32;
+
+// Stage loads for loader thread p (0..255): A rows as k_conv's load_chunk
+// (row p & 127, four k-groups), B pieces strided over the loaders.
+template <int MODE>
+__device__ __forceinline__ void ws_load(const ConvArgs& a, int p, int N, int K, const Pixel& px, int k0,
+                                        unsigned char* sa, unsigned char* sb) {
+    const int r = p & (kTileM - 1);
+    const int cdiv = MODE == FWD ? a.cin : a.cout;
+    for (int j = 0; j < 4; ++j) {
+        const int g = (p >> 7) + 2 * j;
+        const int k = k0 + 8 * g;
+        if (k >= K) continue;
+        const int tap = k / cdiv;
+        const int c = k - tap * cdiv;
+        const int ty = tap / 3, tx = tap - 3 * ty;
+        const bf16* src = a.wt;
+        bool ok = false;
+        if (px.valid) {
+            if (MODE == FWD) {
+                ok = source_at(a, px.img, px.y + ty - 1, px.x + tx - 1, c, src);
+            } else {
+                const int yy = px.y - (ty - 1), xx = px.x - (tx - 1);
+                if (yy >= 0 && xx >= 0 && yy < a.h && xx < a.w) {
+                    src = a.dy + ((size_t(px.img) * a.h + yy) * a.w + xx) * size_t(a.dy_stride) + c;
+                    ok = true;
+                }
+            }
+        }
+        tc::cp_async16(sa + tc::core_offset(r, g, 8), ok ? src : a.wt, ok ? 16u : 0u);
+    }
+    if (MODE == FWD) {
+        for (int idx = p; idx < N * 8; idx += kWsLoaders) {
+            const int row = idx >> 3, g = idx & 7;
+            const int k = k0 + 8 * g;
+            if (k < K) tc::cp_async16(sb + tc::core_offset(row, g, 8), a.wt + size_t(row) * K + k, 16u);
+        }
+    } else {
+        const int kin = 9 * a.cin;
+        for (int idx = p; idx < (N >> 3) * kChunk; idx += kWsLoaders) {
+            const int kl = idx & (kChunk - 1), ng = idx >> 6;
+            const int k = k0 + kl;
+            if (k >= K) continue;
+            const int tap = k / a.cout;
+            const int co = k - tap * a.cout;
+            tc::cp_async16(sb + ng * kSBO + kl * 16, a.wt + size_t(co) * kin + tap * a.cin + 8 * ng, 16u);
+        }
+    }
+}
+
+// Forward and input gradient as persistent, warp-specialised CTAs over
+// pixel tiles (blockIdx.x, + gridDim.x, …). Loaders fill a ring of stages
+// and signal each with cp.async's own mbarrier arrival; the MMA thread
+// consumes stages into one of two tensor-memory accumulators and frees each
+// stage by tcgen05.commit; the epilogue warps drain an accumulator while the
+// next tile accumulates in the other. Every wait is bounded: a wait that
+// runs out records NET_STATUS_TIMEOUT and its role stops, so every role
+// reaches the end (the others' waits run out in turn) and the tensor memory
+// is freed.
+template <int MODE>
+__global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2];
+    __shared__ uint32_t tslot;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int pixels = a.n * a.h * a.w;
+    const int N = MODE == FWD ? a.cout : a.cin;
+    const int K = MODE == FWD ? 9 * a.cin : 9 * a.cout;
+    const uint32_t sbytes = stage_bytes_for(N);
+    const uint32_t tcols = tmem_cols_for(2 * N);
+    const int ntiles = (pixels + kTileM - 1) / kTileM;
+    const int nchunks = (K + kChunk - 1) / kChunk;
+    const int my_tiles = int(blockIdx.x) < ntiles ? (ntiles - 1 - int(blockIdx.x)) / int(gridDim.x) + 1 : 0;
+
+    if (tid == 0) {
+        for (int st = 0; st < kStages; ++st) {
+            tc::mbar_init(&full[st], kWsLoaders);
+            tc::mbar_init(&empty[st], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_empty[b], kWsEpilogueWarps);
+        }
+        tc::fence_barrier_init();
+    }
+    if (warp == kWsMmaWarp) {
+        tc::tmem_alloc(&tslot, tcols);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    tc::tc_fence_after_sync();
+    const uint32_t tbase = tslot;
+    bool ok = true;
+
+    if (warp >= kWsEpilogueWarps && warp < kWsMmaWarp) {
+        // ---- loaders
+        const int p = tid - kWsEpilogueWarps * 32;
+        for (int i = 0; i < my_tiles && ok; ++i) {
+            const int m0 = (int(blockIdx.x) + i * int(gridDim.x)) * kTileM;
+            const Pixel px = decode(m0 + (p & (kTileM - 1)), pixels, a.h, a.w);
+            for (int c = 0; c < nchunks; ++c) {
+                const int j = i * nchunks + c, s = j % kStages;
+                if (!tc::mbar_wait(&empty[s], ((j / kStages) & 1) ^ 1)) {
+                    ok = false;
+                    break;
+                }
+                unsigned char* st = smem + s * sbytes;
+                ws_load<MODE>(a, p, N, K, px, c * kChunk, st, st + kABytes);
+                tc::cp_async_arrive(&full[s]);
+            }
+        }
+        tc::cp_async_wait_all();
+    } else if (warp == kWsMmaWarp) {
+        // ---- MMA issue (one thread)
+        if (lane == 0) {
+            uint32_t idesc = tc::idesc_bf16(kTileM, N);
+            if (MODE == BWD_DATA) idesc |= 1u << 16;
+            for (int i = 0; i < my_tiles && ok; ++i) {
+                const int b = i & 1;
+                if (!tc::mbar_wait(&acc_empty[b], ((i >> 1) & 1) ^ 1)) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after_sync();
+                const uint32_t acc = tbase + uint32_t(b * N);
+                for (int c = 0; c < nchunks; ++c) {
+                    const int j = i * nchunks + c, s = j % kStages;
+                    if (!tc::mbar_wait(&full[s], (j / kStages) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    // the loaders' cp.async writes, seen by the tensor core's proxy
+                    tc::fence_proxy_async_smem();
+                    tc::tc_fence_after_sync();
+                    const uint32_t sa = tc::smem_u32(smem + s * sbytes);
+                    const uint32_t sb = sa + kABytes;
+                    const int slices = min(kChunk, K - c * kChunk) / 16;
+                    for (int q = 0; q < slices; ++q) {
+                        const uint64_t ad = tc::smem_desc(sa + q * 256, kLBO, kSBO);
+                        const uint64_t bd = tc::smem_desc(sb + q * 256, kLBO, kSBO);
+                        tc::mma_bf16(acc, ad, bd, idesc, (c > 0 || q > 0) ? 1u : 0u);
+                    }
+                    tc::mma_commit(&empty[s]);
+                }
+                if (!ok) break;
+                tc::mma_commit(&acc_full[b]);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue: warp w reads tensor-memory lanes 32·w..32·w+31
+        for (int i = 0; i < my_tiles && ok; ++i) {
+            const int b = i & 1;
+            if (!tc::mbar_wait(&acc_full[b], (i >> 1) & 1)) {
+                ok = false;
+                break;
+            }
+            tc::tc_fence_after_sync();
+            const int row = (int(blockIdx.x) + i * int(gridDim.x)) * kTileM + 32 * warp + lane;
+            const uint32_t lane_addr = tbase + (uint32_t(32 * warp) << 16) + uint32_t(b * N);
+            for (int c = 0; c < N; c += 16) {
+                float v[16];
+                tc::tmem_ld16(lane_addr + uint32_t(c), v);  // the whole warp, every row
+                if (row < pixels) {
+                    if (MODE == FWD) {
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) {
+                            float t = v[q] + a.bias[c + q];
+                            if (a.act) t = t > 0.0f ? t : kLeak * t;
+                            v[q] = t;
+                        }
+                    } else if (a.mask) {
+                        const uint4* mk = reinterpret_cast<const uint4*>(a.mask + size_t(row) * a.mask_stride + c);
+                        float mv[16];
+                        unpack8(mk[0], mv);
+                        unpack8(mk[1], mv + 8);
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) v[q] *= slope(mv[q]);
+                    }
+                    if (MODE == FWD && a.out_f32) {
+                        float4* o = reinterpret_cast<float4*>(a.out_f32 + size_t(row) * a.out_stride + c);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                    } else {
+                        uint4* o = reinterpret_cast<uint4*>(a.out + size_t(row) * a.out_stride + c);
+                        o[0] = pack8(v);
+                        o[1] = pack8(v + 8);
+                    }
+                }
+            }
+            tc::tc_fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
+        }
+    }
+    if (!ok) atomicOr(a.status, NET_STATUS_TIMEOUT);
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    if (warp == kWsMmaWarp) {
+        tc::tc_fence_after_sync();
+        tc::tmem_dealloc(tbase, tcols);
+    }
+}
+
 // ---------------------------------------------------------------- launchers
 
 static int smem_for(int n) { return int(kStages * stage_bytes_for(n)); }
+
+// The warp-specialised kernel's dynamic shared memory and resident CTAs per
+// SM, counted from its resources (shared memory with the per-CTA reserve,
+// threads, registers); its two accumulators need 2·n tensor-memory columns,
+// so the shared-memory request grows until the resident CTAs fit in 512.
+template <int MODE>
+static cudaError_t configure_ws(int n, int& smem, int& ctas) {
+    cudaFuncAttributes attr{};
+    cudaError_t e = cudaFuncGetAttributes(&attr, k_conv_ws<MODE>);
+    if (e != cudaSuccess) return e;
+    const int by_threads = 2048 / kWsThreads;
+    const int regs_per_cta = ((attr.numRegs * 32 + 255) / 256 * 256) * (kWsThreads / 32);
+    const int by_regs = 65536 / regs_per_cta;
+    const int max_tmem = 512 / int(tmem_cols_for(2 * n));
+    smem = smem_for(n);
+    for (;;) {
+        const int by_smem = 233472 / (smem + int(attr.sharedSizeBytes) + 1024);
+        ctas = std::min(std::min(by_threads, by_regs), by_smem);
+        if (ctas <= max_tmem) break;
+        smem += 4096;
+    }
+    if (ctas < 1) return cudaErrorInvalidConfiguration;
+    return cudaFuncSetAttribute(k_conv_ws<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
 
 template <int MODE>
 static cudaError_t configure(int n, int& smem) {
@@ -388,12 +628,14 @@ cudaError_t launch_conv(ConvArgs a, int mode, int num_sms, cudaStream_t st) {
     const int pixels = a.n * a.h * a.w;
     int smem = 0;
     cudaError_t e;
+    const int ntiles = (pixels + kTileM - 1) / kTileM;
+    int ctas = 0;
     if (mode == FWD) {
-        if ((e = configure<FWD>(a.cout, smem)) != cudaSuccess) return e;
-        k_conv<FWD><<<(pixels + kTileM - 1) / kTileM, kThreads, smem, st>>>(a);
+        if ((e = configure_ws<FWD>(a.cout, smem, ctas)) != cudaSuccess) return e;
+        k_conv_ws<FWD><<<std::min(ntiles, ctas * num_sms), kWsThreads, smem, st>>>(a);
     } else if (mode == BWD_DATA) {
-        if ((e = configure<BWD_DATA>(a.cin, smem)) != cudaSuccess) return e;
-        k_conv<BWD_DATA><<<(pixels + kTileM - 1) / kTileM, kThreads, smem, st>>>(a);
+        if ((e = configure_ws<BWD_DATA>(a.cin, smem, ctas)) != cudaSuccess) return e;
+        k_conv_ws<BWD_DATA><<<std::min(ntiles, ctas * num_sms), kWsThreads, smem, st>>>(a);
     } else {
         if ((e = configure<BWD_WEIGHT>(a.cout, smem)) != cudaSuccess) return e;
         const int mtiles = (9 * a.cin + 1 + kTileM - 1) / kTileM;
