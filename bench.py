@@ -15,6 +15,8 @@ Other workloads (--workload):
            splatted) and photon mapping (up to 4M photons, r = 0.01) every frame
   batch    64 seeded sphere-field instances as one graph-replayed batched frame
   denoise  the learned denoiser's 1080p inference as its own line
+  primary  closest hits of the Cornell room's 256² jittered primary rays, one
+           traversal launch per step (--size sets the image side)
   rmse     time to RMSE ≤ 0.01 against a 16,384-spp render: the plain
            one-kernel path with à-trous vs the batched wavefront path with
            the learned denoiser
@@ -313,6 +315,142 @@ def run_denoise(args, local):
         "config": {"workload": d["workload"], "l2": d["l2"], "weights": "raymond_gb300/weights/denoiser_unet.npz"},
         "e2e": d["e2e"], "gpu_launches": d["launches_per_frame"] * args.steps, "roofline": d["roofline"],
         "cpu_baseline": d["cpu_baseline"], "clocks": clock_info,
+    }
+
+
+PRIMARY_WORKLOAD = "Cornell room 256x256, one jittered primary ray per pixel (mulberry32 seed 1), closest hit"
+
+
+def primary_case(size):
+    """The Cornell primary-ray case: the room, its f32 camera rays, and the
+    algorithmic bytes of tracing them counted by the oracle's f32 traversal:
+    32·(1 + 2·inner nodes visited) + 64·primitives tested per ray."""
+    import oracle
+    from raymond_gb300 import scenes
+
+    scene, camera, rays = scenes.cornell_primary(size, seed=1)
+    counts = oracle.trace32(scene.pack(), rays)
+    return scene, rays, counts, int(oracle.bytes_per_ray(counts["inner"], counts["tested"]).sum())
+
+
+def primary_cpu(scene, rays, seconds=1.0):
+    """Scene.raycast restated in double (oracle/raycast.cpp) on all host
+    cores, repeated over the whole ray set for about `seconds`: Mrays/s."""
+    import oracle
+
+    packed = scene.pack()
+    threads = os.cpu_count() or 1
+    oracle.raycast(packed, rays[:1024], nthreads=threads)
+    done, t0 = 0, time.perf_counter()
+    while True:
+        oracle.raycast(packed, rays, nthreads=threads)
+        done += len(rays)
+        dt = time.perf_counter() - t0
+        if dt >= seconds:
+            return done / dt / 1e6, threads, dt
+
+
+def run_primary(args, local):
+    """Closest hits of the Cornell room's 65,536 primary rays: one traversal
+    launch per step, rays resident in HBM and L2 flushed between steps
+    (device time by CUDA events on the renderer's stream); end to end
+    through Renderer.tracePrimary with host arrays."""
+    import numpy as np
+    import torch
+
+    import oracle
+    import raymond_gb300 as rg
+    from raymond_gb300 import _native
+
+    size = 256 if args.size == 1024 else args.size
+    scene, rays, counts, algo_bytes = primary_case(size)
+    n = len(rays)
+    r = rg.Renderer.create(rg.Canvas(1, 1), device=local)
+    r.tracePrimary(rays[:32], scene)  # uploads the scene
+    lib = _native.lib()
+    stream = torch.cuda.ExternalStream(lib.raymond_get_stream(r.handle), device=f"cuda:{local}")
+    d_rays = torch.from_numpy(rays).to(f"cuda:{local}")
+    d_prim = torch.empty(n, dtype=torch.int32, device=f"cuda:{local}")
+    d_t = torch.empty(n, dtype=torch.float32, device=f"cuda:{local}")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    def launch():
+        _native.check(lib.raymond_trace_primary_device(r.handle, d_rays.data_ptr(), n, d_prim.data_ptr(),
+                                                       d_t.data_ptr()), r.handle)
+
+    for _ in range(max(args.warmup, 3)):
+        launch()
+    _native.check(lib.raymond_sync(r.handle), r.handle)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = []
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        launch()
+        b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    clock_info = clocks.stop()
+    prim = d_prim.cpu().numpy().view(np.uint32)
+    agree = float(np.mean(prim == counts["prim"]))
+
+    # End to end: numpy rays in, numpy hits out, through the public call.
+    e2e_steps = max(args.steps, 10)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        r.tracePrimary(rays, scene)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    del d_rays, d_prim, d_t, flush
+    r.dispose()
+
+    launch_s = statistics.mean(ms) / 1e3
+    peak, peak_kind = measured_peak_hbm()
+    achieved = algo_bytes / launch_s / 1e9
+    cpu_value, cores, cpu_s = primary_cpu(scene, rays)
+    return {
+        "metric": "Mrays/s (primary, closest hit)", "value": n / launch_s / 1e6, "unit": "Mrays/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32 jitter)",
+        "config": {"workload": PRIMARY_WORKLOAD, "rays": n, "l2": "flushed between steps (512 MB write)",
+                   "hits_equal_to_oracle_f32": agree},
+        "e2e": {"value": n / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 24 * n,
+                "d2h_bytes_per_step": 8 * n},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "kernel": "k_trace_primary", "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "algorithmic_bytes_per_launch": algo_bytes,
+                     "note": "algorithmic bytes are node and primitive reads that the 8-primitive room serves "
+                             "from L1; the launch is latency-bound"},
+        "cpu_baseline": {"value": cpu_value, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                         "sample": f"oracle Scene.raycast (double) over all {n} rays, repeated for {cpu_s:.1f} s"},
+        "clocks": clock_info,
+    }
+
+
+def run_primary_reference(args, rank, world):
+    if rank != 0:
+        return None
+    size = 256 if args.size == 1024 else args.size
+    scene, rays, _, _ = primary_case(size)
+    times = []
+    value = 0.0
+    for _ in range(args.steps):
+        value, cores, dt = primary_cpu(scene, rays, seconds=0.5)
+        times.append(dt)
+    return {
+        "metric": "Mrays/s (primary, closest hit)", "value": value, "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded mulberry32 jitter)", "impl": "reference",
+        "config": {"workload": PRIMARY_WORKLOAD, "rays": len(rays), "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                         "sample": f"oracle Scene.raycast (double) over all {len(rays)} rays for 0.5 s per step"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
@@ -702,7 +840,7 @@ def main():
     ap.add_argument("--bounces", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", default="auto", choices=["auto", "megakernel", "wavefront"])
-    ap.add_argument("--workload", default="field", choices=["field", "caustics", "batch", "denoise", "rmse"])
+    ap.add_argument("--workload", default="field", choices=["field", "caustics", "batch", "denoise", "rmse", "primary"])
     ap.add_argument("--threshold", type=float, default=0.01)
     ap.add_argument("--reference-spp", type=int, default=16384)
     ap.add_argument("--max-spp", type=int, default=4096)
@@ -717,7 +855,9 @@ def main():
         import torch
 
         torch.distributed.init_process_group("nccl")
-    if args.impl == "reference":
+    if args.impl == "reference" and args.workload == "primary":
+        out = run_primary_reference(args, rank, world)
+    elif args.impl == "reference":
         out = run_reference(args, rank, world)
     elif args.workload == "batch":
         out = run_batch(args) if rank == 0 else None
@@ -725,6 +865,8 @@ def main():
         out = run_denoise(args, local) if rank == 0 else None
     elif args.workload == "rmse":
         out = run_rmse(args, local) if rank == 0 else None
+    elif args.workload == "primary":
+        out = run_primary(args, local) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, local)
     if rank == 0 and out is not None:

@@ -379,6 +379,8 @@ typedef struct raymond_conv {
     int32_t activation; /* leaky ReLU, slope 0.1 below zero */
     uint32_t pixels_per_cta; /* backward_weight: 0 chooses */
     uint32_t* status;
+    uint32_t kernel; /* forward, backward_data: 0 chooses, 1 pixel-row tiles, 2 halo tiles (RAYMOND_EINVAL if
+                        the weights do not fit in shared memory) */
 } raymond_conv;
 int raymond_conv3x3_forward(const raymond_conv* c, void* stream);
 int raymond_conv3x3_backward_data(const raymond_conv* c, void* stream);

@@ -76,7 +76,7 @@ class Conv(ctypes.Structure):
                 ("dy_stride", ctypes.c_uint32), ("out", ctypes.c_void_p), ("out_stride", ctypes.c_uint32),
                 ("out_f32", ctypes.c_void_p), ("mask", ctypes.c_void_p), ("mask_stride", ctypes.c_uint32),
                 ("dweight", ctypes.c_void_p), ("dbias", ctypes.c_void_p), ("activation", ctypes.c_int32),
-                ("pixels_per_cta", ctypes.c_uint32), ("status", ctypes.c_void_p)]
+                ("pixels_per_cta", ctypes.c_uint32), ("status", ctypes.c_void_p), ("kernel", ctypes.c_uint32)]
 
 
 # Every symbol include/raymond.h declares, with its ctypes signature.

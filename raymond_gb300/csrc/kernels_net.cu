@@ -544,9 +544,289 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a) {
     }
 }
 
+// ---------------------------------------------------------------- halo tiles, resident weights
+
+// A tile is 8 × 16 output pixels of one image: M row m = 8·py + px, so each
+// 8-row core matrix is one tile row. Its halo of 10 × 18 pixels is staged
+// once per chunk of kc channels, as kc/8 columns of 180 16-byte pieces
+// (pixel (hy, hx) of the halo at (10·hy + hx)·16). Tap (ty, tx)'s A operand
+// is that column read from pixel ty·10 + tx with 160 bytes between core
+// matrices, so the nine taps share one load instead of loading the input
+// nine times. The whole weight tensor sits in shared memory for the CTA's
+// life, as blocks per (chunk, tap) of N × kc in core-matrix order.
+constexpr int kTileW = 8, kTileH = 16;
+constexpr int kHaloW = kTileW + 2, kHaloH = kTileH + 2, kHaloPx = kHaloW * kHaloH;
+constexpr uint32_t kHaloCol = kHaloPx * 16;     // one 8-channel column: 2880 B
+constexpr uint32_t kHaloRowStep = kHaloW * 16;  // between the tile's rows (core matrices along M)
+constexpr int kHaloMaxStages = 4;
+
+struct HaloPlan {
+    int kc;            // K-side channels per stage (16, 32 or 64)
+    int nchunks;       // ceil(K-side channels / kc)
+    int stages;        // 2 … kHaloMaxStages
+    uint32_t a_bytes;  // one stage: kc/8 halo columns
+    uint32_t b_block;  // weights of one (chunk, tap): N · kc · 2 bytes
+    uint32_t b_bytes;  // all weights: nchunks · 9 · b_block
+};
+
+// The weights into shared memory (loader thread p of kWsLoaders): FWD as
+// K-major blocks (row co, k = ci within the chunk), BWD_DATA as MN-major
+// blocks (n = ci, k = co within the chunk), both with 16·kc bytes between
+// 8-row groups and 128 between 8-column groups.
+template <int MODE>
+__device__ __forceinline__ void halo_load_weights(const ConvArgs& a, const HaloPlan& hp, int p, unsigned char* sb) {
+    const int cin8 = a.cin >> 3;
+    const int pieces = a.cout * 9 * cin8;  // 16-byte pieces of [cout][9][cin]
+    for (int i = p; i < pieces; i += kWsLoaders) {
+        const int co = i / (9 * cin8);
+        const int r = i - co * 9 * cin8;
+        const int t = r / cin8, c8 = r - t * cin8;
+        const bf16* src = a.wt + (size_t(co) * 9 + t) * a.cin + 8 * c8;
+        uint32_t off;
+        if (MODE == FWD) {
+            const int ci = 8 * c8, c = ci / hp.kc, g = (ci - c * hp.kc) >> 3;
+            off = uint32_t(c * 9 + t) * hp.b_block + uint32_t(((co >> 3) * (hp.kc >> 3) + g) * 128 + (co & 7) * 16);
+        } else {
+            const int c = co / hp.kc, kl = co - c * hp.kc;
+            off = uint32_t(c * 9 + t) * hp.b_block + uint32_t(c8 * 16 * hp.kc + kl * 16);
+        }
+        tc::cp_async16(sb + off, src, 16u);
+    }
+}
+
+// Forward and input gradient over halo tiles: the roles, rings and bounded
+// waits of k_conv_ws, with the A stages holding halos and the weights
+// loaded once. Tiles (img, row of tiles, column) in row-major order, so CTAs
+// that run at the same time share halo rows in L2.
+template <int MODE>
+__global__ void __launch_bounds__(kWsThreads) k_conv_halo(ConvArgs a, HaloPlan hp) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ uint64_t full[kHaloMaxStages], empty[kHaloMaxStages], acc_full[2], acc_empty[2];
+    __shared__ uint32_t tslot;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int N = MODE == FWD ? a.cout : a.cin;
+    const int CK = MODE == FWD ? a.cin : a.cout;  // K-side channels of one tap
+    const uint32_t tcols = tmem_cols_for(2 * N);
+    const int tiles_x = (a.w + kTileW - 1) / kTileW, tiles_y = (a.h + kTileH - 1) / kTileH;
+    const int per_img = tiles_x * tiles_y;
+    const int ntiles = a.n * per_img;
+    const int my_tiles = int(blockIdx.x) < ntiles ? (ntiles - 1 - int(blockIdx.x)) / int(gridDim.x) + 1 : 0;
+    const int S = hp.stages;
+    unsigned char* sb = smem;
+    unsigned char* sa0 = smem + hp.b_bytes;
+
+    if (tid == 0) {
+        for (int st = 0; st < S; ++st) {
+            tc::mbar_init(&full[st], kWsLoaders);
+            tc::mbar_init(&empty[st], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&acc_full[b], 1);
+            tc::mbar_init(&acc_empty[b], kWsEpilogueWarps);
+        }
+        tc::fence_barrier_init();
+    }
+    if (warp >= kWsEpilogueWarps && warp < kWsMmaWarp) {
+        halo_load_weights<MODE>(a, hp, tid - kWsEpilogueWarps * 32, sb);
+        tc::cp_async_wait_all();
+        tc::fence_proxy_async_smem();
+    }
+    if (warp == kWsMmaWarp) {
+        tc::tmem_alloc(&tslot, tcols);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    tc::tc_fence_after_sync();
+    const uint32_t tbase = tslot;
+    bool ok = true;
+
+    if (warp >= kWsEpilogueWarps && warp < kWsMmaWarp) {
+        // ---- loaders: one halo chunk per stage
+        const int p = tid - kWsEpilogueWarps * 32;
+        for (int i = 0; i < my_tiles && ok; ++i) {
+            const int tile = int(blockIdx.x) + i * int(gridDim.x);
+            const int img = tile / per_img, r = tile - img * per_img;
+            const int ty0 = (r / tiles_x) * kTileH - 1, tx0 = (r - (r / tiles_x) * tiles_x) * kTileW - 1;
+            for (int c = 0; c < hp.nchunks; ++c) {
+                const int j = i * hp.nchunks + c, s = j % S;
+                if (!tc::mbar_wait(&empty[s], ((j / S) & 1) ^ 1)) {
+                    ok = false;
+                    break;
+                }
+                unsigned char* st = sa0 + s * hp.a_bytes;
+                const int cols = min(hp.kc, CK - c * hp.kc) >> 3;
+                for (int idx = p; idx < cols * kHaloPx; idx += kWsLoaders) {
+                    const int g = idx / kHaloPx, q = idx - g * kHaloPx;
+                    const int hy = q / kHaloW, hx = q - hy * kHaloW;
+                    const int cb = c * hp.kc + 8 * g, yy = ty0 + hy, xx = tx0 + hx;
+                    const bf16* src = a.wt;
+                    bool in = false;
+                    if (MODE == FWD) {
+                        in = source_at(a, img, yy, xx, cb, src);
+                    } else if (yy >= 0 && xx >= 0 && yy < a.h && xx < a.w) {
+                        src = a.dy + ((size_t(img) * a.h + yy) * a.w + xx) * size_t(a.dy_stride) + cb;
+                        in = true;
+                    }
+                    tc::cp_async16(st + g * kHaloCol + q * 16, in ? src : a.wt, in ? 16u : 0u);
+                }
+                tc::cp_async_arrive(&full[s]);
+            }
+        }
+        tc::cp_async_wait_all();
+    } else if (warp == kWsMmaWarp) {
+        // ---- MMA issue (one thread): 9 taps × kc/16 slices per stage
+        if (lane == 0) {
+            uint32_t idesc = tc::idesc_bf16(kTileM, N);
+            if (MODE == BWD_DATA) idesc |= 1u << 16;
+            const uint32_t sbase = tc::smem_u32(sb);
+            const uint32_t b_sbo = uint32_t(16 * hp.kc);
+            for (int i = 0; i < my_tiles && ok; ++i) {
+                const int b = i & 1;
+                if (!tc::mbar_wait(&acc_empty[b], ((i >> 1) & 1) ^ 1)) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after_sync();
+                const uint32_t acc = tbase + uint32_t(b * N);
+                for (int c = 0; c < hp.nchunks; ++c) {
+                    const int j = i * hp.nchunks + c, s = j % S;
+                    if (!tc::mbar_wait(&full[s], (j / S) & 1)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::fence_proxy_async_smem();
+                    tc::tc_fence_after_sync();
+                    const uint32_t sa = tc::smem_u32(sa0 + s * hp.a_bytes);
+                    const int slices = min(hp.kc, CK - c * hp.kc) >> 4;
+                    for (int t = 0; t < 9; ++t) {
+                        const int ty = t / 3, tx = t - 3 * ty;
+                        // forward reads x(p + tap − 1); the input gradient reads dy(p − tap + 1)
+                        const int pix = MODE == FWD ? ty * kHaloW + tx : (2 - ty) * kHaloW + (2 - tx);
+                        const uint32_t bt = sbase + uint32_t(c * 9 + t) * hp.b_block;
+                        for (int q = 0; q < slices; ++q) {
+                            const uint64_t ad = tc::smem_desc(sa + uint32_t(2 * q) * kHaloCol + uint32_t(pix) * 16,
+                                                              kHaloCol, kHaloRowStep);
+                            const uint64_t bd = tc::smem_desc(bt + uint32_t(q) * 256, 128, b_sbo);
+                            tc::mma_bf16(acc, ad, bd, idesc, (c > 0 || t > 0 || q > 0) ? 1u : 0u);
+                        }
+                    }
+                    tc::mma_commit(&empty[s]);
+                }
+                if (!ok) break;
+                tc::mma_commit(&acc_full[b]);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue: warp w holds tile rows 4w … 4w+3 (tensor-memory lanes 32·w …)
+        const int py = 4 * warp + (lane >> 3), px = lane & 7;
+        for (int i = 0; i < my_tiles && ok; ++i) {
+            const int b = i & 1;
+            if (!tc::mbar_wait(&acc_full[b], (i >> 1) & 1)) {
+                ok = false;
+                break;
+            }
+            tc::tc_fence_after_sync();
+            const int tile = int(blockIdx.x) + i * int(gridDim.x);
+            const int img = tile / per_img, r = tile - img * per_img;
+            const int y = (r / tiles_x) * kTileH + py, x = (r - (r / tiles_x) * tiles_x) * kTileW + px;
+            const bool valid = y < a.h && x < a.w;
+            const size_t row = (size_t(img) * a.h + y) * a.w + x;
+            const uint32_t lane_addr = tbase + (uint32_t(32 * warp) << 16) + uint32_t(b * N);
+            for (int c = 0; c < N; c += 16) {
+                float v[16];
+                tc::tmem_ld16(lane_addr + uint32_t(c), v);  // the whole warp, every row
+                if (valid) {
+                    if (MODE == FWD) {
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) {
+                            float t = v[q] + a.bias[c + q];
+                            if (a.act) t = t > 0.0f ? t : kLeak * t;
+                            v[q] = t;
+                        }
+                    } else if (a.mask) {
+                        const uint4* mk = reinterpret_cast<const uint4*>(a.mask + row * a.mask_stride + c);
+                        float mv[16];
+                        unpack8(mk[0], mv);
+                        unpack8(mk[1], mv + 8);
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) v[q] *= slope(mv[q]);
+                    }
+                    if (MODE == FWD && a.out_f32) {
+                        float4* o = reinterpret_cast<float4*>(a.out_f32 + row * a.out_stride + c);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                    } else {
+                        uint4* o = reinterpret_cast<uint4*>(a.out + row * a.out_stride + c);
+                        o[0] = pack8(v);
+                        o[1] = pack8(v + 8);
+                    }
+                }
+            }
+            tc::tc_fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&acc_empty[b]);
+        }
+    }
+    if (!ok) atomicOr(a.status, NET_STATUS_TIMEOUT);
+    tc::tc_fence_before_sync();
+    __syncthreads();
+    if (warp == kWsMmaWarp) {
+        tc::tc_fence_after_sync();
+        tc::tmem_dealloc(tbase, tcols);
+    }
+}
+
 // ---------------------------------------------------------------- launchers
 
 static int smem_for(int n) { return int(kStages * stage_bytes_for(n)); }
+
+// The halo kernel's stage size and weight blocks for N output columns and
+// CK K-side channels: the widest chunk (≤ 64 channels) whose weights and at
+// least two stages fit in `budget` bytes; false when none does.
+static bool plan_halo(int N, int CK, int budget, HaloPlan& hp) {
+    for (int kc = 64; kc >= 16; kc >>= 1) {
+        if (kc > CK && kc > 16) continue;
+        hp.kc = kc;
+        hp.nchunks = (CK + kc - 1) / kc;
+        hp.a_bytes = uint32_t(kc / 8) * kHaloCol;
+        hp.b_block = uint32_t(N) * uint32_t(kc) * 2u;
+        hp.b_bytes = uint32_t(hp.nchunks) * 9u * hp.b_block;
+        if (int(hp.b_bytes) >= budget) continue;
+        hp.stages = std::min(kHaloMaxStages, (budget - int(hp.b_bytes)) / int(hp.a_bytes));
+        if (hp.stages >= 2) return true;
+    }
+    return false;
+}
+
+// Dynamic shared memory and resident CTAs of the halo kernel (as
+// configure_ws); false when the weights do not fit.
+template <int MODE>
+static cudaError_t configure_halo(int N, int CK, HaloPlan& hp, int& smem, int& ctas, bool& fits) {
+    cudaFuncAttributes attr{};
+    cudaError_t e = cudaFuncGetAttributes(&attr, k_conv_halo<MODE>);
+    if (e != cudaSuccess) return e;
+    const int budget = 232448 - int(attr.sharedSizeBytes) - 1024;
+    fits = plan_halo(N, CK, budget, hp);
+    if (!fits) return cudaSuccess;
+    smem = int(hp.b_bytes + uint32_t(hp.stages) * hp.a_bytes);
+    const int by_threads = 2048 / kWsThreads;
+    const int regs_per_cta = ((attr.numRegs * 32 + 255) / 256 * 256) * (kWsThreads / 32);
+    const int by_regs = 65536 / regs_per_cta;
+    const int max_tmem = 512 / int(tmem_cols_for(2 * N));
+    for (;;) {
+        const int by_smem = 233472 / (smem + int(attr.sharedSizeBytes) + 1024);
+        ctas = std::min(std::min(by_threads, by_regs), by_smem);
+        if (ctas <= max_tmem) break;
+        smem += 4096;
+    }
+    if (ctas < 1) return cudaErrorInvalidConfiguration;
+    return cudaFuncSetAttribute(k_conv_halo<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
 
 // The warp-specialised kernel's dynamic shared memory and resident CTAs per
 // SM, counted from its resources (shared memory with the per-CTA reserve,
@@ -624,31 +904,57 @@ const char* check_conv(const ConvArgs& a, int mode) {
     return nullptr;
 }
 
+bool conv_halo_fits(int mode, int cin, int cout) {
+    if (mode != FWD && mode != BWD_DATA) return false;
+    HaloPlan hp{};
+    int smem = 0, ctas = 0;
+    bool fits = false;
+    const cudaError_t e = mode == FWD ? configure_halo<FWD>(cout, cin, hp, smem, ctas, fits)
+                                      : configure_halo<BWD_DATA>(cin, cout, hp, smem, ctas, fits);
+    return e == cudaSuccess && fits;
+}
+
+// Forward or input gradient: the halo kernel unless the caller asked for
+// pixel-row tiles or the weights do not fit (then CONV_HALO is an error).
+template <int MODE>
+static cudaError_t launch_fwd_or_data(const ConvArgs& a, int num_sms, cudaStream_t st) {
+    const int N = MODE == FWD ? a.cout : a.cin, CK = MODE == FWD ? a.cin : a.cout;
+    int smem = 0, ctas = 0;
+    cudaError_t e;
+    if (a.kernel != CONV_ROWS) {
+        HaloPlan hp{};
+        bool fits = false;
+        if ((e = configure_halo<MODE>(N, CK, hp, smem, ctas, fits)) != cudaSuccess) return e;
+        if (fits) {
+            const int ntiles = a.n * ((a.w + kTileW - 1) / kTileW) * ((a.h + kTileH - 1) / kTileH);
+            k_conv_halo<MODE><<<std::min(ntiles, ctas * num_sms), kWsThreads, smem, st>>>(a, hp);
+            return cudaGetLastError();
+        }
+        if (a.kernel == CONV_HALO) return cudaErrorInvalidValue;
+    }
+    if ((e = configure_ws<MODE>(N, smem, ctas)) != cudaSuccess) return e;
+    const int ntiles = (a.n * a.h * a.w + kTileM - 1) / kTileM;
+    k_conv_ws<MODE><<<std::min(ntiles, ctas * num_sms), kWsThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_conv(ConvArgs a, int mode, int num_sms, cudaStream_t st) {
+    if (mode == FWD) return launch_fwd_or_data<FWD>(a, num_sms, st);
+    if (mode == BWD_DATA) return launch_fwd_or_data<BWD_DATA>(a, num_sms, st);
     const int pixels = a.n * a.h * a.w;
     int smem = 0;
     cudaError_t e;
-    const int ntiles = (pixels + kTileM - 1) / kTileM;
-    int ctas = 0;
-    if (mode == FWD) {
-        if ((e = configure_ws<FWD>(a.cout, smem, ctas)) != cudaSuccess) return e;
-        k_conv_ws<FWD><<<std::min(ntiles, ctas * num_sms), kWsThreads, smem, st>>>(a);
-    } else if (mode == BWD_DATA) {
-        if ((e = configure_ws<BWD_DATA>(a.cin, smem, ctas)) != cudaSuccess) return e;
-        k_conv_ws<BWD_DATA><<<std::min(ntiles, ctas * num_sms), kWsThreads, smem, st>>>(a);
-    } else {
-        if ((e = configure<BWD_WEIGHT>(a.cout, smem)) != cudaSuccess) return e;
-        const int mtiles = (9 * a.cin + 1 + kTileM - 1) / kTileM;
-        if (a.pixels_per_cta <= 0) {
-            // About two waves of CTAs over the SMs, at least 8 chunks each.
-            const int want = std::max(1, 2 * num_sms / mtiles);
-            int per = (pixels + want - 1) / want;
-            per = std::max(per, 8 * kChunk);
-            a.pixels_per_cta = (per + kChunk - 1) / kChunk * kChunk;
-        }
-        const int ksplit = (pixels + a.pixels_per_cta - 1) / a.pixels_per_cta;
-        k_conv<BWD_WEIGHT><<<dim3(mtiles, ksplit), kThreads, smem, st>>>(a);
+    if ((e = configure<BWD_WEIGHT>(a.cout, smem)) != cudaSuccess) return e;
+    const int mtiles = (9 * a.cin + 1 + kTileM - 1) / kTileM;
+    if (a.pixels_per_cta <= 0) {
+        // About two waves of CTAs over the SMs, at least 8 chunks each.
+        const int want = std::max(1, 2 * num_sms / mtiles);
+        int per = (pixels + want - 1) / want;
+        per = std::max(per, 8 * kChunk);
+        a.pixels_per_cta = (per + kChunk - 1) / kChunk * kChunk;
     }
+    const int ksplit = (pixels + a.pixels_per_cta - 1) / a.pixels_per_cta;
+    k_conv<BWD_WEIGHT><<<dim3(mtiles, ksplit), kThreads, smem, st>>>(a);
     return cudaGetLastError();
 }
 

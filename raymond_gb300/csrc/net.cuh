@@ -12,6 +12,11 @@ namespace net {
 
 enum ConvMode { FWD = 0, BWD_DATA = 1, BWD_WEIGHT = 2 };
 
+// Forward and input-gradient kernels: pixel-row tiles that gather each tap
+// (any size), or 8×16 halo tiles with the weights resident in shared memory
+// (when they fit); CONV_AUTO takes the halo kernel where it can.
+enum ConvKernel { CONV_AUTO = 0, CONV_ROWS = 1, CONV_HALO = 2 };
+
 constexpr float kLeak = 0.1f;  // leaky ReLU slope below zero
 constexpr float kMaxLog = 8.0f;    // clamp of the prediction's exponent (radiance ≤ e⁸ × albedo)
 constexpr float kMaxGrad = 64.0f;  // loss: clip of each element's gradient (before the 1/(3·pixels) scale)
@@ -48,6 +53,7 @@ struct ConvArgs {
     int act;    // forward: apply the leaky ReLU
     int pixels_per_cta;  // weight gradient: K split (0 picks one)
     unsigned* status;
+    int kernel;  // forward and input gradient: CONV_AUTO, CONV_ROWS or CONV_HALO
 };
 
 struct FeatureArgs {
@@ -98,6 +104,7 @@ struct ComposeArgs {
 
 const char* check_conv(const ConvArgs& a, int mode);
 cudaError_t launch_conv(ConvArgs a, int mode, int num_sms, cudaStream_t st);
+bool conv_halo_fits(int mode, int cin, int cout);  // the halo kernel's weights fit in shared memory
 cudaError_t launch_features(const FeatureArgs& f, cudaStream_t st);
 cudaError_t launch_pool(const __nv_bfloat16* in, __nv_bfloat16* out, int n, int h, int w, int c, cudaStream_t st);
 cudaError_t launch_split_up(const __nv_bfloat16* dcat, int cat_stride, __nv_bfloat16* g_coarse,

@@ -638,12 +638,21 @@ static int conv_entry(const raymond_conv* c, void* stream, int mode) {
     a.act = c->activation;
     a.pixels_per_cta = int(c->pixels_per_cta);
     a.status = c->status;
+    a.kernel = int(c->kernel);
     if (mode == BWD_WEIGHT && a.pixels_per_cta == 0) a.pixels_per_cta = 64;  // replaced by the launcher
     if (const char* why = check_conv(a, mode)) {
         rmd::set_handleless_error(why);
         return RAYMOND_EINVAL;
     }
     if (mode == BWD_WEIGHT && c->pixels_per_cta == 0) a.pixels_per_cta = 0;
+    if (a.kernel < CONV_AUTO || a.kernel > CONV_HALO) {
+        rmd::set_handleless_error("conv: kernel must be 0 (choose), 1 (pixel rows) or 2 (halo tiles)");
+        return RAYMOND_EINVAL;
+    }
+    if (a.kernel == CONV_HALO && !conv_halo_fits(mode, a.cin, a.cout)) {
+        rmd::set_handleless_error("conv: the weights do not fit in shared memory for halo tiles");
+        return RAYMOND_EINVAL;
+    }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

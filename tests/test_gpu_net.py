@@ -23,8 +23,9 @@ def _bf16(rng, shape, scale=1.0):
 
 
 def _run_conv(mode, n, h, w, src0, c0, shift0, src1, c1, cout, weight, bias=None, dy=None, out=None, out_f32=None,
-              mask=None, dw=None, db=None, act=0, status=None):
+              mask=None, dw=None, db=None, act=0, status=None, kernel=0):
     c = _native.Conv()
+    c.kernel = kernel
     c.n, c.height, c.width, c.cin, c.cout = n, h, w, c0 + c1, cout
     c.src0, c.src0_channels, c.src0_stride, c.src0_shift = src0.data_ptr(), c0, c0, shift0
     if src1 is not None:
@@ -57,11 +58,16 @@ CASES = [
     (2, 16, 16, 128, 1, 128, 128),
     (1, 12, 20, 96, 0, 0, 16),
     (1, 16, 24, 128, 1, 96, 96),
+    (1, 18, 9, 32, 0, 48, 64),
+    (3, 7, 5, 32, 0, 0, 96),
 ]
+# forward and input-gradient kernels: 0 the library's choice, 1 pixel-row tiles, 2 halo tiles
+KERNELS = [0, 1, 2]
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("case", CASES)
-def test_conv_kernels_match_oracle(gpu, case):
+def test_conv_kernels_match_oracle(gpu, case, kernel):
     n, h, w, c0, shift0, c1, cout = case
     rng = np.random.default_rng(sum(case))
     cin = c0 + c1
@@ -73,13 +79,21 @@ def test_conv_kernels_match_oracle(gpu, case):
 
     # forward, BF16 out with the activation, and FP32 out without
     out = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
-    _run_conv(0, n, h, w, src0, c0, shift0, src1, c1, cout, weight, bias=bias, out=out, act=1, status=status)
+    try:
+        _run_conv(0, n, h, w, src0, c0, shift0, src1, c1, cout, weight, bias=bias, out=out, act=1, status=status,
+                  kernel=kernel)
+    except _native.RaymondError as e:
+        # asked for halo tiles where the weights do not fit in shared memory: refused before any launch
+        assert kernel == 2 and e.code == _native.EINVAL and "do not fit" in str(e), e
+        assert 9 * 2 * cin * cout > 150 * 1024
+        pytest.skip("weights too large for halo tiles")
     want = oracle.conv3x3(0, s0, wv, bias.cpu().numpy(), src1=s1, shift0=shift0, act=1)
     got = out.float().cpu().numpy()
     scale = np.abs(want).max()
     assert np.abs(got - want).max() <= 8e-3 * scale
     out32 = torch.empty((n, h, w, cout), dtype=torch.float32, device="cuda")
-    _run_conv(0, n, h, w, src0, c0, shift0, src1, c1, cout, weight, bias=bias, out_f32=out32, status=status)
+    _run_conv(0, n, h, w, src0, c0, shift0, src1, c1, cout, weight, bias=bias, out_f32=out32, status=status,
+              kernel=kernel)
     want = oracle.conv3x3(0, s0, wv, bias.cpu().numpy(), src1=s1, shift0=shift0, act=0)
     np.testing.assert_allclose(out32.cpu().numpy(), want, rtol=1e-4, atol=1e-4 * scale)
 
@@ -87,10 +101,13 @@ def test_conv_kernels_match_oracle(gpu, case):
     dy, dyv = _bf16(rng, (n, h, w, cout))
     mask, mv = _bf16(rng, (n, h, w, cin))
     dx = torch.empty((n, h, w, cin), dtype=torch.bfloat16, device="cuda")
-    _run_conv(1, n, h, w, src0, c0, shift0, src1, c1, cout, weight, dy=dy, out=dx, mask=mask, status=status)
+    _run_conv(1, n, h, w, src0, c0, shift0, src1, c1, cout, weight, dy=dy, out=dx, mask=mask, status=status,
+              kernel=kernel)
     want = oracle.conv3x3(1, s0, wv, src1=s1, shift0=shift0, dy=dyv, mask=mv)
     got = dx.float().cpu().numpy()
     assert np.abs(got - want).max() <= 8e-3 * np.abs(want).max()
+    if kernel:
+        return
 
     # weight and bias gradients, accumulated onto what is there
     dw = torch.full((cout, 9, cin), 0.5, dtype=torch.float32, device="cuda")
@@ -205,22 +222,26 @@ def test_training_reduces_the_loss(gpu):
     net.dispose()
 
 
-def test_conv_many_tiles_per_cta_match_oracle(gpu):
+@pytest.mark.parametrize("kernel", [1, 2])
+@pytest.mark.parametrize("shape", [(1, 384, 385, 16, 16), (2, 100, 203, 64, 32)])
+def test_conv_many_tiles_per_cta_match_oracle(gpu, kernel, shape):
     """Forward and input gradient run as persistent CTAs over pixel tiles with
-    one pipeline across tile boundaries: an image of 1,152 tiles gives every
-    CTA several, including a partial last one."""
+    one pipeline across tile boundaries: an image of 1,152 row tiles (or
+    1,200 halo tiles) gives every CTA several, including partial ones at the
+    right and bottom edges."""
     rng = np.random.default_rng(77)
-    n, h, w, c0, cout = 1, 384, 385, 16, 16
+    n, h, w, c0, cout = shape
     src0, s0 = _bf16(rng, (n, h, w, c0))
     weight, wv = _bf16(rng, (cout, 9, c0), 1.0 / np.sqrt(9 * c0))
     bias = torch.from_numpy(rng.standard_normal(cout).astype(np.float32)).cuda()
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
     out = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
-    _run_conv(0, n, h, w, src0, c0, 0, None, 0, cout, weight, bias=bias, out=out, act=1, status=status)
+    _run_conv(0, n, h, w, src0, c0, 0, None, 0, cout, weight, bias=bias, out=out, act=1, status=status,
+              kernel=kernel)
     want = oracle.conv3x3(0, s0, wv, bias.cpu().numpy(), act=1)
     assert np.abs(out.float().cpu().numpy() - want).max() <= 8e-3 * np.abs(want).max()
     dy, dyv = _bf16(rng, (n, h, w, cout))
     dx = torch.empty((n, h, w, c0), dtype=torch.bfloat16, device="cuda")
-    _run_conv(1, n, h, w, src0, c0, 0, None, 0, cout, weight, dy=dy, out=dx, status=status)
+    _run_conv(1, n, h, w, src0, c0, 0, None, 0, cout, weight, dy=dy, out=dx, status=status, kernel=kernel)
     want = oracle.conv3x3(1, s0, wv, dy=dyv)
     assert np.abs(dx.float().cpu().numpy() - want).max() <= 8e-3 * np.abs(want).max()

@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _tree(r, width):
-    """Walk the reference's binary nodes (2) or the 4-wide tree derived from them (4)."""
+    """Walk the reference's binary nodes (2), the 4-wide tree derived from them (4), or the automatic choice (0)."""
     import ctypes
 
     from raymond_gb300 import _native
@@ -32,7 +32,7 @@ def test_cornell_primary_rays_match_raycast(gpu, width):
     r = renderer()
     _tree(r, width)
     prim, t = r.tracePrimary(rays, scene)
-    _tree(r, 4)
+    _tree(r, 0)
     packed = scene.pack()
     ref = oracle.raycast(packed, rays)
     c = classify(packed, rays, prim, t, ref)
@@ -59,7 +59,7 @@ def test_sphere_field_primary_rays_match_raycast(gpu, width):
     r = renderer()
     _tree(r, width)
     prim, t = r.tracePrimary(rays, scene)
-    _tree(r, 4)
+    _tree(r, 0)
     packed = scene.pack()
     ref = oracle.raycast(packed, rays)
     c = classify(packed, rays, prim, t, ref)
