@@ -4,6 +4,7 @@
 #include <cudaTypedefs.h>
 
 #include "dev_tcgen05.cuh"
+#include "dev_tma.cuh"
 #include "kernels.cuh"
 
 #include <mutex>
@@ -162,18 +163,6 @@ struct AtrousTile {
     static constexpr uint32_t smem = 2 * stride;
 };
 
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-            tc::smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(tc::smem_u32(bar))
-        : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc::smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
 template <int STEP>
 __global__ void __launch_bounds__(ATROUS_THREADS) k_atrous_tma(DenoiseView v, const __grid_constant__ CUtensorMap light,
                                                                 const __grid_constant__ CUtensorMap guide,
@@ -314,8 +303,6 @@ __global__ void k_tonemap(Params P, const float4* __restrict__ accum, const floa
 
 }  // namespace
 
-namespace {
-
 // cuTensorMapEncodeTiled, from the driver through the runtime (no -lcuda).
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
@@ -329,6 +316,8 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
     }();
     return fn;
 }
+
+namespace {
 
 // A w×h float4 image as a 2D tensor of floats (4w × h) with a box of the
 // tile for one step.

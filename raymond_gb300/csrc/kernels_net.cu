@@ -23,6 +23,7 @@
 #include <cstring>
 
 #include "dev_tcgen05.cuh"
+#include "dev_tma.cuh"
 #include "net.cuh"
 
 namespace rmd {
@@ -554,22 +555,33 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a) {
 // matrices, so the nine taps share one load instead of loading the input
 // nine times. The whole weight tensor sits in shared memory for the CTA's
 // life, as blocks per (chunk, tap) of N × kc in core-matrix order.
+
 constexpr int kTileW = 8, kTileH = 16;
 constexpr int kHaloW = kTileW + 2, kHaloH = kTileH + 2, kHaloPx = kHaloW * kHaloH;
-constexpr uint32_t kHaloCol = kHaloPx * 16;     // one 8-channel column: 2880 B
+constexpr uint32_t kHaloBox = kHaloPx * 16;     // one 8-channel column: 2880 B
+constexpr uint32_t kHaloCol = 23 * 128;         // its slot, 128-byte aligned for the tensor copy
 constexpr uint32_t kHaloRowStep = kHaloW * 16;  // between the tile's rows (core matrices along M)
 constexpr int kHaloMaxStages = 4;
+// Roles of k_conv_halo's 11 warps: 0-3 epilogue (as k_conv_ws), 4-9 load
+// (loader 0 issues the tensor copies; where a source is upsampled, loader
+// p < 180 gathers halo pixel p of its columns), 10 issues the MMAs.
+constexpr int kHaloLoadWarps = 6, kHaloLoaders = kHaloLoadWarps * 32;
+constexpr int kHaloMmaWarp = kWsEpilogueWarps + kHaloLoadWarps;
+constexpr int kHaloThreads = (kHaloMmaWarp + 1) * 32;
+static_assert(kHaloLoaders >= kHaloPx, "one loader thread per halo pixel");
 
 struct HaloPlan {
+    int tma;           // bit k: source k (dy: bit 0) comes by tensor copies of whole halo columns
+    int gather;        // some source is gathered per pixel (an upsampled one)
     int kc;            // K-side channels per stage (16, 32 or 64)
     int nchunks;       // ceil(K-side channels / kc)
     int stages;        // 2 … kHaloMaxStages
-    uint32_t a_bytes;  // one stage: kc/8 halo columns
+    uint32_t a_bytes;  // one stage: kc/8 halo columns of kHaloCol bytes
     uint32_t b_block;  // weights of one (chunk, tap): N · kc · 2 bytes
     uint32_t b_bytes;  // all weights: nchunks · 9 · b_block
 };
 
-// The weights into shared memory (loader thread p of kWsLoaders): FWD as
+// The weights into shared memory (loader thread p of kHaloLoaders): FWD as
 // K-major blocks (row co, k = ci within the chunk), BWD_DATA as MN-major
 // blocks (n = ci, k = co within the chunk), both with 16·kc bytes between
 // 8-row groups and 128 between 8-column groups.
@@ -577,7 +589,7 @@ template <int MODE>
 __device__ __forceinline__ void halo_load_weights(const ConvArgs& a, const HaloPlan& hp, int p, unsigned char* sb) {
     const int cin8 = a.cin >> 3;
     const int pieces = a.cout * 9 * cin8;  // 16-byte pieces of [cout][9][cin]
-    for (int i = p; i < pieces; i += kWsLoaders) {
+    for (int i = p; i < pieces; i += kHaloLoaders) {
         const int co = i / (9 * cin8);
         const int r = i - co * 9 * cin8;
         const int t = r / cin8, c8 = r - t * cin8;
@@ -597,12 +609,17 @@ __device__ __forceinline__ void halo_load_weights(const ConvArgs& a, const HaloP
 // Forward and input gradient over halo tiles: the roles, rings and bounded
 // waits of k_conv_ws, with the A stages holding halos and the weights
 // loaded once. Tiles (img, row of tiles, column) in row-major order, so CTAs
-// that run at the same time share halo rows in L2.
+// that run at the same time share halo rows in L2. A halo column comes as
+// one tensor copy (box of 8 channels × 10 × 18 pixels, zero outside the
+// image) from map0 (source 0, or dy) or map1 (source 1).
 template <int MODE>
-__global__ void __launch_bounds__(kWsThreads) k_conv_halo(ConvArgs a, HaloPlan hp) {
+__global__ void __launch_bounds__(kHaloThreads, 3)
+    k_conv_halo(ConvArgs a, HaloPlan hp, const __grid_constant__ CUtensorMap map0,
+                const __grid_constant__ CUtensorMap map1) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ uint64_t full[kHaloMaxStages], empty[kHaloMaxStages], acc_full[2], acc_empty[2];
     __shared__ uint32_t tslot;
+    __shared__ __align__(16) float sbias[256];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = MODE == FWD ? a.cout : a.cin;
@@ -618,7 +635,7 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_halo(ConvArgs a, HaloPlan h
 
     if (tid == 0) {
         for (int st = 0; st < S; ++st) {
-            tc::mbar_init(&full[st], kWsLoaders);
+            tc::mbar_init(&full[st], hp.gather ? kHaloLoaders + 1 : 1);
             tc::mbar_init(&empty[st], 1);
         }
         for (int b = 0; b < 2; ++b) {
@@ -627,12 +644,13 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_halo(ConvArgs a, HaloPlan h
         }
         tc::fence_barrier_init();
     }
-    if (warp >= kWsEpilogueWarps && warp < kWsMmaWarp) {
+    if (warp >= kWsEpilogueWarps && warp < kHaloMmaWarp) {
         halo_load_weights<MODE>(a, hp, tid - kWsEpilogueWarps * 32, sb);
         tc::cp_async_wait_all();
         tc::fence_proxy_async_smem();
     }
-    if (warp == kWsMmaWarp) {
+    if (MODE == FWD && tid < N) sbias[tid] = a.bias[tid];
+    if (warp == kHaloMmaWarp) {
         tc::tmem_alloc(&tslot, tcols);
         tc::tmem_relinquish();
     }
@@ -642,13 +660,36 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_halo(ConvArgs a, HaloPlan h
     const uint32_t tbase = tslot;
     bool ok = true;
 
-    if (warp >= kWsEpilogueWarps && warp < kWsMmaWarp) {
-        // ---- loaders: one halo chunk per stage
+    if (warp >= kWsEpilogueWarps && warp < kHaloMmaWarp) {
+        // ---- loaders: loader 0 copies the tensor-mapped columns of a stage
+        // (and arrives with their bytes); with an upsampled source every
+        // loader also arrives, after gathering its pixel of the other columns
         const int p = tid - kWsEpilogueWarps * 32;
-        for (int i = 0; i < my_tiles && ok; ++i) {
+        const bool issuer = p == 0, gather = hp.gather != 0;
+        const int hy = p / kHaloW, hx = p - hy * kHaloW;
+        const bool owner = gather && p < kHaloPx;
+        const int c0 = MODE == FWD ? a.src[0].channels : CK;
+        for (int i = 0; i < my_tiles && ok && (issuer || gather); ++i) {
             const int tile = int(blockIdx.x) + i * int(gridDim.x);
             const int img = tile / per_img, r = tile - img * per_img;
-            const int ty0 = (r / tiles_x) * kTileH - 1, tx0 = (r - (r / tiles_x) * tiles_x) * kTileW - 1;
+            const int y0 = (r / tiles_x) * kTileH - 1, x0 = (r - (r / tiles_x) * tiles_x) * kTileW - 1;
+            const int yy = y0 + hy, xx = x0 + hx;
+            const bool in = owner && yy >= 0 && xx >= 0 && yy < a.h && xx < a.w;
+            // this pixel's channel 0 in each source (upsampled sources at half resolution)
+            const bf16* base0 = a.wt;
+            const bf16* base1 = a.wt;
+            if (in) {
+                if (MODE == FWD) {
+                    const int sh0 = a.src[0].shift, sh1 = a.src[1].shift;
+                    base0 = a.src[0].ptr + ((size_t(img) * (a.h >> sh0) + (yy >> sh0)) * (a.w >> sh0) + (xx >> sh0)) *
+                                               size_t(a.src[0].stride);
+                    if (a.src[1].channels)
+                        base1 = a.src[1].ptr + ((size_t(img) * (a.h >> sh1) + (yy >> sh1)) * (a.w >> sh1) +
+                                                (xx >> sh1)) * size_t(a.src[1].stride);
+                } else {
+                    base0 = a.dy + ((size_t(img) * a.h + yy) * a.w + xx) * size_t(a.dy_stride);
+                }
+            }
             for (int c = 0; c < hp.nchunks; ++c) {
                 const int j = i * hp.nchunks + c, s = j % S;
                 if (!tc::mbar_wait(&empty[s], ((j / S) & 1) ^ 1)) {
@@ -657,31 +698,39 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_halo(ConvArgs a, HaloPlan h
                 }
                 unsigned char* st = sa0 + s * hp.a_bytes;
                 const int cols = min(hp.kc, CK - c * hp.kc) >> 3;
-                for (int idx = p; idx < cols * kHaloPx; idx += kWsLoaders) {
-                    const int g = idx / kHaloPx, q = idx - g * kHaloPx;
-                    const int hy = q / kHaloW, hx = q - hy * kHaloW;
-                    const int cb = c * hp.kc + 8 * g, yy = ty0 + hy, xx = tx0 + hx;
-                    const bf16* src = a.wt;
-                    bool in = false;
-                    if (MODE == FWD) {
-                        in = source_at(a, img, yy, xx, cb, src);
-                    } else if (yy >= 0 && xx >= 0 && yy < a.h && xx < a.w) {
-                        src = a.dy + ((size_t(img) * a.h + yy) * a.w + xx) * size_t(a.dy_stride) + cb;
-                        in = true;
+                if (issuer) {
+                    uint32_t bytes = 0;
+                    for (int g = 0; g < cols; ++g) bytes += (hp.tma >> (c * hp.kc + 8 * g < c0 ? 0 : 1)) & 1 ? kHaloBox : 0u;
+                    mbar_expect_tx(&full[s], bytes);
+                    for (int g = 0; g < cols; ++g) {
+                        const int cb = c * hp.kc + 8 * g, src = cb < c0 ? 0 : 1;
+                        if ((hp.tma >> src) & 1)
+                            tma_load_5d(st + g * kHaloCol, src ? &map1 : &map0, 0, (cb - src * c0) >> 3, x0, y0, img,
+                                        &full[s]);
                     }
-                    tc::cp_async16(st + g * kHaloCol + q * 16, in ? src : a.wt, in ? 16u : 0u);
                 }
-                tc::cp_async_arrive(&full[s]);
+                if (gather) {
+                    for (int g = 0; g < cols && owner; ++g) {
+                        const int cb = c * hp.kc + 8 * g, src = cb < c0 ? 0 : 1;
+                        if ((hp.tma >> src) & 1) continue;
+                        const bf16* from = src ? base1 + (cb - c0) : base0 + cb;
+                        tc::cp_async16(st + g * kHaloCol + p * 16, in ? from : a.wt, in ? 16u : 0u);
+                    }
+                    tc::cp_async_arrive(&full[s]);
+                }
             }
         }
         tc::cp_async_wait_all();
-    } else if (warp == kWsMmaWarp) {
-        // ---- MMA issue (one thread): 9 taps × kc/16 slices per stage
+    } else if (warp == kHaloMmaWarp) {
+        // ---- MMA issue (one thread): 9 taps × kc/16 slices per stage. The
+        // descriptors are built once; an MMA adds its operands' offsets in
+        // 16-byte units to their address fields.
         if (lane == 0) {
             uint32_t idesc = tc::idesc_bf16(kTileM, N);
             if (MODE == BWD_DATA) idesc |= 1u << 16;
-            const uint32_t sbase = tc::smem_u32(sb);
-            const uint32_t b_sbo = uint32_t(16 * hp.kc);
+            const uint64_t a0 = tc::smem_desc(tc::smem_u32(sa0), kHaloCol, kHaloRowStep);
+            const uint64_t b0 = tc::smem_desc(tc::smem_u32(sb), 128, uint32_t(16 * hp.kc));
+            const uint32_t a_stage16 = hp.a_bytes >> 4, b_block16 = hp.b_block >> 4;
             for (int i = 0; i < my_tiles && ok; ++i) {
                 const int b = i & 1;
                 if (!tc::mbar_wait(&acc_empty[b], ((i >> 1) & 1) ^ 1)) {
@@ -698,19 +747,19 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_halo(ConvArgs a, HaloPlan h
                     }
                     tc::fence_proxy_async_smem();
                     tc::tc_fence_after_sync();
-                    const uint32_t sa = tc::smem_u32(sa0 + s * hp.a_bytes);
+                    const uint64_t as = a0 + uint64_t(uint32_t(s) * a_stage16);
+                    const uint64_t bc = b0 + uint64_t(uint32_t(c * 9) * b_block16);
                     const int slices = min(hp.kc, CK - c * hp.kc) >> 4;
+#pragma unroll
                     for (int t = 0; t < 9; ++t) {
-                        const int ty = t / 3, tx = t - 3 * ty;
                         // forward reads x(p + tap − 1); the input gradient reads dy(p − tap + 1)
-                        const int pix = MODE == FWD ? ty * kHaloW + tx : (2 - ty) * kHaloW + (2 - tx);
-                        const uint32_t bt = sbase + uint32_t(c * 9 + t) * hp.b_block;
-                        for (int q = 0; q < slices; ++q) {
-                            const uint64_t ad = tc::smem_desc(sa + uint32_t(2 * q) * kHaloCol + uint32_t(pix) * 16,
-                                                              kHaloCol, kHaloRowStep);
-                            const uint64_t bd = tc::smem_desc(bt + uint32_t(q) * 256, 128, b_sbo);
-                            tc::mma_bf16(acc, ad, bd, idesc, (c > 0 || t > 0 || q > 0) ? 1u : 0u);
-                        }
+                        const int ty = t / 3, tx = t % 3;
+                        const uint32_t pix = MODE == FWD ? ty * kHaloW + tx : (2 - ty) * kHaloW + (2 - tx);
+                        const uint64_t at = as + pix;
+                        const uint64_t bt = bc + uint64_t(uint32_t(t) * b_block16);
+                        for (int q = 0; q < slices; ++q)
+                            tc::mma_bf16(acc, at + uint64_t(q * (2 * kHaloCol / 16)), bt + uint64_t(q * 16), idesc,
+                                         (c > 0 || t > 0 || q > 0) ? 1u : 0u);
                     }
                     tc::mma_commit(&empty[s]);
                 }
@@ -742,7 +791,7 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_halo(ConvArgs a, HaloPlan h
                     if (MODE == FWD) {
 #pragma unroll
                         for (int q = 0; q < 16; ++q) {
-                            float t = v[q] + a.bias[c + q];
+                            float t = v[q] + sbias[c + q];
                             if (a.act) t = t > 0.0f ? t : kLeak * t;
                             v[q] = t;
                         }
@@ -774,7 +823,7 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_halo(ConvArgs a, HaloPlan h
     if (!ok) atomicOr(a.status, NET_STATUS_TIMEOUT);
     tc::tc_fence_before_sync();
     __syncthreads();
-    if (warp == kWsMmaWarp) {
+    if (warp == kHaloMmaWarp) {
         tc::tc_fence_after_sync();
         tc::tmem_dealloc(tbase, tcols);
     }
@@ -785,45 +834,59 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_halo(ConvArgs a, HaloPlan h
 static int smem_for(int n) { return int(kStages * stage_bytes_for(n)); }
 
 // The halo kernel's stage size and weight blocks for N output columns and
-// CK K-side channels: the widest chunk (≤ 64 channels) whose weights and at
-// least two stages fit in `budget` bytes; false when none does.
-static bool plan_halo(int N, int CK, int budget, HaloPlan& hp) {
-    for (int kc = 64; kc >= 16; kc >>= 1) {
+// CK K-side channels: of the chunk widths (32 or 64 channels, 16 where CK is
+// 16) whose weights and at least two stages fit in one CTA's shared memory,
+// the one that lets the most CTAs reside on an SM (at most `limit`, the
+// other resources' bound), then the widest; `ctas` is that count. False
+// when no width fits.
+static bool plan_halo(int N, int CK, int static_bytes, int limit, HaloPlan& hp, int& ctas) {
+    const int per_sm = 233472, per_cta = 232448 - static_bytes;
+    bool found = false;
+    ctas = 0;
+    // chunks below 32 channels only where the K side has fewer: a stage's
+    // MMAs are then too few to cover its hand-over
+    const int kc_min = CK >= 32 ? 32 : 16;
+    for (int kc = 64; kc >= kc_min; kc >>= 1) {
         if (kc > CK && kc > 16) continue;
-        hp.kc = kc;
-        hp.nchunks = (CK + kc - 1) / kc;
-        hp.a_bytes = uint32_t(kc / 8) * kHaloCol;
-        hp.b_block = uint32_t(N) * uint32_t(kc) * 2u;
-        hp.b_bytes = uint32_t(hp.nchunks) * 9u * hp.b_block;
-        if (int(hp.b_bytes) >= budget) continue;
-        hp.stages = std::min(kHaloMaxStages, (budget - int(hp.b_bytes)) / int(hp.a_bytes));
-        if (hp.stages >= 2) return true;
+        HaloPlan q{};
+        q.kc = kc;
+        q.nchunks = (CK + kc - 1) / kc;
+        q.a_bytes = uint32_t(kc / 8) * kHaloCol;
+        q.b_block = uint32_t(N) * uint32_t(kc) * 2u;
+        q.b_bytes = uint32_t(q.nchunks) * 9u * q.b_block;
+        for (int t = limit; t > ctas; --t) {
+            const int room = std::min(per_cta, per_sm / t - static_bytes - 1024) - int(q.b_bytes);
+            const int stages = room > 0 ? std::min(kHaloMaxStages, room / int(q.a_bytes)) : 0;
+            if (stages >= 2) {
+                q.stages = stages;
+                hp = q;
+                ctas = t;
+                found = true;
+                break;
+            }
+        }
     }
-    return false;
+    return found;
 }
 
-// Dynamic shared memory and resident CTAs of the halo kernel (as
-// configure_ws); false when the weights do not fit.
+// Dynamic shared memory and resident CTAs of the halo kernel, counted from
+// its resources as configure_ws does; fits is false when the weights do not
+// fit in shared memory.
 template <int MODE>
 static cudaError_t configure_halo(int N, int CK, HaloPlan& hp, int& smem, int& ctas, bool& fits) {
     cudaFuncAttributes attr{};
     cudaError_t e = cudaFuncGetAttributes(&attr, k_conv_halo<MODE>);
     if (e != cudaSuccess) return e;
-    const int budget = 232448 - int(attr.sharedSizeBytes) - 1024;
-    fits = plan_halo(N, CK, budget, hp);
-    if (!fits) return cudaSuccess;
-    smem = int(hp.b_bytes + uint32_t(hp.stages) * hp.a_bytes);
-    const int by_threads = 2048 / kWsThreads;
-    const int regs_per_cta = ((attr.numRegs * 32 + 255) / 256 * 256) * (kWsThreads / 32);
+    const int by_threads = 2048 / kHaloThreads;
+    const int regs_per_cta = ((attr.numRegs * 32 + 255) / 256 * 256) * (kHaloThreads / 32);
     const int by_regs = 65536 / regs_per_cta;
     const int max_tmem = 512 / int(tmem_cols_for(2 * N));
-    for (;;) {
-        const int by_smem = 233472 / (smem + int(attr.sharedSizeBytes) + 1024);
-        ctas = std::min(std::min(by_threads, by_regs), by_smem);
-        if (ctas <= max_tmem) break;
-        smem += 4096;
-    }
-    if (ctas < 1) return cudaErrorInvalidConfiguration;
+    const int limit = std::min(std::min(by_threads, by_regs), max_tmem);
+    fits = limit >= 1 && plan_halo(N, CK, int(attr.sharedSizeBytes), limit, hp, ctas);
+    if (!fits) return cudaSuccess;
+    // a smaller request could let more CTAs reside than tensor memory allows: grow it
+    smem = int(hp.b_bytes + uint32_t(hp.stages) * hp.a_bytes);
+    while (233472 / (smem + int(attr.sharedSizeBytes) + 1024) > max_tmem) smem += 4096;
     return cudaFuncSetAttribute(k_conv_halo<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
@@ -914,8 +977,25 @@ bool conv_halo_fits(int mode, int cin, int cout) {
     return e == cudaSuccess && fits;
 }
 
+// A BF16 NHWC tensor as a rank-5 tensor map (8 channels, channel groups,
+// x, y, image) whose box is one halo column: 8 channels × 10 × 18 pixels.
+static bool encode_halo_map(CUtensorMap* m, const bf16* base, int channels, int stride, int w, int h, int n) {
+    auto enc = tensor_map_encoder();
+    if (!enc || channels % 8 || stride % 8) return false;
+    const cuuint64_t pix = cuuint64_t(stride) * 2;
+    const cuuint64_t dims[5] = {8, cuuint64_t(channels / 8), cuuint64_t(w), cuuint64_t(h), cuuint64_t(n)};
+    const cuuint64_t strides[4] = {16, pix, pix * cuuint64_t(w), pix * cuuint64_t(w) * cuuint64_t(h)};
+    const cuuint32_t box[5] = {8, 1, cuuint32_t(kHaloW), cuuint32_t(kHaloH), 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // Forward or input gradient: the halo kernel unless the caller asked for
 // pixel-row tiles or the weights do not fit (then CONV_HALO is an error).
+// Full-resolution sources (and dy) come by tensor copies; an upsampled
+// source, or one whose map cannot be made, is gathered per pixel.
 template <int MODE>
 static cudaError_t launch_fwd_or_data(const ConvArgs& a, int num_sms, cudaStream_t st) {
     const int N = MODE == FWD ? a.cout : a.cin, CK = MODE == FWD ? a.cin : a.cout;
@@ -926,8 +1006,22 @@ static cudaError_t launch_fwd_or_data(const ConvArgs& a, int num_sms, cudaStream
         bool fits = false;
         if ((e = configure_halo<MODE>(N, CK, hp, smem, ctas, fits)) != cudaSuccess) return e;
         if (fits) {
+            CUtensorMap m[2];
+            std::memset(m, 0, sizeof m);
+            if (MODE == FWD) {
+                for (int k = 0; k < 2; ++k) {
+                    const ConvSrc& src = a.src[k];
+                    if (src.channels > 0 && src.shift == 0 &&
+                        encode_halo_map(&m[k], src.ptr, src.channels, src.stride, a.w, a.h, a.n))
+                        hp.tma |= 1 << k;
+                }
+                hp.gather = !(hp.tma & 1) || (a.src[1].channels > 0 && !(hp.tma & 2));
+            } else {
+                if (encode_halo_map(&m[0], a.dy, a.cout, a.dy_stride, a.w, a.h, a.n)) hp.tma = 1;
+                hp.gather = !(hp.tma & 1);
+            }
             const int ntiles = a.n * ((a.w + kTileW - 1) / kTileW) * ((a.h + kTileH - 1) / kTileH);
-            k_conv_halo<MODE><<<std::min(ntiles, ctas * num_sms), kWsThreads, smem, st>>>(a, hp);
+            k_conv_halo<MODE><<<std::min(ntiles, ctas * num_sms), kHaloThreads, smem, st>>>(a, hp, m[0], m[1]);
             return cudaGetLastError();
         }
         if (a.kernel == CONV_HALO) return cudaErrorInvalidValue;
