@@ -561,24 +561,30 @@ constexpr int kHaloW = kTileW + 2, kHaloH = kTileH + 2, kHaloPx = kHaloW * kHalo
 constexpr uint32_t kHaloBox = kHaloPx * 16;     // one 8-channel column: 2880 B
 constexpr uint32_t kHaloCol = 23 * 128;         // its slot, 128-byte aligned for the tensor copy
 constexpr uint32_t kHaloRowStep = kHaloW * 16;  // between the tile's rows (core matrices along M)
+// An upsampled source's halo column comes from a 6 × 10 box of the
+// half-resolution tensor (960 B, in a 1 KB slot), widened in shared memory.
+constexpr int kUpW = 6, kUpH = 10;
+constexpr uint32_t kUpBox = kUpW * kUpH * 16, kUpCol = 1024;
 constexpr int kHaloMaxStages = 4;
 // Roles of k_conv_halo's 11 warps: 0-3 epilogue (as k_conv_ws), 4-9 load
 // (loader 0 issues the tensor copies; where a source is upsampled, loader
-// p < 180 gathers halo pixel p of its columns), 10 issues the MMAs.
+// p < 180 widens halo pixel p of its columns), 10 issues the MMAs.
 constexpr int kHaloLoadWarps = 6, kHaloLoaders = kHaloLoadWarps * 32;
 constexpr int kHaloMmaWarp = kWsEpilogueWarps + kHaloLoadWarps;
 constexpr int kHaloThreads = (kHaloMmaWarp + 1) * 32;
 static_assert(kHaloLoaders >= kHaloPx, "one loader thread per halo pixel");
 
 struct HaloPlan {
-    int tma;           // bit k: source k (dy: bit 0) comes by tensor copies of whole halo columns
-    int gather;        // some source is gathered per pixel (an upsampled one)
+    int up;            // bit k: source k is upsampled (its columns are widened from half resolution)
+    int stream;        // weights too large to stay: each stage brings its chunk's nine blocks
     int kc;            // K-side channels per stage (16, 32 or 64)
     int nchunks;       // ceil(K-side channels / kc)
     int stages;        // 2 … kHaloMaxStages
-    uint32_t a_bytes;  // one stage: kc/8 halo columns of kHaloCol bytes
+    uint32_t up_off;   // in a stage: the half-resolution boxes, after the kc/8 halo columns
+    uint32_t b_off;    // in a stage (streamed weights): the nine weight blocks, after the boxes
+    uint32_t a_bytes;  // one stage: kc/8 halo columns of kHaloCol bytes (+ boxes, + weight blocks)
     uint32_t b_block;  // weights of one (chunk, tap): N · kc · 2 bytes
-    uint32_t b_bytes;  // all weights: nchunks · 9 · b_block
+    uint32_t b_bytes;  // resident weights: nchunks · 9 · b_block (0 when streamed)
 };
 
 // The weights into shared memory (loader thread p of kHaloLoaders): FWD as
@@ -611,13 +617,16 @@ __device__ __forceinline__ void halo_load_weights(const ConvArgs& a, const HaloP
 // loaded once. Tiles (img, row of tiles, column) in row-major order, so CTAs
 // that run at the same time share halo rows in L2. A halo column comes as
 // one tensor copy (box of 8 channels × 10 × 18 pixels, zero outside the
-// image) from map0 (source 0, or dy) or map1 (source 1).
+// image) from map0 (source 0, or dy) or map1 (source 1); an upsampled
+// source's map is of its half-resolution tensor. Streamed weights come as
+// one copy per tap from mapw, whose box is a (chunk, tap) block already in
+// core-matrix order.
 template <int MODE>
 __global__ void __launch_bounds__(kHaloThreads, 3)
     k_conv_halo(ConvArgs a, HaloPlan hp, const __grid_constant__ CUtensorMap map0,
-                const __grid_constant__ CUtensorMap map1) {
+                const __grid_constant__ CUtensorMap map1, const __grid_constant__ CUtensorMap mapw) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ uint64_t full[kHaloMaxStages], empty[kHaloMaxStages], acc_full[2], acc_empty[2];
+    __shared__ uint64_t full[kHaloMaxStages], empty[kHaloMaxStages], upb[kHaloMaxStages], acc_full[2], acc_empty[2];
     __shared__ uint32_t tslot;
     __shared__ __align__(16) float sbias[256];
 
@@ -635,8 +644,9 @@ __global__ void __launch_bounds__(kHaloThreads, 3)
 
     if (tid == 0) {
         for (int st = 0; st < S; ++st) {
-            tc::mbar_init(&full[st], hp.gather ? kHaloLoaders + 1 : 1);
+            tc::mbar_init(&full[st], hp.up ? kHaloLoaders + 1 : 1);
             tc::mbar_init(&empty[st], 1);
+            tc::mbar_init(&upb[st], 1);
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&acc_full[b], 1);
@@ -644,7 +654,7 @@ __global__ void __launch_bounds__(kHaloThreads, 3)
         }
         tc::fence_barrier_init();
     }
-    if (warp >= kWsEpilogueWarps && warp < kHaloMmaWarp) {
+    if (!hp.stream && warp >= kWsEpilogueWarps && warp < kHaloMmaWarp) {
         halo_load_weights<MODE>(a, hp, tid - kWsEpilogueWarps * 32, sb);
         tc::cp_async_wait_all();
         tc::fence_proxy_async_smem();
@@ -661,35 +671,20 @@ __global__ void __launch_bounds__(kHaloThreads, 3)
     bool ok = true;
 
     if (warp >= kWsEpilogueWarps && warp < kHaloMmaWarp) {
-        // ---- loaders: loader 0 copies the tensor-mapped columns of a stage
-        // (and arrives with their bytes); with an upsampled source every
-        // loader also arrives, after gathering its pixel of the other columns
+        // ---- loaders: loader 0 issues a stage's tensor copies and arrives
+        // with their bytes; with an upsampled source every loader also
+        // arrives, after widening its pixel of that source's columns
         const int p = tid - kWsEpilogueWarps * 32;
-        const bool issuer = p == 0, gather = hp.gather != 0;
+        const bool issuer = p == 0, widen = hp.up != 0;
+        const bool owner = widen && p < kHaloPx;
         const int hy = p / kHaloW, hx = p - hy * kHaloW;
-        const bool owner = gather && p < kHaloPx;
+        // halo pixel (hy, hx) is pixel ((hy+1)/2, (hx+1)/2) of the half-resolution box
+        const uint32_t from = uint32_t(((hy + 1) >> 1) * kUpW + ((hx + 1) >> 1)) * 16u;
         const int c0 = MODE == FWD ? a.src[0].channels : CK;
-        for (int i = 0; i < my_tiles && ok && (issuer || gather); ++i) {
+        for (int i = 0; i < my_tiles && ok && (issuer || widen); ++i) {
             const int tile = int(blockIdx.x) + i * int(gridDim.x);
             const int img = tile / per_img, r = tile - img * per_img;
-            const int y0 = (r / tiles_x) * kTileH - 1, x0 = (r - (r / tiles_x) * tiles_x) * kTileW - 1;
-            const int yy = y0 + hy, xx = x0 + hx;
-            const bool in = owner && yy >= 0 && xx >= 0 && yy < a.h && xx < a.w;
-            // this pixel's channel 0 in each source (upsampled sources at half resolution)
-            const bf16* base0 = a.wt;
-            const bf16* base1 = a.wt;
-            if (in) {
-                if (MODE == FWD) {
-                    const int sh0 = a.src[0].shift, sh1 = a.src[1].shift;
-                    base0 = a.src[0].ptr + ((size_t(img) * (a.h >> sh0) + (yy >> sh0)) * (a.w >> sh0) + (xx >> sh0)) *
-                                               size_t(a.src[0].stride);
-                    if (a.src[1].channels)
-                        base1 = a.src[1].ptr + ((size_t(img) * (a.h >> sh1) + (yy >> sh1)) * (a.w >> sh1) +
-                                                (xx >> sh1)) * size_t(a.src[1].stride);
-                } else {
-                    base0 = a.dy + ((size_t(img) * a.h + yy) * a.w + xx) * size_t(a.dy_stride);
-                }
-            }
+            const int y0 = (r / tiles_x) * kTileH, x0 = (r - (r / tiles_x) * tiles_x) * kTileW;
             for (int c = 0; c < hp.nchunks; ++c) {
                 const int j = i * hp.nchunks + c, s = j % S;
                 if (!tc::mbar_wait(&empty[s], ((j / S) & 1) ^ 1)) {
@@ -699,28 +694,48 @@ __global__ void __launch_bounds__(kHaloThreads, 3)
                 unsigned char* st = sa0 + s * hp.a_bytes;
                 const int cols = min(hp.kc, CK - c * hp.kc) >> 3;
                 if (issuer) {
-                    uint32_t bytes = 0;
-                    for (int g = 0; g < cols; ++g) bytes += (hp.tma >> (c * hp.kc + 8 * g < c0 ? 0 : 1)) & 1 ? kHaloBox : 0u;
-                    mbar_expect_tx(&full[s], bytes);
+                    uint32_t direct = 0, up = 0;
                     for (int g = 0; g < cols; ++g) {
-                        const int cb = c * hp.kc + 8 * g, src = cb < c0 ? 0 : 1;
-                        if ((hp.tma >> src) & 1)
-                            tma_load_5d(st + g * kHaloCol, src ? &map1 : &map0, 0, (cb - src * c0) >> 3, x0, y0, img,
-                                        &full[s]);
+                        if ((hp.up >> (c * hp.kc + 8 * g < c0 ? 0 : 1)) & 1)
+                            up += kUpBox;
+                        else
+                            direct += kHaloBox;
+                    }
+                    if (widen) mbar_expect_tx(&upb[s], up);
+                    mbar_expect_tx(&full[s], direct + (hp.stream ? 9u * hp.b_block : 0u));
+                    if (hp.stream) {
+                        for (int t = 0; t < 9; ++t) {
+                            if (MODE == FWD)  // (ch, row in group, channel group, tap, row group)
+                                tma_load_5d(st + hp.b_off + t * hp.b_block, &mapw, 0, 0, c * (hp.kc >> 3), t, 0, &full[s]);
+                            else  // (ch, k = output channel, channel group, tap)
+                                tma_load_4d(st + hp.b_off + t * hp.b_block, &mapw, 0, c * hp.kc, 0, t, &full[s]);
+                        }
+                    }
+                    for (int g = 0; g < cols; ++g) {
+                        const int cb = c * hp.kc + 8 * g, src = cb < c0 ? 0 : 1, grp = (cb - src * c0) >> 3;
+                        const CUtensorMap* m = src ? &map1 : &map0;
+                        if ((hp.up >> src) & 1)
+                            tma_load_5d(st + hp.up_off + g * kUpCol, m, 0, grp, (x0 >> 1) - 1, (y0 >> 1) - 1, img,
+                                        &upb[s]);
+                        else
+                            tma_load_5d(st + g * kHaloCol, m, 0, grp, x0 - 1, y0 - 1, img, &full[s]);
                     }
                 }
-                if (gather) {
-                    for (int g = 0; g < cols && owner; ++g) {
-                        const int cb = c * hp.kc + 8 * g, src = cb < c0 ? 0 : 1;
-                        if ((hp.tma >> src) & 1) continue;
-                        const bf16* from = src ? base1 + (cb - c0) : base0 + cb;
-                        tc::cp_async16(st + g * kHaloCol + p * 16, in ? from : a.wt, in ? 16u : 0u);
+                if (widen) {
+                    if (!tc::mbar_wait(&upb[s], (j / S) & 1)) {
+                        ok = false;
+                        break;
                     }
-                    tc::cp_async_arrive(&full[s]);
+                    for (int g = 0; g < cols && owner; ++g) {
+                        if (!((hp.up >> (c * hp.kc + 8 * g < c0 ? 0 : 1)) & 1)) continue;
+                        const uint4 v = *reinterpret_cast<const uint4*>(st + hp.up_off + g * kUpCol + from);
+                        *reinterpret_cast<uint4*>(st + g * kHaloCol + p * 16) = v;
+                    }
+                    tc::fence_proxy_async_smem();
+                    tc::mbar_arrive(&full[s]);
                 }
             }
         }
-        tc::cp_async_wait_all();
     } else if (warp == kHaloMmaWarp) {
         // ---- MMA issue (one thread): 9 taps × kc/16 slices per stage. The
         // descriptors are built once; an MMA adds its operands' offsets in
@@ -729,7 +744,8 @@ __global__ void __launch_bounds__(kHaloThreads, 3)
             uint32_t idesc = tc::idesc_bf16(kTileM, N);
             if (MODE == BWD_DATA) idesc |= 1u << 16;
             const uint64_t a0 = tc::smem_desc(tc::smem_u32(sa0), kHaloCol, kHaloRowStep);
-            const uint64_t b0 = tc::smem_desc(tc::smem_u32(sb), 128, uint32_t(16 * hp.kc));
+            // resident weights: block (c, t) at sb; streamed: block t of the stage
+            const uint64_t b0 = tc::smem_desc(tc::smem_u32(hp.stream ? sa0 + hp.b_off : sb), 128, uint32_t(16 * hp.kc));
             const uint32_t a_stage16 = hp.a_bytes >> 4, b_block16 = hp.b_block >> 4;
             for (int i = 0; i < my_tiles && ok; ++i) {
                 const int b = i & 1;
@@ -748,7 +764,7 @@ __global__ void __launch_bounds__(kHaloThreads, 3)
                     tc::fence_proxy_async_smem();
                     tc::tc_fence_after_sync();
                     const uint64_t as = a0 + uint64_t(uint32_t(s) * a_stage16);
-                    const uint64_t bc = b0 + uint64_t(uint32_t(c * 9) * b_block16);
+                    const uint64_t bc = b0 + uint64_t(hp.stream ? uint32_t(s) * a_stage16 : uint32_t(c * 9) * b_block16);
                     const int slices = min(hp.kc, CK - c * hp.kc) >> 4;
 #pragma unroll
                     for (int t = 0; t < 9; ++t) {
@@ -837,32 +853,38 @@ static int smem_for(int n) { return int(kStages * stage_bytes_for(n)); }
 // CK K-side channels: of the chunk widths (32 or 64 channels, 16 where CK is
 // 16) whose weights and at least two stages fit in one CTA's shared memory,
 // the one that lets the most CTAs reside on an SM (at most `limit`, the
-// other resources' bound), then the widest; `ctas` is that count. False
-// when no width fits.
-static bool plan_halo(int N, int CK, int static_bytes, int limit, HaloPlan& hp, int& ctas) {
+// other resources' bound), then the widest; `ctas` is that count. When the
+// weights fit for no width, the stages bring their chunk's weights instead
+// (32 or 16 channels). False when even that does not fit.
+static bool plan_halo(int N, int CK, bool up, int static_bytes, int limit, HaloPlan& hp, int& ctas) {
     const int per_sm = 233472, per_cta = 232448 - static_bytes;
     bool found = false;
     ctas = 0;
     // chunks below 32 channels only where the K side has fewer: a stage's
     // MMAs are then too few to cover its hand-over
     const int kc_min = CK >= 32 ? 32 : 16;
-    for (int kc = 64; kc >= kc_min; kc >>= 1) {
-        if (kc > CK && kc > 16) continue;
-        HaloPlan q{};
-        q.kc = kc;
-        q.nchunks = (CK + kc - 1) / kc;
-        q.a_bytes = uint32_t(kc / 8) * kHaloCol;
-        q.b_block = uint32_t(N) * uint32_t(kc) * 2u;
-        q.b_bytes = uint32_t(q.nchunks) * 9u * q.b_block;
-        for (int t = limit; t > ctas; --t) {
-            const int room = std::min(per_cta, per_sm / t - static_bytes - 1024) - int(q.b_bytes);
-            const int stages = room > 0 ? std::min(kHaloMaxStages, room / int(q.a_bytes)) : 0;
-            if (stages >= 2) {
-                q.stages = stages;
-                hp = q;
-                ctas = t;
-                found = true;
-                break;
+    for (int stream = 0; stream < 2 && !found; ++stream) {
+        for (int kc = stream ? 32 : 64; kc >= (stream ? 16 : kc_min); kc >>= 1) {
+            if (kc > CK && kc > 16) continue;
+            HaloPlan q{};
+            q.stream = stream;
+            q.kc = kc;
+            q.nchunks = (CK + kc - 1) / kc;
+            q.up_off = uint32_t(kc / 8) * kHaloCol;
+            q.b_off = q.up_off + (up ? uint32_t(kc / 8) * kUpCol : 0u);
+            q.b_block = uint32_t(N) * uint32_t(kc) * 2u;
+            q.b_bytes = stream ? 0u : uint32_t(q.nchunks) * 9u * q.b_block;
+            q.a_bytes = q.b_off + (stream ? 9u * q.b_block : 0u);
+            for (int t = limit; t > ctas; --t) {
+                const int room = std::min(per_cta, per_sm / t - static_bytes - 1024) - int(q.b_bytes);
+                const int stages = room > 0 ? std::min(kHaloMaxStages, room / int(q.a_bytes)) : 0;
+                if (stages >= 2) {
+                    q.stages = stages;
+                    hp = q;
+                    ctas = t;
+                    found = true;
+                    break;
+                }
             }
         }
     }
@@ -873,7 +895,7 @@ static bool plan_halo(int N, int CK, int static_bytes, int limit, HaloPlan& hp, 
 // its resources as configure_ws does; fits is false when the weights do not
 // fit in shared memory.
 template <int MODE>
-static cudaError_t configure_halo(int N, int CK, HaloPlan& hp, int& smem, int& ctas, bool& fits) {
+static cudaError_t configure_halo(int N, int CK, bool up, HaloPlan& hp, int& smem, int& ctas, bool& fits) {
     cudaFuncAttributes attr{};
     cudaError_t e = cudaFuncGetAttributes(&attr, k_conv_halo<MODE>);
     if (e != cudaSuccess) return e;
@@ -882,7 +904,7 @@ static cudaError_t configure_halo(int N, int CK, HaloPlan& hp, int& smem, int& c
     const int by_regs = 65536 / regs_per_cta;
     const int max_tmem = 512 / int(tmem_cols_for(2 * N));
     const int limit = std::min(std::min(by_threads, by_regs), max_tmem);
-    fits = limit >= 1 && plan_halo(N, CK, int(attr.sharedSizeBytes), limit, hp, ctas);
+    fits = limit >= 1 && plan_halo(N, CK, up, int(attr.sharedSizeBytes), limit, hp, ctas);
     if (!fits) return cudaSuccess;
     // a smaller request could let more CTAs reside than tensor memory allows: grow it
     smem = int(hp.b_bytes + uint32_t(hp.stages) * hp.a_bytes);
@@ -967,35 +989,65 @@ const char* check_conv(const ConvArgs& a, int mode) {
     return nullptr;
 }
 
-bool conv_halo_fits(int mode, int cin, int cout) {
+bool conv_halo_fits(const ConvArgs& a, int mode) {
     if (mode != FWD && mode != BWD_DATA) return false;
     HaloPlan hp{};
     int smem = 0, ctas = 0;
     bool fits = false;
-    const cudaError_t e = mode == FWD ? configure_halo<FWD>(cout, cin, hp, smem, ctas, fits)
-                                      : configure_halo<BWD_DATA>(cin, cout, hp, smem, ctas, fits);
+    const bool up = mode == FWD && (a.src[0].shift || (a.src[1].channels && a.src[1].shift));
+    const cudaError_t e = mode == FWD ? configure_halo<FWD>(a.cout, a.cin, up, hp, smem, ctas, fits)
+                                      : configure_halo<BWD_DATA>(a.cin, a.cout, false, hp, smem, ctas, fits);
     return e == cudaSuccess && fits;
 }
 
 // A BF16 NHWC tensor as a rank-5 tensor map (8 channels, channel groups,
-// x, y, image) whose box is one halo column: 8 channels × 10 × 18 pixels.
-static bool encode_halo_map(CUtensorMap* m, const bf16* base, int channels, int stride, int w, int h, int n) {
+// x, y, image) whose box is 8 channels × bw × bh pixels: one halo column,
+// or the half-resolution box an upsampled column is widened from.
+static bool encode_halo_map(CUtensorMap* m, const bf16* base, int channels, int stride, int w, int h, int n, int bw,
+                            int bh) {
     auto enc = tensor_map_encoder();
     if (!enc || channels % 8 || stride % 8) return false;
     const cuuint64_t pix = cuuint64_t(stride) * 2;
     const cuuint64_t dims[5] = {8, cuuint64_t(channels / 8), cuuint64_t(w), cuuint64_t(h), cuuint64_t(n)};
     const cuuint64_t strides[4] = {16, pix, pix * cuuint64_t(w), pix * cuuint64_t(w) * cuuint64_t(h)};
-    const cuuint32_t box[5] = {8, 1, cuuint32_t(kHaloW), cuuint32_t(kHaloH), 1};
+    const cuuint32_t box[5] = {8, 1, cuuint32_t(bw), cuuint32_t(bh), 1};
     const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16*>(base), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The weights [cout][9][cin] as a tensor map whose box is one (chunk, tap)
+// block of the halo kernel in core-matrix order: forward (K-major, rows =
+// output channels) dims (8 channels, 8 rows, cin/8 groups, 9 taps, cout/8
+// row groups); input gradient (MN-major, k = output channel) dims (8
+// channels, cout, cin/8 groups, 9 taps).
+template <int MODE>
+static bool encode_weight_map(CUtensorMap* m, const bf16* wt, int cin, int cout, int kc) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t row = cuuint64_t(9) * cin * 2, tap = cuuint64_t(cin) * 2;
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    if (MODE == FWD) {
+        const cuuint64_t dims[5] = {8, 8, cuuint64_t(cin / 8), 9, cuuint64_t(cout / 8)};
+        const cuuint64_t strides[4] = {row, 16, tap, row * 8};
+        const cuuint32_t box[5] = {8, 8, cuuint32_t(kc / 8), 1, cuuint32_t(cout / 8)};
+        return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16*>(wt), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    }
+    const cuuint64_t dims[4] = {8, cuuint64_t(cout), cuuint64_t(cin / 8), 9};
+    const cuuint64_t strides[3] = {row, 16, tap};
+    const cuuint32_t box[4] = {8, cuuint32_t(kc), cuuint32_t(cin / 8), 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16*>(wt), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // Forward or input gradient: the halo kernel unless the caller asked for
 // pixel-row tiles or the weights do not fit (then CONV_HALO is an error).
-// Full-resolution sources (and dy) come by tensor copies; an upsampled
-// source, or one whose map cannot be made, is gathered per pixel.
+// Sources come by tensor copies (an upsampled one from its half-resolution
+// tensor); if a map cannot be made the pixel-row kernel runs instead.
 template <int MODE>
 static cudaError_t launch_fwd_or_data(const ConvArgs& a, int num_sms, cudaStream_t st) {
     const int N = MODE == FWD ? a.cout : a.cin, CK = MODE == FWD ? a.cin : a.cout;
@@ -1004,27 +1056,29 @@ static cudaError_t launch_fwd_or_data(const ConvArgs& a, int num_sms, cudaStream
     if (a.kernel != CONV_ROWS) {
         HaloPlan hp{};
         bool fits = false;
-        if ((e = configure_halo<MODE>(N, CK, hp, smem, ctas, fits)) != cudaSuccess) return e;
-        if (fits) {
-            CUtensorMap m[2];
-            std::memset(m, 0, sizeof m);
-            if (MODE == FWD) {
-                for (int k = 0; k < 2; ++k) {
-                    const ConvSrc& src = a.src[k];
-                    if (src.channels > 0 && src.shift == 0 &&
-                        encode_halo_map(&m[k], src.ptr, src.channels, src.stride, a.w, a.h, a.n))
-                        hp.tma |= 1 << k;
-                }
-                hp.gather = !(hp.tma & 1) || (a.src[1].channels > 0 && !(hp.tma & 2));
-            } else {
-                if (encode_halo_map(&m[0], a.dy, a.cout, a.dy_stride, a.w, a.h, a.n)) hp.tma = 1;
-                hp.gather = !(hp.tma & 1);
+        const bool up = MODE == FWD && (a.src[0].shift || (a.src[1].channels && a.src[1].shift));
+        if ((e = configure_halo<MODE>(N, CK, up, hp, smem, ctas, fits)) != cudaSuccess) return e;
+        CUtensorMap m[3];
+        std::memset(m, 0, sizeof m);
+        bool mapped = true;
+        if (fits && MODE == FWD) {
+            for (int k = 0; k < 2 && mapped; ++k) {
+                const ConvSrc& src = a.src[k];
+                if (src.channels == 0) continue;
+                mapped = encode_halo_map(&m[k], src.ptr, src.channels, src.stride, a.w >> src.shift,
+                                         a.h >> src.shift, a.n, src.shift ? kUpW : kHaloW, src.shift ? kUpH : kHaloH);
+                if (src.shift) hp.up |= 1 << k;
             }
+        } else if (fits) {
+            mapped = encode_halo_map(&m[0], a.dy, a.cout, a.dy_stride, a.w, a.h, a.n, kHaloW, kHaloH);
+        }
+        if (fits && mapped && hp.stream) mapped = encode_weight_map<MODE>(&m[2], a.wt, a.cin, a.cout, hp.kc);
+        if (fits && mapped) {
             const int ntiles = a.n * ((a.w + kTileW - 1) / kTileW) * ((a.h + kTileH - 1) / kTileH);
-            k_conv_halo<MODE><<<std::min(ntiles, ctas * num_sms), kHaloThreads, smem, st>>>(a, hp, m[0], m[1]);
+            k_conv_halo<MODE><<<std::min(ntiles, ctas * num_sms), kHaloThreads, smem, st>>>(a, hp, m[0], m[1], m[2]);
             return cudaGetLastError();
         }
-        if (a.kernel == CONV_HALO) return cudaErrorInvalidValue;
+        if (a.kernel == CONV_HALO) return fits ? cudaErrorNotSupported : cudaErrorInvalidValue;
     }
     if ((e = configure_ws<MODE>(N, smem, ctas)) != cudaSuccess) return e;
     const int ntiles = (a.n * a.h * a.w + kTileM - 1) / kTileM;

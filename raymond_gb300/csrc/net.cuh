@@ -104,7 +104,7 @@ struct ComposeArgs {
 
 const char* check_conv(const ConvArgs& a, int mode);
 cudaError_t launch_conv(ConvArgs a, int mode, int num_sms, cudaStream_t st);
-bool conv_halo_fits(int mode, int cin, int cout);  // the halo kernel's weights fit in shared memory
+bool conv_halo_fits(const ConvArgs& a, int mode);  // the halo kernel's weights fit in shared memory
 cudaError_t launch_features(const FeatureArgs& f, cudaStream_t st);
 cudaError_t launch_pool(const __nv_bfloat16* in, __nv_bfloat16* out, int n, int h, int w, int c, cudaStream_t st);
 cudaError_t launch_split_up(const __nv_bfloat16* dcat, int cat_stride, __nv_bfloat16* g_coarse,

@@ -649,7 +649,7 @@ static int conv_entry(const raymond_conv* c, void* stream, int mode) {
         rmd::set_handleless_error("conv: kernel must be 0 (choose), 1 (pixel rows) or 2 (halo tiles)");
         return RAYMOND_EINVAL;
     }
-    if (a.kernel == CONV_HALO && !conv_halo_fits(mode, a.cin, a.cout)) {
+    if (a.kernel == CONV_HALO && !conv_halo_fits(a, mode)) {
         rmd::set_handleless_error("conv: the weights do not fit in shared memory for halo tiles");
         return RAYMOND_EINVAL;
     }

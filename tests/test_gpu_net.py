@@ -60,6 +60,7 @@ CASES = [
     (1, 16, 24, 128, 1, 96, 96),
     (1, 18, 9, 32, 0, 48, 64),
     (3, 7, 5, 32, 0, 0, 96),
+    (2, 22, 26, 32, 1, 16, 32),
 ]
 # forward and input-gradient kernels: 0 the library's choice, 1 pixel-row tiles, 2 halo tiles
 KERNELS = [0, 1, 2]
