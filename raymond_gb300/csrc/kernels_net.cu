@@ -565,14 +565,17 @@ constexpr uint32_t kHaloRowStep = kHaloW * 16;  // between the tile's rows (core
 // half-resolution tensor (960 B, in a 1 KB slot), widened in shared memory.
 constexpr int kUpW = 6, kUpH = 10;
 constexpr uint32_t kUpBox = kUpW * kUpH * 16, kUpCol = 1024;
-constexpr int kHaloMaxStages = 4;
-// Roles of k_conv_halo's 11 warps: 0-3 epilogue (as k_conv_ws), 4-9 load
-// (loader 0 issues the tensor copies; where a source is upsampled, loader
-// p < 180 widens halo pixel p of its columns), 10 issues the MMAs.
-constexpr int kHaloLoadWarps = 6, kHaloLoaders = kHaloLoadWarps * 32;
+constexpr int kHaloMaxStages = 8;
+// Roles of k_conv_halo's 12 warps: 0-3 epilogue (as k_conv_ws); 4 issues
+// the tensor copies (lane 0), running ahead over free stages; 5-10 widen
+// (where a source is upsampled, thread p < 180 of them widens halo pixel p
+// of its columns once they land); 11 issues the MMAs. Warps 4-10 load the
+// resident weights first.
+constexpr int kHaloIssueWarp = kWsEpilogueWarps, kHaloWidenWarps = 6;
+constexpr int kHaloLoadWarps = 1 + kHaloWidenWarps, kHaloLoaders = kHaloLoadWarps * 32;
 constexpr int kHaloMmaWarp = kWsEpilogueWarps + kHaloLoadWarps;
 constexpr int kHaloThreads = (kHaloMmaWarp + 1) * 32;
-static_assert(kHaloLoaders >= kHaloPx, "one loader thread per halo pixel");
+static_assert(kHaloWidenWarps * 32 >= kHaloPx, "one widening thread per halo pixel");
 
 struct HaloPlan {
     int up;            // bit k: source k is upsampled (its columns are widened from half resolution)
@@ -644,7 +647,7 @@ __global__ void __launch_bounds__(kHaloThreads, 3)
 
     if (tid == 0) {
         for (int st = 0; st < S; ++st) {
-            tc::mbar_init(&full[st], hp.up ? kHaloLoaders + 1 : 1);
+            tc::mbar_init(&full[st], hp.up ? kHaloWidenWarps + 1 : 1);
             tc::mbar_init(&empty[st], 1);
             tc::mbar_init(&upb[st], 1);
         }
@@ -670,18 +673,12 @@ __global__ void __launch_bounds__(kHaloThreads, 3)
     const uint32_t tbase = tslot;
     bool ok = true;
 
-    if (warp >= kWsEpilogueWarps && warp < kHaloMmaWarp) {
-        // ---- loaders: loader 0 issues a stage's tensor copies and arrives
-        // with their bytes; with an upsampled source every loader also
-        // arrives, after widening its pixel of that source's columns
-        const int p = tid - kWsEpilogueWarps * 32;
-        const bool issuer = p == 0, widen = hp.up != 0;
-        const bool owner = widen && p < kHaloPx;
-        const int hy = p / kHaloW, hx = p - hy * kHaloW;
-        // halo pixel (hy, hx) is pixel ((hy+1)/2, (hx+1)/2) of the half-resolution box
-        const uint32_t from = uint32_t(((hy + 1) >> 1) * kUpW + ((hx + 1) >> 1)) * 16u;
-        const int c0 = MODE == FWD ? a.src[0].channels : CK;
-        for (int i = 0; i < my_tiles && ok && (issuer || widen); ++i) {
+    const int c0 = MODE == FWD ? a.src[0].channels : CK;
+    if (warp == kHaloIssueWarp) {
+        // ---- tensor copies (lane 0): a stage's halo columns and streamed
+        // weights arrive on full[s] with their bytes, half-resolution boxes
+        // on upb[s]; the next stage is issued as soon as it is free
+        for (int i = 0; i < my_tiles && ok && lane == 0; ++i) {
             const int tile = int(blockIdx.x) + i * int(gridDim.x);
             const int img = tile / per_img, r = tile - img * per_img;
             const int y0 = (r / tiles_x) * kTileH, x0 = (r - (r / tiles_x) * tiles_x) * kTileW;
@@ -693,47 +690,62 @@ __global__ void __launch_bounds__(kHaloThreads, 3)
                 }
                 unsigned char* st = sa0 + s * hp.a_bytes;
                 const int cols = min(hp.kc, CK - c * hp.kc) >> 3;
-                if (issuer) {
-                    uint32_t direct = 0, up = 0;
-                    for (int g = 0; g < cols; ++g) {
-                        if ((hp.up >> (c * hp.kc + 8 * g < c0 ? 0 : 1)) & 1)
-                            up += kUpBox;
-                        else
-                            direct += kHaloBox;
-                    }
-                    if (widen) mbar_expect_tx(&upb[s], up);
-                    mbar_expect_tx(&full[s], direct + (hp.stream ? 9u * hp.b_block : 0u));
-                    if (hp.stream) {
-                        for (int t = 0; t < 9; ++t) {
-                            if (MODE == FWD)  // (ch, row in group, channel group, tap, row group)
-                                tma_load_5d(st + hp.b_off + t * hp.b_block, &mapw, 0, 0, c * (hp.kc >> 3), t, 0, &full[s]);
-                            else  // (ch, k = output channel, channel group, tap)
-                                tma_load_4d(st + hp.b_off + t * hp.b_block, &mapw, 0, c * hp.kc, 0, t, &full[s]);
-                        }
-                    }
-                    for (int g = 0; g < cols; ++g) {
-                        const int cb = c * hp.kc + 8 * g, src = cb < c0 ? 0 : 1, grp = (cb - src * c0) >> 3;
-                        const CUtensorMap* m = src ? &map1 : &map0;
-                        if ((hp.up >> src) & 1)
-                            tma_load_5d(st + hp.up_off + g * kUpCol, m, 0, grp, (x0 >> 1) - 1, (y0 >> 1) - 1, img,
-                                        &upb[s]);
-                        else
-                            tma_load_5d(st + g * kHaloCol, m, 0, grp, x0 - 1, y0 - 1, img, &full[s]);
+                uint32_t direct = 0, up = 0;
+                for (int g = 0; g < cols; ++g) {
+                    if ((hp.up >> (c * hp.kc + 8 * g < c0 ? 0 : 1)) & 1)
+                        up += kUpBox;
+                    else
+                        direct += kHaloBox;
+                }
+                if (hp.up) mbar_expect_tx(&upb[s], up);
+                mbar_expect_tx(&full[s], direct + (hp.stream ? 9u * hp.b_block : 0u));
+                if (hp.stream) {
+                    for (int t = 0; t < 9; ++t) {
+                        if (MODE == FWD)  // (ch, row in group, channel group, tap, row group)
+                            tma_load_5d(st + hp.b_off + t * hp.b_block, &mapw, 0, 0, c * (hp.kc >> 3), t, 0, &full[s]);
+                        else  // (ch, k = output channel, channel group, tap)
+                            tma_load_4d(st + hp.b_off + t * hp.b_block, &mapw, 0, c * hp.kc, 0, t, &full[s]);
                     }
                 }
-                if (widen) {
-                    if (!tc::mbar_wait(&upb[s], (j / S) & 1)) {
-                        ok = false;
-                        break;
-                    }
-                    for (int g = 0; g < cols && owner; ++g) {
-                        if (!((hp.up >> (c * hp.kc + 8 * g < c0 ? 0 : 1)) & 1)) continue;
-                        const uint4 v = *reinterpret_cast<const uint4*>(st + hp.up_off + g * kUpCol + from);
-                        *reinterpret_cast<uint4*>(st + g * kHaloCol + p * 16) = v;
-                    }
-                    tc::fence_proxy_async_smem();
-                    tc::mbar_arrive(&full[s]);
+                for (int g = 0; g < cols; ++g) {
+                    const int cb = c * hp.kc + 8 * g, src = cb < c0 ? 0 : 1, grp = (cb - src * c0) >> 3;
+                    const CUtensorMap* m = src ? &map1 : &map0;
+                    if ((hp.up >> src) & 1)
+                        tma_load_5d(st + hp.up_off + g * kUpCol, m, 0, grp, (x0 >> 1) - 1, (y0 >> 1) - 1, img,
+                                    &upb[s]);
+                    else
+                        tma_load_5d(st + g * kHaloCol, m, 0, grp, x0 - 1, y0 - 1, img, &full[s]);
                 }
+            }
+        }
+        __syncwarp();
+    } else if (warp > kHaloIssueWarp && warp < kHaloMmaWarp) {
+        // ---- widening (upsampled sources only): once a stage's boxes land,
+        // halo pixel (hy, hx) copies pixel ((hy+1)/2, (hx+1)/2) of its box
+        // into the column, then each warp arrives once on full[s]
+        const int p = tid - (kHaloIssueWarp + 1) * 32;
+        const bool owner = p < kHaloPx;
+        const int hy = p / kHaloW, hx = p - hy * kHaloW;
+        const uint32_t from = uint32_t(((hy + 1) >> 1) * kUpW + ((hx + 1) >> 1)) * 16u;
+        for (int i = 0; i < my_tiles && ok && hp.up; ++i) {
+            for (int c = 0; c < hp.nchunks; ++c) {
+                const int j = i * hp.nchunks + c, s = j % S;
+                // upb[s] completes after the copies into this stage, so after its release
+                if (!__all_sync(0xFFFFFFFFu, tc::mbar_wait(&upb[s], (j / S) & 1))) {
+                    ok = false;
+                    break;
+                }
+                unsigned char* st = sa0 + s * hp.a_bytes;
+                const int cols = min(hp.kc, CK - c * hp.kc) >> 3;
+                for (int g = 0; g < cols && owner; ++g) {
+                    if (!((hp.up >> (c * hp.kc + 8 * g < c0 ? 0 : 1)) & 1)) continue;
+                    const uint4 v = *reinterpret_cast<const uint4*>(st + hp.up_off + g * kUpCol + from);
+                    *reinterpret_cast<uint4*>(st + g * kHaloCol + p * 16) = v;
+                }
+                // each writer's stores to the async proxy, then one arrival per warp
+                tc::fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&full[s]);
             }
         }
     } else if (warp == kHaloMmaWarp) {
@@ -850,15 +862,17 @@ __global__ void __launch_bounds__(kHaloThreads, 3)
 static int smem_for(int n) { return int(kStages * stage_bytes_for(n)); }
 
 // The halo kernel's stage size and weight blocks for N output columns and
-// CK K-side channels: of the chunk widths (32 or 64 channels, 16 where CK is
-// 16) whose weights and at least two stages fit in one CTA's shared memory,
-// the one that lets the most CTAs reside on an SM (at most `limit`, the
-// other resources' bound), then the widest; `ctas` is that count. When the
-// weights fit for no width, the stages bring their chunk's weights instead
-// (32 or 16 channels). False when even that does not fit.
+// CK K-side channels: of the chunk widths (32 or 64 channels, 16 where CK
+// is 16) whose weights and at least two stages fit in a CTA, and of the
+// resident-CTA counts up to `limit` (the other resources' bound), the one
+// with the most CTAs (each brings its own MMA issuer and epilogue), then
+// the widest chunk, with as many stages as fit. When the weights fit for no
+// width, the stages bring their chunk's weights instead (32 or 16
+// channels). False when even that does not fit.
 static bool plan_halo(int N, int CK, bool up, int static_bytes, int limit, HaloPlan& hp, int& ctas) {
     const int per_sm = 233472, per_cta = 232448 - static_bytes;
     bool found = false;
+    long best = 0;
     ctas = 0;
     // chunks below 32 channels only where the K side has fewer: a stage's
     // MMAs are then too few to cover its hand-over
@@ -875,15 +889,16 @@ static bool plan_halo(int N, int CK, bool up, int static_bytes, int limit, HaloP
             q.b_block = uint32_t(N) * uint32_t(kc) * 2u;
             q.b_bytes = stream ? 0u : uint32_t(q.nchunks) * 9u * q.b_block;
             q.a_bytes = q.b_off + (stream ? 9u * q.b_block : 0u);
-            for (int t = limit; t > ctas; --t) {
+            for (int t = limit; t >= 1; --t) {
                 const int room = std::min(per_cta, per_sm / t - static_bytes - 1024) - int(q.b_bytes);
                 const int stages = room > 0 ? std::min(kHaloMaxStages, room / int(q.a_bytes)) : 0;
-                if (stages >= 2) {
+                const long score = long(t) * 1000 + kc;
+                if (stages >= 2 && score > best) {
                     q.stages = stages;
                     hp = q;
                     ctas = t;
+                    best = score;
                     found = true;
-                    break;
                 }
             }
         }
