@@ -319,12 +319,14 @@ int raymond_net_set_params(raymond_net* net, const float* params, uint64_t count
 int raymond_net_get_params(raymond_net* net, float* params, uint64_t count);
 /* The training loss per pixel and channel is lg(f) + lg(p), f the display,
  * p the prediction, lg(v) = w_log · |log(1 + v/a) − log(1 + t/a)| + w_rel ·
- * (v − t)² / (v² + 0.01), t the target radiance, a the clamped albedo (the
- * relative term's denominator held constant; the prediction's exponent
- * clamped to ±8, its gradient passed through); averaged. Each element's
- * gradient is clipped to ±64 before averaging, and Adam skips non-finite
- * gradient elements. Default weights 1 and 0. */
-int raymond_net_set_loss(raymond_net* net, float w_log, float w_rel);
+ * (v − t)² / (v² + rel_eps), t the target radiance, a the clamped albedo
+ * (the relative term's denominator held constant; the prediction's
+ * exponent clamped to ±8, its gradient passed through); averaged. Each
+ * element's gradient is clipped to ±64 before averaging, and Adam skips
+ * non-finite gradient elements. Defaults: weights 1 and 0, rel_eps 0.01; a
+ * larger rel_eps moves the relative term towards the absolute squared
+ * error on all but the brightest pixels. */
+int raymond_net_set_loss(raymond_net* net, float w_log, float w_rel, float rel_eps);
 /* Loss and its gradient with respect to every parameter, without a step.
  * Training crops are multiples of 16 pixels on each side. */
 int raymond_net_gradients(raymond_net* net, const raymond_net_batch* batch, float* grads, uint64_t count, float* loss);

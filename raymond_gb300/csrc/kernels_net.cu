@@ -1161,10 +1161,10 @@ __device__ __forceinline__ Blend blend_at(const float* out, const float4& ac, co
 // d(loss)/d(value) of one channel's value v against target t:
 // w_log · |log(1 + v/a) − log(1 + t/a)| + w_rel · (v − t)² / (v̂² + ε),
 // v̂ = v held constant; adds the loss into *l.
-__device__ __forceinline__ float loss_grad(float v, float t, float a, float w_log, float w_rel, float* l) {
+__device__ __forceinline__ float loss_grad(float v, float t, float a, float w_log, float w_rel, float eps, float* l) {
     const float d = log1pf(v / a) - log1pf(fmaxf(t / a, 0.0f));
     const float e = v - t;
-    const float den = v * v + kRelEps;
+    const float den = v * v + eps;
     *l += w_log * fabsf(d) + w_rel * e * e / den;
     return w_log * (d > 0.0f ? 1.0f : d < 0.0f ? -1.0f : 0.0f) / (a + v) + w_rel * 2.0f * e / den;
 }
@@ -1300,8 +1300,8 @@ __global__ void k_loss(LossArgs L) {
             const float t[3] = {tg.x, tg.y, tg.z};
             float l = 0.0f, g_alpha = 0.0f, go[4];
             for (int c = 0; c < 3; ++c) {
-                const float gf = loss_grad(b.fin[c], t[c], b.a[c], L.w_log, L.w_rel, &l);
-                const float gp = loss_grad(b.pred[c], t[c], b.a[c], L.w_log, L.w_rel, &l);
+                const float gf = loss_grad(b.fin[c], t[c], b.a[c], L.w_log, L.w_rel, L.rel_eps, &l);
+                const float gp = loss_grad(b.pred[c], t[c], b.a[c], L.w_log, L.w_rel, L.rel_eps, &l);
                 g_alpha += gf * (b.pred[c] - b.m[c]);
                 go[c] = (gf * b.alpha + gp) * b.pred[c];
             }

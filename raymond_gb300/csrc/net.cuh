@@ -20,7 +20,7 @@ enum ConvKernel { CONV_AUTO = 0, CONV_ROWS = 1, CONV_HALO = 2 };
 constexpr float kLeak = 0.1f;  // leaky ReLU slope below zero
 constexpr float kMaxLog = 8.0f;    // clamp of the prediction's exponent (radiance ≤ e⁸ × albedo)
 constexpr float kMaxGrad = 64.0f;  // loss: clip of each element's gradient (before the 1/(3·pixels) scale)
-constexpr float kRelEps = 0.01f;   // loss: ε of the relative squared error
+constexpr float kRelEps = 0.01f;   // loss: default ε of the relative squared error
 constexpr float kBlendTau = 0.1f;         // blend guard: relative error below which the average takes over
 constexpr float kGuardMinSamples = 4.0f;  // blend guard: off below this many samples
 constexpr unsigned NET_STATUS_TIMEOUT = 1u;
@@ -78,6 +78,7 @@ struct LossArgs {
     float scale;   // 1 / (3 · pixels)
     float w_log;   // weight of |log radiance error| (over albedo)
     float w_rel;   // weight of the relative squared radiance error
+    float rel_eps; // ε of the relative squared error's denominator (v̂² + ε)
     __nv_bfloat16* grad;  // [n][h][w][16]
     float* loss;
 };

@@ -119,6 +119,7 @@ struct raymond_net {
     DevBuf params, params_bf16, grads, adam_m, adam_v, status, loss;
     uint32_t adam_t = 0;
     float w_log = 1.0f, w_rel = 0.0f;  // loss weights
+    float rel_eps = kRelEps;           // the relative term's ε
 
     DevBuf work;
     int wn = 0, wh = 0, ww = 0;
@@ -337,6 +338,7 @@ static cudaError_t run_loss(raymond_net* net, const raymond_net_batch* b, cudaSt
     L.scale = 1.0f / (3.0f * float(b->n) * float(b->width) * float(b->height));
     L.w_log = net->w_log;
     L.w_rel = net->w_rel;
+    L.rel_eps = net->rel_eps;
     L.grad = net->t(T_GOUT);
     L.loss = static_cast<float*>(net->loss.ptr);
     return launch_loss(L, st);
@@ -538,12 +540,15 @@ int raymond_net_train_step(raymond_net* net, const raymond_net_batch* batch, flo
     return loss ? finish(net, loss) : RAYMOND_OK;
 }
 
-int raymond_net_set_loss(raymond_net* net, float w_log, float w_rel) {
+int raymond_net_set_loss(raymond_net* net, float w_log, float w_rel, float rel_eps) {
     if (!net) return RAYMOND_EINVAL;
     if (!(w_log >= 0.0f) || !(w_rel >= 0.0f) || !(w_log + w_rel > 0.0f) || !std::isfinite(w_log + w_rel))
         return net->fail(RAYMOND_EINVAL, "Loss weights must be finite, non-negative and not both zero.");
+    if (!(rel_eps > 0.0f) || !std::isfinite(rel_eps))
+        return net->fail(RAYMOND_EINVAL, "The relative error's epsilon must be finite and positive.");
     net->w_log = w_log;
     net->w_rel = w_rel;
+    net->rel_eps = rel_eps;
     return RAYMOND_OK;
 }
 

@@ -86,9 +86,10 @@ class Denoiser:
         self.set_params(bits.view(np.float32))
 
     # ---- training
-    def set_loss(self, w_log: float = 1.0, w_rel: float = 0.0) -> None:
-        """Loss weights: w_log on |log radiance error|, w_rel on the relative squared error."""
-        self._check(_native.lib().raymond_net_set_loss(self.handle, float(w_log), float(w_rel)))
+    def set_loss(self, w_log: float = 1.0, w_rel: float = 0.0, rel_eps: float = 0.01) -> None:
+        """Loss weights: w_log on |log radiance error|, w_rel on the relative
+        squared error (v − t)² / (v̂² + rel_eps)."""
+        self._check(_native.lib().raymond_net_set_loss(self.handle, float(w_log), float(w_rel), float(rel_eps)))
 
     def gradients(self, batch):
         """(loss, gradients) of one batch, without a step."""

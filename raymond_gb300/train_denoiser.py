@@ -61,13 +61,13 @@ def render_view(scene, camera, size, target_spp, bounces=8):
     noisy.denoise = False
     noisy.caustics = False
     out = []
-    done = 0
     for spp in NOISY_SPP:
-        noisy.samplesPerFrame = spp - done
-        noisy.render()
-        done = spp
+        # frames of at most 64 samples (samplesPerFrame's range), up to spp in all
+        while noisy.samples < spp:
+            noisy.samplesPerFrame = min(64, spp - noisy.samples)
+            noisy.render()
         a, g, n = noisy.readGuides()
-        out.append((spp, a, g, n))
+        out.append((noisy.samples, a, g, n))
     noisy.dispose()
     return target, out
 
@@ -117,10 +117,11 @@ def evaluate(net, targets, inputs, spp=4):
 
 
 def parse_losses(text):
+    """Variants "w_log,w_rel[,rel_eps]" separated by ';'."""
     out = []
     for item in text.split(";"):
-        w_log, w_rel = (float(v) for v in item.split(","))
-        out.append((w_log, w_rel))
+        vals = [float(v) for v in item.split(",")]
+        out.append((vals[0], vals[1], vals[2] if len(vals) > 2 else 0.01))
     return out
 
 
@@ -179,6 +180,7 @@ def _train_loop(net, targets, inputs, steps, batch, crop, lr, rng, levels, log, 
 
 
 def main(argv=None):
+    global NOISY_SPP
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--views", type=int, default=160)
     ap.add_argument("--holdout", type=int, default=8)
@@ -188,11 +190,15 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--crop", type=int, default=128)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--loss", default="0.5,1", help="variants w_log,w_rel separated by ';'")
+    ap.add_argument("--loss", default="0.5,1", help="variants w_log,w_rel[,rel_eps] separated by ';'")
+    ap.add_argument("--eval-spp", default="1,4,16", help="held-out evaluation sample counts")
+    ap.add_argument("--noisy-spp", default=",".join(str(v) for v in NOISY_SPP),
+                    help="sample counts of the noisy inputs (increasing)")
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     ap.add_argument("--report", default=None)
     args = ap.parse_args(argv)
+    NOISY_SPP = tuple(int(v) for v in args.noisy_spp.split(","))
 
     def log(msg):
         print(msg, flush=True)
@@ -206,21 +212,25 @@ def main(argv=None):
     t_data = time.time() - t0
     variants = []
     best = None
-    for w_log, w_rel in parse_losses(args.loss):
+    eval_spp = [int(v) for v in args.eval_spp.split(",")]
+    for w_log, w_rel, rel_eps in parse_losses(args.loss):
         net = Denoiser(seed=args.seed)
-        net.set_loss(w_log, w_rel)
-        log(f"loss variant w_log={w_log} w_rel={w_rel}")
+        net.set_loss(w_log, w_rel, rel_eps)
+        log(f"loss variant w_log={w_log} w_rel={w_rel} rel_eps={rel_eps}")
         losses, t_train = train(net, targets, inputs, args.steps, args.batch, args.crop, args.lr, seed=args.seed,
                                 log=log)
-        result = {"w_log": w_log, "w_rel": w_rel, "seconds_train": t_train, "loss": losses}
-        for spp in (1, 4, 16):
+        result = {"w_log": w_log, "w_rel": w_rel, "rel_eps": rel_eps, "seconds_train": t_train, "loss": losses}
+        for spp in eval_spp:
             result[f"holdout_rmse_{spp}spp"], rows = evaluate(net, h_targets, h_inputs, spp)
             if spp == 4:
                 result["holdout_rows_4spp"] = rows
-        log(json.dumps({k: result[k] for k in ("w_log", "w_rel", "holdout_rmse_1spp", "holdout_rmse_4spp",
-                                               "holdout_rmse_16spp")}))
+        log(json.dumps({k: v for k, v in result.items() if k.startswith("holdout_rmse") or k in ("w_log", "w_rel",
+                                                                                                "rel_eps")}))
         variants.append(result)
-        score = result["holdout_rmse_4spp"]["learned"]
+        # chosen: the lowest mean ratio of learned to noisy error over the evaluated sample counts
+        score = float(np.mean([result[f"holdout_rmse_{spp}spp"]["learned"] / result[f"holdout_rmse_{spp}spp"]["noisy"]
+                               for spp in eval_spp]))
+        result["score"] = score
         if best is None or score < best[0]:
             if best is not None:
                 best[1].dispose()
@@ -233,7 +243,8 @@ def main(argv=None):
               "views": args.views, "holdout": args.holdout, "size": args.size, "target_spp": args.target_spp,
               "noisy_spp": list(NOISY_SPP), "steps": args.steps, "batch": args.batch, "crop": args.crop,
               "lr": args.lr, "seed": args.seed, "seconds_data": t_data, "variants": variants,
-              "chosen": {"w_log": best[2]["w_log"], "w_rel": best[2]["w_rel"]},
+              "eval_spp": eval_spp,
+              "chosen": {"w_log": best[2]["w_log"], "w_rel": best[2]["w_rel"], "rel_eps": best[2]["rel_eps"]},
               "weights": os.path.basename(args.out)}
     if args.report:
         with open(args.report, "w") as f:

@@ -174,11 +174,11 @@ def test_parameter_layout_matches_oracle(gpu):
     net.dispose()
 
 
-@pytest.mark.parametrize("w_log,w_rel", [(1.0, 0.0), (0.5, 2.0)])
-def test_network_gradients_match_oracle(gpu, w_log, w_rel):
+@pytest.mark.parametrize("w_log,w_rel,rel_eps", [(1.0, 0.0, 0.01), (0.5, 2.0, 0.01), (0.5, 1.0, 0.5)])
+def test_network_gradients_match_oracle(gpu, w_log, w_rel, rel_eps):
     rng = np.random.default_rng(21)
     net = Denoiser(seed=3)
-    net.set_loss(w_log, w_rel)
+    net.set_loss(w_log, w_rel, rel_eps)
     count, layout = oracle.net_layout()
     params = _random_params(count, layout, rng)
     # BF16-exact weights so both sides multiply the same numbers
@@ -191,7 +191,7 @@ def test_network_gradients_match_oracle(gpu, w_log, w_rel):
     batch = make_batch(dev["accum"], dev["albedo"], dev["normal"], dev["target"], samples_all=spp)
     loss, grads = net.gradients(batch)
     want_loss, want, _ = oracle.net_loss_grad(params.astype(np.float64), accum, albedo, normal, target, spp, bf16=True,
-                                              w_log=w_log, w_rel=w_rel)
+                                              w_log=w_log, w_rel=w_rel, rel_eps=rel_eps)
     assert abs(loss - want_loss) <= 2e-3 * want_loss
     cos_all = float(np.dot(grads, want) / (np.linalg.norm(grads) * np.linalg.norm(want)))
     assert cos_all > 0.999
