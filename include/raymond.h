@@ -327,6 +327,12 @@ int raymond_net_get_params(raymond_net* net, float* params, uint64_t count);
  * larger rel_eps moves the relative term towards the absolute squared
  * error on all but the brightest pixels. */
 int raymond_net_set_loss(raymond_net* net, float w_log, float w_rel, float rel_eps);
+/* The display blend's guard τ: α = sigmoid(gate) · v/(v + τ²), v the running
+ * average's relative variance of the mean luminance; smaller τ trusts the
+ * network longer as the average converges. Used by training and inference
+ * alike; default 0.1. */
+int raymond_net_set_blend(raymond_net* net, float tau);
+float raymond_net_get_blend(const raymond_net* net);
 /* Loss and its gradient with respect to every parameter, without a step.
  * Training crops are multiples of 16 pixels on each side. */
 int raymond_net_gradients(raymond_net* net, const raymond_net_batch* batch, float* grads, uint64_t count, float* loss);

@@ -121,6 +121,8 @@ SIGNATURES = {
     "raymond_net_train_step": (_I, [_P, ctypes.POINTER(NetBatch), ctypes.c_float, _P]),
     "raymond_net_sync": (_I, [_P]),
     "raymond_net_set_loss": (_I, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
+    "raymond_net_set_blend": (_I, [_P, ctypes.c_float]),
+    "raymond_net_get_blend": (ctypes.c_float, [_P]),
     "raymond_net_infer": (_I, [_P, ctypes.POINTER(NetBatch), _P, _P]),
     "raymond_net_get_stream": (_P, [_P]),
     "raymond_net_set_stream": (_I, [_P, _P]),

@@ -1129,15 +1129,15 @@ __device__ __forceinline__ float lum3(float r, float g, float b) { return r * 0.
 // prediction p = a·e^o (o = out[0..2] clamped to ±kMaxLog, so p > 0) blended
 // with the running average m: f = α·p + (1 − α)·m, α = sigmoid(out[3])·g.
 // The guard g = v/(v + τ²) (v the average's relative variance of the mean
-// luminance, from the Σ luminance² channel; τ = kBlendTau, about the
-// network's own relative error) goes to zero as the average converges, so
+// luminance, from the Σ luminance² channel; τ the network's setting,
+// about its own relative error) goes to zero as the average converges, so
 // the display converges with it whatever the network predicts; the network
 // learns α within that bound. Below kGuardMinSamples the per-pixel variance
 // says too little and g = 1.
 struct Blend {
     float a[3], m[3], pred[3], fin[3], alpha, gate, guard;
 };
-__device__ __forceinline__ Blend blend_at(const float* out, const float4& ac, const float4& al, float n) {
+__device__ __forceinline__ Blend blend_at(const float* out, const float4& ac, const float4& al, float n, float tau) {
     Blend b;
     b.a[0] = fmaxf(al.x / n, 0.01f);
     b.a[1] = fmaxf(al.y / n, 0.01f);
@@ -1148,7 +1148,7 @@ __device__ __forceinline__ Blend blend_at(const float* out, const float4& ac, co
     const float ml = lum3(b.m[0], b.m[1], b.m[2]);
     const float var_mean = fmaxf(ac.w / n - ml * ml, 0.0f) / n;
     const float v = var_mean / (ml * ml + 1e-4f);
-    b.guard = n < kGuardMinSamples ? 1.0f : v / (v + kBlendTau * kBlendTau);
+    b.guard = n < kGuardMinSamples ? 1.0f : v / (v + tau * tau);
     b.gate = 1.0f / (1.0f + expf(-fminf(fmaxf(out[3], -20.0f), 20.0f)));
     b.alpha = b.gate * b.guard;
     for (int c = 0; c < 3; ++c) {
@@ -1295,7 +1295,7 @@ __global__ void k_loss(LossArgs L) {
             const size_t i = (size_t(img) * L.src_h + y) * L.src_w + x;
             const float n = fmaxf(L.samples ? L.samples[img] : L.samples_all, 1.0f);
             const float* out = L.out + size_t(p) * 16;
-            const Blend b = blend_at(out, L.accum[i], L.albedo[i], n);
+            const Blend b = blend_at(out, L.accum[i], L.albedo[i], n, L.tau);
             const float4 tg = L.target[i];
             const float t[3] = {tg.x, tg.y, tg.z};
             float l = 0.0f, g_alpha = 0.0f, go[4];
@@ -1346,7 +1346,7 @@ __global__ void k_compose(ComposeArgs C) {
     const int img = p / hw, r = p - img * hw, y = r / C.w, x = r - y * C.w;
     const float n = fmaxf(C.samples ? C.samples[img] : C.samples_all, 1.0f);
     const float* o = C.out + ((size_t(img) * C.ph + y) * C.pw + x) * 16;
-    const Blend b = blend_at(o, C.accum[p], C.albedo[p], n);
+    const Blend b = blend_at(o, C.accum[p], C.albedo[p], n, C.tau);
     float c[3];
     for (int k = 0; k < 3; ++k) c[k] = isfinite(b.fin[k]) ? b.fin[k] : b.m[k];
     C.dst[p] = make_float4(c[0], c[1], c[2], 1.0f);

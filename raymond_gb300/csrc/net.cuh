@@ -21,7 +21,7 @@ constexpr float kLeak = 0.1f;  // leaky ReLU slope below zero
 constexpr float kMaxLog = 8.0f;    // clamp of the prediction's exponent (radiance ≤ e⁸ × albedo)
 constexpr float kMaxGrad = 64.0f;  // loss: clip of each element's gradient (before the 1/(3·pixels) scale)
 constexpr float kRelEps = 0.01f;   // loss: default ε of the relative squared error
-constexpr float kBlendTau = 0.1f;         // blend guard: relative error below which the average takes over
+constexpr float kBlendTau = 0.1f;         // blend guard's default τ: relative error below which the average takes over
 constexpr float kGuardMinSamples = 4.0f;  // blend guard: off below this many samples
 constexpr unsigned NET_STATUS_TIMEOUT = 1u;
 
@@ -79,6 +79,7 @@ struct LossArgs {
     float w_log;   // weight of |log radiance error| (over albedo)
     float w_rel;   // weight of the relative squared radiance error
     float rel_eps; // ε of the relative squared error's denominator (v̂² + ε)
+    float tau;     // blend guard
     __nv_bfloat16* grad;  // [n][h][w][16]
     float* loss;
 };
@@ -100,6 +101,7 @@ struct ComposeArgs {
     const float* samples;  // per image, device; null uses samples_all
     float samples_all;
     int n, w, h, pw, ph;
+    float tau;    // blend guard
     float4* dst;  // [n][h][w]
 };
 

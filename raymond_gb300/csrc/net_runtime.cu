@@ -120,6 +120,7 @@ struct raymond_net {
     uint32_t adam_t = 0;
     float w_log = 1.0f, w_rel = 0.0f;  // loss weights
     float rel_eps = kRelEps;           // the relative term's ε
+    float tau = kBlendTau;             // the display blend's guard
 
     DevBuf work;
     int wn = 0, wh = 0, ww = 0;
@@ -339,6 +340,7 @@ static cudaError_t run_loss(raymond_net* net, const raymond_net_batch* b, cudaSt
     L.w_log = net->w_log;
     L.w_rel = net->w_rel;
     L.rel_eps = net->rel_eps;
+    L.tau = net->tau;
     L.grad = net->t(T_GOUT);
     L.loss = static_cast<float*>(net->loss.ptr);
     return launch_loss(L, st);
@@ -552,6 +554,15 @@ int raymond_net_set_loss(raymond_net* net, float w_log, float w_rel, float rel_e
     return RAYMOND_OK;
 }
 
+int raymond_net_set_blend(raymond_net* net, float tau) {
+    if (!net) return RAYMOND_EINVAL;
+    if (!(tau > 0.0f) || !std::isfinite(tau)) return net->fail(RAYMOND_EINVAL, "The blend guard must be finite and positive.");
+    net->tau = tau;
+    return RAYMOND_OK;
+}
+
+float raymond_net_get_blend(const raymond_net* net) { return net ? net->tau : 0.0f; }
+
 int raymond_net_sync(raymond_net* net) {
     if (!net) return RAYMOND_EINVAL;
     cudaSetDevice(net->device);
@@ -588,6 +599,7 @@ int raymond_net_infer(raymond_net* net, const raymond_net_batch* batch, float* o
         C.h = h;
         C.pw = pw;
         C.ph = ph;
+        C.tau = net->tau;
         C.dst = reinterpret_cast<float4*>(out_rgba);
         e = launch_compose(C, st);
     }

@@ -73,17 +73,29 @@ class Denoiser:
         self._check(_native.lib().raymond_net_set_params(self.handle, _native.ptr(p), p.size))
 
     def save(self, path: str) -> None:
-        """Weights as BF16 bit patterns (what the kernels multiply with)."""
+        """Weights as BF16 bit patterns (what the kernels multiply with) and the blend guard."""
         p = self.get_params()
         bits = (p.view(np.uint32) + np.uint32(0x7FFF) + ((p.view(np.uint32) >> 16) & 1)) >> 16
-        np.savez_compressed(path, bf16=bits.astype(np.uint16), count=np.int64(self.param_count))
+        np.savez_compressed(path, bf16=bits.astype(np.uint16), count=np.int64(self.param_count),
+                            tau=np.float32(self.blend))
 
     def load(self, path: str) -> None:
         with np.load(path) as z:
             bits = z["bf16"].astype(np.uint32) << 16
             if int(z["count"]) != self.param_count:
                 raise ValueError(f"{path}: {int(z['count'])} parameters, the network has {self.param_count}")
+            tau = float(z["tau"]) if "tau" in z.files else 0.1
         self.set_params(bits.view(np.float32))
+        self.blend = tau
+
+    @property
+    def blend(self) -> float:
+        """The display blend's guard τ (α = sigmoid(gate) · v/(v + τ²))."""
+        return float(_native.lib().raymond_net_get_blend(self.handle))
+
+    @blend.setter
+    def blend(self, tau: float) -> None:
+        self._check(_native.lib().raymond_net_set_blend(self.handle, float(tau)))
 
     # ---- training
     def set_loss(self, w_log: float = 1.0, w_rel: float = 0.0, rel_eps: float = 0.01) -> None:
