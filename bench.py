@@ -17,6 +17,8 @@ Other workloads (--workload):
   denoise  the learned denoiser's 1080p inference as its own line
   primary  closest hits of the Cornell room's 256² jittered primary rays, one
            traversal launch per step (--size sets the image side)
+  bvh      the scene producer: BVH.build over the sphere field's primitive
+           boxes on the host cores (no GPU), against the oracle's build
   rmse     time to RMSE ≤ 0.01 against a 16,384-spp render: the plain
            one-kernel path with à-trous vs the batched wavefront path with
            the learned denoiser
@@ -454,6 +456,68 @@ def run_primary_reference(args, rank, world):
     }
 
 
+def run_bvh(args):
+    """The scene producer beside the path: BVH.build's binned SAH over the
+    sphere field's 509,281 primitive boxes, natively on all host cores and on
+    one, against the oracle's single-threaded restatement of the same build
+    (src/BVH.mjs:57-234), whose nodes and leaf order must come out identical."""
+    import numpy as np
+
+    import oracle
+    from raymond_gb300 import scene as scene_mod
+    from raymond_gb300 import scenes
+
+    captured = {}
+    native_build = scene_mod.BVH.build
+
+    def capture(mins, maxs, *a, **k):
+        captured["mins"], captured["maxs"] = np.array(mins, dtype=np.float64), np.array(maxs, dtype=np.float64)
+        return native_build(mins, maxs, *a, **k)
+
+    scene_mod.BVH.build = staticmethod(capture)
+    try:
+        scene, _, info = scenes.sphere_field()
+        scene.pack()
+    finally:
+        scene_mod.BVH.build = staticmethod(native_build)
+    mins, maxs = captured["mins"], captured["maxs"]
+    count = len(mins)
+    threads = os.cpu_count() or 1
+
+    def timed(fn, reps):
+        best = math.inf
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            out = fn()
+            best = min(best, time.perf_counter() - t0)
+        return best, out
+
+    for _ in range(max(args.warmup, 1)):
+        scene_mod.BVH.build(mins, maxs, threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        b = scene_mod.BVH.build(mins, maxs, threads=threads)
+        times.append(time.perf_counter() - t0)
+    one_s, _ = timed(lambda: scene_mod.BVH.build(mins, maxs, threads=1), 2)
+    ref_s, (nodes, order) = timed(lambda: oracle.bvh_build(mins, maxs), 1)
+    same = bool(np.array_equal(nodes, b.nodes) and np.array_equal(order, b.order))
+    value = count / statistics.median(times) / 1e6
+    return {
+        "metric": "Mprims/s (BVH build)", "value": value, "unit": "Mprims/s", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(times), "higher_is_better": True,
+        "scaling": "strong", "vs_baseline": None, "dtype": "f64 build, f32 nodes",
+        "data": "synthetic (seeded mulberry32 scene)",
+        "config": {"workload": f"binned-SAH BVH of the sphere field's {count} primitive boxes, leaves of at most 4",
+                   "threads": threads, "nodes": int(b.nodeCount), "identical_to_oracle": same},
+        "single_thread": {"value": count / one_s / 1e6, "unit": "Mprims/s", "ms": 1e3 * one_s},
+        "e2e": {"value": value, "unit": "Mprims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+        "cpu_baseline": {"value": count / ref_s / 1e6, "unit": "Mprims/s", "cores": 1, "kind": "port",
+                         "sample": f"oracle BVH.build restatement over all {count} boxes, once"},
+    }
+
+
 def run_rmse(args, local):
     """Time to RMSE ≤ 0.01 against a 16,384-spp render of the sphere field:
     the plain one-kernel path with the à-trous filter against the batched
@@ -840,7 +904,7 @@ def main():
     ap.add_argument("--bounces", type=int, default=8)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--path", default="auto", choices=["auto", "megakernel", "wavefront"])
-    ap.add_argument("--workload", default="field", choices=["field", "caustics", "batch", "denoise", "rmse", "primary"])
+    ap.add_argument("--workload", default="field", choices=["field", "caustics", "batch", "denoise", "rmse", "primary", "bvh"])
     ap.add_argument("--threshold", type=float, default=0.01)
     ap.add_argument("--reference-spp", type=int, default=16384)
     ap.add_argument("--max-spp", type=int, default=4096)
@@ -867,6 +931,8 @@ def main():
         out = run_rmse(args, local) if rank == 0 else None
     elif args.workload == "primary":
         out = run_primary(args, local) if rank == 0 else None
+    elif args.workload == "bvh":
+        out = run_bvh(args) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, local)
     if rank == 0 and out is not None:

@@ -2,12 +2,17 @@
 // primitive order (src/BVH.mjs:57-234), so packed scenes built here and by
 // the JavaScript library are interchangeable byte for byte.
 //
-// Same decisions as the reference, organized for speed: centroids and boxes
-// in structure-of-arrays form, one pass over a node's primitives bins all
-// three axes at once, and independent subtrees are built on worker threads
-// into private node lists that are spliced into the reference's node
-// numbering afterwards (its numbering is a right-first depth-first order,
-// so a subtree's nodes form one contiguous run once its size is known).
+// Same decisions as the reference, organized for speed: each primitive's
+// centroid and box travel as one record that the partition moves together
+// with its index, so every pass over a node reads memory in order; one pass
+// bins all three axes at once; the passes over the few largest nodes (the
+// top of the tree) are split over the threads, whose bins and bounds merge
+// exactly (counts, minima, maxima); and independent subtrees are built on
+// worker threads into private node lists that are spliced into the
+// reference's node numbering afterwards (its numbering is a right-first
+// depth-first order, so a subtree's nodes form one contiguous run once its
+// size is known). The partition itself stays the reference's sequential
+// two-pointer swap, which decides the primitive order.
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -30,13 +35,37 @@ struct BuildNode {
     uint32_t first, count;  // count 0: inner, first = left child (local index while building a subtree)
 };
 
+struct Rec {
+    double c[3], lo[3], hi[3];  // centroid and box of the primitive order[i]
+};
+
 struct Input {
-    const double* mins;
-    const double* maxs;
-    std::vector<double> cx, cy, cz;  // centroids
+    std::vector<Rec> rec;  // in the current order
     uint32_t max_leaf;
     uint32_t* order;
+    int threads;
 };
+
+// Nodes of at least this many primitives split their passes over the threads.
+constexpr uint32_t kParallelMin = 1u << 16;
+
+// f(lo, hi, t) over [first, first + n) in `parts` contiguous pieces, one per
+// thread (piece t on thread t; the caller runs piece 0).
+template <typename F>
+void parallel_pieces(uint32_t first, uint32_t n, int parts, F&& f) {
+    std::vector<std::thread> pool;
+    const uint32_t step = (n + uint32_t(parts) - 1) / uint32_t(parts);
+    for (int t = 1; t < parts; ++t) {
+        const uint32_t lo = first + std::min(n, step * uint32_t(t)), hi = first + std::min(n, step * uint32_t(t + 1));
+        pool.emplace_back([&f, lo, hi, t] { f(lo, hi, t); });
+    }
+    f(first, first + std::min(n, step), 0);
+    for (auto& th : pool) th.join();
+}
+
+inline int parts_for(const Input& in, uint32_t n, bool par) {
+    return par && in.threads > 1 && n >= kParallelMin ? in.threads : 1;
+}
 
 inline double area3(const double* mn, const double* mx) {
     const double dx = mx[0] - mn[0];
@@ -46,17 +75,29 @@ inline double area3(const double* mn, const double* mx) {
     return dx * dy + dy * dz + dz * dx;
 }
 
-void bounds_of(const Input& in, uint32_t first, uint32_t n, BuildNode& node) {
+void bounds_of(const Input& in, uint32_t first, uint32_t n, BuildNode& node, bool par = false) {
+    const int parts = parts_for(in, n, par);
+    double one_mn[3] = {kInf, kInf, kInf}, one_mx[3] = {-kInf, -kInf, -kInf};
+    std::vector<double> many_mn(parts > 1 ? size_t(parts) * 3 : 0u, kInf), many_mx(parts > 1 ? size_t(parts) * 3 : 0u, -kInf);
+    double* mn = parts > 1 ? many_mn.data() : one_mn;
+    double* mx = parts > 1 ? many_mx.data() : one_mx;
+    parallel_pieces(first, n, parts, [&](uint32_t lo_i, uint32_t hi_i, int t) {
+        double* a_mn = &mn[size_t(t) * 3];
+        double* a_mx = &mx[size_t(t) * 3];
+        for (uint32_t i = lo_i; i < hi_i; ++i) {
+            const Rec& r = in.rec[i];
+            for (int a = 0; a < 3; ++a) {
+                if (r.lo[a] < a_mn[a]) a_mn[a] = r.lo[a];
+                if (r.hi[a] > a_mx[a]) a_mx[a] = r.hi[a];
+            }
+        }
+    });
     for (int a = 0; a < 3; ++a) {
         node.min[a] = kInf;
         node.max[a] = -kInf;
-    }
-    for (uint32_t i = first; i < first + n; ++i) {
-        const size_t p = size_t(in.order[i]) * 3;
-        for (int a = 0; a < 3; ++a) {
-            const double lo = in.mins[p + a], hi = in.maxs[p + a];
-            if (lo < node.min[a]) node.min[a] = lo;
-            if (hi > node.max[a]) node.max[a] = hi;
+        for (int t = 0; t < parts; ++t) {
+            if (mn[size_t(t) * 3 + a] < node.min[a]) node.min[a] = mn[size_t(t) * 3 + a];
+            if (mx[size_t(t) * 3 + a] > node.max[a]) node.max[a] = mx[size_t(t) * 3 + a];
         }
     }
     node.first = first;
@@ -65,18 +106,37 @@ void bounds_of(const Input& in, uint32_t first, uint32_t n, BuildNode& node) {
 
 // The split decision for one node: returns false for "keep as a leaf", else
 // the partition point in the order array.
-bool split_node(const Input& in, const BuildNode& node, uint32_t& mid_out) {
+bool split_node(Input& in, const BuildNode& node, uint32_t& mid_out, bool par = false) {
     const uint32_t first = node.first, n = node.count;
-    const double* cs[3] = {in.cx.data(), in.cy.data(), in.cz.data()};
-    double cmin[3] = {kInf, kInf, kInf}, cmax[3] = {-kInf, -kInf, -kInf};
-    for (uint32_t i = first; i < first + n; ++i) {
-        const uint32_t p = in.order[i];
+    const int parts = parts_for(in, n, par);
+    struct Bins {
+        double cmin[3], cmax[3];
+        double bmin[3][BINS][3], bmax[3][BINS][3];
+        uint32_t bcount[3][BINS];
+    };
+    Bins one;  // the common case needs no allocation
+    std::vector<Bins> many(parts > 1 ? static_cast<size_t>(parts) : 0u);
+    Bins* pb = parts > 1 ? many.data() : &one;
+    // centroid bounds, per piece then merged
+    parallel_pieces(first, n, parts, [&](uint32_t lo_i, uint32_t hi_i, int t) {
+        Bins& B = pb[size_t(t)];
         for (int a = 0; a < 3; ++a) {
-            const double c = cs[a][p];
-            if (c < cmin[a]) cmin[a] = c;
-            if (c > cmax[a]) cmax[a] = c;
+            B.cmin[a] = kInf;
+            B.cmax[a] = -kInf;
         }
-    }
+        for (uint32_t i = lo_i; i < hi_i; ++i)
+            for (int a = 0; a < 3; ++a) {
+                const double c = in.rec[i].c[a];
+                if (c < B.cmin[a]) B.cmin[a] = c;
+                if (c > B.cmax[a]) B.cmax[a] = c;
+            }
+    });
+    double cmin[3] = {kInf, kInf, kInf}, cmax[3] = {-kInf, -kInf, -kInf};
+    for (int t = 0; t < parts; ++t)
+        for (int a = 0; a < 3; ++a) {
+            if (pb[size_t(t)].cmin[a] < cmin[a]) cmin[a] = pb[size_t(t)].cmin[a];
+            if (pb[size_t(t)].cmax[a] > cmax[a]) cmax[a] = pb[size_t(t)].cmax[a];
+        }
     double scale[3];
     bool live[3];
     for (int a = 0; a < 3; ++a) {
@@ -85,32 +145,47 @@ bool split_node(const Input& in, const BuildNode& node, uint32_t& mid_out) {
         scale[a] = live[a] ? double(BINS) / extent : 0.0;
     }
 
-    double bmin[3][BINS][3], bmax[3][BINS][3];
-    uint32_t bcount[3][BINS];
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < BINS; ++b) {
-            bcount[a][b] = 0;
-            for (int k = 0; k < 3; ++k) {
-                bmin[a][b][k] = kInf;
-                bmax[a][b][k] = -kInf;
+    // One pass bins every live axis, per piece.
+    parallel_pieces(first, n, parts, [&](uint32_t lo_i, uint32_t hi_i, int t) {
+        Bins& B = pb[size_t(t)];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < BINS; ++b) {
+                B.bcount[a][b] = 0;
+                for (int k = 0; k < 3; ++k) {
+                    B.bmin[a][b][k] = kInf;
+                    B.bmax[a][b][k] = -kInf;
+                }
+            }
+        for (uint32_t i = lo_i; i < hi_i; ++i) {
+            const Rec& r = in.rec[i];
+            for (int a = 0; a < 3; ++a) {
+                if (!live[a]) continue;
+                // x ≥ 0 (c ≥ cmin), so truncation is the reference's Math.floor
+                const double x = (r.c[a] - cmin[a]) * scale[a];
+                const int b = x < double(BINS - 1) ? int(x) : BINS - 1;
+                B.bcount[a][b]++;
+                for (int k = 0; k < 3; ++k) {
+                    if (r.lo[k] < B.bmin[a][b][k]) B.bmin[a][b][k] = r.lo[k];
+                    if (r.hi[k] > B.bmax[a][b][k]) B.bmax[a][b][k] = r.hi[k];
+                }
             }
         }
-    // One pass bins every live axis.
-    for (uint32_t i = first; i < first + n; ++i) {
-        const uint32_t p = in.order[i];
-        const double* lo = in.mins + size_t(p) * 3;
-        const double* hi = in.maxs + size_t(p) * 3;
-        for (int a = 0; a < 3; ++a) {
-            if (!live[a]) continue;
-            const double f = std::floor((cs[a][p] - cmin[a]) * scale[a]);
-            const int b = f < double(BINS - 1) ? int(f) : BINS - 1;
-            bcount[a][b]++;
-            for (int k = 0; k < 3; ++k) {
-                if (lo[k] < bmin[a][b][k]) bmin[a][b][k] = lo[k];
-                if (hi[k] > bmax[a][b][k]) bmax[a][b][k] = hi[k];
+    });
+    Bins& M = pb[0];  // merged into piece 0's bins
+    for (int t = 1; t < parts; ++t) {
+        const Bins& B = pb[size_t(t)];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < BINS; ++b) {
+                M.bcount[a][b] += B.bcount[a][b];
+                for (int k = 0; k < 3; ++k) {
+                    if (B.bmin[a][b][k] < M.bmin[a][b][k]) M.bmin[a][b][k] = B.bmin[a][b][k];
+                    if (B.bmax[a][b][k] > M.bmax[a][b][k]) M.bmax[a][b][k] = B.bmax[a][b][k];
+                }
             }
-        }
     }
+    auto& bmin = M.bmin;
+    auto& bmax = M.bmax;
+    auto& bcount = M.bcount;
 
     double best_cost = kInf, best_split = 0.0;
     int best_axis = -1;
@@ -159,13 +234,13 @@ bool split_node(const Input& in, const BuildNode& node, uint32_t& mid_out) {
         return true;
     }
     if (n <= in.max_leaf && best_cost + parent_area >= leaf_cost) return false;
-    const double* c = cs[best_axis];
     int64_t i = first, j = int64_t(first) + n - 1;
     while (i <= j) {
-        if (c[in.order[i]] < best_split) {
+        if (in.rec[i].c[best_axis] < best_split) {
             ++i;
         } else {
             std::swap(in.order[i], in.order[j]);
+            std::swap(in.rec[i], in.rec[j]);
             --j;
         }
     }
@@ -178,7 +253,7 @@ bool split_node(const Input& in, const BuildNode& node, uint32_t& mid_out) {
 // Builds the subtree under `root` (already bounded) into a private list
 // whose entry 0 is the root; the list's numbering is the reference's
 // right-first depth-first order, relative to the root.
-void build_subtree(const Input& in, const BuildNode& root, std::vector<BuildNode>& out) {
+void build_subtree(Input& in, const BuildNode& root, std::vector<BuildNode>& out) {
     out.clear();
     out.push_back(root);
     std::vector<uint32_t> stack;
@@ -226,30 +301,30 @@ extern "C" uint32_t raymond_bvh_build(const double* mins, const double* maxs, ui
         std::memset(out, 0, 32);
         return 1;
     }
+    if (threads < 1) threads = 1;
     Input in;
-    in.mins = mins;
-    in.maxs = maxs;
     in.max_leaf = max_leaf;
     in.order = order_out;
-    in.cx.resize(count);
-    in.cy.resize(count);
-    in.cz.resize(count);
+    in.threads = threads;
+    in.rec.resize(count);
     for (uint32_t i = 0; i < count; ++i) {
-        in.cx[i] = (mins[size_t(i) * 3] + maxs[size_t(i) * 3]) * 0.5;
-        in.cy[i] = (mins[size_t(i) * 3 + 1] + maxs[size_t(i) * 3 + 1]) * 0.5;
-        in.cz[i] = (mins[size_t(i) * 3 + 2] + maxs[size_t(i) * 3 + 2]) * 0.5;
+        Rec& r = in.rec[i];
+        for (int a = 0; a < 3; ++a) {
+            r.lo[a] = mins[size_t(i) * 3 + a];
+            r.hi[a] = maxs[size_t(i) * 3 + a];
+            r.c[a] = (r.lo[a] + r.hi[a]) * 0.5;
+        }
     }
 
     BuildNode root;
-    bounds_of(in, 0, count, root);
+    bounds_of(in, 0, count, root, true);
     if (count <= max_leaf) {
         write_node(out, root, 0, root.count);
         return 1;
     }
 
-    // Top levels sequentially, in the reference's order, until there are
-    // enough frontier subtrees to spread over the threads.
-    if (threads < 1) threads = 1;
+    // Top levels one node at a time (each node's passes over the threads),
+    // until there are enough frontier subtrees to spread over the threads.
     const uint32_t want = threads > 1 ? uint32_t(threads) * 8u : 1u;
     // The top tree: nodes whose split happened here; frontier entries are
     // nodes left to split (with count > 1), built later as subtrees.
@@ -270,10 +345,10 @@ extern "C" uint32_t raymond_bvh_build(const double* mins, const double* maxs, ui
         if (top[idx].node.count < big_enough) break;
         open.erase(it);
         uint32_t mid;
-        if (!split_node(in, top[idx].node, mid)) continue;
+        if (!split_node(in, top[idx].node, mid, true)) continue;
         BuildNode l, r;
-        bounds_of(in, top[idx].node.first, mid - top[idx].node.first, l);
-        bounds_of(in, mid, top[idx].node.first + top[idx].node.count - mid, r);
+        bounds_of(in, top[idx].node.first, mid - top[idx].node.first, l, true);
+        bounds_of(in, mid, top[idx].node.first + top[idx].node.count - mid, r, true);
         top[idx].left = int32_t(top.size());
         top.push_back({l, -1, -1});
         top.push_back({r, -1, -1});

@@ -106,3 +106,19 @@ def test_oracle_and_builder_match_golden_on_the_gpu_machine(gpu):
     test_packed_cornell_matches_golden()
     test_oracle_raycast_matches_golden()
     test_oracle_path_tracer_matches_golden()
+
+
+@pytest.mark.parametrize("threads", [1, 3, 8])
+def test_native_bvh_matches_oracle_on_a_large_set(threads):
+    """200,000 boxes: the top nodes' passes run split over the threads
+    (nodes of 65,536 primitives and more), and the result is still the
+    reference's build byte for byte."""
+    rng = np.random.default_rng(5)
+    centre = rng.uniform(-50, 50, (200_000, 3))
+    centre[:100_000] = rng.normal(0, 3, (100_000, 3))  # a dense cluster among sparse ones
+    half = rng.uniform(0.001, 0.3, (200_000, 3))
+    mins, maxs = centre - half, centre + half
+    nodes, order = oracle.bvh_build(mins, maxs)
+    b = BVH.build(mins, maxs, threads=threads)
+    assert np.array_equal(b.nodes, nodes)
+    assert np.array_equal(b.order, order)
