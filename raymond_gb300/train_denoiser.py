@@ -151,6 +151,11 @@ def _train_loop(net, targets, inputs, steps, batch, crop, lr, rng, levels, log, 
     spp = torch.tensor(NOISY_SPP, dtype=torch.float32, device="cuda")
     V, size = acc.shape[0], acc.shape[2]
     losses = []
+    # Divergence guard: the parameters of the best 1,000-step window of the
+    # logged loss are kept, and restored if the last window ends more than
+    # twice as high (a long run at a high rate has collapsed into a pass-
+    # through: blend weight 0 everywhere).
+    window, best = [], (math.inf, None, -1)
     t0 = time.time()
     for step in range(steps):
         vi = torch.from_numpy(rng.integers(0, V, batch)).cuda()
@@ -175,7 +180,18 @@ def _train_loop(net, targets, inputs, steps, batch, crop, lr, rng, levels, log, 
         if want:
             losses.append((step, loss))
             log(f"  step {step:5d}  loss {loss:.4f}  lr {rate:.2e}  {time.time() - t0:.1f} s")
+            window.append(loss)
+            if len(window) == 10:
+                mean = float(np.mean(window))
+                if mean < best[0]:
+                    best = (mean, net.get_params(), step)
+                window = []
     net.sync()
+    tail = float(np.mean([v for _, v in losses[-10:]])) if losses else math.inf
+    if best[1] is not None and tail > 2.0 * best[0]:
+        log(f"  loss ended at {tail:.4f}, twice the best window's {best[0]:.4f}: restoring step {best[2]}")
+        net.set_params(best[1])
+        losses.append(("restored", best[2]))
     return losses, time.time() - t0
 
 
