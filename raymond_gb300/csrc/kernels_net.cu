@@ -9,13 +9,18 @@
 // 16-byte cp.async moves 8 channels of one pixel. Weights are [cout][9][cin]
 // (tap-major rows, cin a multiple of 16).
 //
-// GEMM views (M × N × K, tiles of 128 × N × 64 with a 3-stage pipeline):
-//   forward        M = pixels,    N = cout, K = 9·cin   A K-major  (im2col rows), B K-major  (weights)
+// GEMM views (M × N × K):
+//   forward        M = pixels,    N = cout, K = 9·cin   A K-major  (input taps),   B K-major  (weights)
 //   input grad     M = pixels,    N = cin,  K = 9·cout  A K-major  (flipped taps), B MN-major (weights)
 //   weight grad    M = 9·cin + 1, N = cout, K = pixels  A MN-major (shifted input), B MN-major (dy)
-// The weight gradient's extra row is all ones, so its result row is the
-// bias gradient. A kernel that waits too long on its mbarrier records
-// NET_STATUS_TIMEOUT and returns after freeing its tensor memory.
+// Three kernels: k_conv_halo (forward and input gradient on 8×16-pixel
+// tiles whose halo is staged once per channel chunk and read by all nine
+// taps; the default), k_conv_ws (the same two on 128-pixel row tiles whose
+// taps are gathered as im2col rows) and k_conv (the weight gradient, split
+// over pixels, FP32 atomics). The weight gradient's extra row is all ones,
+// so its result row is the bias gradient. A kernel that waits too long on
+// its mbarrier records NET_STATUS_TIMEOUT and returns after freeing its
+// tensor memory.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -553,8 +558,9 @@ __global__ void __launch_bounds__(kWsThreads) k_conv_ws(ConvArgs a) {
 // (pixel (hy, hx) of the halo at (10·hy + hx)·16). Tap (ty, tx)'s A operand
 // is that column read from pixel ty·10 + tx with 160 bytes between core
 // matrices, so the nine taps share one load instead of loading the input
-// nine times. The whole weight tensor sits in shared memory for the CTA's
-// life, as blocks per (chunk, tap) of N × kc in core-matrix order.
+// nine times. The weights are blocks per (chunk, tap) of N × kc in
+// core-matrix order: all of them in shared memory for the CTA's life when
+// they fit, else the nine blocks of a chunk brought with each stage.
 
 constexpr int kTileW = 8, kTileH = 16;
 constexpr int kHaloW = kTileW + 2, kHaloH = kTileH + 2, kHaloPx = kHaloW * kHaloH;
