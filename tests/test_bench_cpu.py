@@ -1,0 +1,58 @@
+"""bench.py's lines that run without a GPU — the reference arm (the
+oracle's CPU path) and the host BVH build — carry the keys of the bench
+contract: one JSON line, the metric and its unit, the run's shape, the
+e2e object with its copy sizes, and the CPU baseline's description."""
+
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def run(*args):
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], capture_output=True, text=True,
+                       timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1, r.stdout
+    return json.loads(lines[0])
+
+
+def check_common(d, steps, warmup):
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "e2e", "cpu_baseline"):
+        assert key in d, key
+    assert d["value"] > 0 and d["ms_per_step"] > 0
+    assert (d["steps"], d["warmup"]) == (steps, warmup)
+    assert d["scaling"] in ("weak", "strong")
+    assert "workload" in d["config"]
+    e2e = d["e2e"]
+    assert e2e["value"] > 0 and e2e["unit"] == d["unit"]
+    assert e2e["h2d_bytes_per_step"] >= 0 and e2e["d2h_bytes_per_step"] >= 0
+    cpu = d["cpu_baseline"]
+    assert cpu["value"] > 0 and cpu["cores"] >= 1 and cpu["kind"] in ("port", "reference") and cpu["sample"]
+
+
+@pytest.mark.parametrize("workload", ["field", "primary"])
+def test_reference_arm_line(workload):
+    args = ["--impl", "reference", "--steps", "1", "--warmup", "0"]
+    if workload == "field":
+        args += ["--size", "64"]
+    else:
+        args += ["--workload", "primary"]
+    d = run(*args)
+    check_common(d, 1, 0)
+    assert d["impl"] == "reference"
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert d["cpu_baseline"]["value"] == d["value"]
+
+
+def test_bvh_build_line():
+    d = run("--workload", "bvh", "--steps", "1", "--warmup", "1")
+    check_common(d, 1, 1)
+    assert d["unit"] == "Mprims/s" and d["gpu_launches"] == 0
+    assert d["config"]["identical_to_oracle"] is True
