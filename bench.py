@@ -748,15 +748,18 @@ def run_ours(args, rank, world, local):
     paths_per_step = args.size * args.size * args.spp
     value = paths_per_step * args.steps * world / total_s / 1e6
 
-    # End to end through the public API: render, wait, read the image back.
+    # End to end through the public API: render, wait, read the image back
+    # (into one page-locked buffer, as a host would reuse between frames).
     e2e_steps = max(3, args.steps // 2)
     r.render()
     r.device.queue.onSubmittedWorkDone()
+    pinned = torch.empty(args.size * args.size * 4, dtype=torch.float32).pin_memory()
+    host = pinned.numpy()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         r.render()
         r.device.queue.onSubmittedWorkDone()
-        px = r.readPixels()
+        px = r.readPixels(out=host)
     e2e_s = time.perf_counter() - t0
     e2e_value = paths_per_step * e2e_steps / e2e_s / 1e6
     d2h = int(px.nbytes)

@@ -509,15 +509,22 @@ class Renderer:
         radius beyond the reference's sizes (0: the reference's)."""
         check(lib().raymond_set_photons(self._h, int(photonsPerFrame), int(capacity), float(radius)), self._h)
 
-    def readPixels(self, denoised=False) -> np.ndarray:
-        """The average so far, w×h×4 float32 from the top left (src/Renderer.mjs:502-528)."""
+    def readPixels(self, denoised=False, out=None) -> np.ndarray:
+        """The average so far, w×h×4 float32 from the top left (src/Renderer.mjs:502-528).
+        `out`, if given, is a C-contiguous float32 array of w·h·4 elements that
+        is filled and returned (one buffer, say page-locked, reused across
+        frames instead of a new one each time)."""
         if self._batch is not None:
             self._batch.sync()
         if not self._resized or self._samples == 0:
             raise RuntimeError("Nothing has been rendered yet.")
         if denoised and not self._denoising():
             raise RuntimeError("Only the color view is denoised, with denoise on.")
-        out = np.empty(self._width * self._height * 4, dtype=np.float32)
+        n = self._width * self._height * 4
+        if out is None:
+            out = np.empty(n, dtype=np.float32)
+        elif not (isinstance(out, np.ndarray) and out.dtype == np.float32 and out.size == n and out.flags.c_contiguous):
+            raise ValueError(f"readPixels(out=...) needs a C-contiguous float32 array of {n} elements.")
         check(lib().raymond_read_pixels(self._h, ptr(out), out.nbytes, 1 if denoised else 0, self._samples), self._h)
         return out
 
