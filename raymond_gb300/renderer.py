@@ -53,6 +53,31 @@ def _js_round(x: float) -> float:
     return math.floor(x + 0.5)
 
 
+def to_half_array(x) -> np.ndarray:
+    """to_half over an array at once (the environment upload's millions of
+    values): the same steps in float64; the exponent comes from frexp, which
+    gives floor(log2(x)) exactly, and a value that rounds up to the next
+    power of two lands on it either way through the mantissa carry."""
+    x = np.asarray(x, dtype=np.float64)
+    out = np.zeros(x.shape, dtype=np.uint16)
+    pos = x > 0.0
+    sat = pos & (x >= 65504.0)
+    sub = pos & ~sat & (x < 6.1035e-5)
+    norm = pos & ~sat & ~sub
+    out[sat] = 0x7BFF
+    out[sub] = np.floor(x[sub] / 5.9605e-8 + 0.5).astype(np.uint16)
+    xn = x[norm]
+    _, e2 = np.frexp(xn)
+    exponent = e2.astype(np.int64) - 1
+    mantissa = np.floor((xn / np.ldexp(1.0, exponent) - 1.0) * 1024 + 0.5).astype(np.int64)
+    e = exponent + 15
+    carry = mantissa == 1024
+    mantissa[carry] = 0
+    e[carry] += 1
+    out[norm] = ((e << 10) | mantissa).astype(np.uint16)
+    return out
+
+
 def _box_around(points):
     mn = [math.inf] * 3
     mx = [-math.inf] * 3
@@ -605,7 +630,7 @@ class Renderer:
         if env is not None:
             rgba = np.empty(env.width * env.height * 4, dtype=np.uint16)
             src = env.data.reshape(-1, 3)
-            flat = np.array([to_half(float(x)) for x in src.reshape(-1)], dtype=np.uint16).reshape(-1, 3)
+            flat = to_half_array(src.reshape(-1)).reshape(-1, 3)
             rgba.reshape(-1, 4)[:, :3] = flat
             rgba.reshape(-1, 4)[:, 3] = to_half(1.0)
             table = env.importance()
