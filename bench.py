@@ -694,7 +694,7 @@ def run_ours(args, rank, world, local):
 
     tuning = None
     if args.path == "auto":
-        tuning = r.autotune(trials=2, cache=os.path.join(ROOT, "gpurun_out", "tuning.json"))
+        tuning = r.autotune(trials=2)  # cached per GPU and workload in ~/.cache/raymond_gb300
     if args.bvh_width:
         import ctypes
 

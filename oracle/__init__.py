@@ -2,7 +2,7 @@
 
 A restatement of the reference's algorithms (BVH.build, Scene.raycast,
 the trace shader's traversal and, in oracle/pathtrace.cpp, its path
-tracer and denoiser) used only as the checker by tests/,
+tracer and denoiser) used only to check the product, by tests/,
 __graft_entry__.smoke() and the cpu_baseline leg of bench.py. Nothing in
 raymond_gb300 imports it. Parity status: pinned against the known answers
 of the reference's own unit tests; not against executed reference output

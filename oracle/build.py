@@ -1,6 +1,6 @@
 """Builds the CPU oracle (liboracle.so) from oracle/*.cpp — test infrastructure
-only: tests/, __graft_entry__.smoke() and bench.py's cpu_baseline use it as
-the checker; the product library never links it.
+only: tests/, __graft_entry__.smoke() and bench.py's cpu_baseline use it to
+check the product; the product library never links it.
 
 The reference itself is JavaScript + WGSL with no compilable source, so there
 is no oracle/_ref build: this restatement is the oracle."""

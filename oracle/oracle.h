@@ -2,7 +2,7 @@
 //
 // A plain CPU restatement of the reference renderer's algorithms (Raymond,
 // JavaScript + WGSL), used by tests/, __graft_entry__.smoke() and the
-// cpu_baseline leg of bench.py as the checker. The product library
+// cpu_baseline leg of bench.py to check the product. The product library
 // (libraymond_cuda.so) never links, loads or calls anything here.
 //
 // Parity status: the reference is JavaScript/WGSL and no JS engine exists on
