@@ -387,8 +387,9 @@ typedef struct raymond_conv {
     int32_t activation; /* leaky ReLU, slope 0.1 below zero */
     uint32_t pixels_per_cta; /* backward_weight: 0 chooses */
     uint32_t* status;
-    uint32_t kernel; /* forward, backward_data: 0 chooses, 1 pixel-row tiles, 2 halo tiles (RAYMOND_EINVAL if
-                        the weights do not fit in shared memory) */
+    uint32_t kernel; /* forward, backward_data: 0 chooses (halo tiles), 1 pixel-row tiles, 2 halo tiles
+                        (weights kept in shared memory, or streamed per channel chunk when they do not fit;
+                        RAYMOND_EINVAL if even a streamed stage does not fit) */
 } raymond_conv;
 int raymond_conv3x3_forward(const raymond_conv* c, void* stream);
 int raymond_conv3x3_backward_data(const raymond_conv* c, void* stream);
