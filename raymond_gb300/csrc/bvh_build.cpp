@@ -147,15 +147,9 @@ bool split_node(Input& in, const BuildNode& node, uint32_t& mid_out, bool par = 
 
     // One pass bins every live axis, per piece.
     parallel_pieces(first, n, parts, [&](uint32_t lo_i, uint32_t hi_i, int t) {
+        // only the counts are reset: a bin's bounds start at its first primitive
         Bins& B = pb[size_t(t)];
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < BINS; ++b) {
-                B.bcount[a][b] = 0;
-                for (int k = 0; k < 3; ++k) {
-                    B.bmin[a][b][k] = kInf;
-                    B.bmax[a][b][k] = -kInf;
-                }
-            }
+        std::memset(B.bcount, 0, sizeof B.bcount);
         for (uint32_t i = lo_i; i < hi_i; ++i) {
             const Rec& r = in.rec[i];
             for (int a = 0; a < 3; ++a) {
@@ -163,7 +157,13 @@ bool split_node(Input& in, const BuildNode& node, uint32_t& mid_out, bool par = 
                 // x ≥ 0 (c ≥ cmin), so truncation is the reference's Math.floor
                 const double x = (r.c[a] - cmin[a]) * scale[a];
                 const int b = x < double(BINS - 1) ? int(x) : BINS - 1;
-                B.bcount[a][b]++;
+                if (B.bcount[a][b]++ == 0) {
+                    for (int k = 0; k < 3; ++k) {
+                        B.bmin[a][b][k] = r.lo[k];
+                        B.bmax[a][b][k] = r.hi[k];
+                    }
+                    continue;
+                }
                 for (int k = 0; k < 3; ++k) {
                     if (r.lo[k] < B.bmin[a][b][k]) B.bmin[a][b][k] = r.lo[k];
                     if (r.hi[k] > B.bmax[a][b][k]) B.bmax[a][b][k] = r.hi[k];
@@ -176,52 +176,66 @@ bool split_node(Input& in, const BuildNode& node, uint32_t& mid_out, bool par = 
         const Bins& B = pb[size_t(t)];
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < BINS; ++b) {
-                M.bcount[a][b] += B.bcount[a][b];
-                for (int k = 0; k < 3; ++k) {
-                    if (B.bmin[a][b][k] < M.bmin[a][b][k]) M.bmin[a][b][k] = B.bmin[a][b][k];
-                    if (B.bmax[a][b][k] > M.bmax[a][b][k]) M.bmax[a][b][k] = B.bmax[a][b][k];
+                if (B.bcount[a][b] == 0) continue;  // its bounds were never written
+                if (M.bcount[a][b] == 0) {
+                    for (int k = 0; k < 3; ++k) {
+                        M.bmin[a][b][k] = B.bmin[a][b][k];
+                        M.bmax[a][b][k] = B.bmax[a][b][k];
+                    }
+                } else {
+                    for (int k = 0; k < 3; ++k) {
+                        if (B.bmin[a][b][k] < M.bmin[a][b][k]) M.bmin[a][b][k] = B.bmin[a][b][k];
+                        if (B.bmax[a][b][k] > M.bmax[a][b][k]) M.bmax[a][b][k] = B.bmax[a][b][k];
+                    }
                 }
+                M.bcount[a][b] += B.bcount[a][b];
             }
     }
     auto& bmin = M.bmin;
     auto& bmax = M.bmax;
     auto& bcount = M.bcount;
 
+    // The reference sweeps every split position b = 1 … 31 (left: bins < b,
+    // right: bins ≥ b) and keeps the first of the lowest cost. Positions
+    // between two non-empty bins see the same two sets, so the same cost;
+    // the first of them, just after a non-empty bin, is the only one that
+    // can win. Only those are evaluated, with the same arithmetic.
     double best_cost = kInf, best_split = 0.0;
     int best_axis = -1;
     for (int a = 0; a < 3; ++a) {
         if (!live[a]) continue;
-        double right_area[BINS];
+        int nz[BINS], m = 0;
+        for (int b = 0; b < BINS; ++b)
+            if (bcount[a][b]) nz[m++] = b;
+        if (m < 2) continue;
+        double right_area[BINS];  // of the bins nz[k] … nz[m-1]
         uint32_t right_count[BINS];
         double rmn[3] = {kInf, kInf, kInf}, rmx[3] = {-kInf, -kInf, -kInf};
         uint32_t total = 0;
-        for (int b = BINS - 1; b > 0; --b) {
-            if (bcount[a][b]) {
-                for (int k = 0; k < 3; ++k) {
-                    rmn[k] = std::min(rmn[k], bmin[a][b][k]);
-                    rmx[k] = std::max(rmx[k], bmax[a][b][k]);
-                }
+        for (int k = m - 1; k >= 1; --k) {
+            const int b = nz[k];
+            for (int q = 0; q < 3; ++q) {
+                rmn[q] = std::min(rmn[q], bmin[a][b][q]);
+                rmx[q] = std::max(rmx[q], bmax[a][b][q]);
             }
             total += bcount[a][b];
-            right_area[b] = area3(rmn, rmx);
-            right_count[b] = total;
+            right_area[k] = area3(rmn, rmx);
+            right_count[k] = total;
         }
         double lmn[3] = {kInf, kInf, kInf}, lmx[3] = {-kInf, -kInf, -kInf};
         uint32_t left_count = 0;
-        for (int b = 1; b < BINS; ++b) {
-            if (bcount[a][b - 1]) {
-                for (int k = 0; k < 3; ++k) {
-                    lmn[k] = std::min(lmn[k], bmin[a][b - 1][k]);
-                    lmx[k] = std::max(lmx[k], bmax[a][b - 1][k]);
-                }
+        for (int k = 0; k + 1 < m; ++k) {
+            const int b = nz[k];
+            for (int q = 0; q < 3; ++q) {
+                lmn[q] = std::min(lmn[q], bmin[a][b][q]);
+                lmx[q] = std::max(lmx[q], bmax[a][b][q]);
             }
-            left_count += bcount[a][b - 1];
-            if (left_count == 0 || right_count[b] == 0) continue;
-            const double cost = double(left_count) * area3(lmn, lmx) + double(right_count[b]) * right_area[b];
+            left_count += bcount[a][b];
+            const double cost = double(left_count) * area3(lmn, lmx) + double(right_count[k + 1]) * right_area[k + 1];
             if (cost < best_cost) {
                 best_cost = cost;
                 best_axis = a;
-                best_split = cmin[a] + double(b) / scale[a];
+                best_split = cmin[a] + double(b + 1) / scale[a];
             }
         }
     }
