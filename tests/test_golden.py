@@ -122,3 +122,21 @@ def test_native_bvh_matches_oracle_on_a_large_set(threads):
     b = BVH.build(mins, maxs, threads=threads)
     assert np.array_equal(b.nodes, nodes)
     assert np.array_equal(b.order, order)
+
+
+@pytest.mark.parametrize("threads", [1, 8])
+def test_native_bvh_matches_oracle_on_degenerate_sets(threads):
+    """Sets where the reference's fallbacks decide: every centroid equal (no
+    axis to bin: split in the middle), all boxes in one plane (one axis
+    without extent), and heavy duplicates in few bins."""
+    rng = np.random.default_rng(9)
+    same = np.tile([1.0, 2.0, 3.0], (5000, 1))
+    flat = np.column_stack([rng.uniform(-5, 5, 80_000), rng.uniform(-5, 5, 80_000), np.zeros(80_000)])
+    dup = np.repeat(rng.uniform(-1, 1, (7, 3)), 12_000, axis=0)
+    for centre in (same, flat, dup):
+        half = np.full_like(centre, 0.01)
+        mins, maxs = centre - half, centre + half
+        nodes, order = oracle.bvh_build(mins, maxs)
+        b = BVH.build(mins, maxs, threads=threads)
+        assert np.array_equal(b.nodes, nodes)
+        assert np.array_equal(b.order, order)
