@@ -558,19 +558,22 @@ template <uint32_t FEAT>
 __device__ __forceinline__ Scatter scatter_in_volumes(const Scene& s, const Params& P, float3 o, float3 d, float t_max,
                                                       Rng& rng) {
     Scatter sc{t_max, NONE};
-    if (!(FEAT & F_VOLUMES)) return sc;
-    for (uint32_t k = 0; k < P.volume_count; ++k) {
-        const uint32_t i = s.lights[P.light_count + k];
-        const float2 span = volume_span(s, i, o, d);
-        const float end = fminf(span.y, sc.t);
-        if (span.x < end) {
-            const uint32_t mat = __float_as_uint(ldg4(s.prims + size_t(i) * 4).y);
-            const float density = __ldg(&s.materials[size_t(mat) * 6 + 5].x);
-            const float t = span.x - logf(1.0f - rng.rand()) / density;
-            if (t < end) sc = Scatter{t, i};
+    if constexpr (!(FEAT & F_VOLUMES)) {
+        return sc;
+    } else {
+        for (uint32_t k = 0; k < P.volume_count; ++k) {
+            const uint32_t i = s.lights[P.light_count + k];
+            const float2 span = volume_span(s, i, o, d);
+            const float end = fminf(span.y, sc.t);
+            if (span.x < end) {
+                const uint32_t mat = __float_as_uint(ldg4(s.prims + size_t(i) * 4).y);
+                const float density = __ldg(&s.materials[size_t(mat) * 6 + 5].x);
+                const float t = span.x - logf(1.0f - rng.rand()) / density;
+                if (t < end) sc = Scatter{t, i};
+            }
         }
+        return sc;
     }
-    return sc;
 }
 template <uint32_t FEAT>
 __device__ __forceinline__ float transmittance(const Scene& s, const Params& P, float3 o, float3 d, float dist) {

@@ -108,7 +108,6 @@ struct SingleCtx {
     Scene s;
     Params P;
     __device__ __forceinline__ uint32_t job_of(uint32_t) const { return 0; }
-    __device__ __forceinline__ uint32_t pixel_of(uint32_t word) const { return word; }
     __device__ __forceinline__ const Scene& scene(uint32_t) const { return s; }
     __device__ __forceinline__ const Params& params(uint32_t) const { return P; }
     __device__ __forceinline__ uint32_t job_of_path(const WavefrontState&, uint32_t) const { return 0; }
@@ -116,7 +115,6 @@ struct SingleCtx {
 struct BatchCtx {
     const JobDesc* jobs;
     __device__ __forceinline__ uint32_t job_of(uint32_t word) const { return word >> 21; }
-    __device__ __forceinline__ uint32_t pixel_of(uint32_t word) const { return word & 0x1fffffu; }
     __device__ __forceinline__ const Scene& scene(uint32_t j) const { return jobs[j].scene; }
     __device__ __forceinline__ const Params& params(uint32_t j) const { return jobs[j].params; }
     __device__ __forceinline__ uint32_t job_of_path(const WavefrontState& w, uint32_t path) const {
