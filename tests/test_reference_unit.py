@@ -355,7 +355,8 @@ def test_stick_between_points():
     hit = cast(scene, a.subtract(along), along)
     assert abs(hit["distance"] - 1.0) < 1e-5 and np.allclose(hit["normal"], along.negate().tuple(), atol=1e-6)
     middle = a.add(b).scale(0.5)
-    across = stick.transform.column(0).normalized()
+    c = stick.transform.column(0)
+    across = Vec3(c.x, c.y, c.z).normalized()
     assert abs(across.dot(along)) < 1e-9
     side = cast(scene, middle.add(across.scale(5)), across.negate())
     assert abs(side["distance"] - (5 - 0.1)) < 1e-5
