@@ -54,6 +54,20 @@ def dist_env():
     return rank, world, local
 
 
+def replica_throughput(units_per_step, steps, seconds, world, device):
+    """Whole-job rate of `world` independent replicas, each doing the same
+    fixed work per step: all ranks' units over the slowest rank's time (the
+    job ends when its last replica does). Returns (units per second, the
+    time used)."""
+    if world > 1:
+        import torch
+
+        t = torch.tensor([seconds], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        seconds = float(t.item())
+    return units_per_step * steps * world / seconds, seconds
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons, sampled every 200 ms while running."""
 
@@ -751,13 +765,9 @@ def run_ours(args, rank, world, local):
     barrier()
     clock_info = clocks.stop()
 
-    total_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
     paths_per_step = args.size * args.size * args.spp
-    value = paths_per_step * args.steps * world / total_s / 1e6
+    value, total_s = replica_throughput(paths_per_step, args.steps, sum(step_ms) / 1e3, world, f"cuda:{local}")
+    value /= 1e6
 
     # End to end through the public API: render, wait, read the image back
     # (into one page-locked buffer, as a host would reuse between frames).
@@ -766,13 +776,15 @@ def run_ours(args, rank, world, local):
     r.device.queue.onSubmittedWorkDone()
     pinned = torch.empty(args.size * args.size * 4, dtype=torch.float32).pin_memory()
     host = pinned.numpy()
+    barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         r.render()
         r.device.queue.onSubmittedWorkDone()
         px = r.readPixels(out=host)
     e2e_s = time.perf_counter() - t0
-    e2e_value = paths_per_step * e2e_steps / e2e_s / 1e6
+    e2e_value, _ = replica_throughput(paths_per_step, e2e_steps, e2e_s, world, f"cuda:{local}")
+    e2e_value /= 1e6
     d2h = int(px.nbytes)
 
     result = None
