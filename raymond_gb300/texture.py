@@ -219,7 +219,14 @@ class EnvironmentMap:
 
     def importance(self):
         """Row CDFs (cw × ch) and the CDF over rows (one more row), by
-        luminance × sin θ over ≤512×256 cells (src/EnvironmentMap.mjs:202-247)."""
+        luminance × sin θ over ≤512×256 cells (src/EnvironmentMap.mjs:202-247).
+
+        Vectorised across each row of cells with the reference's arithmetic
+        kept step for step, so the table is bit-identical: each cell's light
+        summed in double over its pixels, row-major; the running sum along
+        the row (a sequential cumulative sum) stored as f32, then divided by
+        the row's double total and stored as f32 again; the rows' totals
+        summed in order for the CDF down."""
         if self._importance is not None:
             return self._importance
         W, H = self.width, self.height
@@ -229,32 +236,33 @@ class EnvironmentMap:
         rows = np.zeros(ch)
         img = self.data.reshape(H, W, 3).astype(np.float64)
         lum = 0.2126 * img[..., 0] + 0.7152 * img[..., 1] + 0.0722 * img[..., 2]
+        xs = np.arange(cw)
+        x0 = (xs * W) // cw  # floor(x·W/cw): exact in integers
+        x1 = np.maximum(x0 + 1, ((xs + 1) * W) // cw)
+        widths = x1 - x0
         for y in range(ch):
-            y0 = math.floor(y * H / ch)
-            y1 = max(y0 + 1, math.floor((y + 1) * H / ch))
+            y0 = (y * H) // ch
+            y1 = max(y0 + 1, ((y + 1) * H) // ch)
             sin = math.sin((y + 0.5) / ch * math.pi)
-            s = 0.0
-            cells = []
-            for x in range(cw):
-                x0 = math.floor(x * W / cw)
-                x1 = max(x0 + 1, math.floor((x + 1) * W / cw))
-                light = 0.0
-                for py in range(y0, y1):
-                    for px in range(x0, x1):
-                        light += float(lum[py, px])
-                s += light / ((y1 - y0) * (x1 - x0)) * sin
-                cells.append(s)
-            row = np.array(cells, dtype=np.float32)
-            data[y * cw:(y + 1) * cw] = (row / np.float32(s)) if s > 0 else (np.arange(1, cw + 1) / cw)
+            light = np.zeros(cw)
+            for py in range(y0, y1):
+                line = lum[py]
+                for k in range(int(widths.max())):
+                    inside = k < widths
+                    light += np.where(inside, line[np.minimum(x0 + k, W - 1)], 0.0)
+            running = np.cumsum(light / ((y1 - y0) * widths) * sin)
+            s = float(running[-1])
+            cells = running.astype(np.float32)
+            if s > 0:
+                data[y * cw:(y + 1) * cw] = cells.astype(np.float64) / s
+            else:
+                data[y * cw:(y + 1) * cw] = (xs + 1) / cw
             rows[y] = s
-        total = rows.sum()
-        running = 0.0
-        for y in range(ch):
-            running += rows[y]
-            data[ch * cw + y] = running / total if total > 0 else (y + 1) / ch
+        down = np.cumsum(rows)
+        total = float(down[-1])
+        data[ch * cw:ch * cw + ch] = down / total if total > 0 else (np.arange(ch) + 1) / ch
         data[ch * cw + ch - 1] = 1.0
-        for y in range(ch):
-            data[y * cw + cw - 1] = 1.0
+        data[cw - 1:ch * cw:cw] = 1.0
         self._importance = {"width": cw, "height": ch, "data": data}
         return self._importance
 

@@ -89,3 +89,54 @@ def test_sky_radiance_from_environment():
     assert Sky.environment_sky(env, 2, math.pi).radiance(ahead).x < 0.1
     assert Sky.environment_sky(env, 2, math.pi).radiance(Vec3(-0.9, 0, 0.43).normalized()).x > 1.9
     assert close(Sky().radiance(Vec3(0, 1, 0)), Sky().zenith, 1e-12)
+
+
+def importance_loop(env):
+    """EnvironmentMap.importance (src/EnvironmentMap.mjs:202-247) value by
+    value, for small maps: the check on the vectorised table."""
+    W, H = env.width, env.height
+    px = env.data.astype(np.float64)
+    cw, ch = min(W, 512), min(H, 256, min(W, 512))
+    data = np.zeros(cw * (ch + 1), dtype=np.float32)
+    rows = []
+    for y in range(ch):
+        y0 = math.floor(y * H / ch)
+        y1 = max(y0 + 1, math.floor((y + 1) * H / ch))
+        sin = math.sin((y + 0.5) / ch * math.pi)
+        s = 0.0
+        for x in range(cw):
+            x0 = math.floor(x * W / cw)
+            x1 = max(x0 + 1, math.floor((x + 1) * W / cw))
+            light = 0.0
+            for yy in range(y0, y1):
+                for xx in range(x0, x1):
+                    i = (yy * W + xx) * 3
+                    light += 0.2126 * px[i] + 0.7152 * px[i + 1] + 0.0722 * px[i + 2]
+            s += light / ((y1 - y0) * (x1 - x0)) * sin
+            data[y * cw + x] = s
+        for x in range(cw):
+            data[y * cw + x] = float(data[y * cw + x]) / s if s > 0 else (x + 1) / cw
+        rows.append(s)
+    total = 0.0
+    for r in rows:
+        total += r
+    running = 0.0
+    for y in range(ch):
+        running += rows[y]
+        data[ch * cw + y] = running / total if total > 0 else (y + 1) / ch
+    data[ch * cw + ch - 1] = 1.0
+    for y in range(ch):
+        data[y * cw + cw - 1] = 1.0
+    return cw, ch, data
+
+
+@pytest.mark.parametrize("w,h", [(8, 4), (37, 19), (600, 300), (700, 333)])
+def test_importance_table_is_bit_identical_to_the_loop(w, h):
+    rng = np.random.default_rng(w * 1000 + h)
+    values = rng.exponential(1.0, size=w * h * 3) ** 3  # a few bright pixels among dim ones
+    values[: w * 3 * (h // 3)] = 0.0  # and dark rows, which fall back to uniform
+    env = EnvironmentMap(w, h, values)
+    imp = env.importance()
+    cw, ch, data = importance_loop(env)
+    assert (imp["width"], imp["height"]) == (cw, ch)
+    assert np.array_equal(imp["data"].view(np.uint32), data.view(np.uint32))
