@@ -142,74 +142,69 @@ def pack_objects(objects) -> PackedScene:
             material_index[id(m)] = i
         return i
 
-    # Per object: records (n,16) float32 with header words, bounds (n,3)×2 in double, blocks or None.
-    rec_parts, min_parts, max_parts, block_parts, has_block_parts, owner_parts = [], [], [], [], [], []
-    # Materials are numbered in object order, as the reference meets them.
-    mat_ids = [material_of(o.material) for o in objects]
-    # Unrotated spheres pack in bulk (their globe axes are x and y); records
-    # are put back in object order below.
+    # Every object's records go straight to their place in object order:
+    # records (16 words, header words as u32), bounds in double, attribute
+    # blocks and whether there is one, and the owning object's index.
+    mat_ids = [material_of(o.material) for o in objects]  # numbered as the reference meets them
+    counts = np.array([o.triangleCount if isinstance(o, Mesh) else 1 for o in objects], dtype=np.int64)
+    offsets = np.zeros(len(objects) + 1, dtype=np.int64)
+    np.cumsum(counts, out=offsets[1:])
+    total = int(offsets[-1])
+    records = np.zeros((total, 16), dtype=np.float32)
+    hdr_all = records.view(np.uint32)
+    mins_all = np.zeros((total, 3))
+    maxs_all = np.zeros((total, 3))
+    blocks = np.zeros((total, 16), dtype=np.float32)
+    has_block = np.zeros(total, dtype=bool)
+    owners = np.repeat(np.arange(len(objects), dtype=np.int64), counts)
+    hdr_all[:, 2] = NONE
+    hdr_all[:, 3] = NONE
+
+    # Unrotated spheres pack in bulk (their globe axes are x and y).
     identity = Mat4.identity().v
     bulk = [oi for oi, o in enumerate(objects) if type(o) is Sphere and o.rotation.v == identity]
     bulk_set = set(bulk)
     if bulk:
-        n = len(bulk)
+        at = offsets[np.array(bulk, dtype=np.int64)]
         cr = np.array([(objects[i].center.x, objects[i].center.y, objects[i].center.z, objects[i].radius)
                        for i in bulk], dtype=np.float64)
-        mats = np.array([mat_ids[i] for i in bulk], dtype=np.uint32)
-        rec = np.zeros((n, 16), dtype=np.float32)
-        rec[:, 4:8] = cr
-        rec[:, 8] = 1.0   # globe x axis
-        rec[:, 13] = 1.0  # north pole
-        hdr = rec.view(np.uint32)
-        hdr[:, 0] = PRIMITIVE_KINDS["sphere"]
-        hdr[:, 1] = mats
-        hdr[:, 2] = NONE
-        hdr[:, 3] = NONE
-        mn, mx = _pad_bounds(cr[:, :3] - cr[:, 3:4], cr[:, :3] + cr[:, 3:4])
-        rec_parts.append(rec)
-        min_parts.append(mn)
-        max_parts.append(mx)
-        block_parts.append(np.zeros((n, 16), dtype=np.float32))
-        has_block_parts.append(np.zeros(n, dtype=bool))
-        owner_parts.append(np.array(bulk, dtype=np.int64))
+        records[at, 4:8] = cr
+        records[at, 8] = 1.0   # globe x axis
+        records[at, 13] = 1.0  # north pole
+        hdr_all[at, 0] = PRIMITIVE_KINDS["sphere"]
+        hdr_all[at, 1] = np.array([mat_ids[i] for i in bulk], dtype=np.uint32)
+        mins_all[at], maxs_all[at] = _pad_bounds(cr[:, :3] - cr[:, 3:4], cr[:, :3] + cr[:, 3:4])
     for oi, obj in enumerate(objects):
         if oi in bulk_set:
             continue
         if obj.material.type == "volume" and not isinstance(obj, (Sphere, Box)):
             raise TypeError("A volume must be a Sphere or a Box.")
-        mat = mat_ids[oi]
+        lo, hi = int(offsets[oi]), int(offsets[oi + 1])
+        rec, hdr = records[lo:hi], hdr_all[lo:hi]
+        hdr[:, 1] = mat_ids[oi]
         if isinstance(obj, Mesh):
+            n = hi - lo
             tri = obj.indices.reshape(-1, 3).astype(np.int64)
-            n = len(tri)
-            p = obj.positions
-            a, b, c = p[tri[:, 0]], p[tri[:, 1]], p[tri[:, 2]]
-            rec = np.zeros((n, 16), dtype=np.float32)
-            rec[:, 4:7], rec[:, 8:11], rec[:, 12:15] = a, b, c
-            hdr = rec.view(np.uint32)
+            # Corners in double for the bounds; the records take them
+            # rounded to f32, rounded per vertex before the gather (the same
+            # values, a third of the conversions).
+            pt = np.take(obj.positions, tri, axis=0)
+            rec[:, 4:16].reshape(n, 3, 4)[:, :, :3] = np.take(obj.positions.astype(np.float32), tri, axis=0)
             hdr[:, 0] = PRIMITIVE_KINDS["triangle"]
-            hdr[:, 1] = mat
-            hdr[:, 2] = NONE
-            hdr[:, 3] = NONE
+            a, b, c = pt[:, 0], pt[:, 1], pt[:, 2]
             mn = np.minimum(np.minimum(a, b), c)
             mx = np.maximum(np.maximum(a, b), c)
             if obj.normals is not None or obj.uvs is not None:
-                blk = np.zeros((n, 16), dtype=np.float32)
+                blk = blocks[lo:hi]
                 if obj.normals is not None:
-                    for k in range(3):
-                        blk[:, k * 4: k * 4 + 3] = obj.normals[tri[:, k]]
+                    blk[:, 0:12].reshape(n, 3, 4)[:, :, :3] = np.take(obj.normals.astype(np.float32), tri, axis=0)
                 if obj.uvs is not None:
                     for k in range(3):
                         blk[:, k * 4 + 3] = obj.uvs[tri[:, k], 0]
                         blk[:, 12 + k] = obj.uvs[tri[:, k], 1]
                 blk[:, 15] = (SMOOTH if obj.normals is not None else 0) + (TEXTURED if obj.uvs is not None else 0)
-                block_parts.append(blk)
-                has_block_parts.append(np.ones(n, dtype=bool))
-            else:
-                block_parts.append(np.zeros((n, 16), dtype=np.float32))
-                has_block_parts.append(np.zeros(n, dtype=bool))
+                has_block[lo:hi] = True
         else:
-            rec = np.zeros((1, 16), dtype=np.float32)
-            hdr = rec.view(np.uint32)
             if isinstance(obj, Sphere):
                 c, r = obj.center, obj.radius
                 ax = obj.axes()
@@ -227,37 +222,10 @@ def pack_objects(objects) -> PackedScene:
                 rec[0, 4:16] = [m.value(r_, c_) for r_ in range(3) for c_ in range(4)]
                 hdr[0, 0] = PRIMITIVE_KINDS["box"]
                 pts = obj.corners()
-            hdr[0, 1] = mat
-            hdr[0, 2] = NONE
-            hdr[0, 3] = NONE
             arr = np.array([[p.x, p.y, p.z] for p in pts], dtype=np.float64)
             mn = arr.min(axis=0, keepdims=True)
             mx = arr.max(axis=0, keepdims=True)
-            block_parts.append(np.zeros((1, 16), dtype=np.float32))
-            has_block_parts.append(np.zeros(1, dtype=bool))
-        mn, mx = _pad_bounds(mn, mx)
-        rec_parts.append(rec)
-        min_parts.append(mn)
-        max_parts.append(mx)
-        owner_parts.append(np.full(len(rec), oi, dtype=np.int64))
-
-    if rec_parts:
-        records = np.concatenate(rec_parts)
-        mins_all = np.concatenate(min_parts)
-        maxs_all = np.concatenate(max_parts)
-        blocks = np.concatenate(block_parts)
-        has_block = np.concatenate(has_block_parts)
-        owners = np.concatenate(owner_parts)
-        if bulk:
-            order = np.argsort(owners, kind="stable")
-            records, mins_all, maxs_all = records[order], mins_all[order], maxs_all[order]
-            blocks, has_block, owners = blocks[order], has_block[order], owners[order]
-    else:
-        records = np.zeros((0, 16), dtype=np.float32)
-        mins_all = maxs_all = np.zeros((0, 3))
-        blocks = np.zeros((0, 16), dtype=np.float32)
-        has_block = np.zeros(0, dtype=bool)
-        owners = np.zeros(0, dtype=np.int64)
+        mins_all[lo:hi], maxs_all[lo:hi] = _pad_bounds(mn, mx)
 
     rec_u = records.view(np.uint32)
     vol_material = np.array([m.type == "volume" for m in material_list], dtype=bool)
@@ -310,23 +278,24 @@ def pack_objects(objects) -> PackedScene:
             index[id(t)] = i
         return i
 
-    for i, m in enumerate(material_list):
-        mats[i, 0:3] = [m.color.x, m.color.y, m.color.z]
-        mu[i, 3] = MATERIAL_TYPES[m.type]
-        mats[i, 4:8] = [m.emission.x, m.emission.y, m.emission.z, m.roughness]
-        if m.checker is not None:
-            mats[i, 8:12] = [m.checker.x, m.checker.y, m.checker.z, m.checkerSize]
-        mats[i, 12] = m.ior
-        mu[i, 13] = texture_of(m.texture, tex_index, tex_list)
-        mats[i, 14:16] = [m.textureScale.x, m.textureScale.y]
-        mu[i, 16] = texture_of(m.normalMap, nrm_index, nrm_list)
-        mats[i, 17] = m.normalScale
-        mu[i, 18] = texture_of(m.emissionTexture, tex_index, tex_list)
-        mats[i, 19] = m.dispersion
-        mats[i, 20] = m.density
-        mats[i, 21] = m.anisotropy
+    # The float words of every material in one array (rounded to f32 as
+    # they are stored), then the u32 words over them: type, and the colour,
+    # normal-map and emission textures, numbered in the order met.
+    values, words = [], []
+    for m in material_list:
+        ck = m.checker
+        c4 = (ck.x, ck.y, ck.z, m.checkerSize) if ck is not None else (0.0, 0.0, 0.0, 0.0)
+        values.append((m.color.x, m.color.y, m.color.z, 0.0, m.emission.x, m.emission.y, m.emission.z, m.roughness,
+                       *c4, m.ior, 0.0, m.textureScale.x, m.textureScale.y, 0.0, m.normalScale, 0.0, m.dispersion,
+                       m.density, m.anisotropy))
+        words.append((MATERIAL_TYPES[m.type], texture_of(m.texture, tex_index, tex_list),
+                      texture_of(m.normalMap, nrm_index, nrm_list), texture_of(m.emissionTexture, tex_index, tex_list)))
+    if material_list:
+        k = len(material_list)
+        mats[:k, :22] = np.array(values, dtype=np.float64)
+        mu[:k, [3, 13, 16, 18]] = np.array(words, dtype=np.uint32)
 
-    objs = [objects[int(o)] for o in owners[source]] if count else []
+    objs = list(map(objects.__getitem__, owners[source].tolist())) if count else []
     return PackedScene(
         primitives=prims.reshape(-1),
         primitiveCount=count,
