@@ -11,7 +11,7 @@ import math
 
 import numpy as np
 
-from .vec import Mat4, Vec2, Vec3
+from .vec import Mat4, Vec3
 
 
 class Sphere:

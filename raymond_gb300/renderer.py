@@ -11,7 +11,7 @@ import numpy as np
 
 from . import _native
 from ._native import check, lib, ptr
-from .geometry import Box, Mesh, Quad, Sphere
+from .geometry import Box, Mesh, Quad
 from .scene import NONE, PRIMITIVE_KINDS, Scene
 from .vec import Vec3
 

@@ -17,7 +17,6 @@ filter and of the network."""
 from __future__ import annotations
 
 import argparse
-import ctypes
 import json
 import math
 import os

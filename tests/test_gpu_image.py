@@ -7,7 +7,6 @@ import numpy as np
 import pytest
 
 import oracle
-from fixtures import renderer
 from raymond_gb300 import Canvas, Renderer, scenes
 from raymond_gb300.renderer import light_table
 

@@ -6,7 +6,7 @@ import math
 import numpy as np
 import pytest
 
-from raymond_gb300 import EnvironmentMap, Material, Sky, Texture, Vec2, Vec3
+from raymond_gb300 import EnvironmentMap, Material, Sky, Texture, Vec3
 from raymond_gb300.scenes import mulberry32
 
 
