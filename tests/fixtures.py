@@ -216,28 +216,10 @@ def pixel_rays(camera, size):
     return rays
 
 
-def trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoise=False, caustics=True, seed=0):
-    """Renders scene `name` and returns pixels (size²×4), denoised (or None),
-    hits (per pixel: object index, distance, normal — or None) and rays."""
-    r = renderer()
-    r.canvas.width = size
-    r.canvas.height = size
-    scene, cam_opts = SCENES[name](arg)
-    camera = Camera(**cam_opts)
-    r.scene = scene
-    r.camera = camera
-    r.view = view
-    r.maxBounces = bounces
-    r.fireflyClamp = 0
-    r.samplesPerFrame = min(spp, 16)
-    r.denoise = denoise
-    r.caustics = caustics
-    r.reset()
-    while r.samples < spp:
-        r.render()
-    r.device.queue.onSubmittedWorkDone()
-    pixels = r.readPixels()
-    den = r.readPixels(denoised=True) if denoise else None
+def pixel_hits(scene, camera, size):
+    """The pixel-centre rays and what the oracle's Scene.raycast sees through
+    each (fixture.mjs:311-364): per pixel the object index, distance, facing
+    normal (normal-mapped), albedo and point, or None."""
     rays = pixel_rays(camera, size)
     packed = scene.pack()
     # Scene.raycast in double on the pixel-centre rays (the rays as doubles, not f32).
@@ -269,6 +251,58 @@ def trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoise=Fals
             albedo_ = np.array((m.emission if m.type == "light" else m.color).tuple())
         hits.append({"object": int(packed.objectIndex[p]), "distance": float(ref["t"][i]), "normal": normal,
                      "albedo": albedo_, "point": rays[i, :3] + rays[i, 3:] * ref["t"][i]})
+    return rays, hits
+
+
+def oracle_trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoise=False, caustics=True, seed=0):
+    """trace() with the oracle's path tracer (the trace shader restated, on
+    the CPU) making the image instead of the GPU: one frame of `spp`
+    samples, no firefly clamp, path tracing only (light tracing and photon
+    mapping are the GPU's own estimators of the same light), and the
+    oracle's à-trous denoiser on its guides when asked."""
+    from raymond_gb300.renderer import light_table, params_block
+
+    assert view == "color"
+    scene, cam_opts = SCENES[name](arg)
+    camera = Camera(**cam_opts)
+    packed = scene.pack()
+    # The oracle's path tracer restates neither textures nor environment maps.
+    assert not packed.textures and not packed.normalMaps and scene.sky.environment is None, name
+    words, powers = light_table(packed)
+    params = params_block(scene, camera, size, size, light_count=len(powers), volume_count=len(packed.volumes),
+                          max_bounces=bounces, firefly_clamp=0.0, spp=spp, denoise=False)
+    o = oracle.render(packed, words, params, seed_hash=seed)
+    pixels = (o["accum"] / spp).reshape(-1).astype(np.float32)
+    den = None
+    if denoise:
+        den = oracle.denoise(o["accum"], o["albedo"], o["normal"], size, size, spp).reshape(-1)
+    rays, hits = pixel_hits(scene, camera, size)
+    return {"pixels": pixels, "denoised": den, "hits": hits, "rays": rays, "samples": spp, "scene": scene}
+
+
+def trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoise=False, caustics=True, seed=0):
+    """Renders scene `name` and returns pixels (size²×4), denoised (or None),
+    hits (per pixel: object index, distance, normal — or None) and rays."""
+    r = renderer()
+    r.canvas.width = size
+    r.canvas.height = size
+    scene, cam_opts = SCENES[name](arg)
+    camera = Camera(**cam_opts)
+    r.scene = scene
+    r.camera = camera
+    r.view = view
+    r.maxBounces = bounces
+    r.fireflyClamp = 0
+    r.samplesPerFrame = min(spp, 16)
+    r.denoise = denoise
+    r.caustics = caustics
+    r.reset()
+    while r.samples < spp:
+        r.render()
+    r.device.queue.onSubmittedWorkDone()
+    pixels = r.readPixels()
+    den = r.readPixels(denoised=True) if denoise else None
+    rays, hits = pixel_hits(scene, camera, size)
     return {"pixels": pixels, "denoised": den, "hits": hits, "rays": rays, "samples": r.samples, "scene": scene}
 
 
