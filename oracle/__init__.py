@@ -39,6 +39,10 @@ def lib():
         _lib.ro_surface_double.argtypes = [P, P, U32, P, P, D, D, D, P]
         _lib.ro_render.restype = None
         _lib.ro_render.argtypes = [P, P, P, P, P, P, U32, U32, U32, U32, U32, P, P, P, P, I]
+        _lib.ro_light_trace.restype = U32
+        _lib.ro_light_trace.argtypes = [P, P, P, P, P, P, P, U32, U32, P, P, I]
+        _lib.ro_photon_gather.restype = None
+        _lib.ro_photon_gather.argtypes = [P, P, P, P, P, P, P, U32, U32, P, I]
         _lib.ro_denoise.restype = None
         _lib.ro_denoise.argtypes = [P, P, P, U32, U32, U32, P, I]
         _lib.ro_display.restype = None
@@ -136,6 +140,40 @@ def render(packed, lights_words, params: bytes, region=None, seed_hash=0, nthrea
             "bytes": int(counters[0]), "rays": int(counters[1]), "hits": int(counters[2]), "paths": int(counters[3]),
             "trav_closest": int(counters[4]), "trav_shadow": int(counters[5]), "rays_closest": int(counters[6]),
             "rays_shadow": int(counters[7])}
+
+
+def light_trace(packed, lights_words, params: bytes, emitters, photons, seed_hash=0, nthreads=None):
+    """One frame of light_trace (src/shaders.mjs:1628-1814) for photons
+    0..photons-1: dict splats (h×w×4 u32 fixed-point sums, 1/65536 units)
+    and photons (n×9 float32: where each landed, its power, the direction
+    it came from), in photon order."""
+    import struct
+    width, height = struct.unpack_from("<2I", params, 160)
+    splats = np.zeros(width * height * 4, dtype=np.uint32)
+    out = np.zeros(max(int(photons), 1) * 9, dtype=np.float32)
+    pbuf = np.frombuffer(bytes(params), dtype=np.uint8).copy()
+    words = np.ascontiguousarray(lights_words, dtype=np.uint32)
+    attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
+    em = np.ascontiguousarray(emitters, dtype=np.float32)
+    n = lib().ro_light_trace(_p(packed.primitives), _p(packed.nodes), _p(packed.materials), _p(attrs), _p(words),
+                             _p(pbuf), _p(em), int(photons), seed_hash, _p(splats), _p(out), nthreads or threads())
+    return {"splats": splats.reshape(height, width, 4), "photons": out[: n * 9].reshape(n, 9)}
+
+
+def photon_gather(packed, lights_words, params: bytes, photons, seed_hash=0, nthreads=None):
+    """One frame of photon_gather (src/shaders.mjs:1585-1626): the caustic
+    light the photon map adds to each pixel (h×w×4 float32 sums)."""
+    import struct
+    width, height = struct.unpack_from("<2I", params, 160)
+    accum = np.zeros(width * height * 4, dtype=np.float32)
+    ph = np.ascontiguousarray(photons, dtype=np.float32).reshape(-1)
+    pbuf = np.frombuffer(bytes(params), dtype=np.uint8).copy()
+    words = np.ascontiguousarray(lights_words, dtype=np.uint32)
+    attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
+    lib().ro_photon_gather(_p(packed.primitives), _p(packed.nodes), _p(packed.materials), _p(attrs), _p(words),
+                           _p(pbuf), _p(ph if ph.size else np.zeros(9, np.float32)), ph.size // 9, seed_hash,
+                           _p(accum), nthreads or threads())
+    return accum.reshape(height, width, 4)
 
 
 def denoise(accum, guide_albedo, guide_normal, width, height, total_samples, nthreads=None):

@@ -76,6 +76,18 @@ void ro_render(const void* prims, const void* nodes, const void* materials, cons
                uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out,
                uint64_t* counters, int threads);
 
+// ---- light tracing and photon mapping (src/shaders.mjs:1425-1831) ----
+// One frame's photons 0..photons-1: fixed-point splats added to `splats`
+// (W·H·4 u32) and the stored photons (9 floats: p, power, -d) in photon
+// order; returns how many were stored.
+uint32_t ro_light_trace(const void* prims, const void* nodes, const void* materials, const float* attributes,
+                        const uint32_t* lights, const void* params208, const float* emitters, uint32_t photons,
+                        uint32_t seed_hash, uint32_t* splats, float* photons_out, int threads);
+// The photon map's caustic light through mirrors and glass, added to accum.
+void ro_photon_gather(const void* prims, const void* nodes, const void* materials, const float* attributes,
+                      const uint32_t* lights, const void* params208, const float* photons, uint32_t count,
+                      uint32_t seed_hash, float* accum, int threads);
+
 // ---- the denoiser (src/shaders.mjs:1916-2098) and display (2114-2152) ----
 // Full-image à-trous from the accumulated buffers: prepare, steps 1..16,
 // compose. out: w*h*4 floats.

@@ -1,7 +1,8 @@
-// The trace shader's path tracer (src/shaders.mjs:131-1899), the denoiser
-// (src/shaders.mjs:1916-2098) and the display math (src/shaders.mjs:
-// 2114-2152), restated as scalar f32 C++ on the CPU — TEST INFRASTRUCTURE
-// ONLY. The integer sample hashes are bit-exact; the f32 arithmetic follows
+// The trace shader's path tracer (src/shaders.mjs:131-1899), its light
+// tracing with splats and its photon map (src/shaders.mjs:1425-1831), the
+// denoiser (src/shaders.mjs:1916-2098) and the display math
+// (src/shaders.mjs:2114-2152), restated as scalar f32 C++ on the CPU — TEST
+// INFRASTRUCTURE ONLY. The integer sample hashes are bit-exact; the f32 arithmetic follows
 // the WGSL expression by expression (compiled without contraction), with
 // the math library's sqrt/sin/cos/exp/log/pow/atan2/acos called, never
 // re-implemented. Textured materials and environment maps are not
@@ -795,6 +796,284 @@ V inspect(Ctx& c, float px, float py) {
     return vs(hit.t);
 }
 
+// ---- light tracing and photon mapping (src/shaders.mjs:1425-1831) ----
+const float SPLAT_SCALE = 65536.0f;
+const uint32_t PHOTON_TABLE = 1048576u;
+
+// frame (src/shaders.mjs:217-225): its first two columns.
+inline void frame_cols(V n, V& c0, V& c1) {
+    const float s = n.z >= 0.0f ? 1.0f : -1.0f;
+    const float a = -1.0f / (s + n.z);
+    const float b = n.x * n.y * a;
+    c0 = v3(1.0f + s * n.x * n.x * a, s * b, -s * n.x);
+    c1 = v3(b, s + n.y * n.y * a, -n.y);
+}
+
+// concentric_disk (src/shaders.mjs:245-256), from PCG numbers.
+inline void concentric_disk(Sampler& sm, float& x, float& y) {
+    float a, b;
+    sm.rand2(a, b);
+    const float ux = 2.0f * a - 1.0f, uy = 2.0f * b - 1.0f;
+    x = y = 0.0f;
+    if (ux == 0.0f && uy == 0.0f) return;
+    if (std::fabs(ux) > std::fabs(uy)) {
+        const float phi = (PI / 4.0f) * (uy / ux);
+        x = ux * std::cos(phi);
+        y = ux * std::sin(phi);
+        return;
+    }
+    const float phi = PI / 2.0f - (PI / 4.0f) * (ux / uy);
+    x = uy * std::cos(phi);
+    y = uy * std::sin(phi);
+}
+
+// camera_ray(px, true) (src/shaders.mjs:1148-1166), as radiance() starts.
+void camera_ray(const Params& P, float px, float py, Sampler& s, V& o, V& d) {
+    const float ndcx = 2.0f * px / float(P.width) - 1.0f, ndcy = 1.0f - 2.0f * py / float(P.height);
+    const V fwd = vf(P.cam_forward), right = vf(P.cam_right), up = vf(P.cam_up), pos = vf(P.cam_pos);
+    const V dir = norm(fwd + right * (ndcx * P.tan_half_fov * P.aspect) + up * (ndcy * P.tan_half_fov));
+    o = pos;
+    d = dir;
+    if (P.lens_radius > 0.0f) {
+        const V focus = pos + dir * (P.focus_distance / dot(dir, fwd));
+        float lx, ly;
+        concentric_disk(s, lx, ly);
+        o = pos + right * (lx * P.lens_radius) + up * (ly * P.lens_radius);
+        d = norm(focus - o);
+    }
+}
+
+struct Photon {
+    uint32_t id;
+    V p, beta, wi;  // where it landed, its power, and whence it came (-d)
+};
+
+// splat (src/shaders.mjs:1443-1491): the photon's light added, in fixed
+// point with random rounding, to the pixel that sees the surface.
+void splat(Ctx& c, const Surf& s, const Mat& m, V base, V d, V beta, Sampler& sm, uint32_t* splats) {
+    const Params& P = c.P;
+    const V to_camera = vf(P.cam_pos) - s.p;
+    const float dist = len(to_camera);
+    const V wo = to_camera / dist;
+    const float cos_film = -dot(wo, vf(P.cam_forward));
+    if (cos_film <= 1e-6f || dot(wo, s.ng) <= 0.0f) return;
+    const float x = -dot(wo, vf(P.cam_right)) / (cos_film * P.tan_half_fov * P.aspect);
+    const float y = -dot(wo, vf(P.cam_up)) / (cos_film * P.tan_half_fov);
+    const float px = (x + 1.0f) * 0.5f * float(P.width);
+    const float py = (1.0f - y) * 0.5f * float(P.height);
+    if (px < 0.0f || py < 0.0f || px >= float(P.width) || py >= float(P.height)) return;
+    const V wi = -d;
+    V f;
+    float pdf;
+    eval_bsdf(m, base, s.n, wo, wi, f, pdf);
+    const float cos_in = dot(s.n, wi);
+    if (pdf <= 0.0f || cos_in <= 0.0f) return;
+    const V origin = offset(s, wo);
+    if (trace(c, origin, wo, dist - dot(origin - s.p, wo), true).prim != NONE) return;
+    const float pixel_area = (4.0f * P.tan_half_fov * P.tan_half_fov * P.aspect) / float(P.width * P.height);
+    const V value = beta * (f / cos_in) * dot(wo, s.ng) /
+                    (dist * dist * pixel_area * cos_film * cos_film * cos_film);
+    if (!finite3(value)) return;
+    const uint32_t index = (uint32_t(py) * P.width + uint32_t(px)) * 4u;
+    const float r0 = sm.rand(), r1 = sm.rand(), r2 = sm.rand();
+    const V fixed = value * SPLAT_SCALE + v3(r0, r1, r2);
+    splats[index] += uint32_t(wmin(fixed.x, 4e9f));
+    splats[index + 1] += uint32_t(wmin(fixed.y, 4e9f));
+    splats[index + 2] += uint32_t(wmin(fixed.z, 4e9f));
+}
+
+// light_trace (src/shaders.mjs:1628-1814): photon `id` from a light
+// chosen by power, through mirrors and glass, splatted and stored where it
+// first lands on anything else. E is the emitters buffer's vec4s.
+void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t seed_hash, uint32_t* splats,
+                 std::vector<Photon>& stored) {
+    const Params& P = c.P;
+    Sampler sm;
+    sm.rng_state = pcg(id ^ pcg(P.sample_offset * 2654435769u + 977u)) ^ seed_hash;
+    const float* header = E;
+    const uint32_t sources = fbits(header[0]), targets = fbits(header[1]);
+    const float xi = sm.rand();
+    uint32_t k = 0;
+    while (!(k + 1u >= sources || E[(1 + k) * 4] > xi)) ++k;
+    const float* entry = E + (1 + k) * 4;
+    const float chance = entry[2];
+    if (chance <= 0.0f) return;
+    const uint32_t prim_index = fbits(entry[1]);
+    const uint32_t first_target = 1u + sources;
+    auto target = [&](uint32_t i) { return E + (first_target + i) * 4; };
+
+    V o, d, beta;
+    if (prim_index == NONE) {
+        d = -sample_cone(vf(P.sun_dir), P.sun_omc, sm);
+        float pick = sm.rand() * header[3] / PI;
+        uint32_t j = 0;
+        for (;;) {
+            const float r = target(j)[3];
+            if (j + 1u >= targets || pick < r * r) break;
+            pick -= r * r;
+            ++j;
+        }
+        const float* circle = target(j);
+        V c0, c1;
+        frame_cols(d, c0, c1);
+        float dx, dy;
+        concentric_disk(sm, dx, dy);
+        dx *= circle[3];
+        dy *= circle[3];
+        o = vf(circle) - d * header[2] + c0 * dx + c1 * dy;
+        float through = 1.0f;
+        for (uint32_t i = 0; i < targets; ++i) {
+            const V q = o - vf(target(i));
+            const V across = q - d * dot(q, d);
+            through += (i != j && dot(across, across) < target(i)[3] * target(i)[3]) ? 1.0f : 0.0f;
+        }
+        const V irradiance = vf(P.sun_radiance) * (2.0f * PI * P.sun_omc);
+        beta = irradiance * header[3] / (through * chance * float(photons));
+    } else {
+        const float* pf = c.pf(prim_index);
+        const uint32_t* pu = c.pu(prim_index);
+        const Mat m = material(c, pu[1]);
+        V n;
+        float area;
+        if (pu[0] == 1u) {  // QUAD
+            const float a = sm.rand();
+            const float b = sm.rand();
+            o = vf(pf + 4) + vf(pf + 8) * a + vf(pf + 12) * b;
+            const V cr = cross(vf(pf + 8), vf(pf + 12));
+            area = len(cr);
+            n = cr / area;
+        } else {
+            const float z = 1.0f - 2.0f * sm.rand();
+            const float r = std::sqrt(wmax(0.0f, 1.0f - z * z));
+            const float phi = 2.0f * PI * sm.rand();
+            n = v3(r * std::cos(phi), z, r * std::sin(phi));
+            o = vf(pf + 4) + n * pf[7];
+            area = 4.0f * PI * pf[7] * pf[7];
+        }
+        float cones = 0.0f;
+        bool inside = false;
+        for (uint32_t i = 0; i < targets; ++i) {
+            const float* aim = target(i);
+            const V to = vf(aim) - o;
+            const float d2 = dot(to, to);
+            inside = inside || d2 <= aim[3] * aim[3];
+            cones += sphere_omc(aim[3], wmax(d2, aim[3] * aim[3]));
+        }
+        if (!inside) {
+            float pick = sm.rand() * cones;
+            uint32_t j = 0;
+            for (;;) {
+                const float* aim = target(j);
+                const V to = vf(aim) - o;
+                const float omc = sphere_omc(aim[3], dot(to, to));
+                if (j + 1u >= targets || pick < omc) {
+                    d = sample_cone(to / len(to), omc, sm);
+                    break;
+                }
+                pick -= omc;
+                ++j;
+            }
+            float within = 1.0f;
+            for (uint32_t i = 0; i < targets; ++i) {
+                const float* aim = target(i);
+                const V to = vf(aim) - o;
+                const float omc = sphere_omc(aim[3], dot(to, to));
+                within += (i != j && 1.0f - dot(d, to / len(to)) <= omc) ? 1.0f : 0.0f;
+            }
+            const float cos_out = dot(d, n);
+            if (cos_out <= 0.0f) return;
+            beta = m.emission * (cos_out * area * 2.0f * PI * cones) / (within * chance * float(photons));
+        } else {
+            d = cosine_hemisphere(n, sm);
+            beta = m.emission * (PI * area) / (chance * float(photons));
+        }
+        o = o + n * (1e-4f * wmax(1.0f, wmax(std::fabs(o.x), wmax(std::fabs(o.y), std::fabs(o.z)))));
+    }
+
+    float wavelength = 0.0f;
+    uint32_t bounces = 0;
+    V carried = vs(1.0f);
+    for (uint32_t depth = 0; depth < P.max_bounces; ++depth) {
+        const HitR hit = trace(c, o, d, INF, false);
+        if (hit.prim == NONE) return;
+        const Surf s = surface(c, o, d, hit);
+        const Mat m = material(c, s.material);
+        if (m.kind == 4) return;
+        const V base = albedo(m, s.p);
+        if (!is_delta(m)) {
+            if (bounces > 0u) {
+                splat(c, s, m, base, d, beta * carried, sm, splats);
+                stored.push_back({id, s.p, beta * carried, -d});
+            }
+            return;
+        }
+        // dispersed (src/shaders.mjs:1412-1423), its random number drawn
+        // whether or not the glass splits colours.
+        const float u = sm.rand();
+        Mat dm = m;
+        if (m.kind == 3 && m.dispersion > 0.0f) {
+            if (wavelength == 0.0f) {
+                wavelength = 380.0f + 340.0f * u;
+                carried = carried * wavelength_rgb(wavelength);
+            }
+            const float l = wavelength * 1e-3f;
+            dm.ior = m.ior + m.dispersion * (1.0f / (l * l) - 1.0f / (0.5876f * 0.5876f));
+        }
+        const Bs bs = sample_bsdf(dm, base, s, -d, sm);
+        if (!bs.ok) return;
+        carried = carried * bs.weight;
+        ++bounces;
+        o = offset(s, bs.wi);
+        d = bs.wi;
+        if (!roulette(carried, depth, sm)) return;
+    }
+}
+
+inline uint32_t photon_cell_hash(int32_t x, int32_t y, int32_t z) {
+    return ((uint32_t(x) * 73856093u) ^ (uint32_t(y) * 19349663u) ^ (uint32_t(z) * 83492791u)) & (PHOTON_TABLE - 1u);
+}
+
+struct PhotonMap {
+    const float* ph;                 // 9 floats a photon: p, beta, wi
+    std::vector<uint32_t> heads, next;  // lists through the photons, index + 1, 0 ends
+};
+
+// gather (src/shaders.mjs:1533-1572).
+V gather(const Params& P, const PhotonMap& map, const Surf& s, const Mat& m, V base, V wo) {
+    const float r = P.photon_radius;
+    const float r2 = r * r;
+    const float cell_size = P.photon_cell;
+    const V here = s.p / cell_size;
+    const int32_t cx = int32_t(std::floor(here.x)), cy = int32_t(std::floor(here.y)), cz = int32_t(std::floor(here.z));
+    const int32_t sx = here.x - std::floor(here.x) >= 0.5f ? 1 : -1;
+    const int32_t sy = here.y - std::floor(here.y) >= 0.5f ? 1 : -1;
+    const int32_t sz = here.z - std::floor(here.z) >= 0.5f ? 1 : -1;
+    V sum = vs(0.0f);
+    uint32_t visited = 0;
+    for (uint32_t k = 0; k < 8u; ++k) {
+        uint32_t index = map.heads[photon_cell_hash(cx + int32_t(k & 1u) * sx, cy + int32_t((k >> 1u) & 1u) * sy,
+                                                    cz + int32_t((k >> 2u) & 1u) * sz)];
+        for (;;) {
+            if (index == 0u || visited >= 4096u) break;
+            ++visited;
+            const float* at = map.ph + size_t(index - 1u) * 9;
+            const V off = vf(at) - s.p;
+            if (dot(off, off) < r2 && std::fabs(dot(off, s.ng)) < 0.25f * r) {
+                const V wi = vf(at + 6);
+                const float cos_in = dot(s.n, wi);
+                if (cos_in > 0.0f && dot(s.ng, wi) > 0.0f) {
+                    V f;
+                    float pdf;
+                    eval_bsdf(m, base, s.n, wo, wi, f, pdf);
+                    sum = sum + vf(at + 3) * (f / cos_in);
+                }
+            }
+            index = map.next[index - 1u];
+        }
+    }
+    return sum / (PI * r2);
+}
+
 }  // namespace
 
 extern "C" void ro_render(const void* prims, const void* nodes, const void* materials, const float* attributes,
@@ -882,6 +1161,122 @@ extern "C" void ro_render(const void* prims, const void* nodes, const void* mate
         counters[6] = tot_rc;
         counters[7] = tot_rs;
     }
+}
+
+// light_trace for photons 0..photons-1 of a frame (src/shaders.mjs:1628-1814):
+// splats (W·H·4 u32, added to, wrapping as the GPU's atomics do) and the
+// stored photons (9 floats each: p, beta, -d) in photon order. Returns how
+// many were stored.
+extern "C" uint32_t ro_light_trace(const void* prims, const void* nodes, const void* materials, const float* attributes,
+                                   const uint32_t* lights, const void* params208, const float* emitters,
+                                   uint32_t photons, uint32_t seed_hash, uint32_t* splats, float* photons_out,
+                                   int threads) {
+    Params P;
+    std::memcpy(&P, params208, sizeof P);
+    const uint32_t cells = P.width * P.height * 4u;
+    const int nt = std::max(1, threads);
+    std::vector<std::vector<uint32_t>> part_splats(nt, std::vector<uint32_t>(cells, 0u));
+    std::vector<std::vector<Photon>> part_photons(nt);
+    std::atomic<uint32_t> next{0};
+    auto worker = [&](int t) {
+        Ctx c{static_cast<const uint8_t*>(prims), static_cast<const uint8_t*>(nodes),
+              static_cast<const float*>(materials), attributes, lights, P};
+        for (;;) {
+            const uint32_t k0 = next.fetch_add(256);
+            if (k0 >= photons) break;
+            for (uint32_t k = k0; k < std::min(photons, k0 + 256); ++k)
+                light_trace(c, emitters, photons, k, seed_hash, part_splats[t].data(), part_photons[t]);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(worker, t);
+    worker(0);
+    for (auto& t : pool) t.join();
+    for (int t = 0; t < nt; ++t)
+        for (uint32_t i = 0; i < cells; ++i) splats[i] += part_splats[t][i];
+    std::vector<Photon> all;
+    for (auto& v : part_photons) all.insert(all.end(), v.begin(), v.end());
+    std::sort(all.begin(), all.end(), [](const Photon& a, const Photon& b) { return a.id < b.id; });
+    for (size_t i = 0; i < all.size(); ++i) {
+        float* q = photons_out + i * 9;
+        const V* v[3] = {&all[i].p, &all[i].beta, &all[i].wi};
+        for (int j = 0; j < 3; ++j) {
+            q[j * 3] = v[j]->x;
+            q[j * 3 + 1] = v[j]->y;
+            q[j * 3 + 2] = v[j]->z;
+        }
+    }
+    return uint32_t(all.size());
+}
+
+// photon_gather (src/shaders.mjs:1585-1626): per pixel, from the camera
+// through mirrors and glass to the first other surface, the photons near
+// it; added to accum (W·H·4) once for each of the frame's samples.
+extern "C" void ro_photon_gather(const void* prims, const void* nodes, const void* materials, const float* attributes,
+                                 const uint32_t* lights, const void* params208, const float* photons, uint32_t count,
+                                 uint32_t seed_hash, float* accum, int threads) {
+    Params P;
+    std::memcpy(&P, params208, sizeof P);
+    PhotonMap map{photons, std::vector<uint32_t>(PHOTON_TABLE, 0u), std::vector<uint32_t>(count, 0u)};
+    for (uint32_t i = 0; i < count; ++i) {
+        const float* p = photons + size_t(i) * 9;
+        const uint32_t h = photon_cell_hash(int32_t(std::floor(p[0] / P.photon_cell)),
+                                            int32_t(std::floor(p[1] / P.photon_cell)),
+                                            int32_t(std::floor(p[2] / P.photon_cell)));
+        map.next[i] = map.heads[h];
+        map.heads[h] = i + 1u;
+    }
+    const uint32_t n = P.width * P.height;
+    std::atomic<uint32_t> next{0};
+    auto worker = [&] {
+        Ctx c{static_cast<const uint8_t*>(prims), static_cast<const uint8_t*>(nodes),
+              static_cast<const float*>(materials), attributes, lights, P};
+        for (;;) {
+            const uint32_t k0 = next.fetch_add(64);
+            if (k0 >= n) break;
+            for (uint32_t index = k0; index < std::min(n, k0 + 64); ++index) {
+                Sampler sm;
+                sm.rng_state = pcg(index ^ pcg(P.sample_offset * 2654435769u + 4099u)) ^ seed_hash;
+                const float jx = sm.rand();
+                const float jy = sm.rand();
+                V o, d;
+                camera_ray(P, float(index % P.width) + jx, float(index / P.width) + jy, sm, o, d);
+                V throughput = vs(1.0f);
+                for (uint32_t depth = 0; depth < P.max_bounces; ++depth) {
+                    const HitR hit = trace(c, o, d, INF, false);
+                    if (hit.prim == NONE) break;
+                    const Surf s = surface(c, o, d, hit);
+                    const Mat m = material(c, s.material);
+                    if (m.kind == 4) break;
+                    const V base = albedo(m, s.p);
+                    if (!is_delta(m)) {
+                        if (depth > 0u) {
+                            const V light = throughput * gather(P, map, s, m, base, -d);
+                            if (finite3(light)) {
+                                const float l = lum(light);
+                                const float spf = float(P.samples_per_frame);
+                                accum[size_t(index) * 4] += light.x * spf;
+                                accum[size_t(index) * 4 + 1] += light.y * spf;
+                                accum[size_t(index) * 4 + 2] += light.z * spf;
+                                accum[size_t(index) * 4 + 3] += l * l * spf;
+                            }
+                        }
+                        break;
+                    }
+                    const Bs bs = sample_bsdf(m, base, s, -d, sm);
+                    if (!bs.ok) break;
+                    throughput = throughput * bs.weight;
+                    o = offset(s, bs.wi);
+                    d = bs.wi;
+                }
+            }
+        }
+    };
+    const int nt = std::max(1, threads);
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto& t : pool) t.join();
 }
 
 // ---- denoiser (src/shaders.mjs:1930-2097) ----

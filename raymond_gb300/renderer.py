@@ -157,6 +157,43 @@ def _gpu_name() -> str:
         return "gpu"
 
 
+def emitters_block(light_powers, light_count, deltas, sky):
+    """Renderer.#writeEmitters (src/Renderer.mjs:670-717): a header (sources,
+    targets, the sun's start distance, the targets' circles' total area),
+    then per source its running chance, primitive (NONE for the sun) and
+    chance, chosen by power (the sun's is what falls on the targets'
+    circles), then the target spheres (centre, radius). float32 vec4s, or
+    None if there is nothing for light tracing to do."""
+    if not deltas:
+        return None
+    circles = sum(math.pi * t["radius"] ** 2 for t in deltas["targets"])
+    sources = list(light_powers)
+    if sky.sunStrength > 0:
+        omc = 2.0 * math.sin(sky.sunSize / 2.0) ** 2
+        r = sky.sunRadiance
+        lum = 0.2126 * r.x + 0.7152 * r.y + 0.0722 * r.z
+        sources.append({"prim": NONE, "power": lum * 2 * math.pi * omc * circles})
+    total = sum(src["power"] for src in sources)
+    if not (total > 0):
+        return None
+    data = np.zeros((2 + light_count + MAX_TARGETS) * 4, dtype=np.float32)
+    u = data.view(np.uint32)
+    u[0] = len(sources)
+    u[1] = len(deltas["targets"])
+    data[2] = deltas["reach"]
+    data[3] = circles
+    running = 0.0
+    for k, src in enumerate(sources):
+        running += src["power"] / total
+        data[4 + k * 4] = 1.0 if k == len(sources) - 1 else running
+        u[4 + k * 4 + 1] = src["prim"]
+        data[4 + k * 4 + 2] = src["power"] / total
+    for j, t in enumerate(deltas["targets"]):
+        c = t["centre"]
+        data[4 + (len(sources) + j) * 4: 8 + (len(sources) + j) * 4] = [c.x, c.y, c.z, t["radius"]]
+    return data
+
+
 def light_table(packed):
     """The lights buffer of Renderer.#upload (src/Renderer.mjs:571-607): the
     light primitives, the volumes, then each light's running total chance
@@ -494,38 +531,11 @@ class Renderer:
         return {f: getattr(t, f) for f, _ in _native.Tuning._fields_}
 
     def _caustics_enabled(self, scene) -> bool:
-        """Renderer.#writeEmitters (src/Renderer.mjs:670-717): the lights
-        light tracing starts from, chosen by power (the sun's is what falls
-        on the targets' circles), then the targets. False if there is
+        """Uploads the emitters light tracing starts from; False if there is
         nothing for light tracing to do."""
-        delta, sky = self._deltas, scene.sky
-        if not delta:
+        data = emitters_block(self._light_powers, self._light_count, self._deltas, scene.sky)
+        if data is None:
             return False
-        circles = sum(math.pi * t["radius"] ** 2 for t in delta["targets"])
-        sources = list(self._light_powers)
-        if sky.sunStrength > 0:
-            omc = 2.0 * math.sin(sky.sunSize / 2.0) ** 2
-            r = sky.sunRadiance
-            lum = 0.2126 * r.x + 0.7152 * r.y + 0.0722 * r.z
-            sources.append({"prim": NONE, "power": lum * 2 * math.pi * omc * circles})
-        total = sum(src["power"] for src in sources)
-        if not (total > 0):
-            return False
-        data = np.zeros((2 + self._light_count + MAX_TARGETS) * 4, dtype=np.float32)
-        u = data.view(np.uint32)
-        u[0] = len(sources)
-        u[1] = len(delta["targets"])
-        data[2] = delta["reach"]
-        data[3] = circles
-        running = 0.0
-        for k, src in enumerate(sources):
-            running += src["power"] / total
-            data[4 + k * 4] = 1.0 if k == len(sources) - 1 else running
-            u[4 + k * 4 + 1] = src["prim"]
-            data[4 + k * 4 + 2] = src["power"] / total
-        for j, t in enumerate(delta["targets"]):
-            c = t["centre"]
-            data[4 + (len(sources) + j) * 4: 8 + (len(sources) + j) * 4] = [c.x, c.y, c.z, t["radius"]]
         check(lib().raymond_set_emitters(self._h, ptr(data), data.size // 4), self._h)
         return True
 

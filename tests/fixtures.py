@@ -255,12 +255,14 @@ def pixel_hits(scene, camera, size):
 
 
 def oracle_trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoise=False, caustics=True, seed=0):
-    """trace() with the oracle's path tracer (the trace shader restated, on
-    the CPU) making the image instead of the GPU: one frame of `spp`
-    samples, no firefly clamp, path tracing only (light tracing and photon
-    mapping are the GPU's own estimators of the same light), and the
-    oracle's à-trous denoiser on its guides when asked."""
-    from raymond_gb300.renderer import light_table, params_block
+    """trace() with the oracle (the trace shader restated, on the CPU) making
+    the image instead of the GPU, frame by frame as the renderer does (up
+    to 16 samples a frame, no firefly clamp): path tracing, and when the
+    scene has mirrors or glass for light to be focused by and `caustics`
+    is on, the same frame's light tracing with its splats and the photon
+    map's gather through mirrors and glass (photon radius shrinking frame
+    by frame); then the oracle's à-trous denoiser on the guides if asked."""
+    from raymond_gb300.renderer import PHOTON_CAPACITY, delta_objects, emitters_block, light_table, params_block
 
     assert view == "color"
     scene, cam_opts = SCENES[name](arg)
@@ -269,15 +271,34 @@ def oracle_trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoi
     # The oracle's path tracer restates neither textures nor environment maps.
     assert not packed.textures and not packed.normalMaps and scene.sky.environment is None, name
     words, powers = light_table(packed)
-    params = params_block(scene, camera, size, size, light_count=len(powers), volume_count=len(packed.volumes),
-                          max_bounces=bounces, firefly_clamp=0.0, spp=spp, denoise=False)
-    o = oracle.render(packed, words, params, seed_hash=seed)
-    pixels = (o["accum"] / spp).reshape(-1).astype(np.float32)
-    den = None
-    if denoise:
-        den = oracle.denoise(o["accum"], o["albedo"], o["normal"], size, size, spp).reshape(-1)
+    deltas = delta_objects(scene) if caustics else None
+    emitters = emitters_block(powers, len(powers), deltas, scene.sky) if deltas else None
+    acc = np.zeros((size, size, 4), np.float32)
+    alb = np.zeros((size, size, 4), np.float32)
+    nrm = np.zeros((size, size, 4), np.float32)
+    spf = min(spp, 16)
+    done = 0
+    while done < spp:
+        params = params_block(scene, camera, size, size, light_count=len(powers), volume_count=len(packed.volumes),
+                              max_bounces=bounces, firefly_clamp=0.0, samples=done, spp=spf, denoise=False,
+                              caustics=emitters is not None, deltas=deltas)
+        o = oracle.render(packed, words, params, seed_hash=seed)
+        acc += o["accum"]
+        alb += o["albedo"]
+        nrm += o["normal"]
+        if emitters is not None:
+            lt = oracle.light_trace(packed, words, params, emitters, min(size * size * spf, PHOTON_CAPACITY),
+                                    seed_hash=seed)
+            light = lt["splats"][..., :3].astype(np.float32) / np.float32(65536.0)
+            lum = light[..., 0] * np.float32(0.2126) + light[..., 1] * np.float32(0.7152) + light[..., 2] * np.float32(0.0722)
+            acc[..., :3] += light * np.float32(spf)
+            acc[..., 3] += lum * lum * np.float32(spf)
+            acc += oracle.photon_gather(packed, words, params, lt["photons"], seed_hash=seed)
+        done += spf
+    pixels = (acc / done).reshape(-1).astype(np.float32)
+    den = oracle.denoise(acc, alb, nrm, size, size, done).reshape(-1) if denoise else None
     rays, hits = pixel_hits(scene, camera, size)
-    return {"pixels": pixels, "denoised": den, "hits": hits, "rays": rays, "samples": spp, "scene": scene}
+    return {"pixels": pixels, "denoised": den, "hits": hits, "rays": rays, "samples": done, "scene": scene}
 
 
 def trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoise=False, caustics=True, seed=0):
