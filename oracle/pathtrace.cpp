@@ -2,12 +2,12 @@
 // tracing with splats and its photon map (src/shaders.mjs:1425-1831), the
 // denoiser (src/shaders.mjs:1916-2098) and the display math
 // (src/shaders.mjs:2114-2152), restated as scalar f32 C++ on the CPU — TEST
-// INFRASTRUCTURE ONLY. The integer sample hashes are bit-exact; the f32 arithmetic follows
-// the WGSL expression by expression (compiled without contraction), with
+// INFRASTRUCTURE ONLY. The integer sample hashes are bit-exact; the f32
+// arithmetic follows the WGSL expression by expression (compiled without
+// contraction), with
 // the math library's sqrt/sin/cos/exp/log/pow/atan2/acos called, never
-// re-implemented. Textured materials and environment maps are not
-// restated here (they read like the sky gradient's absence: the oracle
-// scenes use neither).
+// re-implemented. Environment maps are restated (ro_render_env); textured
+// materials and normal maps are not.
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -153,6 +153,15 @@ inline V in_frame(V n, V l) {
     return c0 * l.x + c1 * l.y + n * l.z;
 }
 
+// An environment map as the renderer uploads it: RGBA half floats and the
+// importance table (cw × (ch + 1) floats).
+struct Env {
+    const uint16_t* map;
+    uint32_t w, h;
+    const float* table;
+    uint32_t cw, ch;
+};
+
 struct Ctx {
     const uint8_t* prims;
     const uint8_t* nodes;
@@ -164,6 +173,7 @@ struct Ctx {
     // and rays of closest-hit and of shadow (any-hit) traces apart
     uint64_t bytes = 0, rays = 0, hits = 0;
     uint64_t trav_closest = 0, trav_shadow = 0, rays_closest = 0, rays_shadow = 0;
+    const Env* env = nullptr;
 
     const float* pf(uint32_t i) const { return reinterpret_cast<const float*>(prims + size_t(i) * 64); }
     const uint32_t* pu(uint32_t i) const { return reinterpret_cast<const uint32_t*>(prims + size_t(i) * 64); }
@@ -296,6 +306,84 @@ V sky(const Params& P, V d) {
     return hz * (1.0f - t) + gr * t;
 }
 bool in_sun(const Params& P, V d) { return P.sun_on != 0u && dot(d, vf(P.sun_dir)) >= 1.0f - P.sun_omc; }
+
+// ---- environment map (src/shaders.mjs:611-676) ----
+// IEEE 754 binary16 to binary32, from the format's definition.
+inline float half_to_float(uint16_t h) {
+    const uint32_t sign = uint32_t(h >> 15) << 31, exp = (h >> 10) & 0x1fu, man = h & 0x3ffu;
+    if (exp == 0u) {
+        const float v = std::ldexp(float(man), -24);
+        return sign ? -v : v;
+    }
+    if (exp == 31u) return bitsf(sign | 0x7f800000u | (man << 13));
+    return bitsf(sign | ((exp + 112u) << 23) | (man << 13));
+}
+inline bool env_on(const Ctx& c) { return c.env != nullptr && c.P.env_strength > 0.0f; }
+void env_uv(const Params& P, V d, float& u, float& v) {
+    const float uu = 0.5f + std::atan2(d.x, -d.z) / (2.0f * PI) - P.env_rotation / (2.0f * PI);
+    u = uu - std::floor(uu);
+    v = std::acos(clampf(d.y, -1.0f, 1.0f)) / PI;
+}
+// Bilinear, repeating round the horizon and clamped at the poles (the
+// reference's sampler: repeat in u, clamp-to-edge in v).
+V env_texel(const Env& e, int x, int y) {
+    const int w = int(e.w), h = int(e.h);
+    const int xi = ((x % w) + w) % w;
+    const int yi = y < 0 ? 0 : (y >= h ? h - 1 : y);
+    const uint16_t* t = e.map + (size_t(yi) * w + xi) * 4;
+    return v3(half_to_float(t[0]), half_to_float(t[1]), half_to_float(t[2]));
+}
+V env_radiance(const Ctx& c, V d) {
+    const Env& e = *c.env;
+    float u, v;
+    env_uv(c.P, d, u, v);
+    const float x = u * float(e.w) - 0.5f, y = v * float(e.h) - 0.5f;
+    const float fx0 = std::floor(x), fy0 = std::floor(y);
+    const float fx = x - fx0, fy = y - fy0;
+    const int x0 = int(fx0), y0 = int(fy0);
+    const V col = env_texel(e, x0, y0) * ((1.0f - fx) * (1.0f - fy)) + env_texel(e, x0 + 1, y0) * (fx * (1.0f - fy)) +
+                  env_texel(e, x0, y0 + 1) * ((1.0f - fx) * fy) + env_texel(e, x0 + 1, y0 + 1) * (fx * fy);
+    return col * c.P.env_strength;
+}
+inline float env_cdf(const Env& e, uint32_t x, uint32_t y) { return e.table[size_t(y) * e.cw + x]; }
+uint32_t env_search(const Env& e, uint32_t y, uint32_t n, float xi) {
+    uint32_t lo = 0u, hi = n - 1u;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) / 2u;
+        if (env_cdf(e, mid, y) > xi) hi = mid;
+        else lo = mid + 1u;
+    }
+    return lo;
+}
+float env_pdf(const Ctx& c, V d) {
+    const Env& e = *c.env;
+    const uint32_t cw = e.cw, ch = e.ch;
+    float u, v;
+    env_uv(c.P, d, u, v);
+    const uint32_t x = std::min(uint32_t(u * float(cw)), cw - 1u);
+    const uint32_t y = std::min(uint32_t(v * float(ch)), ch - 1u);
+    const float row = env_cdf(e, y, ch) - (y > 0u ? env_cdf(e, y - 1u, ch) : 0.0f);
+    const float cell = env_cdf(e, x, y) - (x > 0u ? env_cdf(e, x - 1u, y) : 0.0f);
+    const float sn = std::sin(v * PI);
+    return sn > 0.0f ? row * cell * float(cw * ch) / (2.0f * PI * PI * sn) : 0.0f;
+}
+V sample_env(const Ctx& c, Sampler& s) {
+    const Env& e = *c.env;
+    const uint32_t cw = e.cw, ch = e.ch;
+    float cx, cy;
+    s.rand2(cx, cy);
+    const uint32_t y = env_search(e, ch, ch, cy);
+    const uint32_t x = env_search(e, y, cw, cx);
+    float wx, wy;
+    s.rand2(wx, wy);
+    const float u = (float(x) + wx) / float(cw) + c.P.env_rotation / (2.0f * PI);
+    const float v = (float(y) + wy) / float(ch);
+    const float phi = (u - 0.5f) * 2.0f * PI;
+    const float theta = v * PI;
+    return v3(std::sin(theta) * std::sin(phi), std::cos(theta), -std::sin(theta) * std::cos(phi));
+}
+// sky (src/shaders.mjs:678-686): the environment map when there is one.
+V sky_at(const Ctx& c, V d) { return env_on(c) ? env_radiance(c, d) : sky(c.P, d); }
 
 // ---- materials (src/shaders.mjs:693-871) ----
 struct Mat {
@@ -442,11 +530,12 @@ Bs sample_bsdf(const Mat& m, V base, const Surf& sf, V wo, Sampler& s) {
 }
 
 // ---- lights (src/shaders.mjs:877-1018); no environment map ----
-uint32_t choices(const Params& P) { return P.light_count + (P.sun_on != 0u ? 1u : 0u); }
+// light_choices (src/shaders.mjs:877-879): the lights, the sun, then the environment.
+uint32_t choices(const Ctx& c) { return c.P.light_count + (c.P.sun_on != 0u ? 1u : 0u) + (env_on(c) ? 1u : 0u); }
 float light_cdf(const Ctx& c, uint32_t l) { return bitsf(c.lights[c.P.light_count + c.P.volume_count + l]); }
 float light_chance(const Ctx& c, uint32_t l) {
     const float below = l > 0u ? light_cdf(c, l - 1u) : 0.0f;
-    return (light_cdf(c, l) - below) * float(c.P.light_count) / float(choices(c.P));
+    return (light_cdf(c, l) - below) * float(c.P.light_count) / float(choices(c));
 }
 float sphere_omc(float r, float d2) {
     const float x = wmin(r * r / d2, 1.0f);
@@ -465,10 +554,16 @@ struct Ls {
 };
 Ls sample_light(Ctx& c, V p, Sampler& s) {
     const Params& P = c.P;
-    const uint32_t ch = choices(P);
+    const uint32_t ch = choices(c);
     const float x = s.rand() * float(ch);
     uint32_t pick = std::min(uint32_t(x), ch - 1u);
     float chance = 1.0f / float(ch);
+    if (env_on(c) && pick == P.light_count + (P.sun_on != 0u ? 1u : 0u)) {
+        const V wi = sample_env(c, s);
+        const float pdf = env_pdf(c, wi);
+        if (pdf <= 0.0f) return {vs(0), 0.0f, vs(0), 0.0f};
+        return {wi, INF, env_radiance(c, wi), chance * pdf};
+    }
     if (P.sun_on != 0u && pick == P.light_count) {
         const V wi = sample_cone(vf(P.sun_dir), P.sun_omc, s);
         return {wi, INF, vf(P.sun_radiance), chance / (2.0f * PI * P.sun_omc)};
@@ -632,7 +727,7 @@ V radiance(Ctx& c, float px, float py, Sampler& s, float spectrum_u, V& g_albedo
     float last_pdf = 0.0f;
     bool last_delta = true;
     V last_p = o;
-    const uint32_t ch = choices(P);
+    const uint32_t ch = choices(c);
     float wavelength = 0.0f;
     bool caustic = false, diffuse_seen = false;
 
@@ -706,7 +801,10 @@ V radiance(Ctx& c, float px, float py, Sampler& s, float spectrum_u, V& g_albedo
 
         if (hit.prim == NONE) {
             if (!guided) g_albedo = throughput;
-            result = result + throughput * sky(P, d);
+            // An environment is sampled directly too: weigh it against that.
+            float sky_weight = 1.0f;
+            if (env_on(c) && !last_delta) sky_weight = power_heuristic(last_pdf, env_pdf(c, d) / float(ch));
+            result = result + throughput * sky_at(c, d) * sky_weight;
             if (in_sun(P, d) && !(caustic && last_delta)) {
                 float w = 1.0f;
                 if (!last_delta) w = power_heuristic(last_pdf, 1.0f / (float(ch) * 2.0f * PI * P.sun_omc));
@@ -785,7 +883,7 @@ V inspect(Ctx& c, float px, float py) {
                      vf(P.cam_up) * (ndcy * P.tan_half_fov));
     const V o = vf(P.cam_pos);
     const HitR hit = trace(c, o, d, INF, false);
-    if (hit.prim == NONE) return P.view == 1u ? sky(P, d) : vs(0.0f);
+    if (hit.prim == NONE) return P.view == 1u ? sky_at(c, d) : vs(0.0f);
     const Surf sf = surface(c, o, d, hit);
     const Mat m = material(c, sf.material);
     if (P.view == 1u) {
@@ -1076,10 +1174,11 @@ V gather(const Params& P, const PhotonMap& map, const Surf& s, const Mat& m, V b
 
 }  // namespace
 
-extern "C" void ro_render(const void* prims, const void* nodes, const void* materials, const float* attributes,
-                          const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0, uint32_t y0,
-                          uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out,
-                          uint64_t* counters, int threads) {
+namespace {
+void render_impl(const void* prims, const void* nodes, const void* materials, const float* attributes,
+                 const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0, uint32_t y0,
+                 uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out, uint64_t* counters,
+                 int threads, const Env* env) {
     Params P;
     std::memcpy(&P, params208, sizeof P);
     std::atomic<uint32_t> next{0};
@@ -1088,6 +1187,7 @@ extern "C" void ro_render(const void* prims, const void* nodes, const void* mate
     auto worker = [&] {
         Ctx c{static_cast<const uint8_t*>(prims), static_cast<const uint8_t*>(nodes),
               static_cast<const float*>(materials), attributes, lights, P};
+        c.env = env;
         for (;;) {
             const uint32_t k0 = next.fetch_add(64);
             if (k0 >= n) break;
@@ -1161,6 +1261,25 @@ extern "C" void ro_render(const void* prims, const void* nodes, const void* mate
         counters[6] = tot_rc;
         counters[7] = tot_rs;
     }
+}
+}  // namespace
+
+extern "C" void ro_render(const void* prims, const void* nodes, const void* materials, const float* attributes,
+                          const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0, uint32_t y0,
+                          uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out,
+                          uint64_t* counters, int threads) {
+    render_impl(prims, nodes, materials, attributes, lights, params208, seed_hash, x0, y0, rw, rh, accum_out,
+                albedo_out, normal_out, counters, threads, nullptr);
+}
+
+extern "C" void ro_render_env(const void* prims, const void* nodes, const void* materials, const float* attributes,
+                              const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0,
+                              uint32_t y0, uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out,
+                              float* normal_out, uint64_t* counters, int threads, const uint16_t* env_rgba16f,
+                              uint32_t env_w, uint32_t env_h, const float* table, uint32_t cw, uint32_t ch) {
+    const Env env{env_rgba16f, env_w, env_h, table, cw, ch};
+    render_impl(prims, nodes, materials, attributes, lights, params208, seed_hash, x0, y0, rw, rh, accum_out,
+                albedo_out, normal_out, counters, threads, &env);
 }
 
 // light_trace for photons 0..photons-1 of a frame (src/shaders.mjs:1628-1814):

@@ -157,6 +157,15 @@ def _gpu_name() -> str:
         return "gpu"
 
 
+def environment_arrays(env):
+    """What Renderer uploads for an environment map (src/Renderer.mjs:723-760):
+    its pixels as RGBA half floats (alpha 1) and its importance table."""
+    rgba = np.empty(env.width * env.height * 4, dtype=np.uint16)
+    rgba.reshape(-1, 4)[:, :3] = to_half_array(env.data.reshape(-1)).reshape(-1, 3)
+    rgba.reshape(-1, 4)[:, 3] = to_half(1.0)
+    return rgba, env.importance()
+
+
 def emitters_block(light_powers, light_count, deltas, sky):
     """Renderer.#writeEmitters (src/Renderer.mjs:670-717): a header (sources,
     targets, the sun's start distance, the targets' circles' total area),
@@ -638,12 +647,7 @@ class Renderer:
 
     def _upload_environment(self, env):
         if env is not None:
-            rgba = np.empty(env.width * env.height * 4, dtype=np.uint16)
-            src = env.data.reshape(-1, 3)
-            flat = to_half_array(src.reshape(-1)).reshape(-1, 3)
-            rgba.reshape(-1, 4)[:, :3] = flat
-            rgba.reshape(-1, 4)[:, 3] = to_half(1.0)
-            table = env.importance()
+            rgba, table = environment_arrays(env)
             check(lib().raymond_upload_environment(self._h, ptr(rgba), env.width, env.height, ptr(table["data"]),
                                                    table["width"], table["height"] + 1), self._h)
         self._uploaded_environment = env

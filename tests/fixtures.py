@@ -257,21 +257,27 @@ def pixel_hits(scene, camera, size):
 def oracle_trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoise=False, caustics=True, seed=0):
     """trace() with the oracle (the trace shader restated, on the CPU) making
     the image instead of the GPU, frame by frame as the renderer does (up
-    to 16 samples a frame, no firefly clamp): path tracing, and when the
+    to 16 samples a frame, no firefly clamp): path tracing (under an
+    environment map as uploaded, when the sky has one), and when the
     scene has mirrors or glass for light to be focused by and `caustics`
     is on, the same frame's light tracing with its splats and the photon
     map's gather through mirrors and glass (photon radius shrinking frame
     by frame); then the oracle's à-trous denoiser on the guides if asked."""
-    from raymond_gb300.renderer import PHOTON_CAPACITY, delta_objects, emitters_block, light_table, params_block
+    from raymond_gb300.renderer import (PHOTON_CAPACITY, delta_objects, emitters_block, environment_arrays,
+                                        light_table, params_block)
 
-    assert view == "color"
     scene, cam_opts = SCENES[name](arg)
     camera = Camera(**cam_opts)
     packed = scene.pack()
-    # The oracle's path tracer restates neither textures nor environment maps.
-    assert not packed.textures and not packed.normalMaps and scene.sky.environment is None, name
+    # The oracle's path tracer does not restate textures.
+    assert not packed.textures and not packed.normalMaps, name
+    env = scene.sky.environment
+    environment = None
+    if env is not None:
+        rgba, table = environment_arrays(env)
+        environment = (rgba, env.width, env.height, table)
     words, powers = light_table(packed)
-    deltas = delta_objects(scene) if caustics else None
+    deltas = delta_objects(scene) if caustics and view == "color" else None
     emitters = emitters_block(powers, len(powers), deltas, scene.sky) if deltas else None
     acc = np.zeros((size, size, 4), np.float32)
     alb = np.zeros((size, size, 4), np.float32)
@@ -280,9 +286,9 @@ def oracle_trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoi
     done = 0
     while done < spp:
         params = params_block(scene, camera, size, size, light_count=len(powers), volume_count=len(packed.volumes),
-                              max_bounces=bounces, firefly_clamp=0.0, samples=done, spp=spf, denoise=False,
-                              caustics=emitters is not None, deltas=deltas)
-        o = oracle.render(packed, words, params, seed_hash=seed)
+                              max_bounces=bounces, view=view, firefly_clamp=0.0, samples=done, spp=spf,
+                              denoise=False, caustics=emitters is not None, deltas=deltas)
+        o = oracle.render(packed, words, params, seed_hash=seed, environment=environment)
         acc += o["accum"]
         alb += o["albedo"]
         nrm += o["normal"]
