@@ -39,9 +39,9 @@ def lib():
         _lib.ro_surface_double.argtypes = [P, P, U32, P, P, D, D, D, P]
         _lib.ro_render.restype = None
         _lib.ro_render.argtypes = [P, P, P, P, P, P, U32, U32, U32, U32, U32, P, P, P, P, I]
-        _lib.ro_render_env.restype = None
-        _lib.ro_render_env.argtypes = [P, P, P, P, P, P, U32, U32, U32, U32, U32, P, P, P, P, I, P, U32, U32, P, U32,
-                                       U32]
+        _lib.ro_render_scene.restype = None
+        _lib.ro_render_scene.argtypes = [P, P, P, P, P, P, U32, U32, U32, U32, U32, P, P, P, P, I, P, U32, U32, P, U32,
+                                         U32, P, U32, U32, P, U32, U32]
         _lib.ro_light_trace.restype = U32
         _lib.ro_light_trace.argtypes = [P, P, P, P, P, P, P, U32, U32, P, P, I]
         _lib.ro_photon_gather.restype = None
@@ -123,12 +123,14 @@ def bytes_per_ray(inner: np.ndarray, tested: np.ndarray) -> np.ndarray:
     return 32 * (1 + 2 * inner.astype(np.int64)) + 64 * tested.astype(np.int64)
 
 
-def render(packed, lights_words, params: bytes, region=None, seed_hash=0, nthreads=None, environment=None):
+def render(packed, lights_words, params: bytes, region=None, seed_hash=0, nthreads=None, environment=None,
+           textures=None, normal_maps=None):
     """One frame of the trace shader's main() restated in f32 over a region
     (x0, y0, w, h) of the image: dict accum/albedo/normal (h×w×4 sums) and
-    counters (algorithmic bytes, rays, surface hits, paths). `environment`:
-    (RGBA half floats, width, height, importance table dict) as the
-    renderer uploads an environment map, or None."""
+    counters (algorithmic bytes, rays, surface hits, paths). As the renderer
+    uploads them, or None: `environment` (RGBA half floats, width, height,
+    importance table dict), `textures` and `normal_maps` (RGBA bytes of
+    every layer, width, height)."""
     import struct
     width, height = struct.unpack_from("<2I", params, 160)
     x0, y0, rw, rh = region if region else (0, 0, width, height)
@@ -141,13 +143,23 @@ def render(packed, lights_words, params: bytes, region=None, seed_hash=0, nthrea
     attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
     args = (_p(packed.primitives), _p(packed.nodes), _p(packed.materials), _p(attrs), _p(words), _p(pbuf),
             seed_hash, x0, y0, rw, rh, _p(accum), _p(alb), _p(nrm), _p(counters), nthreads or threads())
-    if environment is None:
+    if environment is None and textures is None and normal_maps is None:
         lib().ro_render(*args)
     else:
-        rgba, ew, eh, table = environment
-        rgba = np.ascontiguousarray(rgba, dtype=np.uint16)
-        tdata = np.ascontiguousarray(table["data"], dtype=np.float32)
-        lib().ro_render_env(*args, _p(rgba), ew, eh, _p(tdata), table["width"], table["height"])
+        keep = []  # the arrays the call reads, alive until it returns
+
+        def arr(a, dtype):
+            keep.append(np.ascontiguousarray(a, dtype=dtype))
+            return _p(keep[-1])
+
+        env = (None, 0, 0, None, 0, 0)
+        if environment is not None:
+            rgba, ew, eh, table = environment
+            env = (arr(rgba, np.uint16), ew, eh, arr(table["data"], np.float32), table["width"], table["height"])
+        tex = (None, 0, 0) if textures is None else (arr(textures[0], np.uint8), textures[1], textures[2])
+        nmaps = (None, 0, 0) if normal_maps is None else (arr(normal_maps[0], np.uint8), normal_maps[1],
+                                                          normal_maps[2])
+        lib().ro_render_scene(*args, *env, *tex, *nmaps)
     return {"accum": accum.reshape(rh, rw, 4), "albedo": alb.reshape(rh, rw, 4), "normal": nrm.reshape(rh, rw, 4),
             "bytes": int(counters[0]), "rays": int(counters[1]), "hits": int(counters[2]), "paths": int(counters[3]),
             "trav_closest": int(counters[4]), "trav_shadow": int(counters[5]), "rays_closest": int(counters[6]),

@@ -75,13 +75,16 @@ void ro_render(const void* prims, const void* nodes, const void* materials, cons
                const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0, uint32_t y0,
                uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out,
                uint64_t* counters, int threads);
-// ro_render with an environment map as the renderer uploads it: RGBA half
-// floats (env_w × env_h) and its importance table (cw × (ch + 1) floats).
-void ro_render_env(const void* prims, const void* nodes, const void* materials, const float* attributes,
-                   const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0, uint32_t y0,
-                   uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out,
-                   uint64_t* counters, int threads, const uint16_t* env_rgba16f, uint32_t env_w, uint32_t env_h,
-                   const float* table, uint32_t cw, uint32_t ch);
+// ro_render with what the renderer uploads beside the packed scene, each
+// optional (null): an environment map (RGBA half floats, env_w × env_h,
+// and its importance table, cw × (ch + 1) floats), the colour and emission
+// texture array and the normal-map array (layers of w × h RGBA bytes).
+void ro_render_scene(const void* prims, const void* nodes, const void* materials, const float* attributes,
+                     const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0, uint32_t y0,
+                     uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out,
+                     uint64_t* counters, int threads, const uint16_t* env_rgba16f, uint32_t env_w, uint32_t env_h,
+                     const float* table, uint32_t cw, uint32_t ch, const uint8_t* tex, uint32_t tex_w,
+                     uint32_t tex_h, const uint8_t* nrm, uint32_t nrm_w, uint32_t nrm_h);
 
 // ---- light tracing and photon mapping (src/shaders.mjs:1425-1831) ----
 // One frame's photons 0..photons-1: fixed-point splats added to `splats`

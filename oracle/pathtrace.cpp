@@ -6,8 +6,8 @@
 // arithmetic follows the WGSL expression by expression (compiled without
 // contraction), with
 // the math library's sqrt/sin/cos/exp/log/pow/atan2/acos called, never
-// re-implemented. Environment maps are restated (ro_render_env); textured
-// materials and normal maps are not.
+// re-implemented. Environment maps, textures and normal maps are read as
+// the renderer uploads them (ro_render_scene).
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -162,6 +162,12 @@ struct Env {
     uint32_t cw, ch;
 };
 
+// A texture array as the renderer uploads it: layers of w × h RGBA bytes.
+struct Tex {
+    const uint8_t* data;
+    uint32_t w, h;
+};
+
 struct Ctx {
     const uint8_t* prims;
     const uint8_t* nodes;
@@ -174,6 +180,8 @@ struct Ctx {
     uint64_t bytes = 0, rays = 0, hits = 0;
     uint64_t trav_closest = 0, trav_shadow = 0, rays_closest = 0, rays_shadow = 0;
     const Env* env = nullptr;
+    const Tex* textures = nullptr;     // colour and emission textures (sRGB)
+    const Tex* normal_maps = nullptr;  // normal maps (plain numbers)
 
     const float* pf(uint32_t i) const { return reinterpret_cast<const float*>(prims + size_t(i) * 64); }
     const uint32_t* pu(uint32_t i) const { return reinterpret_cast<const uint32_t*>(prims + size_t(i) * 64); }
@@ -221,12 +229,56 @@ void sphere_uv(V n, const float* p, float& u, float& v) {
     v = std::acos(clampf(dot(n, north), -1.0f, 1.0f)) / PI;
 }
 
-// surface (src/shaders.mjs:460-569), without normal maps.
+// ---- textures: bilinear with repeat, as the reference's sampler does ----
+float srgb_to_linear(uint8_t b) {
+    static const struct Table {
+        float v[256];
+        Table() {
+            for (int i = 0; i < 256; ++i) {
+                const double x = i / 255.0;
+                v[i] = float(x <= 0.04045 ? x / 12.92 : std::pow((x + 0.055) / 1.055, 2.4));
+            }
+        }
+    } table;
+    return table.v[b];
+}
+V texel(const Tex& t, uint32_t layer, int x, int y, bool srgb) {
+    const int xi = ((x % int(t.w)) + int(t.w)) % int(t.w);
+    const int yi = ((y % int(t.h)) + int(t.h)) % int(t.h);
+    const uint8_t* q = t.data + ((size_t(layer) * t.h + yi) * t.w + xi) * 4;
+    if (srgb) return v3(srgb_to_linear(q[0]), srgb_to_linear(q[1]), srgb_to_linear(q[2]));
+    return v3(q[0] / 255.0f, q[1] / 255.0f, q[2] / 255.0f);
+}
+V sample_texture(const Tex& t, uint32_t layer, float u, float v, bool srgb) {
+    const float x = u * float(t.w) - 0.5f, y = v * float(t.h) - 0.5f;
+    const float fx0 = std::floor(x), fy0 = std::floor(y);
+    const float fx = x - fx0, fy = y - fy0;
+    const int x0 = int(fx0), y0 = int(fy0);
+    return texel(t, layer, x0, y0, srgb) * ((1.0f - fx) * (1.0f - fy)) +
+           texel(t, layer, x0 + 1, y0, srgb) * (fx * (1.0f - fy)) +
+           texel(t, layer, x0, y0 + 1, srgb) * ((1.0f - fx) * fy) +
+           texel(t, layer, x0 + 1, y0 + 1, srgb) * (fx * fy);
+}
+
+// bump (src/shaders.mjs:582-594): n tilted by a normal-map texel.
+V bump(V n, V ng, V tangent, V up, V t, float strength) {
+    V right = tangent - n * dot(n, tangent);
+    if (len(right) < 1e-9f) return n;
+    right = norm(right);
+    V above = cross(n, right);
+    if (dot(above, up) < 0.0f) above = -above;
+    const V tilted =
+        norm(right * ((t.x * 2.0f - 1.0f) * strength) + above * ((t.y * 2.0f - 1.0f) * strength) + n * (t.z * 2.0f - 1.0f));
+    return dot(tilted, ng) > 0.0f ? tilted : n;
+}
+
+// surface (src/shaders.mjs:460-569), with the texture's tangent frame and
+// normal maps.
 Surf surface(Ctx& c, V o, V d, const HitR& hit) {
     const float* p = c.pf(hit.prim);
     const uint32_t* pu = c.pu(hit.prim);
     const V point = o + d * hit.t;
-    V ng, ns;
+    V ng, ns, tangent = vs(0.0f), up = vs(0.0f);
     float u = 0, v = 0;
     c.hits++;
     c.bytes += 64 + 96;  // the primitive record and its material
@@ -235,12 +287,17 @@ Surf surface(Ctx& c, V o, V d, const HitR& hit) {
             ng = norm(point - vf(p + 4));
             ns = ng;
             sphere_uv(ng, p, u, v);
+            tangent = cross(vf(p + 12), ng);
+            if (len(tangent) < 1e-6f) tangent = vf(p + 8);
+            up = cross(ng, tangent);
             break;
         case 1:
             ng = norm(cross(vf(p + 8), vf(p + 12)));
             ns = ng;
             u = hit.u;
             v = 1.0f - hit.v;
+            tangent = vf(p + 8);
+            up = vf(p + 12);
             break;
         case 2: {
             const V r0 = vf(p + 4), r1 = vf(p + 8), r2 = vf(p + 12);
@@ -251,14 +308,20 @@ Surf surface(Ctx& c, V o, V d, const HitR& hit) {
                 ng = r0 * sgn(lp.x);
                 u = (1.0f - sgn(lp.x) * lp.z) * half.z;
                 v = (1.0f - lp.y) * half.y;
+                tangent = r2 * -sgn(lp.x);
+                up = r1;
             } else if (a.y >= a.z) {
                 ng = r1 * sgn(lp.y);
                 u = (1.0f + lp.x) * half.x;
                 v = (1.0f + sgn(lp.y) * lp.z) * half.z;
+                tangent = r0;
+                up = r2 * -sgn(lp.y);
             } else {
                 ng = r2 * sgn(lp.z);
                 u = (1.0f + sgn(lp.z) * lp.x) * half.x;
                 v = (1.0f - lp.y) * half.y;
+                tangent = r0 * sgn(lp.z);
+                up = r1;
             }
             ng = norm(ng);
             ns = ng;
@@ -270,6 +333,7 @@ Surf surface(Ctx& c, V o, V d, const HitR& hit) {
             ns = ng;
             u = hit.u;
             v = hit.v;
+            float du1x = 1.0f, du1y = 0.0f, du2x = 0.0f, du2y = 1.0f;
             if (pu[3] != NONE) {
                 c.bytes += 64;  // the attribute block
                 const float* A = c.attrs + size_t(pu[3]) * 4;
@@ -282,9 +346,27 @@ Surf surface(Ctx& c, V o, V d, const HitR& hit) {
                 if (flags & 2u) {
                     u = A[3] * w + A[7] * hit.u + A[11] * hit.v;
                     v = A[12] * w + A[13] * hit.u + A[14] * hit.v;
+                    const float t1x = A[7] - A[3], t1y = A[13] - A[12];
+                    const float t2x = A[11] - A[3], t2y = A[14] - A[12];
+                    if (std::fabs(t1x * t2y - t2x * t1y) > 1e-12f) {
+                        du1x = t1x;
+                        du1y = t1y;
+                        du2x = t2x;
+                        du2y = t2y;
+                    }
                 }
             }
+            // How the position changes with u and v.
+            const float det = du1x * du2y - du2x * du1y;
+            tangent = (e1 * du2y - e2 * du1y) / det;
+            up = -((e2 * du1x - e1 * du2x) / det);
         }
+    }
+    const float* mm = c.mf(pu[1]);
+    const uint32_t nm = fbits(mm[16]);
+    if (c.normal_maps && nm != NONE) {
+        const V t = sample_texture(*c.normal_maps, nm, u * mm[14], v * mm[15], false);
+        ns = bump(ns, ng, tangent, up, t, mm[17]);
     }
     const bool front = dot(ng, d) < 0.0f;
     const float flip = front ? 1.0f : -1.0f;
@@ -393,10 +475,13 @@ struct Mat {
     float roughness;
     V checker;
     float checker_size, ior, dispersion, density, anisotropy;
+    uint32_t texture, emission_texture;
+    float scale_u, scale_v;
 };
 Mat material(const Ctx& c, uint32_t i) {
     const float* m = c.mf(i);
-    return {vf(m), c.mu(i, 3), vf(m + 4), m[7], vf(m + 8), m[11], m[12], m[19], m[20], m[21]};
+    return {vf(m),  c.mu(i, 3), vf(m + 4),   m[7],        vf(m + 8), m[11], m[12],
+            m[19], m[20],      m[21], c.mu(i, 13), c.mu(i, 18), m[14], m[15]};
 }
 V albedo(const Mat& m, V p) {
     V col = m.color;
@@ -409,6 +494,16 @@ V albedo(const Mat& m, V p) {
     return col;
 }
 bool is_delta(const Mat& m) { return m.kind == 3 || (m.kind == 1 && m.roughness < 0.01f); }
+// albedo and emitted (src/shaders.mjs:693-712) at texture coordinate (u, v).
+V albedo_uv(const Ctx& c, const Mat& m, V p, float u, float v) {
+    const V col = albedo(m, p);
+    if (!c.textures || m.texture == NONE) return col;
+    return col * sample_texture(*c.textures, m.texture, u * m.scale_u, v * m.scale_v, true);
+}
+V emitted(const Ctx& c, const Mat& m, float u, float v) {
+    if (!c.textures || m.emission_texture == NONE) return m.emission;
+    return m.emission * sample_texture(*c.textures, m.emission_texture, u * m.scale_u, v * m.scale_v, true);
+}
 float ggx_alpha2(float r) {
     const float a = wmax(r * r, 0.002f);
     return a * a;
@@ -594,7 +689,7 @@ Ls sample_light(Ctx& c, V p, Sampler& s) {
         const float area = len(cr);
         const float cos_l = -dot(wi, cr / area);
         if (cos_l <= 0.0f) return {vs(0), 0.0f, vs(0), 0.0f};
-        return {wi, dist, m.emission, chance * d2 / (cos_l * area)};
+        return {wi, dist, emitted(c, m, a, 1.0f - b), chance * d2 / (cos_l * area)};
     }
     const V to = vf(pr + 4) - p;
     const float d2 = dot(to, to);
@@ -602,8 +697,15 @@ Ls sample_light(Ctx& c, V p, Sampler& s) {
     if (d2 <= r * r) return {vs(0), 0.0f, vs(0), 0.0f};
     const float omc = sphere_omc(r, d2);
     const V wi = sample_cone(to / std::sqrt(d2), omc, s);
-    return {wi, dot(to, wi) - std::sqrt(wmax(dot(to, wi) * dot(to, wi) - (d2 - r * r), 0.0f)), m.emission,
-            chance / (2.0f * PI * omc)};
+    const float b = dot(to, wi);
+    const float dist = b - std::sqrt(wmax(b * b - (d2 - r * r), 0.0f));
+    V e = m.emission;
+    if (c.textures && m.emission_texture != NONE) {
+        float u, v;
+        sphere_uv(norm(p + wi * dist - vf(pr + 4)), pr, u, v);
+        e = emitted(c, m, u, v);
+    }
+    return {wi, dist, e, chance / (2.0f * PI * omc)};
 }
 float light_pdf(const Ctx& c, uint32_t prim, V p, V wi, float t) {
     const float* pr = c.pf(prim);
@@ -818,7 +920,7 @@ V radiance(Ctx& c, float px, float py, Sampler& s, float spectrum_u, V& g_albedo
         travelled += hit.t;
         if (!guided && (m.kind == 4 || !is_delta(m) || depth == P.max_bounces)) {
             guided = true;
-            g_albedo = throughput * (m.kind == 4 ? vs(1.0f) : albedo(m, sf.p));
+            g_albedo = throughput * (m.kind == 4 ? vs(1.0f) : albedo_uv(c, m, sf.p, sf.u, sf.v));
             g_normal[0] = sf.n.x;
             g_normal[1] = sf.n.y;
             g_normal[2] = sf.n.z;
@@ -828,7 +930,7 @@ V radiance(Ctx& c, float px, float py, Sampler& s, float spectrum_u, V& g_albedo
             !(caustic && last_delta && sf.light != NONE)) {
             float w = 1.0f;
             if (!last_delta && sf.light != NONE) w = power_heuristic(last_pdf, light_pdf(c, hit.prim, last_p, d, hit.t));
-            result = result + throughput * m.emission * w;
+            result = result + throughput * emitted(c, m, sf.u, sf.v) * w;
         }
         if (m.kind == 4) break;
         if (!is_delta(m)) {
@@ -837,7 +939,7 @@ V radiance(Ctx& c, float px, float py, Sampler& s, float spectrum_u, V& g_albedo
         }
         if (depth == P.max_bounces) break;
 
-        const V base = albedo(m, sf.p);
+        const V base = albedo_uv(c, m, sf.p, sf.u, sf.v);
         const V wo = -d;
         if (!is_delta(m) && ch > 0u) {
             const Ls ls = sample_light(c, sf.p, s);
@@ -887,8 +989,11 @@ V inspect(Ctx& c, float px, float py) {
     const Surf sf = surface(c, o, d, hit);
     const Mat m = material(c, sf.material);
     if (P.view == 1u) {
-        if (m.kind == 4) return m.emission / wmax(wmax(m.emission.x, m.emission.y), wmax(m.emission.z, 1.0f));
-        return albedo(m, sf.p);
+        if (m.kind == 4) {
+            const V e = emitted(c, m, sf.u, sf.v);
+            return e / wmax(wmax(e.x, e.y), wmax(e.z, 1.0f));
+        }
+        return albedo_uv(c, m, sf.p, sf.u, sf.v);
     }
     if (P.view == 2u) return sf.n;
     return vs(hit.t);
@@ -1032,7 +1137,7 @@ void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t
         const uint32_t* pu = c.pu(prim_index);
         const Mat m = material(c, pu[1]);
         V n;
-        float area;
+        float area, eu = 0.0f, ev = 0.0f;
         if (pu[0] == 1u) {  // QUAD
             const float a = sm.rand();
             const float b = sm.rand();
@@ -1040,6 +1145,8 @@ void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t
             const V cr = cross(vf(pf + 8), vf(pf + 12));
             area = len(cr);
             n = cr / area;
+            eu = a;
+            ev = 1.0f - b;
         } else {
             const float z = 1.0f - 2.0f * sm.rand();
             const float r = std::sqrt(wmax(0.0f, 1.0f - z * z));
@@ -1047,6 +1154,7 @@ void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t
             n = v3(r * std::cos(phi), z, r * std::sin(phi));
             o = vf(pf + 4) + n * pf[7];
             area = 4.0f * PI * pf[7] * pf[7];
+            sphere_uv(n, pf, eu, ev);
         }
         float cones = 0.0f;
         bool inside = false;
@@ -1080,10 +1188,10 @@ void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t
             }
             const float cos_out = dot(d, n);
             if (cos_out <= 0.0f) return;
-            beta = m.emission * (cos_out * area * 2.0f * PI * cones) / (within * chance * float(photons));
+            beta = emitted(c, m, eu, ev) * (cos_out * area * 2.0f * PI * cones) / (within * chance * float(photons));
         } else {
             d = cosine_hemisphere(n, sm);
-            beta = m.emission * (PI * area) / (chance * float(photons));
+            beta = emitted(c, m, eu, ev) * (PI * area) / (chance * float(photons));
         }
         o = o + n * (1e-4f * wmax(1.0f, wmax(std::fabs(o.x), wmax(std::fabs(o.y), std::fabs(o.z)))));
     }
@@ -1097,7 +1205,7 @@ void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t
         const Surf s = surface(c, o, d, hit);
         const Mat m = material(c, s.material);
         if (m.kind == 4) return;
-        const V base = albedo(m, s.p);
+        const V base = albedo_uv(c, m, s.p, s.u, s.v);
         if (!is_delta(m)) {
             if (bounces > 0u) {
                 splat(c, s, m, base, d, beta * carried, sm, splats);
@@ -1178,7 +1286,7 @@ namespace {
 void render_impl(const void* prims, const void* nodes, const void* materials, const float* attributes,
                  const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0, uint32_t y0,
                  uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out, uint64_t* counters,
-                 int threads, const Env* env) {
+                 int threads, const Env* env, const Tex* textures, const Tex* normal_maps) {
     Params P;
     std::memcpy(&P, params208, sizeof P);
     std::atomic<uint32_t> next{0};
@@ -1188,6 +1296,8 @@ void render_impl(const void* prims, const void* nodes, const void* materials, co
         Ctx c{static_cast<const uint8_t*>(prims), static_cast<const uint8_t*>(nodes),
               static_cast<const float*>(materials), attributes, lights, P};
         c.env = env;
+        c.textures = textures;
+        c.normal_maps = normal_maps;
         for (;;) {
             const uint32_t k0 = next.fetch_add(64);
             if (k0 >= n) break;
@@ -1269,17 +1379,21 @@ extern "C" void ro_render(const void* prims, const void* nodes, const void* mate
                           uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out, float* normal_out,
                           uint64_t* counters, int threads) {
     render_impl(prims, nodes, materials, attributes, lights, params208, seed_hash, x0, y0, rw, rh, accum_out,
-                albedo_out, normal_out, counters, threads, nullptr);
+                albedo_out, normal_out, counters, threads, nullptr, nullptr, nullptr);
 }
 
-extern "C" void ro_render_env(const void* prims, const void* nodes, const void* materials, const float* attributes,
-                              const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0,
-                              uint32_t y0, uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out,
-                              float* normal_out, uint64_t* counters, int threads, const uint16_t* env_rgba16f,
-                              uint32_t env_w, uint32_t env_h, const float* table, uint32_t cw, uint32_t ch) {
+extern "C" void ro_render_scene(const void* prims, const void* nodes, const void* materials, const float* attributes,
+                                const uint32_t* lights, const void* params208, uint32_t seed_hash, uint32_t x0,
+                                uint32_t y0, uint32_t rw, uint32_t rh, float* accum_out, float* albedo_out,
+                                float* normal_out, uint64_t* counters, int threads, const uint16_t* env_rgba16f,
+                                uint32_t env_w, uint32_t env_h, const float* table, uint32_t cw, uint32_t ch,
+                                const uint8_t* tex, uint32_t tex_w, uint32_t tex_h, const uint8_t* nrm,
+                                uint32_t nrm_w, uint32_t nrm_h) {
     const Env env{env_rgba16f, env_w, env_h, table, cw, ch};
+    const Tex t{tex, tex_w, tex_h}, n{nrm, nrm_w, nrm_h};
     render_impl(prims, nodes, materials, attributes, lights, params208, seed_hash, x0, y0, rw, rh, accum_out,
-                albedo_out, normal_out, counters, threads, &env);
+                albedo_out, normal_out, counters, threads, env_rgba16f ? &env : nullptr, tex ? &t : nullptr,
+                nrm ? &n : nullptr);
 }
 
 // light_trace for photons 0..photons-1 of a frame (src/shaders.mjs:1628-1814):
@@ -1367,7 +1481,7 @@ extern "C" void ro_photon_gather(const void* prims, const void* nodes, const voi
                     const Surf s = surface(c, o, d, hit);
                     const Mat m = material(c, s.material);
                     if (m.kind == 4) break;
-                    const V base = albedo(m, s.p);
+                    const V base = albedo_uv(c, m, s.p, s.u, s.v);
                     if (!is_delta(m)) {
                         if (depth > 0u) {
                             const V light = throughput * gather(P, map, s, m, base, -d);

@@ -157,6 +157,15 @@ def _gpu_name() -> str:
         return "gpu"
 
 
+def texture_array(textures, srgb):
+    """A texture array as Renderer uploads one (src/Renderer.mjs:637-661):
+    every texture resized to the largest width and height (at most 2048),
+    as colour (sRGB) or as plain numbers; (RGBA bytes, width, height)."""
+    w = min(2048, max(t.width for t in textures))
+    h = min(2048, max(t.height for t in textures))
+    return np.concatenate([t.resized(w, h, srgb).data.reshape(-1) for t in textures]), w, h
+
+
 def environment_arrays(env):
     """What Renderer uploads for an environment map (src/Renderer.mjs:723-760):
     its pixels as RGBA half floats (alpha 1) and its importance table."""
@@ -640,9 +649,7 @@ class Renderer:
         for which, textures, srgb in ((0, packed.textures, True), (1, packed.normalMaps, False)):
             if not textures:
                 continue
-            w = min(2048, max(t.width for t in textures))
-            h = min(2048, max(t.height for t in textures))
-            data = np.concatenate([t.resized(w, h, srgb).data.reshape(-1) for t in textures])
+            data, w, h = texture_array(textures, srgb)
             check(lib().raymond_upload_textures(self._h, which, ptr(data), w, h, len(textures)), self._h)
 
     def _upload_environment(self, env):

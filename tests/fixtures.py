@@ -257,20 +257,20 @@ def pixel_hits(scene, camera, size):
 def oracle_trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoise=False, caustics=True, seed=0):
     """trace() with the oracle (the trace shader restated, on the CPU) making
     the image instead of the GPU, frame by frame as the renderer does (up
-    to 16 samples a frame, no firefly clamp): path tracing (under an
-    environment map as uploaded, when the sky has one), and when the
+    to 16 samples a frame, no firefly clamp): path tracing (with the
+    texture arrays and environment map as uploaded), and when the
     scene has mirrors or glass for light to be focused by and `caustics`
     is on, the same frame's light tracing with its splats and the photon
     map's gather through mirrors and glass (photon radius shrinking frame
     by frame); then the oracle's à-trous denoiser on the guides if asked."""
     from raymond_gb300.renderer import (PHOTON_CAPACITY, delta_objects, emitters_block, environment_arrays,
-                                        light_table, params_block)
+                                        light_table, params_block, texture_array)
 
     scene, cam_opts = SCENES[name](arg)
     camera = Camera(**cam_opts)
     packed = scene.pack()
-    # The oracle's path tracer does not restate textures.
-    assert not packed.textures and not packed.normalMaps, name
+    textures = texture_array(packed.textures, True) if packed.textures else None
+    normal_maps = texture_array(packed.normalMaps, False) if packed.normalMaps else None
     env = scene.sky.environment
     environment = None
     if env is not None:
@@ -279,6 +279,8 @@ def oracle_trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoi
     words, powers = light_table(packed)
     deltas = delta_objects(scene) if caustics and view == "color" else None
     emitters = emitters_block(powers, len(powers), deltas, scene.sky) if deltas else None
+    # The oracle's light tracer and photon map take no textures.
+    assert emitters is None or (textures is None and normal_maps is None), name
     acc = np.zeros((size, size, 4), np.float32)
     alb = np.zeros((size, size, 4), np.float32)
     nrm = np.zeros((size, size, 4), np.float32)
@@ -288,7 +290,8 @@ def oracle_trace(name, arg=None, spp=16, bounces=8, view="color", size=48, denoi
         params = params_block(scene, camera, size, size, light_count=len(powers), volume_count=len(packed.volumes),
                               max_bounces=bounces, view=view, firefly_clamp=0.0, samples=done, spp=spf,
                               denoise=False, caustics=emitters is not None, deltas=deltas)
-        o = oracle.render(packed, words, params, seed_hash=seed, environment=environment)
+        o = oracle.render(packed, words, params, seed_hash=seed, environment=environment, textures=textures,
+                          normal_maps=normal_maps)
         acc += o["accum"]
         alb += o["albedo"]
         nrm += o["normal"]
