@@ -7,9 +7,13 @@
 //
 // Parity status: the reference is JavaScript/WGSL and no JS engine exists on
 // either machine, so no executed reference output is available. The oracle is
-// pinned instead against every known answer the reference's own unit tests
-// hold for this path (tests/unit/bvh.test.mjs, scene.test.mjs,
-// camera.test.mjs, shaders.test.mjs), restated in tests/test_oracle_*.py.
+// pinned instead against every known answer the reference's own tests hold
+// for this path: its unit tests (tests/unit/bvh.test.mjs, scene.test.mjs,
+// camera.test.mjs, shaders.test.mjs, ...) restated in
+// tests/test_reference_*.py, and its browser tests' exact answers and
+// estimator agreements (tests/browser/app.test.mjs: furnaces, direct light,
+// environment, textures, caustics, denoiser) run on this oracle in
+// tests/test_oracle_*.py.
 // Byte-level parity of the BVH build with BVH.mjs is therefore pinned by
 // those invariants only ("parity unpinned" against executed reference code).
 //
