@@ -171,6 +171,42 @@ def oracle_sample(scene, params: bytes, size, rows_per_strip, strips, threads, d
     return out
 
 
+def caustics_cpu_sample(scene, camera, size, spp, bounces, threads, strips=16, rows=2):
+    """The oracle's frame of the caustics workload on a bounded sample: the
+    camera paths (leaving caustic paths to light tracing) on `strips` bands
+    of `rows` rows, the same fraction of the frame's light paths (splatted
+    and deposited), and the photon map's gather on the bands. Returns
+    (camera paths, light paths, seconds)."""
+    import numpy as np
+
+    import oracle
+    from raymond_gb300.renderer import delta_objects, emitters_block, light_table, params_block
+
+    packed = scene.pack()
+    words, powers = light_table(packed)
+    deltas = delta_objects(scene)
+    emitters = emitters_block(powers, len(powers), deltas, scene.sky)
+    block = bytearray(params_block(scene, camera, size, size, light_count=len(powers),
+                                   volume_count=len(packed.volumes), max_bounces=bounces, spp=spp,
+                                   caustics=emitters is not None, deltas=deltas))
+    f = np.frombuffer(block, dtype=np.float32)
+    f[48], f[49] = CAUSTICS_RADIUS, 2 * CAUSTICS_RADIUS  # the fixed radius the GPU run sets
+    params = bytes(block)
+    light_paths = CAUSTICS_LIGHT_PATHS * strips * rows // size
+    paths = 0
+    t0 = time.perf_counter()
+    for k in range(strips):
+        r = oracle.render(packed, words, params, region=(0, (k * size) // strips, size, rows), nthreads=threads)
+        paths += r["paths"]
+    if emitters is not None:
+        lt = oracle.light_trace(packed, words, params, emitters, CAUSTICS_LIGHT_PATHS, ids=(0, light_paths),
+                                nthreads=threads)
+        for k in range(strips):
+            oracle.photon_gather(packed, words, params, lt["photons"], rows=((k * size) // strips, rows),
+                                 nthreads=threads)
+    return paths, light_paths, time.perf_counter() - t0
+
+
 def params_for(scene, camera, size, spp, bounces):
     """The uniform block a renderer writes for frame 0 of this workload."""
     from raymond_gb300.renderer import light_table, params_block
@@ -543,6 +579,57 @@ def run_bvh(args):
     }
 
 
+def run_bvh_reference(args):
+    """The reference arm of the BVH line: the oracle's restatement of
+    BVH.build (src/BVH.mjs:57-234), single-threaded as the reference's is,
+    over the same 509,281 boxes."""
+    import numpy as np
+
+    import oracle
+    from raymond_gb300 import scene as scene_mod
+    from raymond_gb300 import scenes
+
+    captured = {}
+    native_build = scene_mod.BVH.build
+
+    def capture(mins, maxs, *a, **k):
+        captured["mins"], captured["maxs"] = np.array(mins, dtype=np.float64), np.array(maxs, dtype=np.float64)
+        return native_build(mins, maxs, *a, **k)
+
+    scene_mod.BVH.build = staticmethod(capture)
+    try:
+        scene, _, info = scenes.sphere_field()
+        scene.pack()
+    finally:
+        scene_mod.BVH.build = staticmethod(native_build)
+    mins, maxs = captured["mins"], captured["maxs"]
+    count = len(mins)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.bvh_build(mins, maxs)
+        times.append(time.perf_counter() - t0)
+    value = count / statistics.median(times) / 1e6
+    return {
+        "metric": "Mprims/s (BVH build)", "value": value, "unit": "Mprims/s", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(times), "higher_is_better": True,
+        "scaling": "strong", "vs_baseline": None, "dtype": "f64 build, f32 nodes",
+        "data": "synthetic (seeded mulberry32 scene)", "impl": "reference",
+        "config": {"workload": f"binned-SAH BVH of the sphere field's {count} primitive boxes, leaves of at most 4",
+                   "threads": 1},
+        "cpu_baseline": {"value": value, "unit": "Mprims/s", "cores": 1, "kind": "port",
+                         "sample": f"oracle BVH.build restatement over all {count} boxes, each step"},
+        "e2e": {"value": value, "unit": "Mprims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+REFERENCE_UNAVAILABLE = {
+    "batch": "the reference renders one scene per renderer; batched multi-scene frames have no CPU counterpart in it",
+    "denoise": "the reference has no learned denoiser",
+    "rmse": "the reference's CPU path to RMSE 0.01 at 1024x1024 would take hours on the host cores",
+}
+
+
 def run_rmse(args, local):
     """Time to RMSE ≤ 0.01 against a 16,384-spp render of the sphere field:
     the plain one-kernel path with the à-trous filter against the batched
@@ -664,31 +751,39 @@ def run_rmse(args, local):
 
 
 def run_reference(args, rank, world):
-    """The reference's CPU path (the shader's path tracer restated, on all host cores)."""
+    """The reference's CPU path (the shader's path tracer restated, on all
+    host cores; for caustics with its light tracer and photon map too)."""
     if rank != 0:
         return None
-    scene, camera, info = build_workload(args.size, args.spp, args.bounces)
+    caustics = args.workload == "caustics"
+    scene, camera, info = build_workload(args.size, args.spp, args.bounces, "caustics" if caustics else "field")
     params = params_for(scene, camera, args.size, args.spp, args.bounces)
     threads = os.cpu_count() or 1
     strips = 16
     rows = 2
     for _ in range(max(args.warmup, 0) and 1):
         oracle_sample(scene, params, args.size, 1, 1, threads)
-    times, paths = [], 0
+    times, paths, light = [], 0, 0
     for _ in range(args.steps):
-        p, dt, _, _ = oracle_sample(scene, params, args.size, rows, strips, threads)
+        if caustics:
+            p, light, dt = caustics_cpu_sample(scene, camera, args.size, args.spp, args.bounces, threads, strips, rows)
+        else:
+            p, dt, _, _ = oracle_sample(scene, params, args.size, rows, strips, threads)
         times.append(dt)
         paths += p
     value = paths / sum(times) / 1e6
     sample = f"{strips} bands of {rows} rows x {args.size} px, {args.spp} spp per step (1/{args.size // (strips * rows)} of a frame)"
+    if caustics:
+        sample += (f", with {light} of the frame's light paths splatted and deposited and the photon map "
+                   "(those photons only) gathered on the bands")
     return {
         "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32)",
         "impl": "reference",
-        "config": {"workload": WORKLOAD, "width": args.size, "height": args.size, "spp": args.spp,
-                   "bounces": args.bounces, "triangles": info["triangles"], "spheres": info["spheres"],
-                   "l2": "n/a (CPU)"},
+        "config": {"workload": CAUSTICS_WORKLOAD if caustics else WORKLOAD, "width": args.size, "height": args.size,
+                   "spp": args.spp, "bounces": args.bounces, "triangles": info["triangles"],
+                   "spheres": info.get("spheres"), "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": value, "unit": "Mpaths/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -795,8 +890,13 @@ def run_ours(args, rank, world, local):
         params = params_for(scene, camera, args.size, args.spp, args.bounces)
         paths_s, secs_s, bytes_per_path, rays_per_path, split = oracle_sample(scene, params, args.size, 1, 16, threads,
                                                                               detail=True)
-        # CPU baseline: the same port, a bounded sample (16 bands of 2 rows).
-        cpu_paths, cpu_s, _, _ = oracle_sample(scene, params, args.size, 2, 16, threads)
+        # CPU baseline: the same port, a bounded sample (16 bands of 2 rows;
+        # for caustics the same share of the light paths and of the gather).
+        if caustics:
+            cpu_paths, cpu_light, cpu_s = caustics_cpu_sample(scene, camera, args.size, args.spp, args.bounces,
+                                                              threads)
+        else:
+            cpu_paths, cpu_s, _, _ = oracle_sample(scene, params, args.size, 2, 16, threads)
         peak, peak_kind = measured_peak_hbm()
         wavefront = sum(ext_launches) > 0
         if wavefront:
@@ -835,7 +935,8 @@ def run_ours(args, rank, world, local):
                          "traversal_bytes_per_path": split},
             "cpu_baseline": {"value": cpu_paths / cpu_s / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
                              "sample": f"16 bands of 2 rows x {args.size} px at {args.spp} spp (1/32 of a frame)"
-                                       + (", camera paths only (the oracle does not restate light tracing)"
+                                       + (f", with {cpu_light} of the frame's light paths splatted and deposited "
+                                          "and the photon map (those photons only) gathered on the bands"
                                           if caustics else "")},
             "clocks": clock_info,
         }
@@ -947,6 +1048,10 @@ def main():
         torch.distributed.init_process_group("nccl")
     if args.impl == "reference" and args.workload == "primary":
         out = run_primary_reference(args, rank, world)
+    elif args.impl == "reference" and args.workload == "bvh":
+        out = run_bvh_reference(args) if rank == 0 else None
+    elif args.impl == "reference" and args.workload in REFERENCE_UNAVAILABLE:
+        out = {"impl": "reference", "unavailable": REFERENCE_UNAVAILABLE[args.workload]} if rank == 0 else None
     elif args.impl == "reference":
         out = run_reference(args, rank, world)
     elif args.workload == "batch":

@@ -43,9 +43,9 @@ def lib():
         _lib.ro_render_scene.argtypes = [P, P, P, P, P, P, U32, U32, U32, U32, U32, P, P, P, P, I, P, U32, U32, P, U32,
                                          U32, P, U32, U32, P, U32, U32]
         _lib.ro_light_trace.restype = U32
-        _lib.ro_light_trace.argtypes = [P, P, P, P, P, P, P, U32, U32, P, P, I]
+        _lib.ro_light_trace.argtypes = [P, P, P, P, P, P, P, U32, U32, U32, U32, P, P, I]
         _lib.ro_photon_gather.restype = None
-        _lib.ro_photon_gather.argtypes = [P, P, P, P, P, P, P, U32, U32, P, I]
+        _lib.ro_photon_gather.argtypes = [P, P, P, P, P, P, P, U32, U32, U32, U32, P, I]
         _lib.ro_denoise.restype = None
         _lib.ro_denoise.argtypes = [P, P, P, U32, U32, U32, P, I]
         _lib.ro_display.restype = None
@@ -166,27 +166,31 @@ def render(packed, lights_words, params: bytes, region=None, seed_hash=0, nthrea
             "rays_shadow": int(counters[7])}
 
 
-def light_trace(packed, lights_words, params: bytes, emitters, photons, seed_hash=0, nthreads=None):
-    """One frame of light_trace (src/shaders.mjs:1628-1814) for photons
-    0..photons-1: dict splats (h×w×4 u32 fixed-point sums, 1/65536 units)
-    and photons (n×9 float32: where each landed, its power, the direction
-    it came from), in photon order."""
+def light_trace(packed, lights_words, params: bytes, emitters, photons, seed_hash=0, nthreads=None, ids=None):
+    """One frame of light_trace (src/shaders.mjs:1628-1814) for its photons
+    0..photons-1, or the range ids = (first, count) of them: dict splats
+    (h×w×4 u32 fixed-point sums, 1/65536 units) and photons (n×9 float32:
+    where each landed, its power, the direction it came from), in photon
+    order."""
     import struct
     width, height = struct.unpack_from("<2I", params, 160)
     splats = np.zeros(width * height * 4, dtype=np.uint32)
-    out = np.zeros(max(int(photons), 1) * 9, dtype=np.float32)
+    id0, count = ids if ids is not None else (0, int(photons))
+    out = np.zeros(max(int(count), 1) * 9, dtype=np.float32)
     pbuf = np.frombuffer(bytes(params), dtype=np.uint8).copy()
     words = np.ascontiguousarray(lights_words, dtype=np.uint32)
     attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
     em = np.ascontiguousarray(emitters, dtype=np.float32)
     n = lib().ro_light_trace(_p(packed.primitives), _p(packed.nodes), _p(packed.materials), _p(attrs), _p(words),
-                             _p(pbuf), _p(em), int(photons), seed_hash, _p(splats), _p(out), nthreads or threads())
+                             _p(pbuf), _p(em), int(photons), int(id0), int(count), seed_hash, _p(splats), _p(out),
+                             nthreads or threads())
     return {"splats": splats.reshape(height, width, 4), "photons": out[: n * 9].reshape(n, 9)}
 
 
-def photon_gather(packed, lights_words, params: bytes, photons, seed_hash=0, nthreads=None):
-    """One frame of photon_gather (src/shaders.mjs:1585-1626): the caustic
-    light the photon map adds to each pixel (h×w×4 float32 sums)."""
+def photon_gather(packed, lights_words, params: bytes, photons, seed_hash=0, nthreads=None, rows=None):
+    """One frame of photon_gather (src/shaders.mjs:1585-1626), on every row
+    or rows = (first, count): the caustic light the photon map adds to each
+    pixel (h×w×4 float32 sums)."""
     import struct
     width, height = struct.unpack_from("<2I", params, 160)
     accum = np.zeros(width * height * 4, dtype=np.float32)
@@ -195,8 +199,8 @@ def photon_gather(packed, lights_words, params: bytes, photons, seed_hash=0, nth
     words = np.ascontiguousarray(lights_words, dtype=np.uint32)
     attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
     lib().ro_photon_gather(_p(packed.primitives), _p(packed.nodes), _p(packed.materials), _p(attrs), _p(words),
-                           _p(pbuf), _p(ph if ph.size else np.zeros(9, np.float32)), ph.size // 9, seed_hash,
-                           _p(accum), nthreads or threads())
+                           _p(pbuf), _p(ph if ph.size else np.zeros(9, np.float32)), ph.size // 9,
+                           *(rows if rows is not None else (0, height)), seed_hash, _p(accum), nthreads or threads())
     return accum.reshape(height, width, 4)
 
 

@@ -91,16 +91,18 @@ void ro_render_scene(const void* prims, const void* nodes, const void* materials
                      uint32_t tex_h, const uint8_t* nrm, uint32_t nrm_w, uint32_t nrm_h);
 
 // ---- light tracing and photon mapping (src/shaders.mjs:1425-1831) ----
-// One frame's photons 0..photons-1: fixed-point splats added to `splats`
-// (W·H·4 u32) and the stored photons (9 floats: p, power, -d) in photon
-// order; returns how many were stored.
+// Photons id0..id0+count-1 of a frame of `photons`: fixed-point splats
+// added to `splats` (W·H·4 u32) and the stored photons (9 floats: p, power,
+// -d) in photon order; returns how many were stored.
 uint32_t ro_light_trace(const void* prims, const void* nodes, const void* materials, const float* attributes,
                         const uint32_t* lights, const void* params208, const float* emitters, uint32_t photons,
-                        uint32_t seed_hash, uint32_t* splats, float* photons_out, int threads);
-// The photon map's caustic light through mirrors and glass, added to accum.
+                        uint32_t id0, uint32_t count, uint32_t seed_hash, uint32_t* splats, float* photons_out,
+                        int threads);
+// The photon map's caustic light through mirrors and glass on rows
+// y0..y0+rows-1, added to accum (W·H·4).
 void ro_photon_gather(const void* prims, const void* nodes, const void* materials, const float* attributes,
                       const uint32_t* lights, const void* params208, const float* photons, uint32_t count,
-                      uint32_t seed_hash, float* accum, int threads);
+                      uint32_t y0, uint32_t rows, uint32_t seed_hash, float* accum, int threads);
 
 // ---- the denoiser (src/shaders.mjs:1916-2098) and display (2114-2152) ----
 // Full-image à-trous from the accumulated buffers: prepare, steps 1..16,

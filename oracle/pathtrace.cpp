@@ -1396,14 +1396,14 @@ extern "C" void ro_render_scene(const void* prims, const void* nodes, const void
                 nrm ? &n : nullptr);
 }
 
-// light_trace for photons 0..photons-1 of a frame (src/shaders.mjs:1628-1814):
-// splats (W·H·4 u32, added to, wrapping as the GPU's atomics do) and the
-// stored photons (9 floats each: p, beta, -d) in photon order. Returns how
-// many were stored.
+// light_trace for photons id0..id0+count-1 of a frame of `photons`
+// (src/shaders.mjs:1628-1814): splats (W·H·4 u32, added to, wrapping as the
+// GPU's atomics do) and the stored photons (9 floats each: p, beta, -d) in
+// photon order. Returns how many were stored.
 extern "C" uint32_t ro_light_trace(const void* prims, const void* nodes, const void* materials, const float* attributes,
                                    const uint32_t* lights, const void* params208, const float* emitters,
-                                   uint32_t photons, uint32_t seed_hash, uint32_t* splats, float* photons_out,
-                                   int threads) {
+                                   uint32_t photons, uint32_t id0, uint32_t count, uint32_t seed_hash,
+                                   uint32_t* splats, float* photons_out, int threads) {
     Params P;
     std::memcpy(&P, params208, sizeof P);
     const uint32_t cells = P.width * P.height * 4u;
@@ -1416,9 +1416,9 @@ extern "C" uint32_t ro_light_trace(const void* prims, const void* nodes, const v
               static_cast<const float*>(materials), attributes, lights, P};
         for (;;) {
             const uint32_t k0 = next.fetch_add(256);
-            if (k0 >= photons) break;
-            for (uint32_t k = k0; k < std::min(photons, k0 + 256); ++k)
-                light_trace(c, emitters, photons, k, seed_hash, part_splats[t].data(), part_photons[t]);
+            if (k0 >= count) break;
+            for (uint32_t k = k0; k < std::min(count, k0 + 256); ++k)
+                light_trace(c, emitters, photons, id0 + k, seed_hash, part_splats[t].data(), part_photons[t]);
         }
     };
     std::vector<std::thread> pool;
@@ -1442,12 +1442,13 @@ extern "C" uint32_t ro_light_trace(const void* prims, const void* nodes, const v
     return uint32_t(all.size());
 }
 
-// photon_gather (src/shaders.mjs:1585-1626): per pixel, from the camera
-// through mirrors and glass to the first other surface, the photons near
-// it; added to accum (W·H·4) once for each of the frame's samples.
+// photon_gather (src/shaders.mjs:1585-1626) on rows y0..y0+rows-1: per
+// pixel, from the camera through mirrors and glass to the first other
+// surface, the photons near it; added to accum (W·H·4) once for each of the
+// frame's samples.
 extern "C" void ro_photon_gather(const void* prims, const void* nodes, const void* materials, const float* attributes,
                                  const uint32_t* lights, const void* params208, const float* photons, uint32_t count,
-                                 uint32_t seed_hash, float* accum, int threads) {
+                                 uint32_t y0, uint32_t rows, uint32_t seed_hash, float* accum, int threads) {
     Params P;
     std::memcpy(&P, params208, sizeof P);
     PhotonMap map{photons, std::vector<uint32_t>(PHOTON_TABLE, 0u), std::vector<uint32_t>(count, 0u)};
@@ -1459,8 +1460,9 @@ extern "C" void ro_photon_gather(const void* prims, const void* nodes, const voi
         map.next[i] = map.heads[h];
         map.heads[h] = i + 1u;
     }
-    const uint32_t n = P.width * P.height;
-    std::atomic<uint32_t> next{0};
+    const uint32_t first = std::min(y0, P.height) * P.width;
+    const uint32_t n = std::min(y0 + rows, P.height) * P.width;
+    std::atomic<uint32_t> next{first};
     auto worker = [&] {
         Ctx c{static_cast<const uint8_t*>(prims), static_cast<const uint8_t*>(nodes),
               static_cast<const float*>(materials), attributes, lights, P};

@@ -56,3 +56,13 @@ def test_bvh_build_line():
     check_common(d, 1, 1)
     assert d["unit"] == "Mprims/s" and d["gpu_launches"] == 0
     assert d["config"]["identical_to_oracle"] is True
+
+
+def test_reference_arm_follows_the_workload():
+    d = run("--impl", "reference", "--workload", "caustics", "--steps", "1", "--warmup", "0", "--size", "64")
+    check_common(d, 1, 0)
+    assert d["impl"] == "reference" and d["config"]["workload"].startswith("water caustics")
+    assert "light paths" in d["cpu_baseline"]["sample"]
+    for workload in ("batch", "denoise", "rmse"):
+        d = run("--impl", "reference", "--workload", workload, "--steps", "1", "--warmup", "0")
+        assert d["impl"] == "reference" and d["unavailable"]
