@@ -195,11 +195,16 @@ def photon_gather(packed, lights_words, params: bytes, photons, seed_hash=0, nth
     width, height = struct.unpack_from("<2I", params, 160)
     accum = np.zeros(width * height * 4, dtype=np.float32)
     ph = np.ascontiguousarray(photons, dtype=np.float32).reshape(-1)
+    if ph.size == 0:
+        ph = np.zeros(9, np.float32)  # a valid address; the count passed is 0
+        count = 0
+    else:
+        count = ph.size // 9
     pbuf = np.frombuffer(bytes(params), dtype=np.uint8).copy()
     words = np.ascontiguousarray(lights_words, dtype=np.uint32)
     attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
     lib().ro_photon_gather(_p(packed.primitives), _p(packed.nodes), _p(packed.materials), _p(attrs), _p(words),
-                           _p(pbuf), _p(ph if ph.size else np.zeros(9, np.float32)), ph.size // 9,
+                           _p(pbuf), _p(ph), count,
                            *(rows if rows is not None else (0, height)), seed_hash, _p(accum), nthreads or threads())
     return accum.reshape(height, width, 4)
 
