@@ -16,6 +16,9 @@ _SRGB_TO_LINEAR = np.array([(i / 255) / 12.92 if i / 255 <= 0.04045 else ((i / 2
                             for i in range(256)], dtype=np.float64)
 
 
+_PLAIN = np.arange(256) / 255.0  # a byte as a plain number in [0, 1]
+
+
 def _js_round(x):
     return np.floor(np.asarray(x, dtype=np.float64) + 0.5)
 
@@ -73,12 +76,33 @@ class Texture:
         x0, y0 = np.floor(x), np.floor(y)
         fx, fy = x - x0, y - y0
         img = self.data.reshape(self.height, self.width, 4)[..., :3]
-        dec = _SRGB_TO_LINEAR[img] if srgb else img / 255.0
+        # Decoded after the gather: only the texels the samples touch.
+        table = _SRGB_TO_LINEAR if srgb else _PLAIN
         out = np.zeros(u.shape + (3,))
         for dx, dy, w in ((0, 0, (1 - fx) * (1 - fy)), (1, 0, fx * (1 - fy)), (0, 1, (1 - fx) * fy), (1, 1, fx * fy)):
             px = np.mod(x0 + dx, self.width).astype(np.int64)
             py = np.mod(y0 + dy, self.height).astype(np.int64)
-            out += w[..., None] * dec[py, px]
+            out += w[..., None] * table[img[py, px]]
+        return out
+
+    def _sample_grid(self, us, vs, srgb) -> np.ndarray:
+        """sample_many over the grid of columns us × rows vs: (rows, columns,
+        3). Each column's x and each row's y are worked out once and the
+        texels gathered a row and a column at a time; every value is the
+        same as sample_many's (the weights are the same two factors)."""
+        x = us * self.width - 0.5
+        y = vs * self.height - 0.5
+        x0, y0 = np.floor(x), np.floor(y)
+        fx, fy = x - x0, y - y0
+        img = self.data.reshape(self.height, self.width, 4)[..., :3]
+        table = _SRGB_TO_LINEAR if srgb else _PLAIN
+        out = np.zeros((len(vs), len(us), 3))
+        for dx, dy in ((0, 0), (1, 0), (0, 1), (1, 1)):
+            wx = fx if dx else 1 - fx
+            wy = fy if dy else 1 - fy
+            px = np.mod(x0 + dx, self.width).astype(np.int64)
+            py = np.mod(y0 + dy, self.height).astype(np.int64)
+            out += (wy[:, None] * wx[None, :])[..., None] * table[img[py][:, px]]
         return out
 
     def sample(self, u, v, srgb=True) -> Vec3:
@@ -89,8 +113,7 @@ class Texture:
         """Resampled to width × height at texel centres (src/Texture.mjs resized)."""
         if width == self.width and height == self.height:
             return self
-        ys, xs = np.meshgrid(np.arange(height), np.arange(width), indexing="ij")
-        c = self.sample_many((xs + 0.5) / width, (ys + 0.5) / height, srgb)
+        c = self._sample_grid((np.arange(width) + 0.5) / width, (np.arange(height) + 0.5) / height, srgb)
         data = np.zeros((height, width, 4), dtype=np.uint8)
         if srgb:
             data[..., :3] = to_srgb_byte(c)
