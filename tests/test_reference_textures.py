@@ -140,3 +140,18 @@ def test_importance_table_is_bit_identical_to_the_loop(w, h):
     cw, ch, data = importance_loop(env)
     assert (imp["width"], imp["height"]) == (cw, ch)
     assert np.array_equal(imp["data"].view(np.uint32), data.view(np.uint32))
+
+
+@pytest.mark.parametrize("srgb", [True, False])
+def test_resizing_samples_as_sample_many_does(srgb):
+    """Texture.resized samples at texel centres (src/Texture.mjs:193-209);
+    its row-and-column gather gives sample_many's values bit for bit."""
+    rng = np.random.default_rng(7)
+    t = Texture(37, 19, rng.integers(0, 256, 37 * 19 * 4, dtype=np.uint8))
+    w, h = 64, 40
+    ys, xs = np.meshgrid(np.arange(h), np.arange(w), indexing="ij")
+    expected = t.sample_many((xs + 0.5) / w, (ys + 0.5) / h, srgb)
+    got = t._sample_grid((np.arange(w) + 0.5) / w, (np.arange(h) + 0.5) / h, srgb)
+    assert np.array_equal(got.view(np.uint64), expected.view(np.uint64))
+    out = t.resized(w, h, srgb).data.reshape(h, w, 4)
+    assert (out[..., 3] == 255).all()
