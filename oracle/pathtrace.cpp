@@ -624,7 +624,7 @@ Bs sample_bsdf(const Mat& m, V base, const Surf& sf, V wo, Sampler& s) {
     return {wi, f / pdf, pdf, false, true};
 }
 
-// ---- lights (src/shaders.mjs:877-1018); no environment map ----
+// ---- lights (src/shaders.mjs:877-1018), the environment among them ----
 // light_choices (src/shaders.mjs:877-879): the lights, the sun, then the environment.
 uint32_t choices(const Ctx& c) { return c.P.light_count + (c.P.sun_on != 0u ? 1u : 0u) + (env_on(c) ? 1u : 0u); }
 float light_cdf(const Ctx& c, uint32_t l) { return bitsf(c.lights[c.P.light_count + c.P.volume_count + l]); }
