@@ -61,4 +61,4 @@ def test_textured_and_environment_frames_are_the_same_on_any_number_of_threads()
         many = oracle.render(packed, words, params, nthreads=5, **kw)
         for key in ("accum", "albedo", "normal"):
             assert np.array_equal(one[key].view(np.uint32), many[key].view(np.uint32)), (name, key)
-        assert one["accum"][..., :3].sum() > 0, name
+        assert one["albedo"][..., :3].sum() > 0, name  # (the bumpy scene is unlit: its colour is black)
