@@ -623,8 +623,48 @@ def run_bvh_reference(args):
     }
 
 
+def run_batch_reference(args):
+    """The reference arm of the batch line: the oracle's f32 path tracer on
+    every instance of the batch in turn (the reference renders one scene
+    at a time), on a bounded sample of each frame — `rows` rows spread
+    down each image, on all host cores."""
+    import oracle
+    from raymond_gb300 import scenes
+    from raymond_gb300.renderer import light_table, params_block
+
+    inst = scenes.batch_instances(args.batch, spheres=args.batch_spheres)
+    threads = os.cpu_count() or 1
+    rows = 2
+    prepared = []
+    for scene, camera, w, h, spp, info in inst:
+        packed = scene.pack()
+        words, powers = light_table(packed)
+        params = params_block(scene, camera, w, h, light_count=len(powers), volume_count=len(packed.volumes),
+                              max_bounces=args.bounces, spp=spp)
+        prepared.append((packed, words, params, w, h))
+    times, paths = [], 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for packed, words, params, w, h in prepared:
+            for k in range(rows):
+                r = oracle.render(packed, words, params, region=(0, (k * h) // rows, w, 1), nthreads=threads)
+                paths += r["paths"]
+        times.append(time.perf_counter() - t0)
+    value = paths / sum(times) / 1e6
+    sample = f"{rows} rows of each of the {len(inst)} instances' frames per step, one instance after another"
+    return {
+        "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32)",
+        "impl": "reference",
+        "config": {"workload": f"batch of {len(inst)} sphere-field instances", "bounces": args.bounces,
+                   "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "Mpaths/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
 REFERENCE_UNAVAILABLE = {
-    "batch": "the reference renders one scene per renderer; batched multi-scene frames have no CPU counterpart in it",
     "denoise": "the reference has no learned denoiser",
     "rmse": "the reference's CPU path to RMSE 0.01 at 1024x1024 would take hours on the host cores",
 }
@@ -1050,6 +1090,8 @@ def main():
         out = run_primary_reference(args, rank, world)
     elif args.impl == "reference" and args.workload == "bvh":
         out = run_bvh_reference(args) if rank == 0 else None
+    elif args.impl == "reference" and args.workload == "batch":
+        out = run_batch_reference(args) if rank == 0 else None
     elif args.impl == "reference" and args.workload in REFERENCE_UNAVAILABLE:
         out = {"impl": "reference", "unavailable": REFERENCE_UNAVAILABLE[args.workload]} if rank == 0 else None
     elif args.impl == "reference":

@@ -63,6 +63,9 @@ def test_reference_arm_follows_the_workload():
     check_common(d, 1, 0)
     assert d["impl"] == "reference" and d["config"]["workload"].startswith("water caustics")
     assert "light paths" in d["cpu_baseline"]["sample"]
-    for workload in ("batch", "denoise", "rmse"):
+    d = run("--impl", "reference", "--workload", "batch", "--batch", "4", "--steps", "1", "--warmup", "0")
+    check_common(d, 1, 0)
+    assert d["impl"] == "reference" and d["config"]["workload"] == "batch of 4 sphere-field instances"
+    for workload in ("denoise", "rmse"):
         d = run("--impl", "reference", "--workload", workload, "--steps", "1", "--warmup", "0")
         assert d["impl"] == "reference" and d["unavailable"]
