@@ -6,8 +6,8 @@ Renderer. Rendering runs in libraymond_cuda.so through its C ABI
 (include/raymond.h); there is no CPU fallback.
 """
 
-from .vec import Mat4, Vec2, Vec3, Vec4
-from .material import MATERIAL_TYPES, Material, hexColor
+from .vec import Mat4, Vec2, Vec3
+from .material import MATERIAL_TYPES, Material
 from .geometry import Box, Mesh, Quad, Sphere
 from .sky import Camera, Sky
 from .scene import BVH, NONE, PRIMITIVE_KINDS, PackedScene, Scene
@@ -16,5 +16,5 @@ from .texture import EnvironmentMap, Texture
 
 __all__ = [
     "BatchRenderer", "BVH", "Box", "Camera", "Canvas", "MATERIAL_TYPES", "Mat4", "Material", "Mesh", "NONE", "PRIMITIVE_KINDS",
-    "PackedScene", "Quad", "Renderer", "Scene", "Sky", "Sphere", "Vec2", "Vec3", "Vec4", "Texture", "EnvironmentMap", "hexColor",
+    "PackedScene", "Quad", "Renderer", "Scene", "Sky", "Sphere", "Vec2", "Vec3", "Texture", "EnvironmentMap",
 ]

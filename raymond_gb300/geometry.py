@@ -248,58 +248,6 @@ class Mesh:
         return Mesh(pos, faces, material, shading=shading)
 
     @staticmethod
-    def lathe(profile, material, segments=64, shading="smooth") -> "Mesh":
-        """A solid turned about the y axis from profile points (Vec2: radius,
-        height), closed round the axis; textures run round it and down the
-        profile from its end (src/Mesh.mjs:250-273)."""
-        if len(profile) < 2:
-            raise ValueError("A lathe's profile needs at least 2 points.")
-        steps = len(profile) - 1
-
-        def point(u, v):
-            p = profile[math.floor(v * steps + 0.5)]
-            a = u * 2.0 * math.pi
-            return Vec3(p.x * math.cos(a), p.y, -p.x * math.sin(a))
-
-        turned = Mesh.surface(point, segments, steps, material, uWrap="closed", shading=shading)
-        uvs = turned.uvs.copy()
-        uvs[:, 1] = 1.0 - uvs[:, 1]
-        return Mesh(turned.positions, turned.indices, material, shading="flat", normals=turned.normals, uvs=uvs)
-
-    @staticmethod
-    def tube(curve, material, radius=0.3, segments=256, sides=24) -> "Mesh":
-        """A tube round the closed curve curve(t), t in [0, 1) (src/Mesh.mjs:295-351).
-        Each ring's frame is carried along the curve without twisting; the
-        turn it has gathered after one lap is spread evenly along the tube
-        so that the rings meet at the seam."""
-        centres = [curve(s / segments) for s in range(segments)]
-
-        def tangent(s):
-            return centres[(s + 1) % segments].subtract(centres[(s + segments - 1) % segments]).normalized()
-
-        t0 = tangent(0)
-        helper = Vec3(0.0, 1.0, 0.0) if abs(t0.y) < 0.9 else Vec3(1.0, 0.0, 0.0)
-        normal = t0.cross(helper).normalized()
-        normals = [normal]
-        for s in range(1, segments + 1):
-            t = tangent(s % segments)
-            normal = normal.subtract(t.scale(normal.dot(t))).normalized()
-            normals.append(normal)
-        binormal0 = t0.cross(normals[0])
-        twist = math.atan2(normals[segments].dot(binormal0), normals[segments].dot(normals[0]))
-
-        def point(u, v):
-            s = math.floor(u * segments + 0.5) % segments
-            t = tangent(s)
-            n = normals[s]
-            b = t.cross(n)
-            # round the ring from n towards −b, with u along t: ∂u × ∂v points outwards
-            angle = 2.0 * math.pi * v + twist * s / segments
-            return centres[s].add(n.scale(math.cos(angle) * radius)).subtract(b.scale(math.sin(angle) * radius))
-
-        return Mesh.surface(point, segments, sides, material, uWrap="closed", vWrap="closed")
-
-    @staticmethod
     def torus(material, radius=1.0, tube=0.35, segments=64, sides=32) -> "Mesh":
         """src/Mesh.mjs:293-303."""
         def point(u, v):

@@ -3,7 +3,6 @@ constructors as the JavaScript library."""
 
 from __future__ import annotations
 
-import re
 
 from .vec import Vec2, Vec3
 
@@ -104,18 +103,3 @@ class Material:
     def checkered(color, other, size=1.0):
         return Material(type="diffuse", color=color, checker=other, checkerSize=size)
 
-
-def hexColor(hex: str) -> Vec3:
-    """An sRGB hex colour ("#rgb" or "#rrggbb", the # optional) in linear
-    light (src/Material.mjs:352-368). ValueError for anything else."""
-    digits = hex[1:] if hex.startswith("#") else hex
-    if len(digits) == 3:
-        digits = "".join(d + d for d in digits)
-    if not re.fullmatch(r"[0-9a-fA-F]{6}", digits):
-        raise ValueError(f'"{hex}" is not a hex colour.')
-
-    def channel(i):
-        c = int(digits[2 * i:2 * i + 2], 16) / 255.0
-        return c / 12.92 if c <= 0.04045 else ((c + 0.055) / 1.055) ** 2.4
-
-    return Vec3(channel(0), channel(1), channel(2))

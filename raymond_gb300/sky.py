@@ -30,19 +30,6 @@ class Sky:
         b = Vec3(0.0, 0.0, 0.0)
         return Sky(zenith=b, horizon=b, ground=b)
 
-    def with_(self, **changes) -> "Sky":
-        """A copy with the given fields changed (Sky.with, src/Sky.mjs:160-175;
-        `with` is a keyword in Python)."""
-        fields = dict(zenith=self.zenith, horizon=self.horizon, ground=self.ground, sunDirection=self.sunDirection,
-                      sunColor=self.sunColor, sunStrength=self.sunStrength, sunSize=self.sunSize,
-                      environment=self.environment, environmentStrength=self.environmentStrength,
-                      environmentRotation=self.environmentRotation)
-        unknown = set(changes) - set(fields)
-        if unknown:
-            raise TypeError(f"Sky has no field {sorted(unknown)[0]!r}.")
-        fields.update(changes)
-        return Sky(**fields)
-
     @property
     def sunRadiance(self) -> Vec3:
         """Radiance that makes the disc deliver sunStrength at normal incidence (src/Sky.mjs:132-136)."""

@@ -6,7 +6,6 @@ the arithmetic follows the reference's."""
 from __future__ import annotations
 
 import math
-import re
 
 import numpy as np
 
@@ -155,90 +154,6 @@ class EnvironmentMap:
                 c = radiance(EnvironmentMap.direction((x + 0.5) / width, (y + 0.5) / height))
                 data[y, x] = (c.x, c.y, c.z)
         return EnvironmentMap(width, height, data)
-
-    @staticmethod
-    def fromHDR(file) -> "EnvironmentMap":
-        """A Radiance .hdr (RGBE) file, flat or run-length encoded, read as
-        the reference reads it (src/EnvironmentMap.mjs:102-177): a
-        `#?RADIANCE` or `#?RGBE` first line, header lines up to a blank one
-        (only FORMAT=32-bit_rle_rgbe allowed), a `-Y h +X w` size line, then
-        h scanlines. A scanline is run-length encoded when it opens with
-        2, 2 and its width (widths 8 to 32767): each channel in turn as runs
-        (a count above 128 and one byte) and literals (a count and that many
-        bytes). A pixel's value is its mantissa bytes × 2^(e − 136), zero
-        where e is 0. Errors are ValueError with the reference's messages."""
-        data = bytes(file) if not isinstance(file, (bytes, bytearray)) else file
-        n = len(data)
-        at = 0
-
-        def line():
-            nonlocal at
-            end = data.find(b"\n", at)
-            end = n if end < 0 else end
-            text = data[at:end].decode("latin-1")
-            at = end + 1
-            return text
-
-        first = line()
-        if not (first.startswith("#?RADIANCE") or first.startswith("#?RGBE")):
-            raise ValueError("Not a Radiance .hdr file.")
-        header = line()
-        while header != "":
-            if header.startswith("FORMAT=") and header != "FORMAT=32-bit_rle_rgbe":
-                raise ValueError(f"Unsupported .hdr format: {header[7:]}.")
-            if at >= n:
-                raise ValueError("The .hdr file ends in its header.")
-            header = line()
-        size = re.fullmatch(r"-Y (\d+) \+X (\d+)", line())
-        if not size:
-            raise ValueError("Only .hdr files stored top to bottom, left to right, are supported.")
-        height, width = int(size.group(1)), int(size.group(2))
-
-        raw = np.frombuffer(data, dtype=np.uint8)
-        rgbe = np.zeros((height, width, 4), dtype=np.uint8)
-        for y in range(height):
-            rle = (8 <= width < 32768 and at + 2 < n and raw[at] == 2 and raw[at + 1] == 2
-                   and (raw[at + 2] & 0x80) == 0)
-            if rle:
-                if at + 3 >= n or (int(raw[at + 2]) << 8 | int(raw[at + 3])) != width:
-                    raise ValueError("A scanline of the .hdr file has the wrong length.")
-                at += 4
-                for c in range(4):
-                    x = 0
-                    while x < width:
-                        if at >= n:
-                            raise ValueError("A scanline of the .hdr file runs over.")
-                        count = int(raw[at])
-                        at += 1
-                        if count > 128:
-                            count -= 128
-                            if x + count > width or at >= n:
-                                raise ValueError("A scanline of the .hdr file runs over.")
-                            rgbe[y, x:x + count, c] = raw[at]
-                            at += 1
-                        else:
-                            if x + count > width or at + count > n:
-                                raise ValueError("A scanline of the .hdr file runs over.")
-                            rgbe[y, x:x + count, c] = raw[at:at + count]
-                            at += count
-                        x += count
-            else:
-                if at + width * 4 > n:
-                    raise ValueError("The .hdr file ends early.")
-                rgbe[y] = raw[at:at + width * 4].reshape(width, 4)
-                at += width * 4
-
-        e = rgbe[..., 3].astype(np.int64)
-        scale = np.where(e == 0, 0.0, np.ldexp(1.0, e - 136))
-        rgb = rgbe[..., :3].astype(np.float64) * scale[..., None]
-        return EnvironmentMap(width, height, rgb.astype(np.float32))
-
-    @staticmethod
-    def load(path) -> "EnvironmentMap":
-        """Reads a Radiance .hdr file from disk (the reference fetches a URL:
-        src/EnvironmentMap.mjs:183-190)."""
-        with open(path, "rb") as f:
-            return EnvironmentMap.fromHDR(f.read())
 
     def importance(self):
         """Row CDFs (cw × ch) and the CDF over rows (one more row), by

@@ -1,5 +1,5 @@
 """Vectors and 4×4 matrices of the public API (src/Vec2.mjs, src/Vec3.mjs,
-src/Vec4.mjs, src/Mat4.mjs), with the reference's operation order so packed values
+src/Mat4.mjs), with the reference's operation order so packed values
 (a box's inverse matrix, a camera basis) round identically."""
 
 from __future__ import annotations
@@ -66,31 +66,6 @@ class Vec3:
         return f"Vec3({self.x}, {self.y}, {self.z})"
 
 
-class Vec4:
-    """src/Vec4.mjs: a homogeneous point (w = 1) or direction (w = 0)."""
-
-    __slots__ = ("x", "y", "z", "w")
-
-    def __init__(self, x: float = 0.0, y: float = 0.0, z: float = 0.0, w: float = 0.0):
-        self.x = float(x)
-        self.y = float(y)
-        self.z = float(z)
-        self.w = float(w)
-
-    def dot(self, o: "Vec4") -> float:
-        return self.x * o.x + self.y * o.y + self.z * o.z + self.w * o.w
-
-    def lerp(self, o: "Vec4", t: float) -> "Vec4":
-        return Vec4(self.x + (o.x - self.x) * t, self.y + (o.y - self.y) * t, self.z + (o.z - self.z) * t,
-                    self.w + (o.w - self.w) * t)
-
-    def tuple(self):
-        return (self.x, self.y, self.z, self.w)
-
-    def __repr__(self):
-        return f"Vec4({self.x}, {self.y}, {self.z}, {self.w})"
-
-
 class Mat4:
     """Row-major 4×4 matrix acting on column vectors (src/Mat4.mjs)."""
 
@@ -115,14 +90,6 @@ class Mat4:
     def setValue(self, row: int, column: int, value: float) -> None:
         Mat4._check(row, column)
         self.v[row * 4 + column] = float(value)
-
-    def row(self, index: int) -> Vec4:
-        Mat4._check(index, 0)
-        return Vec4(*self.v[index * 4:index * 4 + 4])
-
-    def column(self, index: int) -> Vec4:
-        Mat4._check(0, index)
-        return Vec4(self.v[index], self.v[4 + index], self.v[8 + index], self.v[12 + index])
 
     @staticmethod
     def identity() -> "Mat4":
@@ -160,33 +127,6 @@ class Mat4:
                     right.y, true_up.y, -look.y, eye.y,
                     right.z, true_up.z, -look.z, eye.z,
                     0, 0, 0, 1)
-
-    @staticmethod
-    def orthographic(left, right, bottom, top, near, far) -> "Mat4":
-        """The box [left, right] × [bottom, top] × [-near, -far] onto the clip
-        cube [-1, 1]³, w left at 1 (src/Mat4.mjs:330-337)."""
-        return Mat4(2.0 / (right - left), 0, 0, -((right + left) / (right - left)),
-                    0, 2.0 / (top - bottom), 0, -((top + bottom) / (top - bottom)),
-                    0, 0, -2.0 / (far - near), -((far + near) / (far - near)),
-                    0, 0, 0, 1)
-
-    @staticmethod
-    def perspective(fov, aspectRatio, near, far) -> "Mat4":
-        """OpenGL-style projection: vertical field of view fov (radians), the
-        near and far planes to depth -1 and 1 after the divide by w = -z
-        (src/Mat4.mjs:347-356)."""
-        t = math.tan(fov / 2.0)
-        return Mat4(1.0 / (aspectRatio * t), 0, 0, 0,
-                    0, 1.0 / t, 0, 0,
-                    0, 0, -((far + near) / (far - near)), -(2 * far * near) / (far - near),
-                    0, 0, -1, 0)
-
-    def multiplyVector4(self, p: Vec4) -> Vec4:
-        m = self.v
-        return Vec4(m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3] * p.w,
-                    m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7] * p.w,
-                    m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11] * p.w,
-                    m[12] * p.x + m[13] * p.y + m[14] * p.z + m[15] * p.w)
 
     def multiplyMat4(self, o: "Mat4") -> "Mat4":
         a, b = self.v, o.v

@@ -1,6 +1,5 @@
 """tests/unit/mesh.test.mjs of the reference, restated for the Python
-mirror (the meshes the workloads build: icospheres, surfaces, tori, tubes,
-lathes): closed meshes are watertight and wound outwards, they approximate
+mirror (the meshes the workloads build: icospheres, surfaces, tori): closed meshes are watertight and wound outwards, they approximate
 their shapes, smooth normals point out, transforms keep the winding, and
 degenerate or malformed input is handled as there (ValueError for the
 reference's RangeError)."""
@@ -10,7 +9,7 @@ import math
 import numpy as np
 import pytest
 
-from raymond_gb300 import Mat4, Material, Mesh, Vec2, Vec3
+from raymond_gb300 import Mat4, Material, Mesh, Vec3
 
 WHITE = Material.diffuse(Vec3(0.8, 0.8, 0.8))
 
@@ -38,16 +37,9 @@ def assert_watertight(mesh, name):
         assert edges.get((b, a)) == 1, f"{name}: edge has a twin"
 
 
-def knot(t):
-    phi = t * 2.0 * math.pi
-    r = math.cos(3.0 * phi) + 2.0
-    return Vec3(r * math.cos(2.0 * phi), r * math.sin(2.0 * phi), -math.sin(3.0 * phi))
-
-
 CLOSED = {
     "icosphere": lambda: Mesh.icosphere(WHITE, 2),
     "torus": lambda: Mesh.torus(WHITE, radius=1.0, tube=0.3, segments=24, sides=12),
-    "tube": lambda: Mesh.tube(knot, WHITE, radius=0.3, segments=90, sides=10),
 }
 
 
@@ -64,16 +56,6 @@ def test_meshes_approximate_their_shapes():
     assert abs(signed_volume(torus) - 2.0 * math.pi * math.pi * 1.0 * 0.09) <= 0.01
     for p in Mesh.icosphere(WHITE, 2).positions:
         assert abs(np.linalg.norm(p) - 1.0) < 1e-9
-
-
-def test_tube_rings_stay_round_at_its_radius():
-    segments = 90
-    mesh = Mesh.tube(knot, WHITE, radius=0.3, segments=segments, sides=10)
-    for s in range(segments):
-        c = knot(s / segments)
-        centre = np.array([c.x, c.y, c.z])
-        for k in range(11):  # the first vertex repeated at the seam
-            assert abs(np.linalg.norm(mesh.positions[s * 11 + k] - centre) - 0.3) < 1e-9
 
 
 @pytest.mark.parametrize("name", list(CLOSED))
@@ -123,13 +105,3 @@ def test_bad_meshes_are_refused():
     with pytest.raises(ValueError):
         Mesh(p, [0, 1, 2], WHITE, normals=[Vec3(0, 0, 1)])  # too few normals
 
-
-def test_lathe_turns_a_profile_into_a_solid():
-    profile = [Vec2(0, 0), Vec2(1, 0), Vec2(1, 2), Vec2(0, 2)]
-    cylinder = Mesh.lathe(profile, WHITE, segments=256)
-    assert abs(signed_volume(cylinder) - 2.0 * math.pi) <= 0.001
-    for x, y, z in cylinder.positions:
-        assert round(y * 1e9) / 1e9 in (0, 2)
-        assert any(abs(math.hypot(x, z) - r) < 1e-9 for r in (0, 1))
-    with pytest.raises(ValueError):
-        Mesh.lathe([Vec2(1, 0)], WHITE)

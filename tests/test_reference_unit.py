@@ -355,7 +355,7 @@ def test_stick_between_points():
     hit = cast(scene, a.subtract(along), along)
     assert abs(hit["distance"] - 1.0) < 1e-5 and np.allclose(hit["normal"], along.negate().tuple(), atol=1e-6)
     middle = a.add(b).scale(0.5)
-    c = stick.transform.column(0)
+    c = Vec3(stick.transform.value(0, 0), stick.transform.value(1, 0), stick.transform.value(2, 0))
     across = Vec3(c.x, c.y, c.z).normalized()
     assert abs(across.dot(along)) < 1e-9
     side = cast(scene, middle.add(across.scale(5)), across.negate())
