@@ -146,21 +146,50 @@ def build_workload(size, spp, bounces, workload="field"):
     return scene, camera, info
 
 
-def oracle_sample(scene, params: bytes, size, rows_per_strip, strips, threads, detail=False):
-    """The oracle's f32 path tracer on `strips` bands spread down the image:
+class OracleScene:
+    """A workload scene as the oracle packs it (oracle/pack.py: Scene.#pack
+    restated) with its lights table, delta objects and emitters
+    (oracle/host.py: Renderer's host tables restated). Nothing here touches
+    the product's library, so the reference arm maps only the oracle's."""
+
+    def __init__(self, scene):
+        from oracle import host, pack
+
+        self.scene = scene
+        self.packed = pack.pack(scene.objects)
+        self.words, self.powers = host.light_words(self.packed)
+        self.deltas = host.delta_objects(scene.objects, self.packed)
+
+    def params(self, camera, width, height, spp, bounces, **kw) -> bytes:
+        from oracle import host
+
+        return host.params(self.scene, camera, width, height, light_count=len(self.powers),
+                           volume_count=len(self.packed.volumes), max_bounces=bounces, spp=spp, **kw)
+
+    def emitters(self):
+        from oracle import host
+
+        return host.emitters(self.powers, self.deltas, self.scene.sky, len(self.powers))
+
+
+def band_starts(height, bands, rows):
+    """First rows of `bands` bands of `rows` rows centred at the middles of
+    equal slices of the image, so a sample is not biased towards its top
+    rows (sky, where paths end after one bounce)."""
+    return [max(0, min(height - rows, ((2 * k + 1) * height) // (2 * bands) - rows // 2)) for k in range(bands)]
+
+
+def oracle_sample(osc, params: bytes, width, height, rows_per_band, bands, threads, detail=False):
+    """The oracle's f32 path tracer on `bands` bands spread down the image:
     returns (paths, seconds, algorithmic bytes per path, rays per path), and
     with detail the per-path closest-hit and shadow traversal bytes too."""
     import oracle
-    from raymond_gb300.renderer import light_table
 
-    packed = scene.pack()
-    words, _ = light_table(packed)
     tot = {"paths": 0, "bytes": 0, "rays": 0, "trav_closest": 0, "trav_shadow": 0, "rays_closest": 0,
            "rays_shadow": 0}
     t0 = time.perf_counter()
-    for k in range(strips):
-        y0 = (k * size) // strips
-        r = oracle.render(packed, words, params, region=(0, y0, size, rows_per_strip), nthreads=threads)
+    for y0 in band_starts(height, bands, rows_per_band):
+        r = oracle.render(osc.packed, osc.words, params, region=(0, y0, width, rows_per_band), nthreads=threads)
         for key in tot:
             tot[key] += r[key]
     secs = time.perf_counter() - t0
@@ -171,7 +200,7 @@ def oracle_sample(scene, params: bytes, size, rows_per_strip, strips, threads, d
     return out
 
 
-def caustics_cpu_sample(scene, camera, size, spp, bounces, threads, strips=16, rows=2):
+def caustics_cpu_sample(osc, camera, size, spp, bounces, threads, strips=16, rows=2):
     """The oracle's frame of the caustics workload on a bounded sample: the
     camera paths (leaving caustic paths to light tracing) on `strips` bands
     of `rows` rows, the same fraction of the frame's light paths (splatted
@@ -180,41 +209,25 @@ def caustics_cpu_sample(scene, camera, size, spp, bounces, threads, strips=16, r
     import numpy as np
 
     import oracle
-    from raymond_gb300.renderer import delta_objects, emitters_block, light_table, params_block
 
-    packed = scene.pack()
-    words, powers = light_table(packed)
-    deltas = delta_objects(scene)
-    emitters = emitters_block(powers, len(powers), deltas, scene.sky)
-    block = bytearray(params_block(scene, camera, size, size, light_count=len(powers),
-                                   volume_count=len(packed.volumes), max_bounces=bounces, spp=spp,
-                                   caustics=emitters is not None, deltas=deltas))
+    emitters = osc.emitters()
+    block = bytearray(osc.params(camera, size, size, spp, bounces, caustics=emitters is not None, deltas=osc.deltas))
     f = np.frombuffer(block, dtype=np.float32)
     f[48], f[49] = CAUSTICS_RADIUS, 2 * CAUSTICS_RADIUS  # the fixed radius the GPU run sets
     params = bytes(block)
     light_paths = CAUSTICS_LIGHT_PATHS * strips * rows // size
     paths = 0
+    starts = band_starts(size, strips, rows)
     t0 = time.perf_counter()
-    for k in range(strips):
-        r = oracle.render(packed, words, params, region=(0, (k * size) // strips, size, rows), nthreads=threads)
+    for y0 in starts:
+        r = oracle.render(osc.packed, osc.words, params, region=(0, y0, size, rows), nthreads=threads)
         paths += r["paths"]
     if emitters is not None:
-        lt = oracle.light_trace(packed, words, params, emitters, CAUSTICS_LIGHT_PATHS, ids=(0, light_paths),
+        lt = oracle.light_trace(osc.packed, osc.words, params, emitters, CAUSTICS_LIGHT_PATHS, ids=(0, light_paths),
                                 nthreads=threads)
-        for k in range(strips):
-            oracle.photon_gather(packed, words, params, lt["photons"], rows=((k * size) // strips, rows),
-                                 nthreads=threads)
+        for y0 in starts:
+            oracle.photon_gather(osc.packed, osc.words, params, lt["photons"], rows=(y0, rows), nthreads=threads)
     return paths, light_paths, time.perf_counter() - t0
-
-
-def params_for(scene, camera, size, spp, bounces):
-    """The uniform block a renderer writes for frame 0 of this workload."""
-    from raymond_gb300.renderer import light_table, params_block
-
-    packed = scene.pack()
-    words, powers = light_table(packed)
-    return params_block(scene, camera, size, size, light_count=len(powers), volume_count=len(packed.volumes),
-                        max_bounces=bounces, spp=spp)
 
 
 def device_view(torch, ptr, shape, device):
@@ -384,24 +397,33 @@ def run_denoise(args, local):
 PRIMARY_WORKLOAD = "Cornell room 256x256, one jittered primary ray per pixel (mulberry32 seed 1), closest hit"
 
 
+L2_NOTE = "GPU arm: flushed between steps (512 MB write); CPU arm: not applicable"
+
+
+def primary_config(rays):
+    return {"workload": PRIMARY_WORKLOAD, "rays": rays, "l2": L2_NOTE}
+
+
 def primary_case(size):
-    """The Cornell primary-ray case: the room, its f32 camera rays, and the
-    algorithmic bytes of tracing them counted by the oracle's f32 traversal:
-    32·(1 + 2·inner nodes visited) + 64·primitives tested per ray."""
+    """The Cornell primary-ray case: the room, its f32 camera rays, the
+    oracle's packing of the room, and the algorithmic bytes of tracing the
+    rays counted by the oracle's f32 traversal: 32·(1 + 2·inner nodes
+    visited) + 64·primitives tested per ray."""
     import oracle
+    from oracle import pack
     from raymond_gb300 import scenes
 
     scene, camera, rays = scenes.cornell_primary(size, seed=1)
-    counts = oracle.trace32(scene.pack(), rays)
-    return scene, rays, counts, int(oracle.bytes_per_ray(counts["inner"], counts["tested"]).sum())
+    packed = pack.pack(scene.objects)
+    counts = oracle.trace32(packed, rays)
+    return scene, packed, rays, counts, int(oracle.bytes_per_ray(counts["inner"], counts["tested"]).sum())
 
 
-def primary_cpu(scene, rays, seconds=1.0):
+def primary_cpu(packed, rays, seconds=1.0):
     """Scene.raycast restated in double (oracle/raycast.cpp) on all host
     cores, repeated over the whole ray set for about `seconds`: Mrays/s."""
     import oracle
 
-    packed = scene.pack()
     threads = os.cpu_count() or 1
     oracle.raycast(packed, rays[:1024], nthreads=threads)
     done, t0 = 0, time.perf_counter()
@@ -426,7 +448,7 @@ def run_primary(args, local):
     from raymond_gb300 import _native
 
     size = 256 if args.size == 1024 else args.size
-    scene, rays, counts, algo_bytes = primary_case(size)
+    scene, packed, rays, counts, algo_bytes = primary_case(size)
     n = len(rays)
     r = rg.Renderer.create(rg.Canvas(1, 1), device=local)
     r.tracePrimary(rays[:32], scene)  # uploads the scene
@@ -474,13 +496,13 @@ def run_primary(args, local):
     launch_s = statistics.mean(ms) / 1e3
     peak, peak_kind = measured_peak_hbm()
     achieved = algo_bytes / launch_s / 1e9
-    cpu_value, cores, cpu_s = primary_cpu(scene, rays)
+    cpu_value, cores, cpu_s = primary_cpu(packed, rays)
     return {
         "metric": "Mrays/s (primary, closest hit)", "value": n / launch_s / 1e6, "unit": "Mrays/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(ms), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32 jitter)",
-        "config": {"workload": PRIMARY_WORKLOAD, "rays": n, "l2": "flushed between steps (512 MB write)",
-                   "hits_equal_to_oracle_f32": agree},
+        "config": primary_config(n),
+        "hits_equal_to_oracle_f32": agree,
         "e2e": {"value": n / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 24 * n,
                 "d2h_bytes_per_step": 8 * n},
         "gpu_launches": args.steps,
@@ -499,22 +521,46 @@ def run_primary_reference(args, rank, world):
     if rank != 0:
         return None
     size = 256 if args.size == 1024 else args.size
-    scene, rays, _, _ = primary_case(size)
+    scene, packed, rays, _, _ = primary_case(size)
     times = []
     value = 0.0
     for _ in range(args.steps):
-        value, cores, dt = primary_cpu(scene, rays, seconds=0.5)
+        value, cores, dt = primary_cpu(packed, rays, seconds=0.5)
         times.append(dt)
     return {
         "metric": "Mrays/s (primary, closest hit)", "value": value, "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded mulberry32 jitter)", "impl": "reference",
-        "config": {"workload": PRIMARY_WORKLOAD, "rays": len(rays), "l2": "n/a (CPU)"},
+        "config": primary_config(len(rays)),
         "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": "port",
                          "sample": f"oracle Scene.raycast (double) over all {len(rays)} rays for 0.5 s per step"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+
+
+def field_boxes():
+    """The sphere field's primitive boxes as Scene.#pack hands them to
+    BVH.build (the oracle's packing, oracle/pack.py): (mins, maxs), f64."""
+    import numpy as np
+
+    import oracle
+    from oracle import pack
+    from raymond_gb300 import scenes
+
+    captured = {}
+
+    def capture(mins, maxs):
+        captured["mins"], captured["maxs"] = np.array(mins, dtype=np.float64), np.array(maxs, dtype=np.float64)
+        return oracle.bvh_build(mins, maxs)
+
+    scene, _, _ = scenes.sphere_field()
+    pack.pack(scene.objects, bvh_build=capture)
+    return captured["mins"], captured["maxs"]
+
+
+def bvh_config(count):
+    return {"workload": f"binned-SAH BVH of the sphere field's {count} primitive boxes, leaves of at most 4"}
 
 
 def run_bvh(args):
@@ -526,22 +572,8 @@ def run_bvh(args):
 
     import oracle
     from raymond_gb300 import scene as scene_mod
-    from raymond_gb300 import scenes
 
-    captured = {}
-    native_build = scene_mod.BVH.build
-
-    def capture(mins, maxs, *a, **k):
-        captured["mins"], captured["maxs"] = np.array(mins, dtype=np.float64), np.array(maxs, dtype=np.float64)
-        return native_build(mins, maxs, *a, **k)
-
-    scene_mod.BVH.build = staticmethod(capture)
-    try:
-        scene, _, info = scenes.sphere_field()
-        scene.pack()
-    finally:
-        scene_mod.BVH.build = staticmethod(native_build)
-    mins, maxs = captured["mins"], captured["maxs"]
+    mins, maxs = field_boxes()
     count = len(mins)
     threads = os.cpu_count() or 1
 
@@ -569,8 +601,7 @@ def run_bvh(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(times), "higher_is_better": True,
         "scaling": "strong", "vs_baseline": None, "dtype": "f64 build, f32 nodes",
         "data": "synthetic (seeded mulberry32 scene)",
-        "config": {"workload": f"binned-SAH BVH of the sphere field's {count} primitive boxes, leaves of at most 4",
-                   "threads": threads, "nodes": int(b.nodeCount), "identical_to_oracle": same},
+        "config": bvh_config(count), "threads": threads, "nodes": int(b.nodeCount), "identical_to_oracle": same,
         "single_thread": {"value": count / one_s / 1e6, "unit": "Mprims/s", "ms": 1e3 * one_s},
         "e2e": {"value": value, "unit": "Mprims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
@@ -583,26 +614,9 @@ def run_bvh_reference(args):
     """The reference arm of the BVH line: the oracle's restatement of
     BVH.build (src/BVH.mjs:57-234), single-threaded as the reference's is,
     over the same 509,281 boxes."""
-    import numpy as np
-
     import oracle
-    from raymond_gb300 import scene as scene_mod
-    from raymond_gb300 import scenes
 
-    captured = {}
-    native_build = scene_mod.BVH.build
-
-    def capture(mins, maxs, *a, **k):
-        captured["mins"], captured["maxs"] = np.array(mins, dtype=np.float64), np.array(maxs, dtype=np.float64)
-        return native_build(mins, maxs, *a, **k)
-
-    scene_mod.BVH.build = staticmethod(capture)
-    try:
-        scene, _, info = scenes.sphere_field()
-        scene.pack()
-    finally:
-        scene_mod.BVH.build = staticmethod(native_build)
-    mins, maxs = captured["mins"], captured["maxs"]
+    mins, maxs = field_boxes()
     count = len(mins)
     times = []
     for _ in range(args.steps):
@@ -615,50 +629,56 @@ def run_bvh_reference(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(times), "higher_is_better": True,
         "scaling": "strong", "vs_baseline": None, "dtype": "f64 build, f32 nodes",
         "data": "synthetic (seeded mulberry32 scene)", "impl": "reference",
-        "config": {"workload": f"binned-SAH BVH of the sphere field's {count} primitive boxes, leaves of at most 4",
-                   "threads": 1},
+        "config": bvh_config(count), "threads": 1,
         "cpu_baseline": {"value": value, "unit": "Mprims/s", "cores": 1, "kind": "port",
                          "sample": f"oracle BVH.build restatement over all {count} boxes, each step"},
         "e2e": {"value": value, "unit": "Mprims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
+def batch_config(inst, bounces):
+    """The batch line's workload, the same on both arms."""
+    return {"workload": f"batch of {len(inst)} seeded sphere-field instances",
+            "paths_per_frame": sum(w * h * spp for _, _, w, h, spp, _ in inst),
+            "triangles": [i[5]["triangles"] for i in inst], "resolutions": [f"{i[2]}x{i[3]}" for i in inst],
+            "spp": [i[4] for i in inst], "bounces": bounces,
+            "l2": "inputs larger than L2 (the 64 scenes' records and images)"}
+
+
 def run_batch_reference(args):
     """The reference arm of the batch line: the oracle's f32 path tracer on
     every instance of the batch in turn (the reference renders one scene
-    at a time), on a bounded sample of each frame — `rows` rows spread
-    down each image, on all host cores."""
+    at a time), on a bounded sample of each frame — `rows` single rows at
+    the middles of equal slices of each image, on all host cores. Scenes
+    are packed by the oracle (oracle/pack.py, oracle/host.py)."""
     import oracle
     from raymond_gb300 import scenes
-    from raymond_gb300.renderer import light_table, params_block
 
     inst = scenes.batch_instances(args.batch, spheres=args.batch_spheres)
     threads = os.cpu_count() or 1
     rows = 2
     prepared = []
     for scene, camera, w, h, spp, info in inst:
-        packed = scene.pack()
-        words, powers = light_table(packed)
-        params = params_block(scene, camera, w, h, light_count=len(powers), volume_count=len(packed.volumes),
-                              max_bounces=args.bounces, spp=spp)
-        prepared.append((packed, words, params, w, h))
-    times, paths = [], 0
+        osc = OracleScene(scene)
+        prepared.append((osc, osc.params(camera, w, h, spp, args.bounces), w, h))
+    times, paths, rays = [], 0, 0
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        for packed, words, params, w, h in prepared:
-            for k in range(rows):
-                r = oracle.render(packed, words, params, region=(0, (k * h) // rows, w, 1), nthreads=threads)
+        for osc, params, w, h in prepared:
+            for y0 in band_starts(h, rows, 1):
+                r = oracle.render(osc.packed, osc.words, params, region=(0, y0, w, 1), nthreads=threads)
                 paths += r["paths"]
+                rays += r["rays"]
         times.append(time.perf_counter() - t0)
     value = paths / sum(times) / 1e6
-    sample = f"{rows} rows of each of the {len(inst)} instances' frames per step, one instance after another"
+    sample = (f"{rows} single rows at the middles of the halves of each of the {len(inst)} instances' frames per "
+              "step, one instance after another")
     return {
         "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32)",
-        "impl": "reference",
-        "config": {"workload": f"batch of {len(inst)} sphere-field instances", "bounces": args.bounces,
-                   "l2": "n/a (CPU)"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32 scenes)",
+        "impl": "reference", "config": batch_config(inst, args.bounces),
+        "rays_per_path_in_sample": rays / max(paths, 1),
         "cpu_baseline": {"value": value, "unit": "Mpaths/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -790,43 +810,54 @@ def run_rmse(args, local):
     }
 
 
+def frame_config(args, info, primitives, world, caustics):
+    """The field and caustics lines' workload, the same on both arms."""
+    return {"workload": CAUSTICS_WORKLOAD if caustics else WORKLOAD, "width": args.size, "height": args.size,
+            "spp": args.spp, "bounces": args.bounces, "triangles": info["triangles"], "spheres": info.get("spheres"),
+            "primitives": primitives, "parallelism": f"replicas x{world}", "l2": L2_NOTE}
+
+
 def run_reference(args, rank, world):
     """The reference's CPU path (the shader's path tracer restated, on all
-    host cores; for caustics with its light tracer and photon map too)."""
+    host cores; for caustics with its light tracer and photon map too), on
+    the oracle's packing of the scene."""
     if rank != 0:
         return None
     caustics = args.workload == "caustics"
     scene, camera, info = build_workload(args.size, args.spp, args.bounces, "caustics" if caustics else "field")
-    params = params_for(scene, camera, args.size, args.spp, args.bounces)
+    osc = OracleScene(scene)
+    params = osc.params(camera, args.size, args.size, args.spp, args.bounces)
     threads = os.cpu_count() or 1
     strips = 16
     rows = 2
     for _ in range(max(args.warmup, 0) and 1):
-        oracle_sample(scene, params, args.size, 1, 1, threads)
-    times, paths, light = [], 0, 0
+        oracle_sample(osc, params, args.size, args.size, 1, 1, threads)
+    times, paths, light, rays = [], 0, 0, 0.0
     for _ in range(args.steps):
         if caustics:
-            p, light, dt = caustics_cpu_sample(scene, camera, args.size, args.spp, args.bounces, threads, strips, rows)
+            p, light, dt = caustics_cpu_sample(osc, camera, args.size, args.spp, args.bounces, threads, strips, rows)
         else:
-            p, dt, _, _ = oracle_sample(scene, params, args.size, rows, strips, threads)
+            p, dt, _, rpp = oracle_sample(osc, params, args.size, args.size, rows, strips, threads)
+            rays += rpp * p
         times.append(dt)
         paths += p
     value = paths / sum(times) / 1e6
-    sample = f"{strips} bands of {rows} rows x {args.size} px, {args.spp} spp per step (1/{args.size // (strips * rows)} of a frame)"
+    sample = (f"{strips} bands of {rows} rows x {args.size} px centred in equal slices of the image, {args.spp} spp "
+              f"per step (1/{args.size // (strips * rows)} of a frame)")
     if caustics:
         sample += (f", with {light} of the frame's light paths splatted and deposited and the photon map "
                    "(those photons only) gathered on the bands")
-    return {
+    out = {
         "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32)",
-        "impl": "reference",
-        "config": {"workload": CAUSTICS_WORKLOAD if caustics else WORKLOAD, "width": args.size, "height": args.size,
-                   "spp": args.spp, "bounces": args.bounces, "triangles": info["triangles"],
-                   "spheres": info.get("spheres"), "l2": "n/a (CPU)"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32 scene)",
+        "impl": "reference", "config": frame_config(args, info, osc.packed.primitiveCount, world, caustics),
         "cpu_baseline": {"value": value, "unit": "Mpaths/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not caustics:
+        out["rays_per_path_in_sample"] = rays / max(paths, 1)
+    return out
 
 
 def run_ours(args, rank, world, local):
@@ -927,16 +958,17 @@ def run_ours(args, rank, world, local):
         threads = os.cpu_count() or 1
         # Algorithmic bytes per path from the oracle's instrumented f32 path
         # tracer on 1/64 of the frame (16 bands of 1 row), scaled to a launch.
-        params = params_for(scene, camera, args.size, args.spp, args.bounces)
-        paths_s, secs_s, bytes_per_path, rays_per_path, split = oracle_sample(scene, params, args.size, 1, 16, threads,
-                                                                              detail=True)
+        osc = OracleScene(scene)
+        params = osc.params(camera, args.size, args.size, args.spp, args.bounces)
+        paths_s, secs_s, bytes_per_path, rays_per_path, split = oracle_sample(osc, params, args.size, args.size, 1, 16,
+                                                                              threads, detail=True)
         # CPU baseline: the same port, a bounded sample (16 bands of 2 rows;
         # for caustics the same share of the light paths and of the gather).
         if caustics:
-            cpu_paths, cpu_light, cpu_s = caustics_cpu_sample(scene, camera, args.size, args.spp, args.bounces,
+            cpu_paths, cpu_light, cpu_s = caustics_cpu_sample(osc, camera, args.size, args.spp, args.bounces,
                                                               threads)
         else:
-            cpu_paths, cpu_s, _, _ = oracle_sample(scene, params, args.size, 2, 16, threads)
+            cpu_paths, cpu_s, _, _ = oracle_sample(osc, params, args.size, args.size, 2, 16, threads)
         peak, peak_kind = measured_peak_hbm()
         wavefront = sum(ext_launches) > 0
         if wavefront:
@@ -957,11 +989,8 @@ def run_ours(args, rank, world, local):
             "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32 scene)",
-            "config": {"workload": CAUSTICS_WORKLOAD if caustics else WORKLOAD, "width": args.size,
-                       "height": args.size, "spp": args.spp, "bounces": args.bounces,
-                       "triangles": info["triangles"], "spheres": info.get("spheres"),
-                       "primitives": scene.pack().primitiveCount, "parallelism": f"replicas x{world}",
-                       "path": args.path, "tuning": tuning, "l2": "flushed between steps (512 MB write)"},
+            "config": frame_config(args, info, scene.pack().primitiveCount, world, caustics),
+            "path": args.path, "tuning": tuning,
             "e2e": {"value": e2e_value, "unit": "Mpaths/s", "h2d_bytes_per_step": 208, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "stages_ms": {"trace": statistics.mean(trace_ms), "step": statistics.mean(step_ms),
@@ -974,7 +1003,8 @@ def run_ours(args, rank, world, local):
                          "bytes_per_launch": bytes_per_launch, "bytes_per_path": bytes_per_path,
                          "traversal_bytes_per_path": split},
             "cpu_baseline": {"value": cpu_paths / cpu_s / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
-                             "sample": f"16 bands of 2 rows x {args.size} px at {args.spp} spp (1/32 of a frame)"
+                             "sample": f"16 bands of 2 rows x {args.size} px centred in equal slices of the image, "
+                                       f"at {args.spp} spp (1/32 of a frame)"
                                        + (f", with {cpu_light} of the frame's light paths splatted and deposited "
                                           "and the photon map (those photons only) gathered on the bands"
                                           if caustics else "")},
@@ -1045,10 +1075,8 @@ def run_batch(args):
         "metric": METRIC, "value": paths / batch_s / 1e6, "unit": "Mpaths/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": batch_s * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mulberry32 scenes)",
-        "config": {"workload": f"batch of {len(rs)} sphere-field instances, one graph-replayed launch per frame",
-                   "paths_per_frame": paths, "triangles": [i[5]["triangles"] for i in inst],
-                   "resolutions": [f"{i[2]}x{i[3]}" for i in inst], "spp": [i[4] for i in inst],
-                   "bounces": args.bounces, "setup_s": setup_s},
+        "config": batch_config(inst, args.bounces),
+        "executor": "one graph-replayed batched frame", "setup_s": setup_s,
         "one_at_a_time": {"value": paths / single_s / 1e6, "unit": "Mpaths/s", "ms_per_step": single_s * 1e3},
         "speedup_vs_one_at_a_time": single_s / batch_s,
         "concurrent_streams": {"value": paths / streams_s / 1e6, "unit": "Mpaths/s", "ms_per_step": streams_s * 1e3},

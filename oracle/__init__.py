@@ -2,11 +2,13 @@
 
 A restatement of the reference's algorithms (BVH.build, Scene.raycast,
 the trace shader's traversal and, in oracle/pathtrace.cpp, its path
-tracer and denoiser) used only to check the product, by tests/,
-__graft_entry__.smoke() and the cpu_baseline leg of bench.py. Nothing in
-raymond_gb300 imports it. Parity status: pinned against the known answers
-of the reference's own unit tests; not against executed reference output
-(no JavaScript engine exists on either machine)."""
+tracer and denoiser; in oracle/pack.py, Scene.#pack; in oracle/host.py,
+the Renderer's host tables and uniform block) used only to check the
+product, by tests/, __graft_entry__.smoke() and the cpu_baseline and
+reference legs of bench.py. Nothing in raymond_gb300 imports it. Parity
+status: pinned against the known answers of the reference's own unit
+tests; not against executed reference output (no JavaScript engine exists
+on either machine)."""
 
 from __future__ import annotations
 

@@ -8,12 +8,14 @@ CUDA path can be checked against the same committed bytes on every machine
 Fixtures (numpy .npz):
   bvh_boxes.npz      2,000 seeded boxes and BVH.build's nodes and order for them
                      (oracle/bvh.cpp, src/BVH.mjs:57-234)
-  cornell.npz        the C1 Cornell room packed (primitives, nodes, materials, lights
-                     words), 4,096 of its jittered primary rays (64², mulberry32 seed 1)
+  cornell.npz        the C1 Cornell room packed by the oracle's Scene.#pack and lights
+                     table (oracle/pack.py, oracle/host.py): primitives, nodes,
+                     materials, lights words; 4,096 of its jittered primary rays (64², mulberry32 seed 1)
                      and Scene.raycast's answers for them (oracle/raycast.cpp,
                      src/Scene.mjs:202-283): hit primitive and distance
   cornell_image.npz  the shader's path tracer (oracle/pathtrace.cpp) on the room:
                      16×16, 4 samples, 6 bounces, the 208-byte uniform block used
+                     (the oracle's #writeParams)
 """
 
 from __future__ import annotations
@@ -29,8 +31,8 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 import oracle  # noqa: E402
+from oracle import host, pack  # noqa: E402
 from raymond_gb300 import scenes  # noqa: E402
-from raymond_gb300.renderer import light_table, params_block  # noqa: E402
 
 
 def seeded_boxes(count: int, seed: int):
@@ -42,7 +44,7 @@ def seeded_boxes(count: int, seed: int):
 
 def cornell_case():
     scene, camera = scenes.cornell_scene()
-    packed = scene.pack()
+    packed = pack.pack(scene.objects)
     size = 64
     xi = scenes.mulberry32_array(1, 2 * size * size).reshape(-1, 2)
     ys, xs = np.meshgrid(np.arange(size), np.arange(size), indexing="ij")
@@ -51,10 +53,9 @@ def cornell_case():
 
 
 def image_params(scene, camera, size=16, spp=4, bounces=6):
-    packed = scene.pack()
-    words, powers = light_table(packed)
-    return params_block(scene, camera, size, size, light_count=len(powers), max_bounces=bounces, spp=spp,
-                        firefly_clamp=0.0), words
+    words, powers = host.light_words(pack.pack(scene.objects))
+    return host.params(scene, camera, size, size, light_count=len(powers), max_bounces=bounces, spp=spp,
+                       firefly_clamp=0.0), words
 
 
 def main():
@@ -64,7 +65,7 @@ def main():
 
     scene, camera, packed, rays = cornell_case()
     hits = oracle.raycast(packed, rays)
-    words, _ = light_table(packed)
+    words, _ = host.light_words(packed)
     np.savez_compressed(os.path.join(HERE, "cornell.npz"), primitives=packed.primitives, nodes=packed.nodes,
                         materials=packed.materials, lights_words=np.asarray(words, dtype=np.uint32), rays=rays,
                         prim=hits["prim"], t=hits["t"])

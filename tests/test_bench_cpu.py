@@ -55,7 +55,7 @@ def test_bvh_build_line():
     d = run("--workload", "bvh", "--steps", "1", "--warmup", "1")
     check_common(d, 1, 1)
     assert d["unit"] == "Mprims/s" and d["gpu_launches"] == 0
-    assert d["config"]["identical_to_oracle"] is True
+    assert d["identical_to_oracle"] is True
 
 
 def test_reference_arm_follows_the_workload():
@@ -65,7 +65,24 @@ def test_reference_arm_follows_the_workload():
     assert "light paths" in d["cpu_baseline"]["sample"]
     d = run("--impl", "reference", "--workload", "batch", "--batch", "4", "--steps", "1", "--warmup", "0")
     check_common(d, 1, 0)
-    assert d["impl"] == "reference" and d["config"]["workload"] == "batch of 4 sphere-field instances"
+    assert d["impl"] == "reference" and d["config"]["workload"] == "batch of 4 seeded sphere-field instances"
+    assert len(d["config"]["resolutions"]) == 4 and d["config"]["paths_per_frame"] > 0
     for workload in ("denoise", "rmse"):
         d = run("--impl", "reference", "--workload", workload, "--steps", "1", "--warmup", "0")
         assert d["impl"] == "reference" and d["unavailable"]
+
+
+@pytest.mark.parametrize("workload", ["field", "caustics", "batch", "primary", "bvh"])
+def test_reference_arm_maps_no_product_library(workload):
+    """The reference arm packs its scenes with the oracle (oracle/pack.py,
+    oracle/host.py) and never loads libraymond_cuda.so: after it runs, the
+    process maps the oracle's library and not the product's."""
+    args = ["--impl", "reference", "--workload", workload, "--steps", "1", "--warmup", "0"]
+    args += {"field": ["--size", "32"], "caustics": ["--size", "32"], "batch": ["--batch", "2"]}.get(workload, [])
+    code = ("import runpy, sys; sys.argv = ['bench.py'] + sys.argv[1:]; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPS', 'libraymond_cuda' in maps, 'liboracle' in maps)")
+    r = subprocess.run([sys.executable, "-c", code, *args], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    marker = [ln for ln in r.stdout.splitlines() if ln.startswith("MAPS")]
+    assert marker == ["MAPS False True"], r.stdout[-2000:]

@@ -36,13 +36,19 @@ def test_native_bvh_matches_golden(threads):
     assert np.array_equal(b.order, g["order"])
 
 
-def test_packed_cornell_matches_golden():
+@pytest.mark.parametrize("packer", ["product", "oracle"])
+def test_packed_cornell_matches_golden(packer):
+    """The fixture is the oracle's packing (oracle/pack.py, Scene.#pack
+    restated); the product's packer must reproduce it byte for byte."""
+    from oracle import host, pack
+
     g = load("cornell.npz")
     scene, camera = scenes.cornell_scene()
-    packed = scene.pack()
+    packed = scene.pack() if packer == "product" else pack.pack(scene.objects)
     assert np.array_equal(packed.primitives, g["primitives"])
     assert np.array_equal(packed.nodes, g["nodes"])
     assert np.array_equal(packed.materials, g["materials"])
+    assert np.array_equal(host.light_words(packed)[0], g["lights_words"])
 
 
 def test_oracle_raycast_matches_golden():
