@@ -178,6 +178,22 @@ int raymond_trace_primary_device(raymond_t* h, const float* d_rays, uint32_t n, 
                                  float* d_t);
 
 /*
+ * The sample streams the kernels draw from, for checking them bit for bit
+ * against the reference's (src/shaders.mjs:135-212; seeding :1852-1859 for
+ * camera paths, :1638 for light paths, :1585 for the photon gather). For
+ * each of n (pixel index, sample index) pairs: for each dimension id in
+ * dim_ids, the camera path's rand2() at that dimension (two values) then its
+ * rand() (one); the path's spectrum position (:1857-1859); then `chain`
+ * draws of light path `pixel index`'s PCG chain in a frame starting at
+ * `sample index`, and `chain` draws of that pixel's gather chain. out holds
+ * n × (3·dims + 1 + 2·chain) floats. At most 2^20 pairs, 64 dimensions and
+ * 64 chain draws. Host pointers; synchronous. Test support: no counterpart
+ * call in the reference, whose streams live inside its shader.
+ */
+int raymond_sample_streams(raymond_t* h, const uint32_t* pairs, uint32_t n, const uint32_t* dim_ids, uint32_t dims,
+                           uint32_t chain, uint32_t seed_hash, float* out);
+
+/*
  * Standalone BVH builder producing BVH.build's exact output (src/BVH.mjs:
  * 57-234): mins/maxs 3 doubles per primitive; nodes_out room for
  * max(1, 2*count - 1) 32-byte nodes; order_out count u32. Host only, no

@@ -48,6 +48,8 @@ def lib():
         _lib.ro_light_trace.argtypes = [P, P, P, P, P, P, P, U32, U32, U32, U32, P, P, I]
         _lib.ro_photon_gather.restype = None
         _lib.ro_photon_gather.argtypes = [P, P, P, P, P, P, P, U32, U32, U32, U32, P, I]
+        _lib.ro_sample_streams.restype = None
+        _lib.ro_sample_streams.argtypes = [P, U32, P, U32, U32, U32, P]
         _lib.ro_denoise.restype = None
         _lib.ro_denoise.argtypes = [P, P, P, U32, U32, U32, P, I]
         _lib.ro_display.restype = None
@@ -209,6 +211,20 @@ def photon_gather(packed, lights_words, params: bytes, photons, seed_hash=0, nth
                            _p(pbuf), _p(ph), count,
                            *(rows if rows is not None else (0, height)), seed_hash, _p(accum), nthreads or threads())
     return accum.reshape(height, width, 4)
+
+
+def sample_streams(pairs, dim_ids, chain, seed_hash=0):
+    """The oracle's sample streams (src/shaders.mjs:135-212 and the seedings
+    at :1585, :1638, :1852-1859) in raymond_sample_streams's layout: per
+    (pixel index, sample index) pair, rand2() and rand() at each dimension
+    id, the spectrum position, `chain` light-path draws, `chain` gather draws."""
+    pairs = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1, 2)
+    dims = np.ascontiguousarray(dim_ids, dtype=np.uint32).reshape(-1)
+    per = 3 * dims.size + 1 + 2 * int(chain)
+    out = np.zeros((len(pairs), per), dtype=np.float32)
+    lib().ro_sample_streams(_p(pairs), len(pairs), _p(dims) if dims.size else None, dims.size, int(chain), int(seed_hash),
+                            _p(out))
+    return out
 
 
 def denoise(accum, guide_albedo, guide_normal, width, height, total_samples, nthreads=None):

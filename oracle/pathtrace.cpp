@@ -143,6 +143,31 @@ struct Sampler {
     }
 };
 
+// The streams' seeds: main()'s per sample (src/shaders.mjs:1852-1859),
+// light_trace()'s per photon (:1638), photon_gather()'s per pixel (:1585).
+Sampler camera_sampler(uint32_t index, uint32_t sample, uint32_t seed_hash) {
+    Sampler sm;
+    sm.rng_state = pcg(index ^ pcg(sample)) ^ seed_hash;
+    sm.qmc_on = true;
+    sm.qmc_seed = pcg(index + 0x9e3779b9u) ^ seed_hash;
+    sm.qmc_index = sample;
+    sm.qmc_dim = 0u;
+    return sm;
+}
+float spectrum_at(uint32_t index, uint32_t sample) {
+    return float((pcg(index * 7919u + 1u) + sample * 2654435769u) >> 8u) * (1.0f / 16777216.0f);
+}
+Sampler light_sampler(uint32_t id, uint32_t sample_offset, uint32_t seed_hash) {
+    Sampler sm;
+    sm.rng_state = pcg(id ^ pcg(sample_offset * 2654435769u + 977u)) ^ seed_hash;
+    return sm;
+}
+Sampler gather_sampler(uint32_t index, uint32_t sample_offset, uint32_t seed_hash) {
+    Sampler sm;
+    sm.rng_state = pcg(index ^ pcg(sample_offset * 2654435769u + 4099u)) ^ seed_hash;
+    return sm;
+}
+
 // frame (src/shaders.mjs:217-225): columns c0, c1, n.
 inline V in_frame(V n, V l) {
     const float s = n.z >= 0.0f ? 1.0f : -1.0f;
@@ -1091,8 +1116,7 @@ void splat(Ctx& c, const Surf& s, const Mat& m, V base, V d, V beta, Sampler& sm
 void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t seed_hash, uint32_t* splats,
                  std::vector<Photon>& stored) {
     const Params& P = c.P;
-    Sampler sm;
-    sm.rng_state = pcg(id ^ pcg(P.sample_offset * 2654435769u + 977u)) ^ seed_hash;
+    Sampler sm = light_sampler(id, P.sample_offset, seed_hash);
     const float* header = E;
     const uint32_t sources = fbits(header[0]), targets = fbits(header[1]);
     const float xi = sm.rand();
@@ -1307,15 +1331,8 @@ void render_impl(const void* prims, const void* nodes, const void* materials, co
                 float sum[4] = {0, 0, 0, 0}, sa[3] = {0, 0, 0}, sn[4] = {0, 0, 0, 0};
                 for (uint32_t s = 0; s < P.samples_per_frame; ++s) {
                     // main()'s seeding (src/shaders.mjs:1852-1859)
-                    Sampler sm;
-                    sm.rng_state = pcg(index ^ pcg(P.sample_offset + s)) ^ seed_hash;
-                    sm.qmc_on = true;
-                    sm.qmc_seed = pcg(index + 0x9e3779b9u) ^ seed_hash;
-                    sm.qmc_index = P.sample_offset + s;
-                    sm.qmc_dim = 0u;
-                    const float spectrum_u =
-                        float((pcg(index * 7919u + 1u) + (P.sample_offset + s) * 2654435769u) >> 8u) *
-                        (1.0f / 16777216.0f);
+                    Sampler sm = camera_sampler(index, P.sample_offset + s, seed_hash);
+                    const float spectrum_u = spectrum_at(index, P.sample_offset + s);
                     V col, ga = vs(0.0f);
                     float gn[4] = {0, 0, 0, 0};
                     if (P.view == 0u) {
@@ -1470,8 +1487,7 @@ extern "C" void ro_photon_gather(const void* prims, const void* nodes, const voi
             const uint32_t k0 = next.fetch_add(64);
             if (k0 >= n) break;
             for (uint32_t index = k0; index < std::min(n, k0 + 64); ++index) {
-                Sampler sm;
-                sm.rng_state = pcg(index ^ pcg(P.sample_offset * 2654435769u + 4099u)) ^ seed_hash;
+                Sampler sm = gather_sampler(index, P.sample_offset, seed_hash);
                 const float jx = sm.rand();
                 const float jy = sm.rand();
                 V o, d;
@@ -1700,5 +1716,31 @@ extern "C" void ro_display(const float* accum, const float* denoised, const void
         out[i * 4 + 1] = byte(o[1]);
         out[i * 4 + 2] = byte(o[2]);
         out[i * 4 + 3] = 255;
+    }
+}
+
+// The streams as the product's raymond_sample_streams lays them out: per
+// (pixel index, sample index) pair, rand2() then rand() at each dimension id
+// of the camera path's stream, its spectrum position, then `chain` draws of
+// the light path's and of the gather's PCG chains.
+extern "C" void ro_sample_streams(const uint32_t* pairs, uint32_t n, const uint32_t* dim_ids, uint32_t dims,
+                                  uint32_t chain, uint32_t seed_hash, float* out) {
+    const size_t per = 3u * dims + 1u + 2u * chain;
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t index = pairs[2 * i], sample = pairs[2 * i + 1];
+        float* o = out + size_t(i) * per;
+        for (uint32_t k = 0; k < dims; ++k) {
+            Sampler s = camera_sampler(index, sample, seed_hash);
+            s.qmc_dim = dim_ids[k];
+            s.rand2(o[3 * k], o[3 * k + 1]);
+            s.qmc_dim = dim_ids[k];
+            o[3 * k + 2] = s.rand();
+        }
+        o += 3u * dims;
+        *o++ = spectrum_at(index, sample);
+        Sampler light = light_sampler(index, sample, seed_hash);
+        for (uint32_t k = 0; k < chain; ++k) *o++ = light.rand();
+        Sampler gather = gather_sampler(index, sample, seed_hash);
+        for (uint32_t k = 0; k < chain; ++k) *o++ = gather.rand();
     }
 }

@@ -177,6 +177,36 @@ struct Rng {
     }
 };
 
+// The streams' seeds. A camera path: pixel `index`, sample `sample` (main(),
+// src/shaders.mjs:1852-1859), scrambled Sobol from dimension 0, with its
+// golden-ratio spectrum position. A light path `id` of the frame starting at
+// sample_offset (light_trace(), :1638) and a pixel's photon gather (:1585):
+// PCG chains. seed_hash is 0 for the reference's streams.
+__device__ __forceinline__ Rng camera_rng(uint32_t index, uint32_t sample, uint32_t seed_hash) {
+    Rng r;
+    r.state = pcg(index ^ pcg(sample)) ^ seed_hash;
+    r.qmc = true;
+    r.seed = pcg(index + 0x9e3779b9u) ^ seed_hash;
+    r.index = sample;
+    r.dim = 0u;
+    return r;
+}
+__device__ __forceinline__ float spectrum_position(uint32_t index, uint32_t sample) {
+    return float((pcg(index * 7919u + 1u) + sample * 2654435769u) >> 8u) * (1.0f / 16777216.0f);
+}
+__device__ __forceinline__ Rng light_rng(uint32_t id, uint32_t sample_offset, uint32_t seed_hash) {
+    Rng r{};
+    r.qmc = false;
+    r.state = pcg(id ^ pcg(sample_offset * 2654435769u + 977u)) ^ seed_hash;
+    return r;
+}
+__device__ __forceinline__ Rng gather_rng(uint32_t index, uint32_t sample_offset, uint32_t seed_hash) {
+    Rng r{};
+    r.qmc = false;
+    r.state = pcg(index ^ pcg(sample_offset * 2654435769u + 4099u)) ^ seed_hash;
+    return r;
+}
+
 // ---- sampling (src/shaders.mjs:217-256) ----
 // Orthonormal basis whose third axis is n (Duff et al., 2017); returns the
 // world vector for local coordinates l.

@@ -688,12 +688,8 @@ __device__ __forceinline__ void path_begin(const Params& P, uint32_t seed_hash, 
                                            PathState& ps) {
     const uint32_t index = y * P.width + x;
     const uint32_t sample = P.sample_offset + k;
-    ps.rng.state = pcg(index ^ pcg(sample)) ^ seed_hash;
-    ps.rng.qmc = true;
-    ps.rng.seed = pcg(index + 0x9e3779b9u) ^ seed_hash;
-    ps.rng.index = sample;
-    ps.rng.dim = 0u;
-    ps.spectrum_u = float((pcg(index * 7919u + 1u) + sample * 2654435769u) >> 8u) * (1.0f / 16777216.0f);
+    ps.rng = camera_rng(index, sample, seed_hash);
+    ps.spectrum_u = spectrum_position(index, sample);
     const float2 j = ps.rng.rand2();
     ps.g_albedo = f3(1.0f);
     ps.g_normal = make_float4(0.0f, 0.0f, 0.0f, 0.0f);

@@ -90,6 +90,8 @@ struct WavefrontTuning {
 // launches it enqueued.
 int launch_trace_primary(const Scene& s, const float* rays, uint32_t n, uint32_t* prim, float* t,
                          uint32_t* work_counter, int num_sms, cudaStream_t st);
+int launch_sample_streams(const uint32_t* pairs, uint32_t n, const uint32_t* dim_ids, uint32_t dims, uint32_t chain,
+                          uint32_t seed_hash, float* out, cudaStream_t st);
 int launch_megakernel(const Scene& s, const Params& P, uint32_t features, const PixelBuffers& px, int num_sms,
                       cudaStream_t st);
 int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,

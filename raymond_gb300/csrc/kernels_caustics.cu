@@ -68,9 +68,7 @@ __global__ void __launch_bounds__(CAUSTIC_BLOCK) k_light_trace(Scene s, Params P
     uint32_t* col = stack + threadIdx.x;
     const uint32_t photons = cb.photons_per_frame;
     for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < photons; id += gridDim.x * blockDim.x) {
-        Rng rng{};
-        rng.qmc = false;
-        rng.state = pcg(id ^ pcg(P.sample_offset * 2654435769u + 977u)) ^ s.seed_hash;
+        Rng rng = light_rng(id, P.sample_offset, s.seed_hash);
 
         const float4 header = s.emitters[0];
         const uint32_t sources = __float_as_uint(header.x);
@@ -262,9 +260,7 @@ __global__ void __launch_bounds__(CAUSTIC_BLOCK) k_photon_gather(Scene s, Params
     uint32_t* col = stack + threadIdx.x;
     const uint32_t n = P.width * P.height;
     for (uint32_t index = blockIdx.x * blockDim.x + threadIdx.x; index < n; index += gridDim.x * blockDim.x) {
-        Rng rng{};
-        rng.qmc = false;
-        rng.state = pcg(index ^ pcg(P.sample_offset * 2654435769u + 4099u)) ^ s.seed_hash;
+        Rng rng = gather_rng(index, P.sample_offset, s.seed_hash);
         const float jx = rng.rand();
         const float jy = rng.rand();
         float3 o, d;

@@ -43,6 +43,42 @@ int launch_trace_primary(const Scene& s, const float* rays, uint32_t n, uint32_t
     return 1;
 }
 
+// The sample streams, drawn as the kernels draw them (camera_rng, light_rng,
+// gather_rng and Rng's rand/rand2), for bit-for-bit checks. Per pair: for
+// each dimension id, rand2()'s two values then rand()'s one at that
+// dimension; the spectrum position; `chain` draws of the light path's and of
+// the gather's PCG chains.
+__global__ void k_sample_streams(const uint32_t* __restrict__ pairs, uint32_t n, const uint32_t* __restrict__ dim_ids,
+                                 uint32_t dims, uint32_t chain, uint32_t seed_hash, float* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t index = pairs[2 * i], sample = pairs[2 * i + 1];
+    float* o = out + size_t(i) * (3u * dims + 1u + 2u * chain);
+    for (uint32_t k = 0; k < dims; ++k) {
+        Rng r = camera_rng(index, sample, seed_hash);
+        r.dim = dim_ids[k];
+        const float2 two = r.rand2();
+        r.dim = dim_ids[k];
+        const float one = r.rand();
+        o[3 * k] = two.x;
+        o[3 * k + 1] = two.y;
+        o[3 * k + 2] = one;
+    }
+    o += 3u * dims;
+    *o++ = spectrum_position(index, sample);
+    Rng light = light_rng(index, sample, seed_hash);
+    for (uint32_t k = 0; k < chain; ++k) *o++ = light.rand();
+    Rng gather = gather_rng(index, sample, seed_hash);
+    for (uint32_t k = 0; k < chain; ++k) *o++ = gather.rand();
+}
+
+int launch_sample_streams(const uint32_t* pairs, uint32_t n, const uint32_t* dim_ids, uint32_t dims, uint32_t chain,
+                          uint32_t seed_hash, float* out, cudaStream_t st) {
+    if (n == 0) return 0;
+    k_sample_streams<<<(n + 127u) / 128u, 128, 0, st>>>(pairs, n, dim_ids, dims, chain, seed_hash, out);
+    return 1;
+}
+
 // ---- the megakernel: main() (src/shaders.mjs:1838-1895), one thread per pixel ----
 constexpr int MK_BLOCK_X = 16, MK_BLOCK_Y = 8, MK_BLOCK = MK_BLOCK_X * MK_BLOCK_Y;
 

@@ -891,6 +891,32 @@ int raymond_trace_primary(raymond_t* h, const float* rays, uint32_t n, uint32_t*
     return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "trace read-back");
 }
 
+int raymond_sample_streams(raymond_t* h, const uint32_t* pairs, uint32_t n, const uint32_t* dim_ids, uint32_t dims,
+                           uint32_t chain, uint32_t seed_hash, float* out) {
+    if (!h) return RAYMOND_EINVAL;
+    if (n == 0) return RAYMOND_OK;
+    if (!pairs || !out || (dims && !dim_ids)) return h->fail(RAYMOND_EINVAL, "Null buffer.");
+    if (n > (1u << 20) || dims > 64u || chain > 64u)
+        return h->fail(RAYMOND_EINVAL, "At most 2^20 pairs, 64 dimensions and 64 chain draws.");
+    cudaSetDevice(h->device);
+    const size_t per = 3u * dims + 1u + 2u * chain;
+    const size_t in_bytes = size_t(n) * 8 + size_t(dims) * 4;
+    cudaError_t e;
+    if ((e = h->ray_scratch.reserve(in_bytes)) != cudaSuccess) return h->cuda_fail(e, "stream inputs");
+    if ((e = h->prim_scratch.reserve(size_t(n) * per * 4)) != cudaSuccess) return h->cuda_fail(e, "stream outputs");
+    uint32_t* d_pairs = static_cast<uint32_t*>(h->ray_scratch.ptr);
+    uint32_t* d_dims = d_pairs + size_t(n) * 2;
+    e = cudaMemcpyAsync(d_pairs, pairs, size_t(n) * 8, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess && dims) e = cudaMemcpyAsync(d_dims, dim_ids, size_t(dims) * 4, cudaMemcpyHostToDevice, h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "stream inputs");
+    float* d_out = static_cast<float*>(h->prim_scratch.ptr);
+    launch_sample_streams(d_pairs, n, d_dims, dims, chain, seed_hash, d_out, h->stream);
+    if ((e = cudaGetLastError()) != cudaSuccess) return h->cuda_fail(e, "sample streams");
+    e = cudaMemcpyAsync(out, d_out, size_t(n) * per * 4, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "stream read-back");
+}
+
 int raymond_get_buffers(raymond_t* h, raymond_buffers* out) {
     if (!h || !out) return RAYMOND_EINVAL;
     out->accum = static_cast<float*>(h->accum.ptr);
