@@ -9,7 +9,11 @@ denoiser and the tone map. Prints one JSON line (rank 0).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--spp S] [--impl ours|reference]
 
 The default line also carries "learned_denoiser": the learned denoiser's
-inference on a 1920×1080 frame of the same scene against the tensor peak.
+inference on a 1920×1080 frame of the same scene against the tensor peak;
+and "time_to_rmse": the wall time to RMSE ≤ 0.01 against a 16,384-spp
+render of the scene, for the one-kernel path with the à-trous filter, the
+wavefront path's raw running average, and the wavefront path with the
+learned denoiser on the display (about 45 s; --no-rmse skips it).
 Other workloads (--workload):
   caustics the water-caustics scene at 1024² with light tracing (1M light paths
            splatted) and photon mapping (up to 4M photons, r = 0.01) every frame
@@ -19,9 +23,7 @@ Other workloads (--workload):
            traversal launch per step (--size sets the image side)
   bvh      the scene producer: BVH.build over the sphere field's primitive
            boxes on the host cores (no GPU), against the oracle's build
-  rmse     time to RMSE ≤ 0.01 against a 16,384-spp render: the plain
-           one-kernel path with à-trous vs the batched wavefront path with
-           the learned denoiser
+  rmse     the time-to-RMSE measurement alone, as its own line
 
 Under torchrun each rank renders its own copy of the frame (replicas; the
 scene does not shard across GPUs here): value = paths of all ranks ÷ the
@@ -690,29 +692,29 @@ REFERENCE_UNAVAILABLE = {
 }
 
 
-def run_rmse(args, local):
-    """Time to RMSE ≤ 0.01 against a 16,384-spp render of the sphere field:
-    the plain one-kernel path with the à-trous filter against the batched
-    wavefront path with the learned denoiser, both displaying after every
-    frame of --spp samples. Frame times are wall-clock (each frame waited
-    for); the RMSE check after a frame is not timed."""
-    import numpy as np
+def time_to_rmse(scene, camera, local, size, spp, bounces, threshold=0.01, reference_spp=16384, max_spp=4096):
+    """Time to RMSE ≤ threshold against a reference_spp render of the scene
+    (RMSE over linear RGB as tests/browser/app.test.mjs:574-580 computes it),
+    displaying after every frame of `spp` samples, for three ways of
+    showing the image:
+      plain_atrous    the one-kernel path, the display the à-trous filter's
+      raw_average     the wavefront path, the display the running average
+      learned         the wavefront path with the learned denoiser on the
+                      display (the running average is left as it is)
+    Frame times are wall-clock, each frame waited for; the RMSE check after
+    a frame is not timed."""
     import torch
 
     import raymond_gb300 as rg
     from raymond_gb300 import _native
     from raymond_gb300.denoiser import DEFAULT_WEIGHTS, Denoiser
 
-    size = args.size
-    scene, camera, info = build_workload(size, args.spp, args.bounces)
     dev = f"cuda:{local}"
-    clocks = ClockSampler(local)
-    clocks.start()
 
     def renderer(seed, flags):
         r = rg.Renderer.create(rg.Canvas(size, size), device=local, seed=seed)
         r.scene, r.camera = scene, camera
-        r.maxBounces = args.bounces
+        r.maxBounces = bounces
         r.caustics = False
         r.flags = flags
         return r
@@ -721,92 +723,96 @@ def run_rmse(args, local):
     ref = renderer(0x2545F491, _native.FLAG_WAVEFRONT)
     ref.denoise = False
     ref.samplesPerFrame = 64
-    for _ in range(args.reference_spp // 64):
+    for _ in range(reference_spp // 64):
         ref.render()
     target = torch.from_numpy(ref.readPixels().reshape(size, size, 4)).to(dev)
     ref.dispose()
     ref_s = time.perf_counter() - t0
 
-    def denoised_view(r):
+    def view(r, which):
         b = _native.Buffers()
         _native.check(_native.lib().raymond_get_buffers(r.handle, b), r.handle)
-        return device_view(torch, b.denoised, (size, size, 4), local)
+        return device_view(torch, b.denoised if which == "denoised" else b.accum, (size, size, 4), local)
 
-    def err(view):
-        d = view[..., :3] - target[..., :3]
+    def rmse(img):
+        d = img[..., :3] - target[..., :3]
         return float(torch.sqrt(torch.mean(d * d)).item())
 
-    def accum_view(r):
-        b = _native.Buffers()
-        _native.check(_native.lib().raymond_get_buffers(r.handle, b), r.handle)
-        return device_view(torch, b.accum, (size, size, 4), local)
-
-    def run(r, frame):
-        view = None  # the renderer's buffers exist from its first frame on
-        elapsed, curve = 0.0, []
-        reached = None
-        while r.samples < args.max_spp:
+    def run(r, display):
+        """Frames until the displayed image (and the running average) reach
+        the threshold: (first (spp, seconds) for the display, the same for
+        the running average, the curve)."""
+        views, elapsed, curve = None, 0.0, []
+        shown = raw = None
+        while r.samples < max_spp and (shown is None or raw is None):
             torch.cuda.synchronize()
             t = time.perf_counter()
-            frame()
+            r.render()
+            r._sync()
             elapsed += time.perf_counter() - t
-            if view is None:
-                view, raw = denoised_view(r), accum_view(r)
-            e = err(view)
-            # the running average itself, for reference (not what is displayed)
-            d = raw[..., :3] / r.samples - target[..., :3]
-            curve.append((r.samples, elapsed, e, float(torch.sqrt(torch.mean(d * d)).item())))
-            if e <= args.threshold:
-                reached = (r.samples, elapsed)
-                break
-        return reached, curve
+            if views is None:
+                views = (view(r, display), view(r, "accum"))
+            e_raw = rmse(views[1] / r.samples)
+            e = e_raw if display == "accum" else rmse(views[0])
+            curve.append((r.samples, round(elapsed, 4), round(e, 5), round(e_raw, 5)))
+            if shown is None and e <= threshold:
+                shown = (r.samples, elapsed)
+            if raw is None and e_raw <= threshold:
+                raw = (r.samples, elapsed)
+        return shown, raw, curve
+
+    def summary(reached, curve):
+        return {"reached": reached is not None, "seconds": reached[1] if reached else None,
+                "spp": reached[0] if reached else None, "ms_per_frame": 1e3 * curve[-1][1] / len(curve),
+                "curve_spp_seconds_rmse_rawrmse": curve[:: max(1, len(curve) // 24)]}
 
     plain = renderer(0, _native.FLAG_MEGAKERNEL)
     plain.denoise = True
-    plain.samplesPerFrame = args.spp
-
-    def plain_frame():
-        plain.render()
-        plain.device.queue.onSubmittedWorkDone()
-
-    plain_reached, plain_curve = run(plain, plain_frame)
+    plain.samplesPerFrame = spp
+    p_shown, _, p_curve = run(plain, "denoised")
     plain.dispose()
+
+    raw = renderer(0, _native.FLAG_WAVEFRONT)
+    raw.denoise = False
+    raw.samplesPerFrame = spp
+    r_shown, _, r_curve = run(raw, "accum")
+    raw.dispose()
 
     net = Denoiser(device=local, weights=DEFAULT_WEIGHTS)
     ours = renderer(0, _native.FLAG_WAVEFRONT)
     ours.denoise = True
     ours.learnedDenoiser = net
-    ours.samplesPerFrame = args.spp
-    batch = rg.BatchRenderer(device=local, graph=True)
-
-    def ours_frame():
-        batch.render([ours])
-        ours._sync()
-
-    ours_reached, ours_curve = run(ours, ours_frame)
+    ours.samplesPerFrame = spp
+    o_shown, _, o_curve = run(ours, "denoised")
     ours.dispose()
-    batch.dispose()
     net.dispose()
 
-    def summary(reached, curve):
-        last = curve[-1]
-        return {"reached": reached is not None, "seconds": reached[1] if reached else None,
-                "spp": reached[0] if reached else None, "final_spp": last[0], "final_rmse": last[2],
-                "curve_spp_seconds_rmse_rawrmse": [(s, round(t, 4), round(e, 5), round(q, 5))
-                                                   for s, t, e, q in curve[:: max(1, len(curve) // 40)]]}
-
-    clock_info = clocks.stop()
-    p = summary(plain_reached, plain_curve)
-    o = summary(ours_reached, ours_curve)
-    speedup = (p["seconds"] / o["seconds"]) if (p["reached"] and o["reached"]) else None
+    p, a, o = summary(p_shown, p_curve), summary(r_shown, r_curve), summary(o_shown, o_curve)
+    ok = p["reached"] and o["reached"]
     return {
-        "metric": "time-to-RMSE 0.01 (batched wavefront + learned denoiser)", "value": o["seconds"], "unit": "s",
+        "workload": f"sphere field {size}x{size}, {spp} spp per displayed frame, {bounces} bounces",
+        "threshold": threshold, "reference_spp": reference_spp, "reference_seconds": ref_s, "max_spp": max_spp,
+        "plain_atrous": p, "raw_average": a, "learned": o,
+        "speedup_vs_plain_atrous": p["seconds"] / o["seconds"] if ok else None,
+        "speedup_vs_raw_average": a["seconds"] / o["seconds"] if (a["reached"] and o["reached"]) else None,
+    }
+
+
+def run_rmse(args, local):
+    """Time to RMSE ≤ 0.01 against a 16,384-spp render as its own line."""
+    scene, camera, info = build_workload(args.size, args.spp, args.bounces)
+    clocks = ClockSampler(local)
+    clocks.start()
+    t = time_to_rmse(scene, camera, local, args.size, args.spp, args.bounces, args.threshold, args.reference_spp,
+                     args.max_spp)
+    clock_info = clocks.stop()
+    return {
+        "metric": "time-to-RMSE 0.01 (wavefront + learned denoiser)", "value": t["learned"]["seconds"], "unit": "s",
         "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 trace, bf16 network", "data": "synthetic (seeded mulberry32 scene)",
-        "config": {"workload": f"sphere field {size}x{size}, {args.spp} spp per displayed frame, {args.bounces} bounces",
-                   "threshold": args.threshold, "reference_spp": args.reference_spp, "reference_seconds": ref_s,
-                   "max_spp": args.max_spp},
-        "plain_atrous": p, "batched_learned": o, "speedup_vs_plain_atrous": speedup, "clocks": clock_info,
+        "config": {"workload": t["workload"], "threshold": args.threshold, "reference_spp": args.reference_spp,
+                   "max_spp": args.max_spp, "l2": L2_NOTE},
+        "time_to_rmse": t, "clocks": clock_info,
     }
 
 
@@ -1017,6 +1023,12 @@ def run_ours(args, rank, world, local):
     r.dispose()
     if rank == 0 and not args.no_denoiser and not caustics:
         result["learned_denoiser"] = measure_denoiser(scene, camera, local, 10, 3)
+    if rank == 0 and not args.no_rmse and not caustics and args.size == 1024:
+        clocks = ClockSampler(local)
+        clocks.start()
+        result["time_to_rmse"] = time_to_rmse(scene, camera, local, args.size, args.spp, args.bounces,
+                                              args.threshold, args.reference_spp, args.max_spp)
+        result["time_to_rmse"]["clocks"] = clocks.stop()
     return result
 
 
@@ -1104,6 +1116,7 @@ def main():
     ap.add_argument("--reference-spp", type=int, default=16384)
     ap.add_argument("--max-spp", type=int, default=4096)
     ap.add_argument("--no-denoiser", action="store_true", help="skip the learned-denoiser sub-measurement")
+    ap.add_argument("--no-rmse", action="store_true", help="skip the time-to-RMSE sub-measurement")
     ap.add_argument("--bvh-width", type=int, default=0, choices=[0, 2, 4],
                     help="force the binary (2) or 4-wide (4) traversal tree; 0 keeps the tuned choice")
     ap.add_argument("--batch", type=int, default=64)

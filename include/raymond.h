@@ -194,6 +194,36 @@ int raymond_sample_streams(raymond_t* h, const uint32_t* pairs, uint32_t n, cons
                            uint32_t chain, uint32_t seed_hash, float* out);
 
 /*
+ * One frame's light tracing alone, for checking it against the reference's
+ * light_trace (src/shaders.mjs:1628-1814): runs the light-tracing kernel a
+ * caustics frame runs, with params208 on the uploaded scene and emitters
+ * (the photon count, capacity and radius of raymond_set_photons), and copies
+ * out its fixed-point splat sums before they are resolved into the image
+ * (width × height × 4 u32, 1/65536 units; splat_bytes ≥ width·height·16)
+ * and the photons it deposited, 10 floats each: where it landed, its power,
+ * the direction it came from, and its light path's id (u32 bits). Photons
+ * come in the order the GPU's atomics stored them; *photon_count is their
+ * number (at most the map's capacity) and photon_floats must hold 10 per
+ * photon (NULL photons: the count alone). The image is untouched. Host
+ * pointers; synchronous.
+ */
+int raymond_light_trace(raymond_t* h, const void* params208, uint32_t features, uint32_t* splats, uint64_t splat_bytes,
+                        float* photons, uint64_t photon_floats, uint32_t* photon_count);
+
+/*
+ * The photon map's gather alone, on a caller's photons (n × 9 floats:
+ * position, power, direction it came from; n at most the map's capacity),
+ * for checking it against the reference's photon_gather (src/shaders.mjs:
+ * 1577-1626): links them into the hashed grid and runs the gather kernel a
+ * caustics frame runs, writing the light it adds to each pixel (width ×
+ * height × 4 floats: RGB × samples_per_frame and luminance² ×
+ * samples_per_frame, as the frame accumulates it) into out. Host pointers;
+ * synchronous.
+ */
+int raymond_photon_gather(raymond_t* h, const void* params208, uint32_t features, const float* photons, uint32_t n,
+                          float* out, uint64_t out_bytes);
+
+/*
  * Standalone BVH builder producing BVH.build's exact output (src/BVH.mjs:
  * 57-234): mins/maxs 3 doubles per primitive; nodes_out room for
  * max(1, 2*count - 1) 32-byte nodes; order_out count u32. Host only, no

@@ -45,9 +45,11 @@ def lib():
         _lib.ro_render_scene.argtypes = [P, P, P, P, P, P, U32, U32, U32, U32, U32, P, P, P, P, I, P, U32, U32, P, U32,
                                          U32, P, U32, U32, P, U32, U32]
         _lib.ro_light_trace.restype = U32
-        _lib.ro_light_trace.argtypes = [P, P, P, P, P, P, P, U32, U32, U32, U32, P, P, I]
+        _lib.ro_light_trace.argtypes = [P, P, P, P, P, P, P, U32, U32, U32, U32, P, P, P, I]
         _lib.ro_photon_gather.restype = None
-        _lib.ro_photon_gather.argtypes = [P, P, P, P, P, P, P, U32, U32, U32, U32, P, I]
+        _lib.ro_photon_gather.argtypes = [P, P, P, P, P, P, P, U32, U32, U32, U32, P, P, I]
+        _lib.ro_set_jitter.restype = None
+        _lib.ro_set_jitter.argtypes = [U32, F]
         _lib.ro_sample_streams.restype = None
         _lib.ro_sample_streams.argtypes = [P, U32, P, U32, U32, U32, P]
         _lib.ro_denoise.restype = None
@@ -173,28 +175,31 @@ def render(packed, lights_words, params: bytes, region=None, seed_hash=0, nthrea
 def light_trace(packed, lights_words, params: bytes, emitters, photons, seed_hash=0, nthreads=None, ids=None):
     """One frame of light_trace (src/shaders.mjs:1628-1814) for its photons
     0..photons-1, or the range ids = (first, count) of them: dict splats
-    (h×w×4 u32 fixed-point sums, 1/65536 units) and photons (n×9 float32:
+    (h×w×4 u32 fixed-point sums, 1/65536 units), photons (n×9 float32:
     where each landed, its power, the direction it came from), in photon
-    order."""
+    order, and photon_ids (each one's light path)."""
     import struct
     width, height = struct.unpack_from("<2I", params, 160)
     splats = np.zeros(width * height * 4, dtype=np.uint32)
     id0, count = ids if ids is not None else (0, int(photons))
     out = np.zeros(max(int(count), 1) * 9, dtype=np.float32)
+    ids_out = np.zeros(max(int(count), 1), dtype=np.uint32)
     pbuf = np.frombuffer(bytes(params), dtype=np.uint8).copy()
     words = np.ascontiguousarray(lights_words, dtype=np.uint32)
     attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
     em = np.ascontiguousarray(emitters, dtype=np.float32)
     n = lib().ro_light_trace(_p(packed.primitives), _p(packed.nodes), _p(packed.materials), _p(attrs), _p(words),
                              _p(pbuf), _p(em), int(photons), int(id0), int(count), seed_hash, _p(splats), _p(out),
-                             nthreads or threads())
-    return {"splats": splats.reshape(height, width, 4), "photons": out[: n * 9].reshape(n, 9)}
+                             _p(ids_out), nthreads or threads())
+    return {"splats": splats.reshape(height, width, 4), "photons": out[: n * 9].reshape(n, 9),
+            "photon_ids": ids_out[:n]}
 
 
-def photon_gather(packed, lights_words, params: bytes, photons, seed_hash=0, nthreads=None, rows=None):
+def photon_gather(packed, lights_words, params: bytes, photons, seed_hash=0, nthreads=None, rows=None, visits=False):
     """One frame of photon_gather (src/shaders.mjs:1585-1626), on every row
     or rows = (first, count): the caustic light the photon map adds to each
-    pixel (h×w×4 float32 sums)."""
+    pixel (h×w×4 float32 sums); with visits, also each pixel's count of
+    photons visited (h×w; the gather stops at 4096), as (light, visits)."""
     import struct
     width, height = struct.unpack_from("<2I", params, 160)
     accum = np.zeros(width * height * 4, dtype=np.float32)
@@ -207,10 +212,34 @@ def photon_gather(packed, lights_words, params: bytes, photons, seed_hash=0, nth
     pbuf = np.frombuffer(bytes(params), dtype=np.uint8).copy()
     words = np.ascontiguousarray(lights_words, dtype=np.uint32)
     attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
+    vis = np.zeros(width * height, dtype=np.uint32) if visits else None
     lib().ro_photon_gather(_p(packed.primitives), _p(packed.nodes), _p(packed.materials), _p(attrs), _p(words),
                            _p(pbuf), _p(ph), count,
-                           *(rows if rows is not None else (0, height)), seed_hash, _p(accum), nthreads or threads())
+                           *(rows if rows is not None else (0, height)), seed_hash, _p(accum), _p(vis),
+                           nthreads or threads())
+    if visits:
+        return accum.reshape(height, width, 4), vis.reshape(height, width)
     return accum.reshape(height, width, 4)
+
+
+class jitter:
+    """Perturbation runs (oracle/pathtrace.cpp, nudge): inside the block
+    every ray the oracle traces has its origin and direction scaled
+    componentwise by 1 ± size, signs hashed from the ray and `seed`; seeds
+    2k and 2k + 1 nudge each ray opposite ways. Results that move under it
+    rest on a near-tie decision, where rounding may send the GPU the other
+    way. Not thread-safe across concurrent oracle calls."""
+
+    def __init__(self, seed: int, size: float):
+        self.seed, self.size = int(seed), float(size)
+
+    def __enter__(self):
+        lib().ro_set_jitter(self.seed, self.size)
+        return self
+
+    def __exit__(self, *exc):
+        lib().ro_set_jitter(0, 0.0)
+        return False
 
 
 def sample_streams(pairs, dim_ids, chain, seed_hash=0):

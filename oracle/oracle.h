@@ -93,16 +93,19 @@ void ro_render_scene(const void* prims, const void* nodes, const void* materials
 // ---- light tracing and photon mapping (src/shaders.mjs:1425-1831) ----
 // Photons id0..id0+count-1 of a frame of `photons`: fixed-point splats
 // added to `splats` (W·H·4 u32) and the stored photons (9 floats: p, power,
-// -d) in photon order; returns how many were stored.
+// -d) in photon order, with their light paths' ids in ids_out (or NULL);
+// returns how many were stored.
 uint32_t ro_light_trace(const void* prims, const void* nodes, const void* materials, const float* attributes,
                         const uint32_t* lights, const void* params208, const float* emitters, uint32_t photons,
                         uint32_t id0, uint32_t count, uint32_t seed_hash, uint32_t* splats, float* photons_out,
-                        int threads);
+                        uint32_t* ids_out, int threads);
 // The photon map's caustic light through mirrors and glass on rows
-// y0..y0+rows-1, added to accum (W·H·4).
+// y0..y0+rows-1, added to accum (W·H·4); each gathering pixel's count of
+// photons visited in visits_out (W·H, or NULL).
 void ro_photon_gather(const void* prims, const void* nodes, const void* materials, const float* attributes,
                       const uint32_t* lights, const void* params208, const float* photons, uint32_t count,
-                      uint32_t y0, uint32_t rows, uint32_t seed_hash, float* accum, int threads);
+                      uint32_t y0, uint32_t rows, uint32_t seed_hash, float* accum, uint32_t* visits_out,
+                      int threads);
 
 // ---- the denoiser (src/shaders.mjs:1916-2098) and display (2114-2152) ----
 // Full-image à-trous from the accumulated buffers: prepare, steps 1..16,
@@ -111,6 +114,12 @@ void ro_denoise(const float* accum, const float* guide_albedo, const float* guid
                 uint32_t total_samples, float* out, int threads);
 // The display pass into RGBA8.
 void ro_display(const float* accum, const float* denoised, const void* params208, uint8_t* out);
+
+// The sample streams in raymond_sample_streams's layout, and the
+// perturbation runs' size (0: off) and seed.
+void ro_sample_streams(const uint32_t* pairs, uint32_t n, const uint32_t* dim_ids, uint32_t dims, uint32_t chain,
+                       uint32_t seed_hash, float* out);
+void ro_set_jitter(uint32_t seed, float size);
 
 /* The learned denoiser's network (net.cpp): parameter layout, loss and
  * gradients in double (bf16 != 0 rounds weights and stored tensors to BF16

@@ -220,7 +220,27 @@ struct HitR {
     float u, v;
 };
 
+// Perturbation runs, for classifying disagreements with the GPU (off unless
+// ro_set_jitter set a size): every traced ray's origin and direction
+// components are scaled by 1 ± size, the signs a hash of the ray's own bits
+// and the run's seed, and an odd seed flipping them all, so a pair of runs
+// (2k, 2k+1) nudges each ray both ways. Results that change under such runs
+// hang on a decision within rounding of its threshold (an edge, a pixel
+// boundary, a lobe or roulette choice), where f32 arithmetic that rounds
+// differently may legitimately take the other branch.
+float g_jitter_size = 0.0f;
+uint32_t g_jitter_seed = 0u;
+
+void nudge(V& o, V& d) {
+    uint32_t h = pcg(g_jitter_seed >> 1u ^ pcg(fbits(o.x) ^ pcg(fbits(o.y) ^ pcg(fbits(o.z) ^ pcg(fbits(d.x) ^
+                     pcg(fbits(d.y) ^ pcg(fbits(d.z))))))));
+    const float s = (g_jitter_seed & 1u) ? -g_jitter_size : g_jitter_size;
+    float* f[6] = {&o.x, &o.y, &o.z, &d.x, &d.y, &d.z};
+    for (int k = 0; k < 6; ++k) *f[k] *= 1.0f + (((h >> k) & 1u) ? s : -s);
+}
+
 HitR trace(Ctx& c, V o, V d, float t_max, bool any_hit) {
+    if (g_jitter_size != 0.0f) nudge(o, d);
     const float of[3] = {o.x, o.y, o.z}, df[3] = {d.x, d.y, d.z};
     uint32_t prim, inner, tested;
     float tuv[3];
@@ -1269,7 +1289,7 @@ struct PhotonMap {
 };
 
 // gather (src/shaders.mjs:1533-1572).
-V gather(const Params& P, const PhotonMap& map, const Surf& s, const Mat& m, V base, V wo) {
+V gather(const Params& P, const PhotonMap& map, const Surf& s, const Mat& m, V base, V wo, uint32_t* visits = nullptr) {
     const float r = P.photon_radius;
     const float r2 = r * r;
     const float cell_size = P.photon_cell;
@@ -1301,6 +1321,7 @@ V gather(const Params& P, const PhotonMap& map, const Surf& s, const Mat& m, V b
             index = map.next[index - 1u];
         }
     }
+    if (visits) *visits = visited;
     return sum / (PI * r2);
 }
 
@@ -1420,7 +1441,7 @@ extern "C" void ro_render_scene(const void* prims, const void* nodes, const void
 extern "C" uint32_t ro_light_trace(const void* prims, const void* nodes, const void* materials, const float* attributes,
                                    const uint32_t* lights, const void* params208, const float* emitters,
                                    uint32_t photons, uint32_t id0, uint32_t count, uint32_t seed_hash,
-                                   uint32_t* splats, float* photons_out, int threads) {
+                                   uint32_t* splats, float* photons_out, uint32_t* ids_out, int threads) {
     Params P;
     std::memcpy(&P, params208, sizeof P);
     const uint32_t cells = P.width * P.height * 4u;
@@ -1449,6 +1470,7 @@ extern "C" uint32_t ro_light_trace(const void* prims, const void* nodes, const v
     std::sort(all.begin(), all.end(), [](const Photon& a, const Photon& b) { return a.id < b.id; });
     for (size_t i = 0; i < all.size(); ++i) {
         float* q = photons_out + i * 9;
+        if (ids_out) ids_out[i] = all[i].id;
         const V* v[3] = {&all[i].p, &all[i].beta, &all[i].wi};
         for (int j = 0; j < 3; ++j) {
             q[j * 3] = v[j]->x;
@@ -1465,7 +1487,8 @@ extern "C" uint32_t ro_light_trace(const void* prims, const void* nodes, const v
 // frame's samples.
 extern "C" void ro_photon_gather(const void* prims, const void* nodes, const void* materials, const float* attributes,
                                  const uint32_t* lights, const void* params208, const float* photons, uint32_t count,
-                                 uint32_t y0, uint32_t rows, uint32_t seed_hash, float* accum, int threads) {
+                                 uint32_t y0, uint32_t rows, uint32_t seed_hash, float* accum, uint32_t* visits_out,
+                                 int threads) {
     Params P;
     std::memcpy(&P, params208, sizeof P);
     PhotonMap map{photons, std::vector<uint32_t>(PHOTON_TABLE, 0u), std::vector<uint32_t>(count, 0u)};
@@ -1502,7 +1525,9 @@ extern "C" void ro_photon_gather(const void* prims, const void* nodes, const voi
                     const V base = albedo_uv(c, m, s.p, s.u, s.v);
                     if (!is_delta(m)) {
                         if (depth > 0u) {
-                            const V light = throughput * gather(P, map, s, m, base, -d);
+                            uint32_t visits = 0;
+                            const V light = throughput * gather(P, map, s, m, base, -d, &visits);
+                            if (visits_out) visits_out[index] = visits;
                             if (finite3(light)) {
                                 const float l = lum(light);
                                 const float spf = float(P.samples_per_frame);
@@ -1743,4 +1768,10 @@ extern "C" void ro_sample_streams(const uint32_t* pairs, uint32_t n, const uint3
         Sampler gather = gather_sampler(index, sample, seed_hash);
         for (uint32_t k = 0; k < chain; ++k) *o++ = gather.rand();
     }
+}
+
+// Sets the perturbation runs' size (0: off, the reference's arithmetic) and seed.
+extern "C" void ro_set_jitter(uint32_t seed, float size) {
+    g_jitter_seed = seed;
+    g_jitter_size = size;
 }

@@ -102,6 +102,8 @@ SIGNATURES = {
     "raymond_trace_primary_device": (_I, [_P, _P, _U32, _P, _P]),
     "raymond_bvh_build": (_U32, [_P, _P, _U32, _U32, _P, _P, _I]),
     "raymond_sample_streams": (_I, [_P, _P, _U32, _P, _U32, _U32, _U32, _P]),
+    "raymond_light_trace": (_I, [_P, _P, _U32, _P, _U64, _P, _U64, _P]),
+    "raymond_photon_gather": (_I, [_P, _P, _U32, _P, _U32, _P, _U64]),
     "raymond_get_buffers": (_I, [_P, ctypes.POINTER(Buffers)]),
     "raymond_get_stats": (_I, [_P, ctypes.POINTER(Stats)]),
     "raymond_get_stream": (_P, [_P]),

@@ -11,6 +11,7 @@ struct PixelBuffers {
     float4* guide_normal;
     float4* light_a;
     float4* light_b;
+    float4* guide_unit;  // the à-trous passes' guide: unit normal and mean depth
     float4* denoised;
     uint32_t* splats;
     uchar4* display;
@@ -106,6 +107,10 @@ int launch_caustics(const Scene& s, const Params& P, uint32_t features, const Ca
                     const PixelBuffers& px, int num_sms, cudaStream_t st);
 // status: a device word set non-zero if a staged tile's wait runs out (null:
 // every pass reads through L2).
+int launch_light_trace_alone(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb, int num_sms,
+                             cudaStream_t st);
+int launch_gather_alone(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb, uint32_t n,
+                        float4* out, int num_sms, cudaStream_t st);
 int launch_denoise(const Params& P, const PixelBuffers& px, unsigned* status, cudaStream_t st);
 int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st);
 // Fill each kernel unit's sRGB decode table on the current device.

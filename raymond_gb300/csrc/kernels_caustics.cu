@@ -49,15 +49,17 @@ __device__ void splat(const Scene& s, const Params& P, const CausticBuffers& cb,
     atomicAdd(&cb.splats[index + 2], uint32_t(fminf(value.z * SPLAT_SCALE + r2, 4e9f)));
 }
 
-// deposit (src/shaders.mjs:1518-1528): one photon into the hashed grid.
-__device__ void deposit(const Params& P, const CausticBuffers& cb, float3 p, float3 d, float3 beta) {
+// deposit (src/shaders.mjs:1518-1528): one photon into the hashed grid. The
+// power record's fourth word keeps the light path's id, so a photon can be
+// told apart from the others whatever order the atomics stored it in.
+__device__ void deposit(const Params& P, const CausticBuffers& cb, float3 p, float3 d, float3 beta, uint32_t id) {
     const uint32_t i = atomicAdd(&cb.heads[cb.table], 1u);
     if (i >= cb.capacity) return;
     const int cx = int(floorf(p.x / P.photon_cell)), cy = int(floorf(p.y / P.photon_cell)),
               cz = int(floorf(p.z / P.photon_cell));
     const uint32_t next = atomicExch(&cb.heads[photon_cell_hash(cx, cy, cz, cb.table)], i + 1u);
     cb.photons[size_t(i) * 3] = make_float4(p.x, p.y, p.z, __uint_as_float(next));
-    cb.photons[size_t(i) * 3 + 1] = make_float4(beta.x, beta.y, beta.z, 0.0f);
+    cb.photons[size_t(i) * 3 + 1] = make_float4(beta.x, beta.y, beta.z, __uint_as_float(id));
     cb.photons[size_t(i) * 3 + 2] = make_float4(-d.x, -d.y, -d.z, 0.0f);
 }
 
@@ -188,7 +190,7 @@ __global__ void __launch_bounds__(CAUSTIC_BLOCK) k_light_trace(Scene s, Params P
                 // Straight from the lamp is the path tracer's; after mirrors or glass, a caustic.
                 if (bounces > 0u) {
                     splat<FEAT>(s, P, cb, sf, m, base, d, beta * carried, rng, col, CAUSTIC_BLOCK);
-                    deposit(P, cb, sf.p, d, beta * carried);
+                    deposit(P, cb, sf.p, d, beta * carried, id);
                 }
                 break;
             }
@@ -295,6 +297,35 @@ __global__ void __launch_bounds__(CAUSTIC_BLOCK) k_photon_gather(Scene s, Params
     }
 }
 
+// Links a given photon list (cb.photons, 3 float4 each) into the hashed
+// grid, as deposit does, for gathering a caller's photons.
+__global__ void k_link_photons(Params P, CausticBuffers cb, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 at = cb.photons[size_t(i) * 3];
+        const int cx = int(floorf(at.x / P.photon_cell)), cy = int(floorf(at.y / P.photon_cell)),
+                  cz = int(floorf(at.z / P.photon_cell));
+        const uint32_t next = atomicExch(&cb.heads[photon_cell_hash(cx, cy, cz, cb.table)], i + 1u);
+        at.w = __uint_as_float(next);
+        cb.photons[size_t(i) * 3] = at;
+    }
+}
+
+template <uint32_t FEAT>
+int light_trace_alone(const Scene& s, const Params& P, const CausticBuffers& cb, int num_sms, cudaStream_t st) {
+    cudaMemsetAsync(cb.heads, 0, (size_t(cb.table) + 1) * sizeof(uint32_t), st);
+    k_light_trace<FEAT><<<num_sms * 8, CAUSTIC_BLOCK, 0, st>>>(s, P, cb);
+    return 1;
+}
+
+template <uint32_t FEAT>
+int gather_alone(const Scene& s, const Params& P, const CausticBuffers& cb, uint32_t n, float4* out, int num_sms,
+                 cudaStream_t st) {
+    cudaMemsetAsync(cb.heads, 0, (size_t(cb.table) + 1) * sizeof(uint32_t), st);
+    k_link_photons<<<num_sms * 8, 256, 0, st>>>(P, cb, n);
+    k_photon_gather<FEAT><<<num_sms * 8, CAUSTIC_BLOCK, 0, st>>>(s, P, cb, out);
+    return 2;
+}
+
 template <uint32_t FEAT>
 int caustics_frame(const Scene& s, const Params& P, const CausticBuffers& cb, const PixelBuffers& px, int num_sms,
                    cudaStream_t st) {
@@ -309,6 +340,24 @@ int caustics_frame(const Scene& s, const Params& P, const CausticBuffers& cb, co
 }  // namespace
 
 cudaError_t upload_srgb_table_caustics() { return upload_srgb_table_here(); }
+
+int launch_light_trace_alone(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb, int num_sms,
+                             cudaStream_t st) {
+    switch (features & 15u) {
+        case 0: return light_trace_alone<0>(s, P, cb, num_sms, st);
+        case F_DISPERSION: return light_trace_alone<F_DISPERSION>(s, P, cb, num_sms, st);
+        default: return light_trace_alone<15u>(s, P, cb, num_sms, st);
+    }
+}
+
+int launch_gather_alone(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb, uint32_t n,
+                        float4* out, int num_sms, cudaStream_t st) {
+    switch (features & 15u) {
+        case 0: return gather_alone<0>(s, P, cb, n, out, num_sms, st);
+        case F_DISPERSION: return gather_alone<F_DISPERSION>(s, P, cb, n, out, num_sms, st);
+        default: return gather_alone<15u>(s, P, cb, n, out, num_sms, st);
+    }
+}
 
 int launch_caustics(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb,
                     const PixelBuffers& px, int num_sms, cudaStream_t st) {

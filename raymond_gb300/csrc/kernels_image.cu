@@ -22,6 +22,7 @@ struct DenoiseView {
     const float4* accum;
     const float4* guide_albedo;
     const float4* guide_normal;
+    const float4* guide_unit;  // the passes' guides, written by prepare; null: worked out per tap
     uint32_t w, h;
     float n;  // samples(): max(total_samples, 1)
 };
@@ -30,38 +31,56 @@ __device__ __forceinline__ float3 albedo_at(const DenoiseView& v, uint32_t i) {
     const float4 g = v.guide_albedo[i];
     return make_float3(fmaxf(g.x / v.n, 0.01f), fmaxf(g.y / v.n, 0.01f), fmaxf(g.z / v.n, 0.01f));
 }
-__device__ __forceinline__ float4 normal_of(float4 g, const DenoiseView& v) {
-    const float d2 = g.x * g.x + g.y * g.y + g.z * g.z;
-    float3 n = make_float3(0.0f, 0.0f, 0.0f);
+// normal_at (src/shaders.mjs:1944-1952): the unit shading normal (zero where
+// nothing was hit) and the mean depth of a guide sum. Explicitly rounded
+// operations, so that prepare's copy and a per-tap recomputation agree bit
+// for bit whichever kernel computes them.
+__device__ __forceinline__ float4 unit_guide(float4 g, float n) {
+    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(g.x, g.x), __fmul_rn(g.y, g.y)), __fmul_rn(g.z, g.z));
+    float3 u = make_float3(0.0f, 0.0f, 0.0f);
     if (d2 > 0.0f) {
-        const float l = sqrtf(d2);
-        n = make_float3(g.x / l, g.y / l, g.z / l);
+        const float l = __fsqrt_rn(d2);
+        u = make_float3(__fdiv_rn(g.x, l), __fdiv_rn(g.y, l), __fdiv_rn(g.z, l));
     }
-    return make_float4(n.x, n.y, n.z, g.w / v.n);
+    return make_float4(u.x, u.y, u.z, __fdiv_rn(g.w, n));
 }
-__device__ __forceinline__ float4 normal_at(const DenoiseView& v, uint32_t i) { return normal_of(v.guide_normal[i], v); }
+__device__ __forceinline__ float4 guide_at(const DenoiseView& v, uint32_t i) {
+    return v.guide_unit ? v.guide_unit[i] : unit_guide(v.guide_normal[i], v.n);
+}
 __device__ __forceinline__ float3 light_at(const DenoiseView& v, uint32_t i) {
     const float4 a = v.accum[i];
     const float3 al = albedo_at(v, i);
     return make_float3(a.x / v.n / al.x, a.y / v.n / al.y, a.z / v.n / al.z);
 }
-// similarity (src/shaders.mjs:1958-1968).
+// similarity (src/shaders.mjs:1958-1968): normal^64 by six squarings and the
+// depth term's exponential, for prepare's variance estimate.
+__device__ __forceinline__ float pow64(float x) {
+    x *= x;
+    x *= x;
+    x *= x;
+    x *= x;
+    x *= x;
+    return x * x;
+}
 __device__ __forceinline__ float similarity(float4 p, float4 q, float step) {
     if (p.w <= 0.0f || q.w <= 0.0f) return (p.w <= 0.0f && q.w <= 0.0f) ? 1.0f : 0.0f;
     if (p.x * p.x + p.y * p.y + p.z * p.z == 0.0f) return 0.0f;
-    const float wn = powf(fmaxf(p.x * q.x + p.y * q.y + p.z * q.z, 0.0f), 64.0f);
+    const float wn = pow64(fmaxf(p.x * q.x + p.y * q.y + p.z * q.z, 0.0f));
     const float wz = expf(-fabsf(p.w - q.w) / (p.w * 0.02f * step + 1e-6f));
     return wn * wz;
 }
 
 __constant__ float c_kernel[3] = {0.375f, 0.25f, 0.0625f};
+constexpr float LOG2E = 1.4426950408889634f;
 
-// prepare (src/shaders.mjs:1974-2021).
-__device__ void prepare_at(const DenoiseView& v, uint32_t x, uint32_t y, float4* __restrict__ out) {
+// prepare (src/shaders.mjs:1974-2021), and the passes' guide for this pixel.
+__device__ void prepare_at(const DenoiseView& v, uint32_t x, uint32_t y, float4* __restrict__ out,
+                           float4* __restrict__ unit_out) {
     const uint32_t i = y * v.w + x;
     const float n = v.n;
     const float3 light = light_at(v, i);
-    const float4 gp = normal_at(v, i);
+    const float4 gp = unit_guide(v.guide_normal[i], n);
+    if (unit_out) unit_out[i] = gp;
     const float a = lum(albedo_at(v, i));
     float variance;
     if (n >= 4.0f) {
@@ -76,7 +95,7 @@ __device__ void prepare_at(const DenoiseView& v, uint32_t x, uint32_t y, float4*
                 const int xx = int(x) + dx, yy = int(y) + dy;
                 if (xx < 0 || yy < 0 || xx >= int(v.w) || yy >= int(v.h)) continue;
                 const uint32_t j = uint32_t(yy) * v.w + uint32_t(xx);
-                const float w = similarity(gp, normal_at(v, j), 1.0f);
+                const float w = similarity(gp, unit_guide(v.guide_normal[j], n), 1.0f);
                 const float l = lum(light_at(v, j));
                 sum += w * l;
                 sum2 += w * l * l;
@@ -88,43 +107,72 @@ __device__ void prepare_at(const DenoiseView& v, uint32_t x, uint32_t y, float4*
     }
     out[i] = make_float4(light.x, light.y, light.z, variance);
 }
-__global__ void k_prepare(DenoiseView v, float4* __restrict__ out) {
+__global__ void k_prepare(DenoiseView v, float4* __restrict__ out, float4* __restrict__ unit_out) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= v.w || y >= v.h) return;
-    prepare_at(v, x, y, out);
+    prepare_at(v, x, y, out, unit_out);
 }
 
-// atrous (src/shaders.mjs:2023-2086), one pass of the given step.
-__device__ void atrous_at(const DenoiseView& v, const float4* __restrict__ in, float4* __restrict__ out, int step,
-                          uint32_t x, uint32_t y) {
-    const uint32_t i = y * v.w + x;
-    const float4 centre = in[i];
-    const float4 gp = normal_at(v, i);
-    const float lp = lum(xyz4(centre));
+// atrous (src/shaders.mjs:2023-2086) for one pixel of one pass. The centre's
+// constants are worked out once: its guide, luminance, and the two
+// exponentials' scales, so that a tap's weight
+//   k(dx)·k(dy) · max(n_p·n_q, 0)^64 · exp(−|z_p − z_q| / (z_p·0.02·step + 1e-6)) · exp(−|l_p − l_q| / σ)
+// costs six squarings and one exp2 of the two exponents' sum. LOAD(dx, dy,
+// light, guide) fetches a tap (from a staged tile or from memory); INTERIOR
+// drops the image-edge tests where every tap is inside.
+struct PassCentre {
+    float4 c, gp;
+    float lp, kz, kl;
+    bool background, flat;
+};
 
+template <bool INTERIOR, typename Load>
+__device__ __forceinline__ float4 atrous_pixel(const DenoiseView& v, int x, int y, int step, Load load) {
+    float4 c, gp;
+    load(0, 0, c, gp);
+    // σ from the 3×3 binomial blur of the variance (src/shaders.mjs:2037-2050).
     float variance = 0.0f, variance_weight = 0.0f;
+#pragma unroll
     for (int dy = -1; dy <= 1; ++dy) {
+#pragma unroll
         for (int dx = -1; dx <= 1; ++dx) {
-            const int xx = int(x) + dx, yy = int(y) + dy;
-            if (xx >= 0 && yy >= 0 && xx < int(v.w) && yy < int(v.h)) {
+            if (INTERIOR || (x + dx >= 0 && y + dy >= 0 && x + dx < int(v.w) && y + dy < int(v.h))) {
                 const float w = c_kernel[dx < 0 ? -dx : dx] * c_kernel[dy < 0 ? -dy : dy];
-                variance += w * in[uint32_t(yy) * v.w + uint32_t(xx)].w;
+                float4 q, g;
+                load(dx, dy, q, g);
+                variance += w * q.w;
                 variance_weight += w;
             }
         }
     }
     const float sigma = 4.0f * sqrtf(variance / variance_weight) + 1e-4f;
+    const float lp = lum(xyz4(c));
+    const float kl = LOG2E / sigma;
+    const float kz = LOG2E / (gp.w * 0.02f * float(step) + 1e-6f);
+    const bool background = gp.w <= 0.0f;
+    const bool flat = gp.x * gp.x + gp.y * gp.y + gp.z * gp.z == 0.0f;
 
     float3 sum = make_float3(0.0f, 0.0f, 0.0f);
     float sum_variance = 0.0f, weight = 0.0f;
+#pragma unroll
     for (int dy = -2; dy <= 2; ++dy) {
+#pragma unroll
         for (int dx = -2; dx <= 2; ++dx) {
-            const int xx = int(x) + dx * step, yy = int(y) + dy * step;
-            if (xx < 0 || yy < 0 || xx >= int(v.w) || yy >= int(v.h)) continue;
-            const uint32_t j = uint32_t(yy) * v.w + uint32_t(xx);
-            const float4 q = in[j];
-            const float w = c_kernel[dx < 0 ? -dx : dx] * c_kernel[dy < 0 ? -dy : dy] *
-                            similarity(gp, normal_at(v, j), float(step)) * expf(-fabsf(lp - lum(xyz4(q))) / sigma);
+            const int xx = x + dx * step, yy = y + dy * step;
+            if (!INTERIOR && (xx < 0 || yy < 0 || xx >= int(v.w) || yy >= int(v.h))) continue;
+            float4 q, gq;
+            load(dx * step, dy * step, q, gq);
+            const float k = c_kernel[dx < 0 ? -dx : dx] * c_kernel[dy < 0 ? -dy : dy];
+            const float dl = fabsf(lp - lum(xyz4(q)));
+            float w;
+            if (background || gq.w <= 0.0f) {
+                w = (background && gq.w <= 0.0f) ? k * exp2f(-dl * kl) : 0.0f;
+            } else if (flat) {
+                w = 0.0f;
+            } else {
+                const float wn = pow64(fmaxf(gp.x * gq.x + gp.y * gq.y + gp.z * gq.z, 0.0f));
+                w = k * wn * exp2f(-(fabsf(gp.w - gq.w) * kz + dl * kl));
+            }
             sum.x += w * q.x;
             sum.y += w * q.y;
             sum.z += w * q.z;
@@ -132,26 +180,48 @@ __device__ void atrous_at(const DenoiseView& v, const float4* __restrict__ in, f
             weight += w;
         }
     }
-    if (weight > 0.0f)
-        out[i] = make_float4(sum.x / weight, sum.y / weight, sum.z / weight, sum_variance / (weight * weight));
-    else
-        out[i] = centre;
+    if (weight > 0.0f) return make_float4(sum.x / weight, sum.y / weight, sum.z / weight, sum_variance / (weight * weight));
+    return c;
 }
-__global__ void k_atrous(DenoiseView v, const float4* __restrict__ in, float4* __restrict__ out, int step) {
+
+// A pass reading its taps from memory (L1/L2): the passes of the allocation-
+// free entry, the batch's, and every renderer's last pass (step 16, whose
+// 32-pixel halo makes a staged tile too large). With `compose`, the pass
+// writes compose()'s product with the albedo (src/shaders.mjs:2088-2097)
+// into out instead of the filtered light.
+__device__ __forceinline__ void atrous_at(const DenoiseView& v, const float4* __restrict__ in, float4* __restrict__ out,
+                                          int step, uint32_t x, uint32_t y, bool compose) {
+    const uint32_t i = y * v.w + x;
+    auto load = [&](int ox, int oy, float4& q, float4& g) {
+        const uint32_t j = uint32_t(int(i) + oy * int(v.w) + ox);
+        q = __ldg(in + j);
+        g = guide_at(v, j);
+    };
+    const int reach = 2 * step;
+    const bool interior = int(x) >= reach && int(y) >= reach && int(x) + reach < int(v.w) && int(y) + reach < int(v.h);
+    const float4 l = interior ? atrous_pixel<true>(v, int(x), int(y), step, load)
+                              : atrous_pixel<false>(v, int(x), int(y), step, load);
+    if (compose) {
+        const float3 a = albedo_at(v, i);
+        out[i] = make_float4(l.x * a.x, l.y * a.y, l.z * a.z, 0.0f);
+    } else {
+        out[i] = l;
+    }
+}
+__global__ void k_atrous(DenoiseView v, const float4* __restrict__ in, float4* __restrict__ out, int step, int compose) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= v.w || y >= v.h) return;
-    atrous_at(v, in, out, step, x, y);
+    atrous_at(v, in, out, step, x, y, compose != 0);
 }
 
 // The same pass with its input staged in shared memory by the tensor memory
 // accelerator: a 32×16 block of outputs reads a (32 + 4·step) × (16 + 4·step)
-// tile of the light buffer and of the normal guide, two 2D box copies that
+// tile of the light buffer and of the passes' guide, two 2D box copies that
 // complete on one mbarrier (a bounded wait; a wait that runs out sets the
 // status word and the block writes nothing). Taps outside the image are
 // skipped by coordinate, as in atrous_at; the box's out-of-image part is
-// zero-filled and never read. Same arithmetic in the same order as
-// atrous_at (the two agree to float rounding: the compiler may fuse
-// multiply-adds differently).
+// zero-filled and never read. Blocks whose whole tile lies inside the image
+// skip the tests. Same arithmetic as atrous_at.
 constexpr int ATROUS_TW = 32, ATROUS_TH = 16, ATROUS_THREADS = 256;
 
 template <int STEP>
@@ -193,65 +263,20 @@ __global__ void __launch_bounds__(ATROUS_THREADS) k_atrous_tma(DenoiseView v, co
         __syncthreads();
         return;
     }
+    const bool interior = bx >= T::halo && by >= T::halo && bx + ATROUS_TW + T::halo <= int(v.w) &&
+                          by + ATROUS_TH + T::halo <= int(v.h);
     const int tx = int(threadIdx.x) % ATROUS_TW;
     for (int ty = int(threadIdx.x) / ATROUS_TW; ty < ATROUS_TH; ty += ATROUS_THREADS / ATROUS_TW) {
         const int x = bx + tx, y = by + ty;
         if (x >= int(v.w) || y >= int(v.h)) continue;
-        auto at = [&](const float4* t, int xx, int yy) { return t[(yy - by + T::halo) * T::w + (xx - bx + T::halo)]; };
-        const float4 centre = at(s_light, x, y);
-        const float4 gp = normal_of(at(s_guide, x, y), v);
-        const float lp = lum(xyz4(centre));
-
-        float variance = 0.0f, variance_weight = 0.0f;
-        for (int dy = -1; dy <= 1; ++dy) {
-            for (int dx = -1; dx <= 1; ++dx) {
-                const int xx = x + dx, yy = y + dy;
-                if (xx >= 0 && yy >= 0 && xx < int(v.w) && yy < int(v.h)) {
-                    const float w = c_kernel[dx < 0 ? -dx : dx] * c_kernel[dy < 0 ? -dy : dy];
-                    variance += w * at(s_light, xx, yy).w;
-                    variance_weight += w;
-                }
-            }
-        }
-        const float sigma = 4.0f * sqrtf(variance / variance_weight) + 1e-4f;
-
-        float3 sum = make_float3(0.0f, 0.0f, 0.0f);
-        float sum_variance = 0.0f, weight = 0.0f;
-        for (int dy = -2; dy <= 2; ++dy) {
-            for (int dx = -2; dx <= 2; ++dx) {
-                const int xx = x + dx * STEP, yy = y + dy * STEP;
-                if (xx < 0 || yy < 0 || xx >= int(v.w) || yy >= int(v.h)) continue;
-                const float4 q = at(s_light, xx, yy);
-                const float w = c_kernel[dx < 0 ? -dx : dx] * c_kernel[dy < 0 ? -dy : dy] *
-                                similarity(gp, normal_of(at(s_guide, xx, yy), v), float(STEP)) *
-                                expf(-fabsf(lp - lum(xyz4(q))) / sigma);
-                sum.x += w * q.x;
-                sum.y += w * q.y;
-                sum.z += w * q.z;
-                sum_variance += w * w * q.w;
-                weight += w;
-            }
-        }
-        const uint32_t i = uint32_t(y) * v.w + uint32_t(x);
-        if (weight > 0.0f)
-            out[i] = make_float4(sum.x / weight, sum.y / weight, sum.z / weight, sum_variance / (weight * weight));
-        else
-            out[i] = centre;
+        const int base = (ty + T::halo) * T::w + (tx + T::halo);
+        auto load = [&](int ox, int oy, float4& q, float4& g) {
+            q = s_light[base + oy * T::w + ox];
+            g = s_guide[base + oy * T::w + ox];
+        };
+        out[uint32_t(y) * v.w + uint32_t(x)] =
+            interior ? atrous_pixel<true>(v, x, y, STEP, load) : atrous_pixel<false>(v, x, y, STEP, load);
     }
-}
-
-// compose (src/shaders.mjs:2088-2097).
-__device__ void compose_at(const DenoiseView& v, const float4* __restrict__ in, float4* __restrict__ out, uint32_t x,
-                           uint32_t y) {
-    const uint32_t i = y * v.w + x;
-    const float3 a = albedo_at(v, i);
-    const float4 l = in[i];
-    out[i] = make_float4(l.x * a.x, l.y * a.y, l.z * a.z, 0.0f);
-}
-__global__ void k_compose(DenoiseView v, const float4* __restrict__ in, float4* __restrict__ out) {
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= v.w || y >= v.h) return;
-    compose_at(v, in, out, x, y);
 }
 
 // Narkowicz's ACES fit and the sRGB OETF (src/shaders.mjs:2115-2122).
@@ -337,7 +362,8 @@ bool encode_tile_map(CUtensorMap* map, const float4* base, uint32_t w, uint32_t 
 template <int STEP>
 bool launch_atrous_tma(const DenoiseView& v, const float4* in, float4* out, unsigned* status, cudaStream_t st) {
     CUtensorMap light, guide;
-    if (!encode_tile_map<STEP>(&light, in, v.w, v.h) || !encode_tile_map<STEP>(&guide, v.guide_normal, v.w, v.h))
+    if (!v.guide_unit || !encode_tile_map<STEP>(&light, in, v.w, v.h) ||
+        !encode_tile_map<STEP>(&guide, v.guide_unit, v.w, v.h))
         return false;
     static const bool configured = cudaFuncSetAttribute(k_atrous_tma<STEP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                         int(AtrousTile<STEP>::smem)) == cudaSuccess;
@@ -350,34 +376,35 @@ bool launch_atrous_tma(const DenoiseView& v, const float4* in, float4* out, unsi
 }  // namespace
 
 int launch_denoise(const Params& P, const PixelBuffers& px, unsigned* status, cudaStream_t st) {
-    DenoiseView v{px.accum, px.guide_albedo, px.guide_normal, P.width, P.height,
+    DenoiseView v{px.accum, px.guide_albedo, px.guide_normal, px.guide_unit, P.width, P.height,
                   float(P.total_samples > 1u ? P.total_samples : 1u)};
     const dim3 block(16, 8), grid((P.width + 15) / 16, (P.height + 7) / 8);
-    // prepare fills light a; the passes go a→b, b→a, …; compose reads the last (src/Renderer.mjs:893-912).
-    k_prepare<<<grid, block, 0, st>>>(v, px.light_a);
-    const int steps[5] = {1, 2, 4, 8, 16};
+    // prepare fills light a and the passes' guide; the passes go a→b, b→a,
+    // …; the last writes compose()'s product into denoised (src/Renderer.mjs:893-912).
+    k_prepare<<<grid, block, 0, st>>>(v, px.light_a, px.guide_unit);
+    const int steps[4] = {1, 2, 4, 8};
     float4* from = px.light_a;
     float4* to = px.light_b;
-    for (int k = 0; k < 5; ++k) {
-        // Steps 1-8 stage their tiles with TMA; step 16's halo (32 pixels a
-        // side) would need 200 KB of tile for 512 outputs, so it reads L2.
+    for (int k = 0; k < 4; ++k) {
+        // Steps 1-8 stage their tiles with TMA.
         bool staged = false;
         if (status) {
             switch (steps[k]) {
                 case 1: staged = launch_atrous_tma<1>(v, from, to, status, st); break;
                 case 2: staged = launch_atrous_tma<2>(v, from, to, status, st); break;
                 case 4: staged = launch_atrous_tma<4>(v, from, to, status, st); break;
-                case 8: staged = launch_atrous_tma<8>(v, from, to, status, st); break;
-                default: break;
+                default: staged = launch_atrous_tma<8>(v, from, to, status, st); break;
             }
         }
-        if (!staged) k_atrous<<<grid, block, 0, st>>>(v, from, to, steps[k]);
+        if (!staged) k_atrous<<<grid, block, 0, st>>>(v, from, to, steps[k], 0);
         float4* t = from;
         from = to;
         to = t;
     }
-    k_compose<<<grid, block, 0, st>>>(v, from, px.denoised);
-    return 7;
+    // Step 16's halo (32 pixels a side) would need 200 KB of tile for 512
+    // outputs, so it reads L1/L2, and composes as it writes.
+    k_atrous<<<grid, block, 0, st>>>(v, from, px.denoised, 16, 1);
+    return 6;
 }
 
 int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st) {
@@ -403,11 +430,11 @@ __device__ __forceinline__ uint32_t find_job(const JobPixels* seg, uint32_t n, u
 
 __device__ __forceinline__ DenoiseView job_view(const JobDesc& jd) {
     const Params& P = jd.params;
-    return DenoiseView{jd.px.accum, jd.px.guide_albedo, jd.px.guide_normal, P.width, P.height,
+    return DenoiseView{jd.px.accum, jd.px.guide_albedo, jd.px.guide_normal, jd.px.guide_unit, P.width, P.height,
                        float(P.total_samples > 1u ? P.total_samples : 1u)};
 }
 
-// pass: 0 prepare, 1..5 à-trous steps 1..16, 6 compose.
+// pass: 0 prepare, 1..4 à-trous steps 1..8, 5 step 16 composed into denoised.
 __global__ void k_denoise_batch(const JobDesc* __restrict__ jobs, const JobPixels* __restrict__ seg, uint32_t n_seg,
                                 uint32_t total, int pass) {
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
@@ -417,15 +444,16 @@ __global__ void k_denoise_batch(const JobDesc* __restrict__ jobs, const JobPixel
         const DenoiseView v = job_view(jd);
         const uint32_t i = t - g.pixel_offset;
         const uint32_t x = i % v.w, y = i / v.w;
-        // prepare fills light a; passes go a→b, b→a, …; compose reads light b (after 5 passes).
+        // prepare fills light a and the guide; passes go a→b, b→a, …; the
+        // fifth reads light a and writes the composed image.
         if (pass == 0) {
-            prepare_at(v, x, y, jd.px.light_a);
-        } else if (pass <= 5) {
+            prepare_at(v, x, y, jd.px.light_a, jd.px.guide_unit);
+        } else if (pass <= 4) {
             const bool even = (pass - 1) % 2 == 0;
             atrous_at(v, even ? jd.px.light_a : jd.px.light_b, even ? jd.px.light_b : jd.px.light_a,
-                      1 << (pass - 1), x, y);
+                      1 << (pass - 1), x, y, false);
         } else {
-            compose_at(v, jd.px.light_b, jd.px.denoised, x, y);
+            atrous_at(v, jd.px.light_a, jd.px.denoised, 16, x, y, true);
         }
     }
 }
@@ -445,9 +473,9 @@ __global__ void k_tonemap_batch(const JobDesc* __restrict__ jobs, const JobPixel
 int launch_image_batch(const JobDesc* d_jobs, const JobPixels* d_pix, uint32_t n_jobs, uint32_t total_pixels,
                        int num_sms, cudaStream_t st) {
     const int grid = num_sms * 8;
-    for (int pass = 0; pass <= 6; ++pass) k_denoise_batch<<<grid, 256, 0, st>>>(d_jobs, d_pix, n_jobs, total_pixels, pass);
+    for (int pass = 0; pass <= 5; ++pass) k_denoise_batch<<<grid, 256, 0, st>>>(d_jobs, d_pix, n_jobs, total_pixels, pass);
     k_tonemap_batch<<<grid, 256, 0, st>>>(d_jobs, d_pix, n_jobs, total_pixels);
-    return 8;
+    return 7;
 }
 
 // ---- Denoising into a caller's buffers without allocating ----
@@ -486,8 +514,13 @@ extern "C" int raymond_denoise_static(const float* accum, const float* guide_alb
     }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    if (e != cudaSuccess || dev < 0) {
         set_handleless_error("raymond_denoise_static: no current CUDA device.");
+        return RAYMOND_ECUDA;
+    }
+    if (dev >= kMaxDevices) {
+        set_handleless_error("raymond_denoise_static: the current device's index is beyond the static scratch "
+                             "table's 64 devices.");
         return RAYMOND_ECUDA;
     }
     float4* scratch;
@@ -508,21 +541,23 @@ extern "C" int raymond_denoise_static(const float* accum, const float* guide_alb
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const uint32_t pixels = width * height;
+    // No third buffer here for the passes' guide: each tap works it out from
+    // guide_normal (the same bits prepare would have stored).
     DenoiseView v{reinterpret_cast<const float4*>(accum), reinterpret_cast<const float4*>(guide_albedo),
-                  reinterpret_cast<const float4*>(guide_normal), width, height,
+                  reinterpret_cast<const float4*>(guide_normal), nullptr, width, height,
                   float(total_samples > 1u ? total_samples : 1u)};
     const dim3 block(16, 8), grid((width + 15) / 16, (height + 7) / 8);
     float4* from = scratch;
     float4* to = scratch + pixels;
-    k_prepare<<<grid, block, 0, st>>>(v, from);
-    const int steps[5] = {1, 2, 4, 8, 16};
-    for (int k = 0; k < 5; ++k) {
-        k_atrous<<<grid, block, 0, st>>>(v, from, to, steps[k]);
+    k_prepare<<<grid, block, 0, st>>>(v, from, nullptr);
+    const int steps[4] = {1, 2, 4, 8};
+    for (int k = 0; k < 4; ++k) {
+        k_atrous<<<grid, block, 0, st>>>(v, from, to, steps[k], 0);
         float4* t = from;
         from = to;
         to = t;
     }
-    k_compose<<<grid, block, 0, st>>>(v, from, reinterpret_cast<float4*>(out));
+    k_atrous<<<grid, block, 0, st>>>(v, from, reinterpret_cast<float4*>(out), 16, 1);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_handleless_error("raymond_denoise_static: kernel launch failed.");

@@ -62,7 +62,7 @@ struct raymond {
     bool has_scene = false;
 
     // Per-pixel buffers.
-    DevBuf accum, guide_albedo, guide_normal, light_a, light_b, denoised, splats, display;
+    DevBuf accum, guide_albedo, guide_normal, light_a, light_b, guide_unit, denoised, splats, display;
     uint32_t width = 0, height = 0;
     uint64_t capacity = 0;
 
@@ -161,6 +161,7 @@ struct raymond {
         p.guide_normal = static_cast<float4*>(guide_normal.ptr);
         p.light_a = static_cast<float4*>(light_a.ptr);
         p.light_b = static_cast<float4*>(light_b.ptr);
+        p.guide_unit = static_cast<float4*>(guide_unit.ptr);
         p.denoised = static_cast<float4*>(denoised.ptr);
         p.splats = static_cast<uint32_t*>(splats.ptr);
         p.display = static_cast<uchar4*>(display.ptr);
@@ -294,7 +295,7 @@ void raymond_destroy(raymond_t* h) {
     cudaStreamSynchronize(h->stream);
     for (DevBuf* b : {&h->prims, &h->nodes, &h->materials, &h->attributes, &h->lights, &h->emitters, &h->textures,
                       &h->normal_maps, &h->env_map, &h->env_table, &h->accum, &h->guide_albedo, &h->guide_normal,
-                      &h->light_a, &h->light_b, &h->denoised, &h->splats, &h->display, &h->ray_scratch,
+                      &h->light_a, &h->light_b, &h->guide_unit, &h->denoised, &h->splats, &h->display, &h->ray_scratch,
                       &h->prim_scratch, &h->t_scratch, &h->counter, &h->wf_hit, &h->wf_queue[0], &h->wf_queue[1],
                       &h->wf_sorted, &h->wf_sort_key, &h->wf_shadow, &h->wf_counters, &h->photon_heads,
                       &h->photons, &h->wide})
@@ -468,7 +469,8 @@ int raymond_resize(raymond_t* h, uint32_t w, uint32_t hgt) {
     const uint64_t px = uint64_t(w) * hgt;
     if (px > h->capacity) {
         // Buffers kept while big enough (src/Renderer.mjs:766-778).
-        for (DevBuf* b : {&h->accum, &h->guide_albedo, &h->guide_normal, &h->light_a, &h->light_b, &h->denoised,
+        for (DevBuf* b : {&h->accum, &h->guide_albedo, &h->guide_normal, &h->light_a, &h->light_b, &h->guide_unit,
+                          &h->denoised,
                           &h->splats}) {
             cudaError_t e = b->reserve(px * 16);
             if (e != cudaSuccess) return h->cuda_fail(e, "pixel buffers");
@@ -484,11 +486,38 @@ int raymond_resize(raymond_t* h, uint32_t w, uint32_t hgt) {
     return RAYMOND_OK;
 }
 
-int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint32_t flags) {
-    if (!h) return RAYMOND_EINVAL;
+// The photon map (grown to the capacity asked for, its table at least twice
+// that and 2^20) and the frame's light-path count and photon radius.
+static int caustic_buffers(raymond_t* h, Params& P, CausticBuffers& cb) {
+    if (h->emitter_vec4s == 0) return h->fail(RAYMOND_ESTATE, "Caustics need raymond_set_emitters first.");
+    uint32_t table = 1u << 20;
+    while (table < 2ull * h->photon_capacity) table <<= 1;
+    if (table != h->photon_table || h->photon_capacity != h->photon_capacity_alloc) {
+        cudaError_t e = h->photon_heads.reserve((size_t(table) + 1) * 4);
+        if (e == cudaSuccess) e = h->photons.reserve(size_t(h->photon_capacity) * 48);
+        if (e != cudaSuccess) return h->cuda_fail(e, "photon map");
+        h->photon_table = table;
+        h->photon_capacity_alloc = h->photon_capacity;
+    }
+    cb.splats = static_cast<uint32_t*>(h->splats.ptr);
+    cb.heads = static_cast<uint32_t*>(h->photon_heads.ptr);
+    cb.photons = static_cast<float4*>(h->photons.ptr);
+    cb.table = h->photon_table;
+    cb.capacity = h->photon_capacity;
+    const uint64_t frame = uint64_t(P.width) * P.height * P.samples_per_frame;
+    cb.photons_per_frame = h->photons_override ? h->photons_override
+                                               : uint32_t(frame < h->photon_capacity ? frame : h->photon_capacity);
+    if (h->photon_radius_override > 0.0f) {
+        P.photon_radius = h->photon_radius_override;
+        P.photon_cell = 2.0f * h->photon_radius_override;
+    }
+    return RAYMOND_OK;
+}
+
+// The checks raymond_render makes of a frame's parameters.
+static int check_frame(raymond_t* h, const void* params208, Params& P) {
     if (!params208) return h->fail(RAYMOND_EINVAL, "No parameters.");
     if (!h->has_scene) return h->fail(RAYMOND_ESTATE, "No scene has been uploaded.");
-    Params P;
     std::memcpy(&P, params208, sizeof P);
     if (P.width != h->width || P.height != h->height || h->capacity == 0)
         return h->fail(RAYMOND_ESTATE, "Resize to %ux%u before rendering at that size.", P.width, P.height);
@@ -496,6 +525,87 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
         return h->fail(RAYMOND_EINVAL, "The parameters' light and volume counts don't match the scene.");
     if (P.samples_per_frame == 0 || P.max_bounces > 64)
         return h->fail(RAYMOND_EINVAL, "samples_per_frame must be at least 1 and max_bounces at most 64.");
+    return RAYMOND_OK;
+}
+
+int raymond_light_trace(raymond_t* h, const void* params208, uint32_t features, uint32_t* splats, uint64_t splat_bytes,
+                        float* photons, uint64_t photon_floats, uint32_t* photon_count) {
+    if (!h) return RAYMOND_EINVAL;
+    Params P;
+    int rc = check_frame(h, params208, P);
+    if (rc) return rc;
+    const size_t px = size_t(P.width) * P.height;
+    if (!splats || !photon_count || splat_bytes < px * 16)
+        return h->fail(RAYMOND_EINVAL, "The splat buffer needs width x height x 16 bytes.");
+    cudaSetDevice(h->device);
+    CausticBuffers cb{};
+    if ((rc = caustic_buffers(h, P, cb))) return rc;
+    cudaMemsetAsync(cb.splats, 0, px * 16, h->stream);
+    launch_light_trace_alone(h->scene_view(), P, features, cb, h->num_sms, h->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return h->cuda_fail(e, "light tracing");
+    uint32_t attempted = 0;
+    e = cudaMemcpyAsync(&attempted, cb.heads + cb.table, 4, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(splats, cb.splats, px * 16, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "light tracing read-back");
+    const uint32_t count = attempted < cb.capacity ? attempted : cb.capacity;
+    *photon_count = count;
+    if (photons && count) {
+        if (photon_floats < uint64_t(count) * 10)
+            return h->fail(RAYMOND_ECAPACITY, "%u photons need %llu floats.", count,
+                           (unsigned long long)(uint64_t(count) * 10));
+        std::vector<float4> rec(size_t(count) * 3);
+        e = cudaMemcpy(rec.data(), cb.photons, rec.size() * 16, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return h->cuda_fail(e, "photon read-back");
+        for (uint32_t i = 0; i < count; ++i) {
+            const float4 a = rec[size_t(i) * 3], b = rec[size_t(i) * 3 + 1], c = rec[size_t(i) * 3 + 2];
+            const float row[10] = {a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, b.w};
+            std::memcpy(photons + size_t(i) * 10, row, sizeof row);
+        }
+    }
+    // The splat buffer starts the next frame empty, as a frame leaves it.
+    cudaMemsetAsync(cb.splats, 0, px * 16, h->stream);
+    return RAYMOND_OK;
+}
+
+int raymond_photon_gather(raymond_t* h, const void* params208, uint32_t features, const float* photons, uint32_t n,
+                          float* out, uint64_t out_bytes) {
+    if (!h) return RAYMOND_EINVAL;
+    Params P;
+    int rc = check_frame(h, params208, P);
+    if (rc) return rc;
+    const size_t px = size_t(P.width) * P.height;
+    if (!out || out_bytes < px * 16 || (n && !photons))
+        return h->fail(RAYMOND_EINVAL, "The output needs width x height x 16 bytes.");
+    if (n > h->photon_capacity) return h->fail(RAYMOND_ECAPACITY, "More photons than the map's capacity.");
+    cudaSetDevice(h->device);
+    CausticBuffers cb{};
+    if ((rc = caustic_buffers(h, P, cb))) return rc;
+    std::vector<float4> rec(size_t(n) * 3);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* q = photons + size_t(i) * 9;
+        rec[size_t(i) * 3] = make_float4(q[0], q[1], q[2], 0.0f);
+        rec[size_t(i) * 3 + 1] = make_float4(q[3], q[4], q[5], 0.0f);
+        rec[size_t(i) * 3 + 2] = make_float4(q[6], q[7], q[8], 0.0f);
+    }
+    cudaError_t e = h->prim_scratch.reserve(px * 16);
+    if (e != cudaSuccess) return h->cuda_fail(e, "gather output");
+    float4* d_out = static_cast<float4*>(h->prim_scratch.ptr);
+    if (n) e = cudaMemcpyAsync(cb.photons, rec.data(), rec.size() * 16, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, px * 16, h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "gather input");
+    launch_gather_alone(h->scene_view(), P, features, cb, n, d_out, h->num_sms, h->stream);
+    if ((e = cudaGetLastError()) != cudaSuccess) return h->cuda_fail(e, "gather");
+    e = cudaMemcpyAsync(out, d_out, px * 16, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "gather read-back");
+}
+
+int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint32_t flags) {
+    if (!h) return RAYMOND_EINVAL;
+    Params P;
+    if (const int rc = check_frame(h, params208, P)) return rc;
     cudaSetDevice(h->device);
     // The wavefront runs colour frames when asked; inspection views always
     // take the one-kernel path.
@@ -511,28 +621,8 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
     }
     CausticBuffers cb{};
     if (P.caustics != 0u) {
-        if (h->emitter_vec4s == 0) return h->fail(RAYMOND_ESTATE, "Caustics need raymond_set_emitters first.");
-        uint32_t table = 1u << 20;
-        while (table < 2ull * h->photon_capacity) table <<= 1;
-        if (table != h->photon_table || h->photon_capacity != h->photon_capacity_alloc) {
-            cudaError_t e = h->photon_heads.reserve((size_t(table) + 1) * 4);
-            if (e == cudaSuccess) e = h->photons.reserve(size_t(h->photon_capacity) * 48);
-            if (e != cudaSuccess) return h->cuda_fail(e, "photon map");
-            h->photon_table = table;
-            h->photon_capacity_alloc = h->photon_capacity;
-        }
-        cb.splats = static_cast<uint32_t*>(h->splats.ptr);
-        cb.heads = static_cast<uint32_t*>(h->photon_heads.ptr);
-        cb.photons = static_cast<float4*>(h->photons.ptr);
-        cb.table = h->photon_table;
-        cb.capacity = h->photon_capacity;
-        const uint64_t frame = uint64_t(P.width) * P.height * P.samples_per_frame;
-        cb.photons_per_frame = h->photons_override ? h->photons_override
-                                                   : uint32_t(frame < h->photon_capacity ? frame : h->photon_capacity);
-        if (h->photon_radius_override > 0.0f) {
-            P.photon_radius = h->photon_radius_override;
-            P.photon_cell = 2.0f * h->photon_radius_override;
-        }
+        const int rc = caustic_buffers(h, P, cb);
+        if (rc) return rc;
     }
     int launches = 0;
     cudaEventRecord(h->ev[0], h->stream);

@@ -28,18 +28,22 @@ def _static_denoise(r, out_tensor, stream):
     return out_tensor.cpu().numpy().reshape(-1)
 
 
-def test_static_denoise_matches_renderer_denoise(gpu):
+@pytest.mark.parametrize("width,height", [(64, 64), (100, 37), (512, 512)])
+def test_static_denoise_matches_renderer_denoise(gpu, width, height):
+    """A square image; one whose sides are no multiple of the kernels' 16×8
+    blocks (the scratch's second half starts at width·height, not at a
+    rounded size); and one of exactly RAYMOND_DENOISE_STATIC_MAX_PIXELS,
+    which the limit check (more pixels than the maximum) must accept."""
     import torch
 
-    size = 64
     scene, camera = scenes.cornell_scene()
-    r = Renderer.create(Canvas(size, size))
+    r = Renderer.create(Canvas(width, height))
     r.scene, r.camera = scene, camera
     r.samplesPerFrame = 2
     r.denoise = True
     lib = _native.lib()
     stream = lib.raymond_get_stream(r.handle)
-    out = torch.zeros(size * size * 4, dtype=torch.float32, device="cuda:0")
+    out = torch.zeros(width * height * 4, dtype=torch.float32, device="cuda:0")
     for call in range(2):  # two calls in a row, the second on a further frame
         r.render()
         r.device.queue.onSubmittedWorkDone()
