@@ -910,7 +910,7 @@ def run_ours(args, rank, world, local):
 
     stats = _native.Stats()
     step_ms, trace_ms, launches = [], [], 0
-    ext_ms, ext_launches, shade_ms, shadow_ms, caustics_ms = [], [], [], [], []
+    ext_ms, ext_launches, shade_ms, shadow_ms, caustics_ms, denoise_ms, display_ms = [], [], [], [], [], [], []
     clocks = ClockSampler(local)
     barrier()
     torch.cuda.synchronize()
@@ -933,6 +933,8 @@ def run_ours(args, rank, world, local):
         shade_ms.append(stats.ms_shade)
         shadow_ms.append(stats.ms_shadow)
         caustics_ms.append(stats.ms_caustics)
+        denoise_ms.append(stats.ms_denoise)
+        display_ms.append(stats.ms_display)
     torch.cuda.synchronize()
     barrier()
     clock_info = clocks.stop()
@@ -1001,7 +1003,8 @@ def run_ours(args, rank, world, local):
             "gpu_launches": launches,
             "stages_ms": {"trace": statistics.mean(trace_ms), "step": statistics.mean(step_ms),
                           "extend": statistics.mean(ext_ms), "shade": statistics.mean(shade_ms),
-                          "shadow": statistics.mean(shadow_ms), "caustics": statistics.mean(caustics_ms)},
+                          "shadow": statistics.mean(shadow_ms), "caustics": statistics.mean(caustics_ms),
+                          "denoise": statistics.mean(denoise_ms), "display": statistics.mean(display_ms)},
             "mrays_per_s": rays_per_path * paths_per_step * args.steps * world / total_s / 1e6,
             "rays_per_path": rays_per_path,
             "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak,

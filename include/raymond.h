@@ -200,12 +200,13 @@ int raymond_sample_streams(raymond_t* h, const uint32_t* pairs, uint32_t n, cons
  * (the photon count, capacity and radius of raymond_set_photons), and copies
  * out its fixed-point splat sums before they are resolved into the image
  * (width × height × 4 u32, 1/65536 units; splat_bytes ≥ width·height·16)
- * and the photons it deposited, 10 floats each: where it landed, its power,
- * the direction it came from, and its light path's id (u32 bits). Photons
- * come in the order the GPU's atomics stored them; *photon_count is their
- * number (at most the map's capacity) and photon_floats must hold 10 per
- * photon (NULL photons: the count alone). The image is untouched. Host
- * pointers; synchronous.
+ * and the photons it deposited, 11 floats each: where it landed, its power,
+ * the direction it came from, its light path's id and the pixel its splat
+ * went to (both u32 bits; 0xffffffff for no splat). Photons come in the
+ * order the GPU's atomics stored them; *photon_count is their number (at
+ * most the map's capacity) and photon_floats must hold 11 per photon (NULL
+ * photons: the count alone). The image is untouched. Host pointers;
+ * synchronous.
  */
 int raymond_light_trace(raymond_t* h, const void* params208, uint32_t features, uint32_t* splats, uint64_t splat_bytes,
                         float* photons, uint64_t photon_floats, uint32_t* photon_count);

@@ -45,7 +45,7 @@ def lib():
         _lib.ro_render_scene.argtypes = [P, P, P, P, P, P, U32, U32, U32, U32, U32, P, P, P, P, I, P, U32, U32, P, U32,
                                          U32, P, U32, U32, P, U32, U32]
         _lib.ro_light_trace.restype = U32
-        _lib.ro_light_trace.argtypes = [P, P, P, P, P, P, P, U32, U32, U32, U32, P, P, P, I]
+        _lib.ro_light_trace.argtypes = [P, P, P, P, P, P, P, U32, U32, U32, U32, P, P, P, P, P, P, I]
         _lib.ro_photon_gather.restype = None
         _lib.ro_photon_gather.argtypes = [P, P, P, P, P, P, P, U32, U32, U32, U32, P, P, I]
         _lib.ro_set_jitter.restype = None
@@ -172,27 +172,39 @@ def render(packed, lights_words, params: bytes, region=None, seed_hash=0, nthrea
             "rays_shadow": int(counters[7])}
 
 
-def light_trace(packed, lights_words, params: bytes, emitters, photons, seed_hash=0, nthreads=None, ids=None):
+def light_trace(packed, lights_words, params: bytes, emitters, photons, seed_hash=0, nthreads=None, ids=None,
+                margins=False):
     """One frame of light_trace (src/shaders.mjs:1628-1814) for its photons
     0..photons-1, or the range ids = (first, count) of them: dict splats
     (h×w×4 u32 fixed-point sums, 1/65536 units), photons (n×9 float32:
     where each landed, its power, the direction it came from), in photon
-    order, and photon_ids (each one's light path)."""
+    order, photon_ids (each one's light path), photon_splats (n×4 u32: the
+    pixel each splatted into, or NONE, and the fixed-point amounts) and
+    with margins, photon_margins (the smallest edge margin of the
+    primitives each photon's path hit, 0 where a hit tied with another
+    primitive's) and path_margins (that margin for every path
+    id0..id0+count-1, 1 where a path hit nothing); margins cost a second
+    traversal per hit."""
     import struct
     width, height = struct.unpack_from("<2I", params, 160)
     splats = np.zeros(width * height * 4, dtype=np.uint32)
     id0, count = ids if ids is not None else (0, int(photons))
     out = np.zeros(max(int(count), 1) * 9, dtype=np.float32)
     ids_out = np.zeros(max(int(count), 1), dtype=np.uint32)
+    splat_out = np.zeros(max(int(count), 1) * 4, dtype=np.uint32)
+    margin_out = np.zeros(max(int(count), 1), dtype=np.float32) if margins else None
+    path_margins = np.ones(max(int(count), 1), dtype=np.float32) if margins else None
     pbuf = np.frombuffer(bytes(params), dtype=np.uint8).copy()
     words = np.ascontiguousarray(lights_words, dtype=np.uint32)
     attrs = np.ascontiguousarray(packed.attributes, dtype=np.float32)
     em = np.ascontiguousarray(emitters, dtype=np.float32)
     n = lib().ro_light_trace(_p(packed.primitives), _p(packed.nodes), _p(packed.materials), _p(attrs), _p(words),
                              _p(pbuf), _p(em), int(photons), int(id0), int(count), seed_hash, _p(splats), _p(out),
-                             _p(ids_out), nthreads or threads())
+                             _p(ids_out), _p(splat_out), _p(margin_out), _p(path_margins), nthreads or threads())
     return {"splats": splats.reshape(height, width, 4), "photons": out[: n * 9].reshape(n, 9),
-            "photon_ids": ids_out[:n]}
+            "photon_ids": ids_out[:n], "photon_splats": splat_out[: n * 4].reshape(n, 4),
+            "photon_margins": margin_out[:n] if margins else None,
+            "path_margins": path_margins[: int(count)] if margins else None, "first_id": int(id0)}
 
 
 def photon_gather(packed, lights_words, params: bytes, photons, seed_hash=0, nthreads=None, rows=None, visits=False):

@@ -93,12 +93,16 @@ void ro_render_scene(const void* prims, const void* nodes, const void* materials
 // ---- light tracing and photon mapping (src/shaders.mjs:1425-1831) ----
 // Photons id0..id0+count-1 of a frame of `photons`: fixed-point splats
 // added to `splats` (W·H·4 u32) and the stored photons (9 floats: p, power,
-// -d) in photon order, with their light paths' ids in ids_out (or NULL);
-// returns how many were stored.
+// -d) in photon order, with (each optional, NULL for none) their light
+// paths' ids, their splats (4 u32: pixel or NONE, then the fixed-point
+// amounts added) and their paths' smallest edge margins; and every path's
+// smallest edge margin, whether or not it stored a photon (count floats,
+// 1 for a path that hit nothing); returns how many were stored.
 uint32_t ro_light_trace(const void* prims, const void* nodes, const void* materials, const float* attributes,
                         const uint32_t* lights, const void* params208, const float* emitters, uint32_t photons,
                         uint32_t id0, uint32_t count, uint32_t seed_hash, uint32_t* splats, float* photons_out,
-                        uint32_t* ids_out, int threads);
+                        uint32_t* ids_out, uint32_t* splat_out, float* margin_out, float* path_margin_out,
+                        int threads);
 // The photon map's caustic light through mirrors and glass on rows
 // y0..y0+rows-1, added to accum (W·H·4); each gathering pixel's count of
 // photons visited in visits_out (W·H, or NULL).
@@ -114,6 +118,10 @@ void ro_denoise(const float* accum, const float* guide_albedo, const float* guid
                 uint32_t total_samples, float* out, int threads);
 // The display pass into RGBA8.
 void ro_display(const float* accum, const float* denoised, const void* params208, uint8_t* out);
+
+// Whether another primitive than `exclude` is crossed within rtol·t of t.
+int ro_tie32(const void* prims, const void* nodes, const float* o3, const float* d3, float t, float rtol,
+             uint32_t exclude);
 
 // The sample streams in raymond_sample_streams's layout, and the
 // perturbation runs' size (0: off) and seed.

@@ -1094,11 +1094,42 @@ void camera_ray(const Params& P, float px, float py, Sampler& s, V& o, V& d) {
 struct Photon {
     uint32_t id;
     V p, beta, wi;  // where it landed, its power, and whence it came (-d)
+    // Its splat: the pixel (NONE if the camera doesn't see it) and the
+    // fixed-point amounts added; and the smallest edge margin (barycentric
+    // distance to an edge) of the triangles and quads its path hit.
+    uint32_t splat_pixel = NONE, splat_rgb[3] = {0u, 0u, 0u};
+    float margin = INF;
 };
+
+// How close a closest hit came to its primitive's edge: a triangle's or a
+// quad's barycentric distance to its nearest edge; for a box, the hit
+// point's distance (in box space, where the box is [-1, 1]³) to the
+// nearest edge of the face it lies on; for a sphere, the cosine between
+// the ray and the surface (near 0 at the silhouette).
+float edge_margin(const Ctx& c, V o, V d, const HitR& h) {
+    if (h.prim == NONE) return 1.0f;
+    const uint32_t kind = c.pu(h.prim)[0];
+    if (kind == 3u) return wmin(wmin(h.u, h.v), 1.0f - h.u - h.v);
+    if (kind == 1u) return wmin(wmin(h.u, 1.0f - h.u), wmin(h.v, 1.0f - h.v));
+    const float* f = c.pf(h.prim);
+    const V p = o + d * h.t;
+    if (kind == 2u) {
+        float gap[3];
+        for (int k = 0; k < 3; ++k) {
+            const float* row = f + 4 + 4 * k;
+            gap[k] = 1.0f - std::fabs(row[0] * p.x + row[1] * p.y + row[2] * p.z + row[3]);
+        }
+        // the smallest gap is the face the point lies on; the next is its nearest edge
+        const float lo = wmin(gap[0], wmin(gap[1], gap[2])), hi = wmax(gap[0], wmax(gap[1], gap[2]));
+        return gap[0] + gap[1] + gap[2] - lo - hi;
+    }
+    if (kind == 0u) return std::fabs(dot(norm(p - vf(f + 4)), norm(d)));
+    return 1.0f;
+}
 
 // splat (src/shaders.mjs:1443-1491): the photon's light added, in fixed
 // point with random rounding, to the pixel that sees the surface.
-void splat(Ctx& c, const Surf& s, const Mat& m, V base, V d, V beta, Sampler& sm, uint32_t* splats) {
+void splat(Ctx& c, const Surf& s, const Mat& m, V base, V d, V beta, Sampler& sm, uint32_t* splats, Photon& rec) {
     const Params& P = c.P;
     const V to_camera = vf(P.cam_pos) - s.p;
     const float dist = len(to_camera);
@@ -1125,16 +1156,20 @@ void splat(Ctx& c, const Surf& s, const Mat& m, V base, V d, V beta, Sampler& sm
     const uint32_t index = (uint32_t(py) * P.width + uint32_t(px)) * 4u;
     const float r0 = sm.rand(), r1 = sm.rand(), r2 = sm.rand();
     const V fixed = value * SPLAT_SCALE + v3(r0, r1, r2);
-    splats[index] += uint32_t(wmin(fixed.x, 4e9f));
-    splats[index + 1] += uint32_t(wmin(fixed.y, 4e9f));
-    splats[index + 2] += uint32_t(wmin(fixed.z, 4e9f));
+    rec.splat_pixel = index / 4u;
+    rec.splat_rgb[0] = uint32_t(wmin(fixed.x, 4e9f));
+    rec.splat_rgb[1] = uint32_t(wmin(fixed.y, 4e9f));
+    rec.splat_rgb[2] = uint32_t(wmin(fixed.z, 4e9f));
+    splats[index] += rec.splat_rgb[0];
+    splats[index + 1] += rec.splat_rgb[1];
+    splats[index + 2] += rec.splat_rgb[2];
 }
 
 // light_trace (src/shaders.mjs:1628-1814): photon `id` from a light
 // chosen by power, through mirrors and glass, splatted and stored where it
 // first lands on anything else. E is the emitters buffer's vec4s.
 void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t seed_hash, uint32_t* splats,
-                 std::vector<Photon>& stored) {
+                 std::vector<Photon>& stored, float* margin_out = nullptr) {
     const Params& P = c.P;
     Sampler sm = light_sampler(id, P.sample_offset, seed_hash);
     const float* header = E;
@@ -1168,6 +1203,7 @@ void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t
         dx *= circle[3];
         dy *= circle[3];
         o = vf(circle) - d * header[2] + c0 * dx + c1 * dy;
+        if (g_jitter_size != 0.0f) nudge(o, d);  // the counts below decide on the ray before it is traced
         float through = 1.0f;
         for (uint32_t i = 0; i < targets; ++i) {
             const V q = o - vf(target(i));
@@ -1200,6 +1236,10 @@ void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t
             area = 4.0f * PI * pf[7] * pf[7];
             sphere_uv(n, pf, eu, ev);
         }
+        if (g_jitter_size != 0.0f) {  // the aim below decides on the emission point before any ray is traced
+            V normal = n;
+            nudge(o, normal);
+        }
         float cones = 0.0f;
         bool inside = false;
         for (uint32_t i = 0; i < targets; ++i) {
@@ -1223,6 +1263,7 @@ void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t
                 pick -= omc;
                 ++j;
             }
+            if (g_jitter_size != 0.0f) nudge(o, d);
             float within = 1.0f;
             for (uint32_t i = 0; i < targets; ++i) {
                 const float* aim = target(i);
@@ -1243,17 +1284,26 @@ void light_trace(Ctx& c, const float* E, uint32_t photons, uint32_t id, uint32_t
     float wavelength = 0.0f;
     uint32_t bounces = 0;
     V carried = vs(1.0f);
+    float margin = INF;
     for (uint32_t depth = 0; depth < P.max_bounces; ++depth) {
         const HitR hit = trace(c, o, d, INF, false);
         if (hit.prim == NONE) return;
+        if (margin_out) {  // tracked only when asked for: it costs a second traversal per hit
+            margin = wmin(margin, edge_margin(c, o, d, hit));
+            const float of[3] = {o.x, o.y, o.z}, df[3] = {d.x, d.y, d.z};
+            if (ro_tie32(c.prims, c.nodes, of, df, hit.t, 1e-5f, hit.prim)) margin = 0.0f;
+            *margin_out = margin;
+        }
         const Surf s = surface(c, o, d, hit);
         const Mat m = material(c, s.material);
         if (m.kind == 4) return;
         const V base = albedo_uv(c, m, s.p, s.u, s.v);
         if (!is_delta(m)) {
             if (bounces > 0u) {
-                splat(c, s, m, base, d, beta * carried, sm, splats);
-                stored.push_back({id, s.p, beta * carried, -d});
+                Photon rec{id, s.p, beta * carried, -d};
+                rec.margin = margin;
+                splat(c, s, m, base, d, beta * carried, sm, splats, rec);
+                stored.push_back(rec);
             }
             return;
         }
@@ -1441,7 +1491,8 @@ extern "C" void ro_render_scene(const void* prims, const void* nodes, const void
 extern "C" uint32_t ro_light_trace(const void* prims, const void* nodes, const void* materials, const float* attributes,
                                    const uint32_t* lights, const void* params208, const float* emitters,
                                    uint32_t photons, uint32_t id0, uint32_t count, uint32_t seed_hash,
-                                   uint32_t* splats, float* photons_out, uint32_t* ids_out, int threads) {
+                                   uint32_t* splats, float* photons_out, uint32_t* ids_out, uint32_t* splat_out,
+                                   float* margin_out, float* path_margin_out, int threads) {
     Params P;
     std::memcpy(&P, params208, sizeof P);
     const uint32_t cells = P.width * P.height * 4u;
@@ -1456,7 +1507,8 @@ extern "C" uint32_t ro_light_trace(const void* prims, const void* nodes, const v
             const uint32_t k0 = next.fetch_add(256);
             if (k0 >= count) break;
             for (uint32_t k = k0; k < std::min(count, k0 + 256); ++k)
-                light_trace(c, emitters, photons, id0 + k, seed_hash, part_splats[t].data(), part_photons[t]);
+                light_trace(c, emitters, photons, id0 + k, seed_hash, part_splats[t].data(), part_photons[t],
+                            path_margin_out ? path_margin_out + k : nullptr);
         }
     };
     std::vector<std::thread> pool;
@@ -1471,6 +1523,11 @@ extern "C" uint32_t ro_light_trace(const void* prims, const void* nodes, const v
     for (size_t i = 0; i < all.size(); ++i) {
         float* q = photons_out + i * 9;
         if (ids_out) ids_out[i] = all[i].id;
+        if (splat_out) {
+            splat_out[i * 4] = all[i].splat_pixel;
+            for (int k = 0; k < 3; ++k) splat_out[i * 4 + 1 + k] = all[i].splat_rgb[k];
+        }
+        if (margin_out) margin_out[i] = all[i].margin;
         const V* v[3] = {&all[i].p, &all[i].beta, &all[i].wi};
         for (int j = 0; j < 3; ++j) {
             q[j * 3] = v[j]->x;

@@ -620,3 +620,41 @@ extern "C" void ro_surface_double(const void* prims, const float* attributes, ui
     const double vals[14] = {g.x, g.y, g.z, sh.x, sh.y, sh.z, u, v, tangent.x, tangent.y, tangent.z, up.x, up.y, up.z};
     for (int k = 0; k < 14; ++k) out[k] = vals[k];
 }
+
+// Whether a primitive other than `exclude` is crossed within rtol·t of
+// distance t along the ray (coincident faces, shared edges): there the
+// nearest hit is a tie that rounding decides.
+extern "C" int ro_tie32(const void* prims, const void* nodes, const float* o3, const float* d3_, float t, float rtol,
+                        uint32_t exclude) {
+    const F3 o = f3(o3), d = f3(d3_);
+    const F3 inv = {1.0f / safe1(d.x), 1.0f / safe1(d.y), 1.0f / safe1(d.z)};
+    const float lo = t * (1.0f - rtol), hi = t * (1.0f + rtol);
+    if (slabs32(node_f(nodes, 0), o, inv, hi) >= INF32) return 0;
+    uint32_t stack[64];
+    uint32_t sp = 0, current = 0;
+    for (;;) {
+        const uint32_t* nu = node_u(nodes, current);
+        bool descend = false;
+        if (nu[7] > 0) {
+            for (uint32_t i = nu[3]; i < nu[3] + nu[7]; ++i) {
+                if (i == exclude) continue;
+                float h[3];
+                intersect32(prims, i, o, d, hi, h);
+                if (h[0] > 0.0f && h[0] >= lo) return 1;
+            }
+        } else {
+            const uint32_t left = nu[3], right = nu[3] + 1;
+            const float t_left = slabs32(node_f(nodes, left), o, inv, hi);
+            const float t_right = slabs32(node_f(nodes, right), o, inv, hi);
+            if (t_left < INF32 && t_right < INF32 && sp < 64u) stack[sp++] = right;
+            if (t_left < INF32 || t_right < INF32) {
+                current = t_left < INF32 ? left : right;
+                descend = true;
+            }
+        }
+        if (!descend) {
+            if (sp == 0) return 0;
+            current = stack[--sp];
+        }
+    }
+}

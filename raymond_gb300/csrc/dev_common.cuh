@@ -100,11 +100,16 @@ __device__ __forceinline__ float maxc(float3 a) { return fmaxf(a.x, fmaxf(a.y, a
 __device__ __forceinline__ float clampf(float x, float lo, float hi) { return fminf(fmaxf(x, lo), hi); }
 __device__ __forceinline__ float signf(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
 __device__ __forceinline__ float3 mix3(float3 a, float3 b, float t) { return a * (1.0f - t) + b * t; }
+// 1 − x·x with the square rounded on its own, as the reference's shader
+// arithmetic has it. Where x is near 1 (a small cone's cos, a pole's z) the
+// subtraction cancels, and a fused multiply-add would round that result
+// differently by up to 1e-4 relative; the sample directions follow it.
+__device__ __forceinline__ float one_minus_sq(float x) { return 1.0f - __fmul_rn(x, x); }
 __device__ __forceinline__ float3 reflect3(float3 i, float3 n) { return i - n * (2.0f * dot(n, i)); }
 // WGSL refract(e1, e2, e3): the zero vector under total internal reflection.
 __device__ __forceinline__ float3 refract3(float3 i, float3 n, float eta) {
     const float ni = dot(n, i);
-    const float k = 1.0f - eta * eta * (1.0f - ni * ni);
+    const float k = 1.0f - __fmul_rn(__fmul_rn(eta, eta), one_minus_sq(ni));
     if (k < 0.0f) return f3(0.0f);
     return i * eta - n * (eta * ni + sqrtf(k));
 }
@@ -231,12 +236,12 @@ __device__ __forceinline__ float3 cosine_hemisphere(float3 n, Rng& rng) {
     const float phi = 2.0f * PI * u.y;
     float s, c;
     sincosf(phi, &s, &c);
-    return normalize(from_frame(n, f3(r * c, r * s, sqrtf(fmaxf(0.0f, 1.0f - r * r)))));
+    return normalize(from_frame(n, f3(r * c, r * s, sqrtf(fmaxf(0.0f, one_minus_sq(r))))));
 }
 __device__ __forceinline__ float3 sample_cone(float3 axis, float omc, Rng& rng) {
     const float2 u = rng.rand2();
     const float cos_t = 1.0f - u.x * omc;
-    const float sin_t = sqrtf(fmaxf(0.0f, 1.0f - cos_t * cos_t));
+    const float sin_t = sqrtf(fmaxf(0.0f, one_minus_sq(cos_t)));
     const float phi = 2.0f * PI * u.y;
     float s, c;
     sincosf(phi, &s, &c);

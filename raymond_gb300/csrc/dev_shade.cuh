@@ -336,7 +336,7 @@ __device__ __forceinline__ float3 sample_ggx(float3 n, float a2, Rng& rng) {
     const float2 u = rng.rand2();
     const float r = u.x;
     const float cos_t = sqrtf((1.0f - r) / (1.0f + (a2 - 1.0f) * r));
-    const float sin_t = sqrtf(fmaxf(0.0f, 1.0f - cos_t * cos_t));
+    const float sin_t = sqrtf(fmaxf(0.0f, one_minus_sq(cos_t)));
     const float phi = 2.0f * PI * u.y;
     float sn, cs;
     sincosf(phi, &sn, &cs);
@@ -354,7 +354,7 @@ __device__ __forceinline__ float dielectric_f0(float ior) {
     return r * r;
 }
 __device__ __forceinline__ float fresnel_dielectric(float cos_i, float eta) {
-    const float sin2_t = (1.0f - cos_i * cos_i) / (eta * eta);
+    const float sin2_t = one_minus_sq(cos_i) / (eta * eta);
     if (sin2_t >= 1.0f) return 1.0f;
     const float cos_t = sqrtf(1.0f - sin2_t);
     const float rs = (cos_i - eta * cos_t) / (cos_i + eta * cos_t);
@@ -601,7 +601,7 @@ __device__ __forceinline__ float3 sample_henyey_greenstein(float3 d, float g, Rn
         const float sq = (1.0f - g * g) / (1.0f + g - 2.0f * g * u.x);
         c = clampf((1.0f + g * g - sq * sq) / (2.0f * g), -1.0f, 1.0f);
     }
-    const float sin_t = sqrtf(fmaxf(0.0f, 1.0f - c * c));
+    const float sin_t = sqrtf(fmaxf(0.0f, one_minus_sq(c)));
     const float phi = 2.0f * PI * u.y;
     float sn, cs;
     sincosf(phi, &sn, &cs);

@@ -17,42 +17,48 @@ __device__ __forceinline__ uint32_t photon_cell_hash(int cx, int cy, int cz, uin
     return ((uint32_t(cx) * 73856093u) ^ (uint32_t(cy) * 19349663u) ^ (uint32_t(cz) * 83492791u)) & (table - 1u);
 }
 
-// splat (src/shaders.mjs:1444-1491): the photon's light at the pixel that sees sf.
+// splat (src/shaders.mjs:1444-1491): the photon's light at the pixel that
+// sees sf. Returns that pixel, or NONE when nothing was added.
 template <uint32_t FEAT>
-__device__ void splat(const Scene& s, const Params& P, const CausticBuffers& cb, const Surface& sf, const Material& m,
-                      float3 base, float3 d, float3 beta, Rng& rng, uint32_t* stack_col, uint32_t stride) {
+__device__ uint32_t splat(const Scene& s, const Params& P, const CausticBuffers& cb, const Surface& sf,
+                          const Material& m, float3 base, float3 d, float3 beta, Rng& rng, uint32_t* stack_col,
+                          uint32_t stride) {
     const float3 cam = f3(P.cam_pos);
     const float3 to_camera = cam - sf.p;
     const float dist = length(to_camera);
     const float3 wo = to_camera / dist;
     const float cos_film = -dot(wo, f3(P.cam_forward));
-    if (cos_film <= 1e-6f || dot(wo, sf.ng) <= 0.0f) return;
+    if (cos_film <= 1e-6f || dot(wo, sf.ng) <= 0.0f) return NONE;
     const float x = -dot(wo, f3(P.cam_right)) / (cos_film * P.tan_half_fov * P.aspect);
     const float y = -dot(wo, f3(P.cam_up)) / (cos_film * P.tan_half_fov);
     const float px = (x + 1.0f) * 0.5f * float(P.width);
     const float py = (1.0f - y) * 0.5f * float(P.height);
-    if (px < 0.0f || py < 0.0f || px >= float(P.width) || py >= float(P.height)) return;
+    if (px < 0.0f || py < 0.0f || px >= float(P.width) || py >= float(P.height)) return NONE;
     const float3 wi = -d;
     const Eval e = eval_bsdf(m, base, sf.n, wo, wi);
     const float cos_in = dot(sf.n, wi);
-    if (e.pdf <= 0.0f || cos_in <= 0.0f) return;
+    if (e.pdf <= 0.0f || cos_in <= 0.0f) return NONE;
     const float3 origin = offset_origin(sf, wo);
-    if (trace_ray<true>(s, origin, wo, dist - dot(origin - sf.p, wo), stack_col, stride).prim != NONE) return;
+    if (trace_ray<true>(s, origin, wo, dist - dot(origin - sf.p, wo), stack_col, stride).prim != NONE) return NONE;
     const float pixel_area = (4.0f * P.tan_half_fov * P.tan_half_fov * P.aspect) / float(P.width * P.height);
     const float3 value =
         beta * (e.f / cos_in) * (dot(wo, sf.ng) / (dist * dist * pixel_area * cos_film * cos_film * cos_film));
-    if (!finite3(value)) return;
+    if (!finite3(value)) return NONE;
     const uint32_t index = (uint32_t(py) * P.width + uint32_t(px)) * 4u;
     const float r0 = rng.rand(), r1 = rng.rand(), r2 = rng.rand();
     atomicAdd(&cb.splats[index], uint32_t(fminf(value.x * SPLAT_SCALE + r0, 4e9f)));
     atomicAdd(&cb.splats[index + 1], uint32_t(fminf(value.y * SPLAT_SCALE + r1, 4e9f)));
     atomicAdd(&cb.splats[index + 2], uint32_t(fminf(value.z * SPLAT_SCALE + r2, 4e9f)));
+    return index / 4u;
 }
 
 // deposit (src/shaders.mjs:1518-1528): one photon into the hashed grid. The
-// power record's fourth word keeps the light path's id, so a photon can be
-// told apart from the others whatever order the atomics stored it in.
-__device__ void deposit(const Params& P, const CausticBuffers& cb, float3 p, float3 d, float3 beta, uint32_t id) {
+// power record's fourth word keeps the light path's id and the direction
+// record's the pixel its splat went to (NONE for none), so a photon and its
+// splat can be told apart from the others whatever order the atomics
+// stored them in.
+__device__ void deposit(const Params& P, const CausticBuffers& cb, float3 p, float3 d, float3 beta, uint32_t id,
+                        uint32_t splat_pixel) {
     const uint32_t i = atomicAdd(&cb.heads[cb.table], 1u);
     if (i >= cb.capacity) return;
     const int cx = int(floorf(p.x / P.photon_cell)), cy = int(floorf(p.y / P.photon_cell)),
@@ -60,7 +66,7 @@ __device__ void deposit(const Params& P, const CausticBuffers& cb, float3 p, flo
     const uint32_t next = atomicExch(&cb.heads[photon_cell_hash(cx, cy, cz, cb.table)], i + 1u);
     cb.photons[size_t(i) * 3] = make_float4(p.x, p.y, p.z, __uint_as_float(next));
     cb.photons[size_t(i) * 3 + 1] = make_float4(beta.x, beta.y, beta.z, __uint_as_float(id));
-    cb.photons[size_t(i) * 3 + 2] = make_float4(-d.x, -d.y, -d.z, 0.0f);
+    cb.photons[size_t(i) * 3 + 2] = make_float4(-d.x, -d.y, -d.z, __uint_as_float(splat_pixel));
 }
 
 // light_trace (src/shaders.mjs:1630-1814).
@@ -127,7 +133,7 @@ __global__ void __launch_bounds__(CAUSTIC_BLOCK) k_light_trace(Scene s, Params P
                 uv = make_float2(a, 1.0f - b);
             } else {
                 const float z = 1.0f - 2.0f * rng.rand();
-                const float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+                const float r = sqrtf(fmaxf(0.0f, one_minus_sq(z)));
                 const float phi = 2.0f * PI * rng.rand();
                 n = f3(r * cosf(phi), z, r * sinf(phi));
                 o = xyz(p0) + n * p0.w;
@@ -189,8 +195,8 @@ __global__ void __launch_bounds__(CAUSTIC_BLOCK) k_light_trace(Scene s, Params P
             if (!is_delta(m)) {
                 // Straight from the lamp is the path tracer's; after mirrors or glass, a caustic.
                 if (bounces > 0u) {
-                    splat<FEAT>(s, P, cb, sf, m, base, d, beta * carried, rng, col, CAUSTIC_BLOCK);
-                    deposit(P, cb, sf.p, d, beta * carried, id);
+                    const uint32_t pixel = splat<FEAT>(s, P, cb, sf, m, base, d, beta * carried, rng, col, CAUSTIC_BLOCK);
+                    deposit(P, cb, sf.p, d, beta * carried, id, pixel);
                 }
                 break;
             }

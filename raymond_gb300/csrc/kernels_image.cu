@@ -55,12 +55,12 @@ __device__ __forceinline__ float3 light_at(const DenoiseView& v, uint32_t i) {
 // similarity (src/shaders.mjs:1958-1968): normal^64 by six squarings and the
 // depth term's exponential, for prepare's variance estimate.
 __device__ __forceinline__ float pow64(float x) {
-    x *= x;
-    x *= x;
-    x *= x;
-    x *= x;
-    x *= x;
-    return x * x;
+    x = __fmul_rn(x, x);
+    x = __fmul_rn(x, x);
+    x = __fmul_rn(x, x);
+    x = __fmul_rn(x, x);
+    x = __fmul_rn(x, x);
+    return __fmul_rn(x, x);
 }
 __device__ __forceinline__ float similarity(float4 p, float4 q, float step) {
     if (p.w <= 0.0f || q.w <= 0.0f) return (p.w <= 0.0f && q.w <= 0.0f) ? 1.0f : 0.0f;
@@ -119,7 +119,15 @@ __global__ void k_prepare(DenoiseView v, float4* __restrict__ out, float4* __res
 //   k(dx)·k(dy) · max(n_p·n_q, 0)^64 · exp(−|z_p − z_q| / (z_p·0.02·step + 1e-6)) · exp(−|l_p − l_q| / σ)
 // costs six squarings and one exp2 of the two exponents' sum. LOAD(dx, dy,
 // light, guide) fetches a tap (from a staged tile or from memory); INTERIOR
-// drops the image-edge tests where every tap is inside.
+// drops the image-edge tests where every tap is inside. Every multiply-add
+// is written out (__fmaf_rn, __fmul_rn), so the staged and the unstaged
+// kernels, each instantiation compiled on its own, give the same bits.
+__device__ __forceinline__ float lum_rn(float4 c) {
+    return __fmaf_rn(c.z, 0.0722f, __fmaf_rn(c.y, 0.7152f, __fmul_rn(c.x, 0.2126f)));
+}
+__device__ __forceinline__ float dot3_rn(float4 a, float4 b) {
+    return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)));
+}
 struct PassCentre {
     float4 c, gp;
     float lp, kz, kl;
@@ -137,20 +145,20 @@ __device__ __forceinline__ float4 atrous_pixel(const DenoiseView& v, int x, int 
 #pragma unroll
         for (int dx = -1; dx <= 1; ++dx) {
             if (INTERIOR || (x + dx >= 0 && y + dy >= 0 && x + dx < int(v.w) && y + dy < int(v.h))) {
-                const float w = c_kernel[dx < 0 ? -dx : dx] * c_kernel[dy < 0 ? -dy : dy];
+                const float w = __fmul_rn(c_kernel[dx < 0 ? -dx : dx], c_kernel[dy < 0 ? -dy : dy]);
                 float4 q, g;
                 load(dx, dy, q, g);
-                variance += w * q.w;
-                variance_weight += w;
+                variance = __fmaf_rn(w, q.w, variance);
+                variance_weight = __fadd_rn(variance_weight, w);
             }
         }
     }
-    const float sigma = 4.0f * sqrtf(variance / variance_weight) + 1e-4f;
-    const float lp = lum(xyz4(c));
-    const float kl = LOG2E / sigma;
-    const float kz = LOG2E / (gp.w * 0.02f * float(step) + 1e-6f);
+    const float sigma = __fmaf_rn(4.0f, __fsqrt_rn(__fdiv_rn(variance, variance_weight)), 1e-4f);
+    const float lp = lum_rn(c);
+    const float kl = __fdiv_rn(LOG2E, sigma);
+    const float kz = __fdiv_rn(LOG2E, __fmaf_rn(__fmul_rn(gp.w, 0.02f), float(step), 1e-6f));
     const bool background = gp.w <= 0.0f;
-    const bool flat = gp.x * gp.x + gp.y * gp.y + gp.z * gp.z == 0.0f;
+    const bool flat = dot3_rn(gp, gp) == 0.0f;
 
     float3 sum = make_float3(0.0f, 0.0f, 0.0f);
     float sum_variance = 0.0f, weight = 0.0f;
@@ -162,25 +170,29 @@ __device__ __forceinline__ float4 atrous_pixel(const DenoiseView& v, int x, int 
             if (!INTERIOR && (xx < 0 || yy < 0 || xx >= int(v.w) || yy >= int(v.h))) continue;
             float4 q, gq;
             load(dx * step, dy * step, q, gq);
-            const float k = c_kernel[dx < 0 ? -dx : dx] * c_kernel[dy < 0 ? -dy : dy];
-            const float dl = fabsf(lp - lum(xyz4(q)));
+            const float k = __fmul_rn(c_kernel[dx < 0 ? -dx : dx], c_kernel[dy < 0 ? -dy : dy]);
+            const float dl = fabsf(__fsub_rn(lp, lum_rn(q)));
             float w;
             if (background || gq.w <= 0.0f) {
-                w = (background && gq.w <= 0.0f) ? k * exp2f(-dl * kl) : 0.0f;
+                w = (background && gq.w <= 0.0f) ? __fmul_rn(k, exp2f(-__fmul_rn(dl, kl))) : 0.0f;
             } else if (flat) {
                 w = 0.0f;
             } else {
-                const float wn = pow64(fmaxf(gp.x * gq.x + gp.y * gq.y + gp.z * gq.z, 0.0f));
-                w = k * wn * exp2f(-(fabsf(gp.w - gq.w) * kz + dl * kl));
+                const float wn = pow64(fmaxf(dot3_rn(gp, gq), 0.0f));
+                w = __fmul_rn(__fmul_rn(k, wn), exp2f(-__fmaf_rn(fabsf(__fsub_rn(gp.w, gq.w)), kz, __fmul_rn(dl, kl))));
             }
-            sum.x += w * q.x;
-            sum.y += w * q.y;
-            sum.z += w * q.z;
-            sum_variance += w * w * q.w;
-            weight += w;
+            sum.x = __fmaf_rn(w, q.x, sum.x);
+            sum.y = __fmaf_rn(w, q.y, sum.y);
+            sum.z = __fmaf_rn(w, q.z, sum.z);
+            sum_variance = __fmaf_rn(__fmul_rn(w, w), q.w, sum_variance);
+            weight = __fadd_rn(weight, w);
         }
     }
-    if (weight > 0.0f) return make_float4(sum.x / weight, sum.y / weight, sum.z / weight, sum_variance / (weight * weight));
+    if (weight > 0.0f) {
+        const float w2 = __fmul_rn(weight, weight);
+        return make_float4(__fdiv_rn(sum.x, weight), __fdiv_rn(sum.y, weight), __fdiv_rn(sum.z, weight),
+                           __fdiv_rn(sum_variance, w2));
+    }
     return c;
 }
 
@@ -203,7 +215,7 @@ __device__ __forceinline__ void atrous_at(const DenoiseView& v, const float4* __
                               : atrous_pixel<false>(v, int(x), int(y), step, load);
     if (compose) {
         const float3 a = albedo_at(v, i);
-        out[i] = make_float4(l.x * a.x, l.y * a.y, l.z * a.z, 0.0f);
+        out[i] = make_float4(__fmul_rn(l.x, a.x), __fmul_rn(l.y, a.y), __fmul_rn(l.z, a.z), 0.0f);
     } else {
         out[i] = l;
     }

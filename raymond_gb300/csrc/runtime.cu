@@ -552,16 +552,16 @@ int raymond_light_trace(raymond_t* h, const void* params208, uint32_t features, 
     const uint32_t count = attempted < cb.capacity ? attempted : cb.capacity;
     *photon_count = count;
     if (photons && count) {
-        if (photon_floats < uint64_t(count) * 10)
+        if (photon_floats < uint64_t(count) * 11)
             return h->fail(RAYMOND_ECAPACITY, "%u photons need %llu floats.", count,
-                           (unsigned long long)(uint64_t(count) * 10));
+                           (unsigned long long)(uint64_t(count) * 11));
         std::vector<float4> rec(size_t(count) * 3);
         e = cudaMemcpy(rec.data(), cb.photons, rec.size() * 16, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return h->cuda_fail(e, "photon read-back");
         for (uint32_t i = 0; i < count; ++i) {
             const float4 a = rec[size_t(i) * 3], b = rec[size_t(i) * 3 + 1], c = rec[size_t(i) * 3 + 2];
-            const float row[10] = {a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, b.w};
-            std::memcpy(photons + size_t(i) * 10, row, sizeof row);
+            const float row[11] = {a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, b.w, c.w};
+            std::memcpy(photons + size_t(i) * 11, row, sizeof row);
         }
     }
     // The splat buffer starts the next frame empty, as a frame leaves it.

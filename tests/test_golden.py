@@ -109,7 +109,8 @@ def test_oracle_and_builder_match_golden_on_the_gpu_machine(gpu):
     on the GPU machine's own (Arm) cores, are pinned to the same bytes."""
     test_oracle_bvh_matches_golden()
     test_native_bvh_matches_golden(8)
-    test_packed_cornell_matches_golden()
+    test_packed_cornell_matches_golden("product")
+    test_packed_cornell_matches_golden("oracle")
     test_oracle_raycast_matches_golden()
     test_oracle_path_tracer_matches_golden()
 

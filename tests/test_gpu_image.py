@@ -29,24 +29,26 @@ def gpu_frame(scene, camera, size, spp, bounces=8, denoise=False, seed=0, view="
     return out
 
 
-def test_cornell_frame_matches_oracle_per_pixel(gpu):
+def test_cornell_frame_and_guides_match_oracle_per_pixel(gpu):
+    """The colour sums and the denoiser's albedo and normal guides, pixel by
+    pixel, with every difference classified (tests/parity.py)."""
+    from parity import classify_pixels, perturbation_runs
+
     scene, camera = scenes.cornell_scene()
     size, spp = 64, 8
     g = gpu_frame(scene, camera, size, spp)
     words, _ = light_table(scene.pack())
-    o = oracle.render(scene.pack(), words, g["params"])
-    ga, oa = g["guides"][0], o["accum"]
-    assert np.isfinite(ga).all()
-    # Same sample streams and f32 arithmetic: most pixels agree to 1e-3.
-    rel = np.abs(ga[..., :3] - oa[..., :3]) / np.maximum(np.abs(oa[..., :3]), 1e-3)
-    close = (rel.max(axis=2) < 1e-3).mean()
-    assert close > 0.9, close
-    # And the image means agree to well within the noise.
-    assert abs(ga[..., :3].mean() / oa[..., :3].mean() - 1) < 0.01
-    # Guides: albedo and normal sums agree the same way.
-    for k, key in ((1, "albedo"), (2, "normal")):
-        d = np.abs(g["guides"][k] - o[key]).max(axis=2)
-        assert (d < 1e-3).mean() > 0.9, key
+
+    def run():
+        return oracle.render(scene.pack(), words, g["params"])
+
+    o = run()
+    runs = perturbation_runs(run)
+    assert np.isfinite(g["guides"][0]).all()
+    for k, key in ((0, "accum"), (1, "albedo"), (2, "normal")):
+        c = classify_pixels(g["guides"][k], o[key], [r[key] for r in runs])
+        assert c["unexplained"] == 0, (key, c)
+        assert c["agree"] >= 0.99 * c["n"], (key, c)
 
 
 def test_inspection_views_match_oracle(gpu):
