@@ -97,6 +97,42 @@ int raymond_upload_textures(raymond_t* h, int which, const uint8_t* rgba, uint32
 int raymond_upload_environment(raymond_t* h, const uint16_t* rgba16f, uint32_t w, uint32_t hgt,
                                const float* table, uint32_t cw, uint32_t ch_plus_1);
 
+/*
+ * The texture array built on the GPU from the scene's own images, as
+ * Renderer.#uploadTextures builds it on the host (src/Renderer.mjs:637-661):
+ * `count` RGBA8 images (widths[k] × heights[k], host pointers) become the
+ * layers of an array whose layers are the largest width and height (at most
+ * 2048); an image of another size is resampled to it as Texture.resized
+ * does (src/Texture.mjs:193-209): bilinear with wrap at texel centres, in
+ * double, its bytes decoded by decode256 (the 256 values a byte stands for:
+ * sRGB to linear light for colour, byte/255 for normal maps) and, with
+ * srgb, re-encoded by toSrgbByte, else rounded as plain numbers. which: 0
+ * colour and emission textures, 1 normal maps. Does what
+ * raymond_upload_textures does with an array resized on the host; the
+ * bytes are the same.
+ */
+int raymond_upload_texture_images(raymond_t* h, int which, const uint8_t* const* images, const uint32_t* widths,
+                                  const uint32_t* heights, uint32_t count, int srgb, const double* decode256);
+
+/*
+ * The environment map built on the GPU from its float RGB pixels (w × h × 3,
+ * host), as Renderer.#uploadEnvironment builds it on the host
+ * (src/Renderer.mjs:723-760): RGBA half floats by toHalf's steps
+ * (src/Renderer.mjs:1143-1160) and the importance table of
+ * EnvironmentMap.importance (src/EnvironmentMap.mjs:202-247: min(w, 512) ×
+ * min(h, 256, that) cells, each row's running sums, then the CDF over
+ * rows). row_sines holds sin((y + 0.5) / rows · π) for each of the `rows`
+ * rows of cells, computed by the caller as the reference computes it. Does
+ * what raymond_upload_environment does with arrays made on the host; the
+ * halves and the table are the same.
+ */
+int raymond_upload_environment_rgb(raymond_t* h, const float* rgb, uint32_t w, uint32_t hgt, const double* row_sines,
+                                   uint32_t rows);
+
+/* The uploaded texture array (which 0 or 1) and environment, copied back to host memory. */
+int raymond_read_textures(raymond_t* h, int which, uint8_t* out, uint64_t bytes);
+int raymond_read_environment(raymond_t* h, uint16_t* rgba16f, uint64_t map_bytes, float* table, uint64_t table_bytes);
+
 /* Renderer.#writeEmitters' buffer (src/Renderer.mjs:670-717): vec4_count vec4s. */
 int raymond_set_emitters(raymond_t* h, const float* data, uint32_t vec4_count);
 

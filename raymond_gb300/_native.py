@@ -92,6 +92,10 @@ SIGNATURES = {
     "raymond_upload_textures": (_I, [_P, _I, _P, _U32, _U32, _U32]),
     "raymond_upload_environment": (_I, [_P, _P, _U32, _U32, _P, _U32, _U32]),
     "raymond_set_emitters": (_I, [_P, _P, _U32]),
+    "raymond_upload_texture_images": (_I, [_P, _I, _P, _P, _P, _U32, _I, _P]),
+    "raymond_upload_environment_rgb": (_I, [_P, _P, _U32, _U32, _P, _U32]),
+    "raymond_read_textures": (_I, [_P, _I, _P, _U64]),
+    "raymond_read_environment": (_I, [_P, _P, _U64, _P, _U64]),
     "raymond_resize": (_I, [_P, _U32, _U32]),
     "raymond_render": (_I, [_P, _P, _U32, _U32]),
     "raymond_sync": (_I, [_P]),

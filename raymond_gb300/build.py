@@ -20,6 +20,7 @@ CUDA_SOURCES = [
     "kernels_wavefront.cu",
     "kernels_caustics.cu",
     "kernels_image.cu",
+    "kernels_upload.cu",
     "kernels_net.cu",
     "net_runtime.cu",
     "runtime.cu",

@@ -111,6 +111,10 @@ int launch_light_trace_alone(const Scene& s, const Params& P, uint32_t features,
                              cudaStream_t st);
 int launch_gather_alone(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb, uint32_t n,
                         float4* out, int num_sms, cudaStream_t st);
+int launch_texture_layer(const uint8_t* src, uint32_t tw, uint32_t th, uint8_t* dst, uint32_t w, uint32_t h, int srgb,
+                         const double* decode, int num_sms, cudaStream_t st);
+int launch_environment(const float* rgb, uint32_t W, uint32_t H, uint32_t cw, uint32_t ch, const double* sines,
+                       uint16_t* halves, float* table, double* rows, int num_sms, cudaStream_t st);
 int launch_denoise(const Params& P, const PixelBuffers& px, unsigned* status, cudaStream_t st);
 int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st);
 // Fill each kernel unit's sRGB decode table on the current device.

@@ -68,6 +68,7 @@ struct raymond {
 
     // Scratch for host-pointer trace calls, and the work counter.
     DevBuf ray_scratch, prim_scratch, t_scratch, counter;
+    DevBuf upload_scratch;  // images staged for building texture arrays and the environment on the GPU
 
     // Wavefront path state (allocated on first wavefront frame).
     DevBuf wf_state[8], wf_hit, wf_queue[2], wf_sorted, wf_sort_key, wf_shadow, wf_counters;
@@ -296,7 +297,7 @@ void raymond_destroy(raymond_t* h) {
     for (DevBuf* b : {&h->prims, &h->nodes, &h->materials, &h->attributes, &h->lights, &h->emitters, &h->textures,
                       &h->normal_maps, &h->env_map, &h->env_table, &h->accum, &h->guide_albedo, &h->guide_normal,
                       &h->light_a, &h->light_b, &h->guide_unit, &h->denoised, &h->splats, &h->display, &h->ray_scratch,
-                      &h->prim_scratch, &h->t_scratch, &h->counter, &h->wf_hit, &h->wf_queue[0], &h->wf_queue[1],
+                      &h->prim_scratch, &h->t_scratch, &h->counter, &h->upload_scratch, &h->wf_hit, &h->wf_queue[0], &h->wf_queue[1],
                       &h->wf_sorted, &h->wf_sort_key, &h->wf_shadow, &h->wf_counters, &h->photon_heads,
                       &h->photons, &h->wide})
         b->release();
@@ -449,6 +450,113 @@ int raymond_upload_environment(raymond_t* h, const uint16_t* rgba16f, uint32_t w
     h->env_ch = ch_plus_1 - 1;
     cudaError_t e = cudaStreamSynchronize(h->stream);
     return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "environment");
+}
+
+int raymond_upload_texture_images(raymond_t* h, int which, const uint8_t* const* images, const uint32_t* widths,
+                                  const uint32_t* heights, uint32_t count, int srgb, const double* decode256) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!images || !widths || !heights || !decode256 || count == 0 || (which != 0 && which != 1))
+        return h->fail(RAYMOND_EINVAL, "Textures need images, sizes and a decoding table.");
+    uint32_t w = 0, hgt = 0;
+    size_t total = 0;
+    for (uint32_t k = 0; k < count; ++k) {
+        if (!images[k] || widths[k] == 0 || heights[k] == 0 || widths[k] > 16384 || heights[k] > 16384)
+            return h->fail(RAYMOND_EINVAL, "Texture %u has no data or a size outside 1..16384.", k);
+        w = std::max(w, widths[k]);
+        hgt = std::max(hgt, heights[k]);
+        total += size_t(widths[k]) * heights[k] * 4;
+    }
+    // The array's layers take the largest width and height, at most 2048 (src/Renderer.mjs:637-661).
+    w = std::min(w, 2048u);
+    hgt = std::min(hgt, 2048u);
+    cudaSetDevice(h->device);
+    DevBuf& buf = which == 0 ? h->textures : h->normal_maps;
+    cudaError_t e = buf.reserve(size_t(w) * hgt * 4 * count);
+    if (e == cudaSuccess) e = h->upload_scratch.reserve(256 * sizeof(double) + total);
+    if (e != cudaSuccess) return h->cuda_fail(e, "texture array");
+    uint8_t* stage = static_cast<uint8_t*>(h->upload_scratch.ptr);
+    double* decode = reinterpret_cast<double*>(stage);
+    e = cudaMemcpyAsync(decode, decode256, 256 * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+    size_t at = 256 * sizeof(double);
+    for (uint32_t k = 0; k < count && e == cudaSuccess; ++k) {
+        const size_t bytes = size_t(widths[k]) * heights[k] * 4;
+        e = cudaMemcpyAsync(stage + at, images[k], bytes, cudaMemcpyHostToDevice, h->stream);
+        if (e != cudaSuccess) break;
+        launch_texture_layer(stage + at, widths[k], heights[k], static_cast<uint8_t*>(buf.ptr) + size_t(w) * hgt * 4 * k,
+                             w, hgt, srgb, decode, h->num_sms, h->stream);
+        at += bytes;
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "texture array");
+    if (which == 0) {
+        h->tex_w = w;
+        h->tex_h = hgt;
+        h->tex_layers = count;
+    } else {
+        h->nrm_w = w;
+        h->nrm_h = hgt;
+        h->nrm_layers = count;
+    }
+    return RAYMOND_OK;
+}
+
+int raymond_upload_environment_rgb(raymond_t* h, const float* rgb, uint32_t w, uint32_t hgt, const double* row_sines,
+                                   uint32_t rows) {
+    if (!h) return RAYMOND_EINVAL;
+    if (!rgb || !row_sines || w == 0 || hgt == 0 || w > 16384 || hgt > 16384)
+        return h->fail(RAYMOND_EINVAL, "The environment needs a map of 1..16384 pixels a side and its rows' sines.");
+    const uint32_t cw = std::min(w, 512u), ch = std::min(std::min(hgt, 256u), cw);
+    if (rows != ch) return h->fail(RAYMOND_EINVAL, "The table has %u rows of cells; %u sines were given.", ch, rows);
+    cudaSetDevice(h->device);
+    const size_t n = size_t(w) * hgt;
+    const size_t rgb_bytes = (n * 12 + 7) & ~size_t(7);  // then the sines and the rows' totals, 8-byte aligned
+    cudaError_t e = h->env_map.reserve(n * 8);
+    if (e == cudaSuccess) e = h->env_table.reserve(size_t(cw) * (ch + 1) * 4);
+    if (e == cudaSuccess) e = h->upload_scratch.reserve(rgb_bytes + size_t(ch) * 16);
+    if (e != cudaSuccess) return h->cuda_fail(e, "environment");
+    float* d_rgb = static_cast<float*>(h->upload_scratch.ptr);
+    double* d_sines = reinterpret_cast<double*>(static_cast<uint8_t*>(h->upload_scratch.ptr) + rgb_bytes);
+    double* d_rows = d_sines + ch;
+    e = cudaMemcpyAsync(d_rgb, rgb, n * 12, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_sines, row_sines, size_t(ch) * 8, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->env_table.ptr, 0, size_t(cw) * (ch + 1) * 4, h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "environment");
+    launch_environment(d_rgb, w, hgt, cw, ch, d_sines, static_cast<uint16_t*>(h->env_map.ptr),
+                       static_cast<float*>(h->env_table.ptr), d_rows, h->num_sms, h->stream);
+    if ((e = cudaGetLastError()) == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "environment");
+    h->env_w = w;
+    h->env_h = hgt;
+    h->env_cw = cw;
+    h->env_ch = ch;
+    return RAYMOND_OK;
+}
+
+int raymond_read_textures(raymond_t* h, int which, uint8_t* out, uint64_t bytes) {
+    if (!h) return RAYMOND_EINVAL;
+    if (which != 0 && which != 1) return h->fail(RAYMOND_EINVAL, "which is 0 (colour) or 1 (normal maps).");
+    const size_t need = which == 0 ? size_t(h->tex_w) * h->tex_h * 4 * h->tex_layers
+                                   : size_t(h->nrm_w) * h->nrm_h * 4 * h->nrm_layers;
+    if (!out || bytes < need) return h->fail(RAYMOND_EINVAL, "The texture array needs %zu bytes.", need);
+    cudaSetDevice(h->device);
+    const DevBuf& buf = which == 0 ? h->textures : h->normal_maps;
+    cudaError_t e = need ? cudaMemcpyAsync(out, buf.ptr, need, cudaMemcpyDeviceToHost, h->stream) : cudaSuccess;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "texture read-back");
+}
+
+int raymond_read_environment(raymond_t* h, uint16_t* rgba16f, uint64_t map_bytes, float* table, uint64_t table_bytes) {
+    if (!h) return RAYMOND_EINVAL;
+    if (h->env_ch == 0) return h->fail(RAYMOND_ESTATE, "No environment has been uploaded.");
+    const size_t map = size_t(h->env_w) * h->env_h * 8, tab = size_t(h->env_cw) * (h->env_ch + 1) * 4;
+    if (!rgba16f || !table || map_bytes < map || table_bytes < tab)
+        return h->fail(RAYMOND_EINVAL, "The environment needs %zu and %zu bytes.", map, tab);
+    cudaSetDevice(h->device);
+    cudaError_t e = cudaMemcpyAsync(rgba16f, h->env_map.ptr, map, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(table, h->env_table.ptr, tab, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? RAYMOND_OK : h->cuda_fail(e, "environment read-back");
 }
 
 int raymond_set_emitters(raymond_t* h, const float* data, uint32_t vec4_count) {

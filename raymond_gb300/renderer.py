@@ -166,6 +166,22 @@ def texture_array(textures, srgb):
     return np.concatenate([t.resized(w, h, srgb).data.reshape(-1) for t in textures]), w, h
 
 
+def byte_decoding(srgb):
+    """What each byte value of a texture stands for when sampled
+    (src/Texture.mjs fromSrgbByte, fromByte): linear light, or byte/255."""
+    from .texture import _PLAIN, _SRGB_TO_LINEAR
+
+    return _SRGB_TO_LINEAR if srgb else _PLAIN
+
+
+def table_row_sines(width, height):
+    """sin((y + 0.5) / rows · π) for each row of the environment's importance
+    table (src/EnvironmentMap.mjs:208-213)."""
+    cw = min(width, 512)
+    rows = min(height, 256, cw)
+    return [math.sin((y + 0.5) / rows * math.pi) for y in range(rows)]
+
+
 def environment_arrays(env):
     """What Renderer uploads for an environment map (src/Renderer.mjs:723-760):
     its pixels as RGBA half floats (alpha 1) and its importance table."""
@@ -646,17 +662,27 @@ class Renderer:
         self._samples = 0
 
     def _upload_textures(self, packed):
+        """The texture arrays, each texture resized into its layer on the GPU
+        (raymond_upload_texture_images; the same bytes as texture_array)."""
         for which, textures, srgb in ((0, packed.textures, True), (1, packed.normalMaps, False)):
             if not textures:
                 continue
-            data, w, h = texture_array(textures, srgb)
-            check(lib().raymond_upload_textures(self._h, which, ptr(data), w, h, len(textures)), self._h)
+            images = [np.ascontiguousarray(t.data, dtype=np.uint8) for t in textures]
+            ptrs = (ctypes.c_void_p * len(images))(*[ptr(a) for a in images])
+            widths = np.array([t.width for t in textures], dtype=np.uint32)
+            heights = np.array([t.height for t in textures], dtype=np.uint32)
+            decode = np.ascontiguousarray(byte_decoding(srgb), dtype=np.float64)
+            check(lib().raymond_upload_texture_images(self._h, which, ptrs, ptr(widths), ptr(heights), len(images),
+                                                      1 if srgb else 0, ptr(decode)), self._h)
 
     def _upload_environment(self, env):
+        """The environment's half floats and importance table, built on the GPU
+        (raymond_upload_environment_rgb; the same as environment_arrays)."""
         if env is not None:
-            rgba, table = environment_arrays(env)
-            check(lib().raymond_upload_environment(self._h, ptr(rgba), env.width, env.height, ptr(table["data"]),
-                                                   table["width"], table["height"] + 1), self._h)
+            rgb = np.ascontiguousarray(env.data, dtype=np.float32)
+            sines = np.ascontiguousarray(table_row_sines(env.width, env.height), dtype=np.float64)
+            check(lib().raymond_upload_environment_rgb(self._h, ptr(rgb), env.width, env.height, ptr(sines),
+                                                       len(sines)), self._h)
         self._uploaded_environment = env
         self._samples = 0
 
