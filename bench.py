@@ -131,6 +131,13 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+# k_wf_extend's measured traffic per path on the sphere field (ncu, 512²
+# frame, 4-wide tree): DRAM read + write, bytes through L2, and the mean
+# share of active lanes per executed instruction.
+EXTEND_DRAM_BYTES_PER_PATH = (227_195_392 + 53_279_232) / 1_048_576
+EXTEND_L2_BYTES_PER_PATH = 5_481_172_960 / 1_048_576
+EXTEND_LANES_PER_INSTRUCTION = 11.7
+
 CAUSTICS_WORKLOAD = ("water caustics 1024x1024 (130,050-triangle water surface, glass sphere, r=0.1 lamp), "
                      "8 bounces, 1M light paths splatted + photon map of up to 4M photons gathered at r=0.01")
 CAUSTICS_LIGHT_PATHS = 1_000_000
@@ -992,7 +999,17 @@ def run_ours(args, rank, world, local):
             bytes_per_launch = bytes_per_path * paths_per_step
             launch_s = statistics.mean(trace_ms) / 1e3
         achieved = bytes_per_launch / launch_s / 1e9
-        traffic = None  # no full-size DRAM capture of this kernel; see the 512² profile
+        traffic = l2_bytes = lanes = None
+        if wavefront and not caustics:
+            # From the ncu capture of a 512² frame of this scene (profile
+            # k_wf_extend_shadow_traffic_sphere_field_512): per path over a
+            # frame's extension launches, DRAM 267 B and 5,227 B through L2;
+            # 11.7 of 32 lanes active per instruction. Scaled by this frame's
+            # paths over its extend launches (traffic grows with the paths:
+            # the scene stays in L2, the path state streams).
+            traffic = EXTEND_DRAM_BYTES_PER_PATH * paths_per_step / launches_per_step
+            l2_bytes = EXTEND_L2_BYTES_PER_PATH * paths_per_step / launches_per_step
+            lanes = EXTEND_LANES_PER_INSTRUCTION
         result = {
             "metric": METRIC, "value": value, "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
@@ -1009,6 +1026,11 @@ def run_ours(args, rank, world, local):
             "rays_per_path": rays_per_path,
             "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "traffic_source": ("ncu capture of a 512² frame (dram__bytes_read + write of its extension "
+                                            "launches), scaled by paths" if traffic else None),
+                         "l2_bytes_per_launch": l2_bytes,
+                         "l2_GBps": l2_bytes / launch_s / 1e9 if l2_bytes else None,
+                         "active_lanes_per_instruction": lanes,
                          "bytes_per_launch": bytes_per_launch, "bytes_per_path": bytes_per_path,
                          "traversal_bytes_per_path": split},
             "cpu_baseline": {"value": cpu_paths / cpu_s / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
