@@ -89,7 +89,17 @@ struct raymond {
     cudaEvent_t b_copy_done = nullptr;
     cudaEvent_t order = nullptr;  // orders a batch frame against the job renderers' own streams
     bool b_copy_pending = false;
+    // The jobs run as up to kBatchGroups groups, each with its own slice of
+    // the path pool, its own counters and its own stream (forked from and
+    // joined to `stream`), so that one group's kernels fill the SMs another
+    // group's persistent kernels leave idle at their tails. Group g's waves
+    // are b_waves[b_group_first[g] .. + b_group_waves[g]).
+    static constexpr int kBatchGroups = 8;
     std::vector<WavePlan> b_waves;
+    std::vector<uint32_t> b_group_first, b_group_waves;
+    uint64_t b_group_cap = 0;
+    cudaStream_t b_group_stream[kBatchGroups] = {};
+    cudaEvent_t b_fork = nullptr, b_join[kBatchGroups] = {};
     std::vector<uint64_t> b_signature;
     uint32_t b_max_bounces = 0, b_total_pixels = 0, b_n = 0;
     uint64_t b_paths = 0;
@@ -306,6 +316,11 @@ void raymond_destroy(raymond_t* h) {
         if (ev) cudaEventDestroy(ev);
     if (h->b_graph) cudaGraphExecDestroy(h->b_graph);
     if (h->b_copy_done) cudaEventDestroy(h->b_copy_done);
+    if (h->b_fork) cudaEventDestroy(h->b_fork);
+    for (int g = 0; g < raymond::kBatchGroups; ++g) {
+        if (h->b_join[g]) cudaEventDestroy(h->b_join[g]);
+        if (h->b_group_stream[g]) cudaStreamDestroy(h->b_group_stream[g]);
+    }
     if (h->order) cudaEventDestroy(h->order);
     if (h->b_staging) cudaFreeHost(h->b_staging);
     for (DevBuf* b : {&h->b_jobs, &h->b_segments, &h->b_jobpix}) b->release();
@@ -816,29 +831,51 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
             cudaGraphExecDestroy(h->b_graph);
             h->b_graph = nullptr;
         }
-        // Plan: each job's samples in order, packed into waves of `cap` paths.
+        // Groups: jobs dealt to the least-loaded group, largest first; each
+        // group's jobs keep their order.
+        const uint32_t groups = std::min<uint32_t>(raymond::kBatchGroups, n);
+        std::vector<uint32_t> group_of(n), by_size(n);
+        std::vector<uint64_t> load(groups, 0);
+        for (uint32_t j = 0; j < n; ++j) by_size[j] = j;
+        auto paths_of = [&](uint32_t j) {
+            return uint64_t(desc[j].params.width) * desc[j].params.height * desc[j].params.samples_per_frame;
+        };
+        std::stable_sort(by_size.begin(), by_size.end(), [&](uint32_t a, uint32_t b) { return paths_of(a) > paths_of(b); });
+        for (uint32_t j : by_size) {
+            const uint32_t g = uint32_t(std::min_element(load.begin(), load.end()) - load.begin());
+            group_of[j] = g;
+            load[g] += paths_of(j);
+        }
+        const uint64_t group_cap = std::max<uint64_t>(cap / groups, max_pixels);
+        // Plan: per group, its jobs' samples in order, packed into waves of group_cap paths.
         std::vector<WaveSegment> segs;
         std::vector<WavePlan> waves;
-        WavePlan cur{0, 0, 0, 0};
-        for (uint32_t j = 0; j < n; ++j) {
-            const uint32_t pixels = desc[j].params.width * desc[j].params.height;
-            uint32_t k = 0;
-            while (k < desc[j].params.samples_per_frame) {
-                const uint64_t room = (cap - cur.paths) / pixels;
-                if (room == 0) {
-                    waves.push_back(cur);
-                    cur = WavePlan{uint32_t(segs.size()), 0, 0, 0};
-                    continue;
+        std::vector<uint32_t> group_first(groups), group_waves(groups);
+        for (uint32_t g = 0; g < groups; ++g) {
+            group_first[g] = uint32_t(waves.size());
+            WavePlan cur{uint32_t(segs.size()), 0, 0, 0};
+            for (uint32_t j = 0; j < n; ++j) {
+                if (group_of[j] != g) continue;
+                const uint32_t pixels = desc[j].params.width * desc[j].params.height;
+                uint32_t k = 0;
+                while (k < desc[j].params.samples_per_frame) {
+                    const uint64_t room = (group_cap - cur.paths) / pixels;
+                    if (room == 0) {
+                        waves.push_back(cur);
+                        cur = WavePlan{uint32_t(segs.size()), 0, 0, 0};
+                        continue;
+                    }
+                    const uint32_t nk = uint32_t(std::min<uint64_t>(desc[j].params.samples_per_frame - k, room));
+                    segs.push_back(WaveSegment{j, k, nk, pixels, cur.paths, cur.pixels});
+                    cur.segments++;
+                    cur.paths += nk * pixels;
+                    cur.pixels += pixels;
+                    k += nk;
                 }
-                const uint32_t nk = uint32_t(std::min<uint64_t>(desc[j].params.samples_per_frame - k, room));
-                segs.push_back(WaveSegment{j, k, nk, pixels, cur.paths, cur.pixels});
-                cur.segments++;
-                cur.paths += nk * pixels;
-                cur.pixels += pixels;
-                k += nk;
             }
+            if (cur.segments) waves.push_back(cur);
+            group_waves[g] = uint32_t(waves.size()) - group_first[g];
         }
-        if (cur.segments) waves.push_back(cur);
         std::vector<JobPixels> jp(n);
         uint32_t off = 0;
         for (uint32_t j = 0; j < n; ++j) {
@@ -852,19 +889,20 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
             e = cudaMemcpy(h->b_segments.ptr, segs.data(), segs.size() * sizeof(WaveSegment), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(h->b_jobpix.ptr, jp.data(), n * sizeof(JobPixels), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return h->cuda_fail(e, "batch plan");
-        // The pool, as for a single frame of `cap` paths.
-        if (cap > h->wf_capacity) {
+        // The pool: every group's slice, as for a single frame of that many paths.
+        const uint64_t pool = group_cap * groups;
+        if (pool > h->wf_capacity) {
             for (DevBuf& b : h->wf_state)
-                if (e == cudaSuccess) e = b.reserve(cap * 16);
-            if (e == cudaSuccess) e = h->wf_hit.reserve(cap * 16);
-            if (e == cudaSuccess) e = h->wf_queue[0].reserve(cap * 4);
-            if (e == cudaSuccess) e = h->wf_queue[1].reserve(cap * 4);
-            if (e == cudaSuccess) e = h->wf_sorted.reserve(cap * 4);
-            if (e == cudaSuccess) e = h->wf_sort_key.reserve(cap * 4);
-            if (e == cudaSuccess) e = h->wf_shadow.reserve(cap * 48);
-            if (e == cudaSuccess) e = h->wf_counters.reserve(256);
+                if (e == cudaSuccess) e = b.reserve(pool * 16);
+            if (e == cudaSuccess) e = h->wf_hit.reserve(pool * 16);
+            if (e == cudaSuccess) e = h->wf_queue[0].reserve(pool * 4);
+            if (e == cudaSuccess) e = h->wf_queue[1].reserve(pool * 4);
+            if (e == cudaSuccess) e = h->wf_sorted.reserve(pool * 4);
+            if (e == cudaSuccess) e = h->wf_sort_key.reserve(pool * 4);
+            if (e == cudaSuccess) e = h->wf_shadow.reserve(pool * 48);
+            if (e == cudaSuccess) e = h->wf_counters.reserve(256 * raymond::kBatchGroups);
             if (e != cudaSuccess) return h->cuda_fail(e, "batch path pool");
-            h->wf_capacity = cap;
+            h->wf_capacity = pool;
         }
         if (n > h->b_staging_cap) {
             if (h->b_staging) cudaFreeHost(h->b_staging);
@@ -874,7 +912,18 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
             h->b_staging_cap = n;
         }
         if (!h->b_copy_done) cudaEventCreateWithFlags(&h->b_copy_done, cudaEventDisableTiming);
+        if (!h->b_fork) {
+            e = cudaEventCreateWithFlags(&h->b_fork, cudaEventDisableTiming);
+            for (int g = 0; g < raymond::kBatchGroups && e == cudaSuccess; ++g) {
+                e = cudaEventCreateWithFlags(&h->b_join[g], cudaEventDisableTiming);
+                if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->b_group_stream[g], cudaStreamNonBlocking);
+            }
+            if (e != cudaSuccess) return h->cuda_fail(e, "batch streams");
+        }
         h->b_waves = waves;
+        h->b_group_first = group_first;
+        h->b_group_waves = group_waves;
+        h->b_group_cap = group_cap;
         h->b_signature = sig;
         h->b_max_bounces = max_bounces;
         h->b_total_pixels = uint32_t(total_pixels);
@@ -912,8 +961,30 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
     const WaveSegment* d_segs = static_cast<const WaveSegment*>(h->b_segments.ptr);
     const JobPixels* d_pix = static_cast<const JobPixels*>(h->b_jobpix.ptr);
     auto enqueue = [&]() {
-        int launches = launch_wavefront_batch(d_jobs, d_segs, h->b_waves.data(), uint32_t(h->b_waves.size()),
-                                              h->b_max_bounces, features, w, h->tuning, h->num_sms, h->stream);
+        int launches = 0;
+        const uint32_t groups = uint32_t(h->b_group_first.size());
+        cudaEventRecord(h->b_fork, h->stream);
+        for (uint32_t g = 0; g < groups; ++g) {
+            // The group's slice of the pool, with its own counters.
+            const uint64_t base = h->b_group_cap * g;
+            WavefrontState wg = w;
+            for (int k = 0; k < 8; ++k) wg.s[k] += base;
+            wg.hit += base;
+            wg.queue[0] += base;
+            wg.queue[1] += base;
+            wg.sorted += base;
+            wg.sort_key += base;
+            wg.shadow += base * 3;
+            wg.counters += 64 * g;
+            wg.capacity = h->b_group_cap;
+            cudaStream_t sg = h->b_group_stream[g];
+            cudaStreamWaitEvent(sg, h->b_fork, 0);
+            launches += launch_wavefront_batch(d_jobs, d_segs, h->b_waves.data() + h->b_group_first[g],
+                                               h->b_group_waves[g], h->b_max_bounces, features, wg, h->tuning,
+                                               h->num_sms, sg);
+            cudaEventRecord(h->b_join[g], sg);
+            cudaStreamWaitEvent(h->stream, h->b_join[g], 0);
+        }
         launches += launch_image_batch(d_jobs, d_pix, h->b_n, h->b_total_pixels, h->num_sms, h->stream);
         return launches;
     };
