@@ -81,6 +81,13 @@ struct WavePlan {
 };
 
 // Launch shape of the wavefront kernels (chosen by the tuner).
+// A second stream and the two events that fork work onto it from a frame's
+// stream and join it back.
+struct SideStream {
+    cudaStream_t stream;
+    cudaEvent_t fork, join;
+};
+
 struct WavefrontTuning {
     int steps;                    // traversal steps between lane refills
     int traversal_blocks_per_sm;  // persistent extend/shadow blocks per SM
@@ -97,7 +104,7 @@ int launch_megakernel(const Scene& s, const Params& P, uint32_t features, const 
                       cudaStream_t st);
 int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,
                      const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st,
-                     StageEvents* events);
+                     const SideStream* side, StageEvents* events);
 int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments, const WavePlan* waves,
                            uint32_t n_waves, uint32_t max_bounces, uint32_t features, const WavefrontState& w,
                            const WavefrontTuning& tune, int num_sms, cudaStream_t st);

@@ -6,9 +6,10 @@
 // are persistent: a warp's lanes each hold one ray, run a few traversal
 // steps, and lanes whose ray finished refill from the queue together
 // (__ballot_sync picks them, one atomicAdd claims their entries), so warps
-// stay full while rays of very different lengths drain. Queue pushes are
-// warp-aggregated the same way. Every kernel reads its work count from device
-// memory, so a frame's launches never wait on the host.
+// stay full while rays of very different lengths drain. Queues are built a
+// tile of 2,048 entries at a time, one atomic per tile. Every kernel reads
+// its work count from device memory, so a frame's launches never wait on
+// the host.
 #include "dev_shade.cuh"
 #include "kernels.cuh"
 
@@ -21,18 +22,6 @@ constexpr uint32_t FULL = 0xffffffffu;
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 __device__ __forceinline__ uint32_t lanemask_lt() { return (1u << lane_id()) - 1u; }
-
-// Warp-aggregated push: the lanes with pred set get consecutive slots from
-// one atomicAdd on *counter. Call with every lane of the warp present.
-__device__ __forceinline__ uint32_t push_slot(uint32_t* counter, bool pred) {
-    const uint32_t mask = __ballot_sync(FULL, pred);
-    if (!mask) return 0;
-    const uint32_t leader = __ffs(mask) - 1u;
-    uint32_t base = 0;
-    if (lane_id() == leader) base = atomicAdd(counter, __popc(mask));
-    base = __shfl_sync(FULL, base, leader);
-    return base + __popc(mask & lanemask_lt());
-}
 
 // ---- path state <-> SoA ----
 __device__ __forceinline__ void store_path(const WavefrontState& w, uint32_t p, const PathState& ps, uint32_t pixel) {
@@ -70,11 +59,13 @@ __device__ __forceinline__ uint32_t load_path(const WavefrontState& w, uint32_t 
     return r.w;
 }
 
-// Counters (u32) in w.counters: queue sizes [0], [1], shadow size [2],
-// per-launch fetch counters [4..7], the shading-key bucket sizes [8..23] and
-// the scatter's bucket cursors [24..39], all of [4..39] zeroed before each
-// extension launch.
-enum { C_QUEUE0 = 0, C_QUEUE1 = 1, C_SHADOW = 2, C_FETCH = 4, C_BUCKET = 8, C_CURSOR = 24 };
+// Counters (u32) in w.counters: queue sizes [0], [1], shadow size [2] and
+// the shadow kernel's fetch counter [3] (both zeroed before shading), the
+// extension kernel's fetch counter [4], the shading-key bucket sizes
+// [8..23] and the scatter's bucket cursors [24..39], all of [4..39] zeroed
+// before each extension launch (while the previous bounce's shadow rays may
+// still be tracing).
+enum { C_QUEUE0 = 0, C_QUEUE1 = 1, C_SHADOW = 2, C_SHADOW_FETCH = 3, C_FETCH = 4, C_BUCKET = 8, C_CURSOR = 24 };
 constexpr int SORT_BUCKETS = 16;
 constexpr int C_ZEROED = 4 + 2 * SORT_BUCKETS;  // words from C_FETCH on
 
@@ -141,6 +132,7 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_generate(Params P, WavefrontSta
         w.counters[C_QUEUE0] = n_paths;
         w.counters[C_QUEUE1] = 0;
         w.counters[C_SHADOW] = 0;
+        w.counters[C_SHADOW_FETCH] = 0;
     }
 }
 
@@ -325,34 +317,78 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Ctx ctx, WavefrontState 
     }
 }
 
+// ---- queue building in tiles ----
+// The scatter and the compaction take the queue in tiles of TILE consecutive
+// entries per block (item k of thread t at k·TILE_THREADS + t). Each entry's
+// place within its tile's share of an output comes from warp ballots (or
+// key matches) and a scan, in shared memory, of the counts of each (item,
+// warp) in tile order; the tile then claims its range of the output with one
+// atomic per counter. Entries keep their queue order within a tile, and a
+// counter takes one atomic per 2,048 entries instead of one per warp.
+constexpr int TILE_THREADS = 256, TILE_ITEMS = 8, TILE = TILE_THREADS * TILE_ITEMS;
+constexpr int TILE_WARPS = TILE_THREADS / 32, TILE_PARTS = TILE_ITEMS * TILE_WARPS;  // 64 parts
+static_assert(TILE_PARTS == 64, "a warp scans a tile's parts two per lane");
+
+// Exclusive scan of part[0..63] in place by one warp; returns the total.
+__device__ __forceinline__ uint32_t scan_parts(uint32_t* part) {
+    const uint32_t l = lane_id();
+    const uint32_t a = part[2 * l], b = part[2 * l + 1];
+    uint32_t incl = a + b;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(FULL, incl, o);
+        if (l >= uint32_t(o)) incl += v;
+    }
+    const uint32_t excl = incl - a - b;
+    part[2 * l] = excl;
+    part[2 * l + 1] = excl + a;
+    return __shfl_sync(FULL, incl, 31);
+}
+
 // ---- scatter: this bounce's queue in shading-key order ----
-// Places are taken warp by warp in queue order (one atomic per key a warp
-// holds), so within a bucket paths keep roughly their queue order and the
+// Within a bucket, paths keep their queue order inside each tile, so the
 // rays shading emits stay coherent.
-__global__ void __launch_bounds__(WF_BLOCK) k_wf_scatter(WavefrontState w, int q) {
-    __shared__ uint32_t base[SORT_BUCKETS];
+__global__ void __launch_bounds__(TILE_THREADS) k_wf_scatter(WavefrontState w, int q) {
+    __shared__ uint32_t start[SORT_BUCKETS];  // each bucket's first place in the sorted queue
+    __shared__ uint32_t base[SORT_BUCKETS];   // the tile's first place within each bucket
+    __shared__ uint32_t part[SORT_BUCKETS][TILE_PARTS];
     if (threadIdx.x == 0) {
         uint32_t sum = 0;
         for (int k = 0; k < SORT_BUCKETS; ++k) {
-            base[k] = sum;
+            start[k] = sum;
             sum += w.counters[C_BUCKET + k];
         }
     }
-    __syncthreads();
     const uint32_t n = w.counters[C_QUEUE0 + q];
     const uint32_t* queue = w.queue[q];
-    const uint32_t rounds = (n + gridDim.x * blockDim.x - 1) / (gridDim.x * blockDim.x);
-    for (uint32_t r = 0; r < rounds; ++r) {  // whole warps together, for the match
-        const uint32_t i = (r * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
-        const bool have = i < n;
-        const uint32_t path = have ? queue[i] : 0u;
-        const uint32_t key = have ? w.sort_key[path] : 0xFFFFFFFFu;
-        const uint32_t peers = __match_any_sync(FULL, key) & __ballot_sync(FULL, have);
-        uint32_t at = 0;
-        const uint32_t leader = have ? uint32_t(__ffs(peers) - 1) : lane_id();
-        if (have && lane_id() == leader) at = atomicAdd(w.counters + C_CURSOR + key, uint32_t(__popc(peers)));
-        at = __shfl_sync(FULL, at, int(leader));
-        if (have) w.sorted[base[key] + at + uint32_t(__popc(peers & lanemask_lt()))] = path;
+    const uint32_t warp = threadIdx.x >> 5;
+    for (uint32_t t0 = blockIdx.x * TILE; t0 < n; t0 += gridDim.x * TILE) {
+        for (int i = threadIdx.x; i < SORT_BUCKETS * TILE_PARTS; i += TILE_THREADS) (&part[0][0])[i] = 0u;
+        __syncthreads();
+        uint32_t path[TILE_ITEMS], key[TILE_ITEMS], peers[TILE_ITEMS];
+#pragma unroll
+        for (int k = 0; k < TILE_ITEMS; ++k) {
+            const uint32_t idx = t0 + k * TILE_THREADS + threadIdx.x;
+            path[k] = idx < n ? queue[idx] : 0u;
+            key[k] = idx < n ? w.sort_key[path[k]] : 0xFFFFFFFFu;
+            peers[k] = __match_any_sync(FULL, key[k]);
+            if (key[k] != 0xFFFFFFFFu && lane_id() == uint32_t(__ffs(peers[k]) - 1))
+                part[key[k]][k * TILE_WARPS + warp] = __popc(peers[k]);
+        }
+        __syncthreads();
+        for (int b = warp; b < SORT_BUCKETS; b += TILE_WARPS) {
+            const uint32_t total = scan_parts(part[b]);
+            uint32_t at = 0;
+            if (lane_id() == 0 && total) at = atomicAdd(w.counters + C_CURSOR + b, total);
+            if (lane_id() == 0) base[b] = start[b] + at;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < TILE_ITEMS; ++k)
+            if (key[k] != 0xFFFFFFFFu)
+                w.sorted[base[key[k]] + part[key[k]][k * TILE_WARPS + warp] + __popc(peers[k] & lanemask_lt())] =
+                    path[k];
+        __syncthreads();  // the next tile reuses part and base
     }
 }
 
@@ -387,22 +423,43 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shade(Ctx ctx, WavefrontState w
 }
 
 // ---- compact: the next extension queue and the shadow list, in queue order ----
-__global__ void __launch_bounds__(WF_BLOCK) k_wf_compact(WavefrontState w, int q) {
+__global__ void __launch_bounds__(TILE_THREADS) k_wf_compact(WavefrontState w, int q) {
+    __shared__ uint32_t base[2];
+    __shared__ uint32_t part[2][TILE_PARTS];  // [0]: paths that continue, [1]: paths with a shadow ray
     const uint32_t n = w.counters[C_QUEUE0 + q];
     const uint32_t* queue = w.queue[q];
     uint32_t* out_queue = w.queue[q ^ 1];
-    uint32_t* out_count = w.counters + C_QUEUE0 + (q ^ 1);
-    uint32_t* shadow_count = w.counters + C_SHADOW;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (n + stride - 1) / stride;
-    for (uint32_t r = 0; r < rounds; ++r) {  // whole warps together, so the pushes aggregate
-        const uint32_t idx = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        const uint32_t path = idx < n ? queue[idx] : 0u;
-        const uint32_t f = idx < n ? w.sort_key[path] : 0u;
-        const uint32_t slot = push_slot(out_count, (f & 1u) != 0u);
-        if (f & 1u) out_queue[slot] = path;
-        const uint32_t sslot = push_slot(shadow_count, (f & 2u) != 0u);
-        if (f & 2u) w.sorted[sslot] = path;  // the shadow list (the shade order is no longer needed)
+    const uint32_t warp = threadIdx.x >> 5;
+    for (uint32_t t0 = blockIdx.x * TILE; t0 < n; t0 += gridDim.x * TILE) {
+        uint32_t path[TILE_ITEMS], more[TILE_ITEMS], shadow[TILE_ITEMS];
+#pragma unroll
+        for (int k = 0; k < TILE_ITEMS; ++k) {
+            const uint32_t idx = t0 + k * TILE_THREADS + threadIdx.x;
+            path[k] = idx < n ? queue[idx] : 0u;
+            const uint32_t f = idx < n ? w.sort_key[path[k]] : 0u;
+            more[k] = __ballot_sync(FULL, (f & 1u) != 0u);
+            shadow[k] = __ballot_sync(FULL, (f & 2u) != 0u);
+            if (lane_id() == 0) {
+                part[0][k * TILE_WARPS + warp] = __popc(more[k]);
+                part[1][k * TILE_WARPS + warp] = __popc(shadow[k]);
+            }
+        }
+        __syncthreads();
+        if (warp < 2) {
+            const uint32_t total = scan_parts(part[warp]);
+            uint32_t at = 0;
+            if (lane_id() == 0 && total) at = atomicAdd(w.counters + (warp ? C_SHADOW : C_QUEUE0 + (q ^ 1)), total);
+            if (lane_id() == 0) base[warp] = at;
+        }
+        __syncthreads();
+        const uint32_t below = lanemask_lt(), bit = 1u << lane_id();
+#pragma unroll
+        for (int k = 0; k < TILE_ITEMS; ++k) {
+            if (more[k] & bit) out_queue[base[0] + part[0][k * TILE_WARPS + warp] + __popc(more[k] & below)] = path[k];
+            if (shadow[k] & bit)  // the shadow list (the shade order is no longer needed)
+                w.sorted[base[1] + part[1][k * TILE_WARPS + warp] + __popc(shadow[k] & below)] = path[k];
+        }
+        __syncthreads();  // the next tile reuses part and base
     }
 }
 
@@ -417,7 +474,7 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState 
     wst.col = st.col;
     wst.stride = WF_BLOCK;
     const uint32_t n = w.counters[C_SHADOW];
-    uint32_t* fetch = w.counters + C_FETCH + 1;
+    uint32_t* fetch = w.counters + C_SHADOW_FETCH;
     Traversal tr;
     uint32_t rec = 0, job = 0;
     bool active = false, exhausted = false;
@@ -512,8 +569,9 @@ struct StageTimer {
     StageEvents* ev;
     cudaStream_t st;
     int slot = -1;
-    void begin(int kind) {
+    void begin(int kind, cudaStream_t on) {
         slot = -1;
+        st = on;
         if (!ev || ev->count >= ev->capacity) return;
         slot = ev->count++;
         ev->kind[slot] = kind;
@@ -524,15 +582,26 @@ struct StageTimer {
     }
 };
 
+// With a side stream, each bounce's shadow rays trace on it while the next
+// bounce's extension rays trace on st: neither kernel reads what the other
+// writes (extension: hits, shading keys, its own fetch and bucket counters;
+// shadow: the shadow list and records, the paths' radiance sums, its own
+// fetch counter), and each persistent kernel's tail, where its last and
+// longest rays leave most of the GPU idle, is filled by the other's blocks.
+// The scatter that follows waits for the shadow rays: it reuses the shadow
+// list, and shading rewrites the shadow records and radiance sums.
 template <uint32_t FEAT>
 int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, const PixelBuffers& px,
-                    const WavefrontTuning& tune, int num_sms, cudaStream_t st, StageEvents* events) {
+                    const WavefrontTuning& tune, int num_sms, cudaStream_t st, const SideStream* side,
+                    StageEvents* events) {
     StageTimer timer{events, st};
+    const cudaStream_t shadow_st = side ? side->stream : st;
     const SingleCtx ctx{s, P};
     const uint32_t pixels = P.width * P.height;
     const uint32_t batch = uint32_t(w.capacity / pixels) > 0 ? uint32_t(w.capacity / pixels) : 1u;
     const int grid_trav = num_sms * tune.traversal_blocks_per_sm;
     const int grid_shade = num_sms * tune.shade_blocks_per_sm;
+    const int grid_tiles = num_sms * 4;
     int launches = 0;
     for (uint32_t k0 = 0; k0 < P.samples_per_frame; k0 += batch) {
         const uint32_t nk = (P.samples_per_frame - k0) < batch ? (P.samples_per_frame - k0) : batch;
@@ -542,23 +611,30 @@ int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, co
         int q = 0;
         for (uint32_t depth = 0; depth <= P.max_bounces; ++depth) {
             cudaMemsetAsync(w.counters + C_FETCH, 0, C_ZEROED * sizeof(uint32_t), st);
-            timer.begin(0);
+            timer.begin(0, st);
             k_wf_extend<SingleCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
             timer.end();
-            k_wf_scatter<<<grid_shade, WF_BLOCK, 0, st>>>(w, q);
+            if (side && depth > 0) cudaStreamWaitEvent(st, side->join, 0);
+            k_wf_scatter<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
             // The next queue and the shadow queue start empty.
             cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
-            cudaMemsetAsync(w.counters + C_SHADOW, 0, sizeof(uint32_t), st);
-            timer.begin(1);
+            cudaMemsetAsync(w.counters + C_SHADOW, 0, 2 * sizeof(uint32_t), st);
+            timer.begin(1, st);
             k_wf_shade<FEAT, SingleCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q);
             timer.end();
-            k_wf_compact<<<grid_shade, WF_BLOCK, 0, st>>>(w, q);
-            timer.begin(2);
-            k_wf_shadow<SingleCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, tune.steps);
+            k_wf_compact<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
+            if (side) {
+                cudaEventRecord(side->fork, st);
+                cudaStreamWaitEvent(shadow_st, side->fork, 0);
+            }
+            timer.begin(2, shadow_st);
+            k_wf_shadow<SingleCtx><<<grid_trav, WF_BLOCK, 0, shadow_st>>>(ctx, w, tune.steps);
             timer.end();
+            if (side) cudaEventRecord(side->join, shadow_st);
             launches += 5;
             q ^= 1;
         }
+        if (side) cudaStreamWaitEvent(st, side->join, 0);
         k_wf_finalize<<<grid_shade, WF_BLOCK, 0, st>>>(P, w, px, nk, P.sample_offset == 0u && k0 == 0);
         ++launches;
     }
@@ -598,6 +674,7 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wfb_generate(const JobDesc* __rest
         w.counters[C_QUEUE0] = n_paths;
         w.counters[C_QUEUE1] = 0;
         w.counters[C_SHADOW] = 0;
+        w.counters[C_SHADOW_FETCH] = 0;
     }
 }
 
@@ -656,6 +733,7 @@ static int batch_frame(const JobDesc* d_jobs, const WaveSegment* d_segments, con
     const BatchCtx ctx{d_jobs};
     const int grid_trav = num_sms * tune.traversal_blocks_per_sm;
     const int grid_shade = num_sms * tune.shade_blocks_per_sm;
+    const int grid_tiles = num_sms * 4;
     int launches = 0;
     for (uint32_t v = 0; v < n_waves; ++v) {
         const WavePlan& wp = waves[v];
@@ -666,11 +744,11 @@ static int batch_frame(const JobDesc* d_jobs, const WaveSegment* d_segments, con
         for (uint32_t depth = 0; depth <= max_bounces; ++depth) {
             cudaMemsetAsync(w.counters + C_FETCH, 0, C_ZEROED * sizeof(uint32_t), st);
             k_wf_extend<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
-            k_wf_scatter<<<grid_shade, WF_BLOCK, 0, st>>>(w, q);
+            k_wf_scatter<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
             cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
-            cudaMemsetAsync(w.counters + C_SHADOW, 0, sizeof(uint32_t), st);
+            cudaMemsetAsync(w.counters + C_SHADOW, 0, 2 * sizeof(uint32_t), st);
             k_wf_shade<FEAT, BatchCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q);
-            k_wf_compact<<<grid_shade, WF_BLOCK, 0, st>>>(w, q);
+            k_wf_compact<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
             k_wf_shadow<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, tune.steps);
             launches += 5;
             q ^= 1;
@@ -696,19 +774,17 @@ int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments,
     }
 }
 
-namespace {
-}  // namespace
 
 cudaError_t upload_srgb_table_wavefront() { return upload_srgb_table_here(); }
 
 int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,
                      const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st,
-                     StageEvents* events) {
+                     const SideStream* side, StageEvents* events) {
     switch (features & 15u) {
-        case 0: return wavefront_frame<0>(s, P, w, px, tune, num_sms, st, events);
-        case F_VOLUMES: return wavefront_frame<F_VOLUMES>(s, P, w, px, tune, num_sms, st, events);
-        case F_DISPERSION: return wavefront_frame<F_DISPERSION>(s, P, w, px, tune, num_sms, st, events);
-        default: return wavefront_frame<15u>(s, P, w, px, tune, num_sms, st, events);
+        case 0: return wavefront_frame<0>(s, P, w, px, tune, num_sms, st, side, events);
+        case F_VOLUMES: return wavefront_frame<F_VOLUMES>(s, P, w, px, tune, num_sms, st, side, events);
+        case F_DISPERSION: return wavefront_frame<F_DISPERSION>(s, P, w, px, tune, num_sms, st, side, events);
+        default: return wavefront_frame<15u>(s, P, w, px, tune, num_sms, st, side, events);
     }
 }
 

@@ -118,6 +118,7 @@ struct raymond {
     std::vector<cudaEvent_t> stage_begin, stage_end;
     std::vector<int> stage_kind;
     StageEvents stage{};
+    SideStream side{};  // a wavefront frame's shadow rays trace on side.stream
 
     int fail(int code, const char* fmt, ...) {
         char buf[512];
@@ -272,6 +273,14 @@ int raymond_create(raymond_t** out, const raymond_config* cfg) {
     }
     for (cudaEvent_t& ev : h->ev) cudaEventCreate(&ev);
     cudaEventCreateWithFlags(&h->order, cudaEventDisableTiming);
+    e = cudaStreamCreateWithFlags(&h->side.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->side.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->side.join, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+        raymond_destroy(h);
+        return RAYMOND_ECUDA;
+    }
     h->stage_begin.resize(raymond_stage_events);
     h->stage_end.resize(raymond_stage_events);
     h->stage_kind.resize(raymond_stage_events);
@@ -322,6 +331,12 @@ void raymond_destroy(raymond_t* h) {
         if (h->b_group_stream[g]) cudaStreamDestroy(h->b_group_stream[g]);
     }
     if (h->order) cudaEventDestroy(h->order);
+    if (h->side.fork) cudaEventDestroy(h->side.fork);
+    if (h->side.join) cudaEventDestroy(h->side.join);
+    if (h->side.stream) {
+        cudaStreamSynchronize(h->side.stream);
+        cudaStreamDestroy(h->side.stream);
+    }
     if (h->b_staging) cudaFreeHost(h->b_staging);
     for (DevBuf* b : {&h->b_jobs, &h->b_segments, &h->b_jobpix}) b->release();
     for (cudaEvent_t ev : h->stage_begin) cudaEventDestroy(ev);
@@ -751,7 +766,7 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
     cudaEventRecord(h->ev[0], h->stream);
     h->stage.count = 0;
     if (wavefront)
-        launches += launch_wavefront(s, P, features, w, px, h->tuning, h->num_sms, h->stream, &h->stage);
+        launches += launch_wavefront(s, P, features, w, px, h->tuning, h->num_sms, h->stream, &h->side, &h->stage);
     else
         launches += launch_megakernel(s, P, features, px, h->num_sms, h->stream);
     cudaEventRecord(h->ev[1], h->stream);
