@@ -28,7 +28,13 @@ struct WavefrontState {
     uint32_t* queue[2];
     uint32_t* sorted;    // this bounce's queue ordered by shading key, for the shade kernel
     uint32_t* sort_key;  // per path: its shading key
-    float4* shadow;
+    // Shadow rays by bounce parity, so one bounce's can trace while the next
+    // bounce shades: each path's ray at its slot (3 float4: origin and
+    // reach, direction and path, light and job), and the list of paths
+    // that have one.
+    float4* shadow[2];
+    uint32_t* shadow_list[2];
+    float4* shadow_sum;  // per path: the light its unoccluded shadow rays brought
     uint32_t* counters;
     uint64_t capacity;  // paths in flight
 };
@@ -85,7 +91,7 @@ struct WavePlan {
 // stream and join it back.
 struct SideStream {
     cudaStream_t stream;
-    cudaEvent_t fork, join;
+    cudaEvent_t fork, join[2];
 };
 
 struct WavefrontTuning {

@@ -59,13 +59,12 @@ __device__ __forceinline__ uint32_t load_path(const WavefrontState& w, uint32_t 
     return r.w;
 }
 
-// Counters (u32) in w.counters: queue sizes [0], [1], shadow size [2] and
-// the shadow kernel's fetch counter [3] (both zeroed before shading), the
-// extension kernel's fetch counter [4], the shading-key bucket sizes
-// [8..23] and the scatter's bucket cursors [24..39], all of [4..39] zeroed
-// before each extension launch (while the previous bounce's shadow rays may
-// still be tracing).
-enum { C_QUEUE0 = 0, C_QUEUE1 = 1, C_SHADOW = 2, C_SHADOW_FETCH = 3, C_FETCH = 4, C_BUCKET = 8, C_CURSOR = 24 };
+// Counters (u32) in w.counters: queue sizes [0], [1], the extension
+// kernel's fetch counter [4], the shading-key bucket sizes [8..23] and the
+// scatter's bucket cursors [24..39], all of [4..39] zeroed before each
+// extension launch; per bounce parity p, the shadow list's size [40 + 2p]
+// and the shadow kernel's fetch counter [41 + 2p], zeroed before shading.
+enum { C_QUEUE0 = 0, C_QUEUE1 = 1, C_FETCH = 4, C_BUCKET = 8, C_CURSOR = 24, C_SHADOW = 40 };
 constexpr int SORT_BUCKETS = 16;
 constexpr int C_ZEROED = 4 + 2 * SORT_BUCKETS;  // words from C_FETCH on
 
@@ -126,13 +125,12 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_generate(Params P, WavefrontSta
         PathState ps;
         path_begin(P, seed_hash, pixel % P.width, pixel / P.width, k, ps);
         store_path(w, p, ps, pixel);
+        w.shadow_sum[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         w.queue[0][p] = p;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         w.counters[C_QUEUE0] = n_paths;
         w.counters[C_QUEUE1] = 0;
-        w.counters[C_SHADOW] = 0;
-        w.counters[C_SHADOW_FETCH] = 0;
     }
 }
 
@@ -395,11 +393,13 @@ __global__ void __launch_bounds__(TILE_THREADS) k_wf_scatter(WavefrontState w, i
 // ---- shade: one bounce of radiance() per live path ----
 // Shading runs in key order (the scatter's `sorted` queue) but queues
 // nothing: it records per path whether it continues (bit 0) and whether it
-// has a shadow ray (bit 1, the ray stored at the path's slot), and
-// k_wf_compact builds the next queues in the previous queue's order, which
-// keeps neighbouring paths' rays together for traversal.
+// has a shadow ray (bit 1, the ray stored at the path's slot of this bounce
+// parity's records), and k_wf_compact builds the next queues in the
+// previous queue's order, which keeps neighbouring paths' rays together for
+// traversal.
 template <uint32_t FEAT, typename Ctx>
-__global__ void __launch_bounds__(WF_BLOCK) k_wf_shade(Ctx ctx, WavefrontState w, int q) {
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_shade(Ctx ctx, WavefrontState w, int q, int par) {
+    float4* const shadow = w.shadow[par];
     const uint32_t n = w.counters[C_QUEUE0 + q];
     for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
         const uint32_t path = w.sorted[idx];
@@ -414,16 +414,16 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shade(Ctx ctx, WavefrontState w
         store_path(w, path, ps, word);
         w.sort_key[path] = (more ? 1u : 0u) | (sh.valid ? 2u : 0u);
         if (sh.valid) {
-            w.shadow[size_t(path) * 3 + 0] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.reach);
-            w.shadow[size_t(path) * 3 + 1] = make_float4(sh.d.x, sh.d.y, sh.d.z, __uint_as_float(path));
-            w.shadow[size_t(path) * 3 + 2] =
+            shadow[size_t(path) * 3 + 0] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.reach);
+            shadow[size_t(path) * 3 + 1] = make_float4(sh.d.x, sh.d.y, sh.d.z, __uint_as_float(path));
+            shadow[size_t(path) * 3 + 2] =
                 make_float4(sh.contribution.x, sh.contribution.y, sh.contribution.z, __uint_as_float(job));
         }
     }
 }
 
 // ---- compact: the next extension queue and the shadow list, in queue order ----
-__global__ void __launch_bounds__(TILE_THREADS) k_wf_compact(WavefrontState w, int q) {
+__global__ void __launch_bounds__(TILE_THREADS) k_wf_compact(WavefrontState w, int q, int par) {
     __shared__ uint32_t base[2];
     __shared__ uint32_t part[2][TILE_PARTS];  // [0]: paths that continue, [1]: paths with a shadow ray
     const uint32_t n = w.counters[C_QUEUE0 + q];
@@ -448,7 +448,8 @@ __global__ void __launch_bounds__(TILE_THREADS) k_wf_compact(WavefrontState w, i
         if (warp < 2) {
             const uint32_t total = scan_parts(part[warp]);
             uint32_t at = 0;
-            if (lane_id() == 0 && total) at = atomicAdd(w.counters + (warp ? C_SHADOW : C_QUEUE0 + (q ^ 1)), total);
+            if (lane_id() == 0 && total)
+                at = atomicAdd(w.counters + (warp ? C_SHADOW + 2 * par : C_QUEUE0 + (q ^ 1)), total);
             if (lane_id() == 0) base[warp] = at;
         }
         __syncthreads();
@@ -456,8 +457,8 @@ __global__ void __launch_bounds__(TILE_THREADS) k_wf_compact(WavefrontState w, i
 #pragma unroll
         for (int k = 0; k < TILE_ITEMS; ++k) {
             if (more[k] & bit) out_queue[base[0] + part[0][k * TILE_WARPS + warp] + __popc(more[k] & below)] = path[k];
-            if (shadow[k] & bit)  // the shadow list (the shade order is no longer needed)
-                w.sorted[base[1] + part[1][k * TILE_WARPS + warp] + __popc(shadow[k] & below)] = path[k];
+            if (shadow[k] & bit)
+                w.shadow_list[par][base[1] + part[1][k * TILE_WARPS + warp] + __popc(shadow[k] & below)] = path[k];
         }
         __syncthreads();  // the next tile reuses part and base
     }
@@ -465,7 +466,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_wf_compact(WavefrontState w, i
 
 // ---- shadow: any-hit occlusion; unoccluded rays add their light ----
 template <typename Ctx>
-__global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState w, int steps) {
+__global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState w, int steps, int par) {
     __shared__ uint32_t stack[STACK_SHARED * WF_BLOCK];
     TraversalStack<STACK_SHARED> st;
     st.col = stack + threadIdx.x;
@@ -473,8 +474,10 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState 
     WideStack<WIDE_STACK_SHARED> wst;
     wst.col = st.col;
     wst.stride = WF_BLOCK;
-    const uint32_t n = w.counters[C_SHADOW];
-    uint32_t* fetch = w.counters + C_SHADOW_FETCH;
+    const uint32_t n = w.counters[C_SHADOW + 2 * par];
+    uint32_t* fetch = w.counters + C_SHADOW + 2 * par + 1;
+    const uint32_t* list = w.shadow_list[par];
+    const float4* shadow = w.shadow[par];
     Traversal tr;
     uint32_t rec = 0, job = 0;
     bool active = false, exhausted = false;
@@ -489,16 +492,15 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState 
             if (need) {
                 const uint32_t idx = base + __popc(mask & lanemask_lt());
                 if (idx < n) {
-                    rec = w.sorted[idx];  // the shadow list holds paths; each path's ray sits at its slot
-                    const float4 a = w.shadow[size_t(rec) * 3], b = w.shadow[size_t(rec) * 3 + 1];
-                    job = __float_as_uint(w.shadow[size_t(rec) * 3 + 2].w);
+                    rec = list[idx];  // the list holds paths; each path's ray sits at its slot
+                    const float4 a = shadow[size_t(rec) * 3], b = shadow[size_t(rec) * 3 + 1];
+                    job = __float_as_uint(shadow[size_t(rec) * 3 + 2].w);
                     active = trav_begin(ctx.scene(job), tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w);
                     if (!active) {
                         // Misses the scene's box: unoccluded.
-                        const uint32_t path = __float_as_uint(b.w);
-                        const float4 c = w.shadow[size_t(rec) * 3 + 2];
-                        float4 r = w.s[3][path];
-                        w.s[3][path] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, r.w);
+                        const float4 c = shadow[size_t(rec) * 3 + 2];
+                        const float4 r = w.shadow_sum[rec];
+                        w.shadow_sum[rec] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
                     }
                 } else {
                     exhausted = true;
@@ -512,10 +514,9 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState 
                 if (!trav_step<true>(sc, tr, st, wst)) {
                     active = false;
                     if (tr.prim == NONE) {
-                        const uint32_t path = __float_as_uint(w.shadow[size_t(rec) * 3 + 1].w);
-                        const float4 c = w.shadow[size_t(rec) * 3 + 2];
-                        float4 r = w.s[3][path];
-                        w.s[3][path] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, r.w);
+                        const float4 c = shadow[size_t(rec) * 3 + 2];
+                        const float4 r = w.shadow_sum[rec];
+                        w.shadow_sum[rec] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
                     }
                 }
             }
@@ -533,8 +534,8 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_finalize(Params P, WavefrontSta
         float4 sn = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         for (uint32_t k = 0; k < batch_samples; ++k) {
             const uint32_t p = k * pixels + pixel;
-            const float4 rr = w.s[3][p];
-            float3 c = f3(rr.x, rr.y, rr.z);
+            const float4 rr = w.s[3][p], sr = w.shadow_sum[p];
+            float3 c = f3(rr.x + sr.x, rr.y + sr.y, rr.z + sr.z);
             const float peak = maxc(c);
             if (P.firefly_clamp > 0.0f && peak > P.firefly_clamp) c *= P.firefly_clamp / peak;
             const float4 ga = w.s[5][p];
@@ -583,13 +584,13 @@ struct StageTimer {
 };
 
 // With a side stream, each bounce's shadow rays trace on it while the next
-// bounce's extension rays trace on st: neither kernel reads what the other
-// writes (extension: hits, shading keys, its own fetch and bucket counters;
-// shadow: the shadow list and records, the paths' radiance sums, its own
-// fetch counter), and each persistent kernel's tail, where its last and
-// longest rays leave most of the GPU idle, is filled by the other's blocks.
-// The scatter that follows waits for the shadow rays: it reuses the shadow
-// list, and shading rewrites the shadow records and radiance sums.
+// bounce extends, sorts, shades and compacts on st: the shadow kernel reads
+// only its parity's list, records and counters and adds to the paths'
+// shadow sums, which nothing else on st touches until the frame's sums, and
+// each kernel's tail, where its last rays or paths leave most of the GPU
+// idle, is filled by the other stream's blocks. A bounce waits, before it
+// resets its parity's shadow list, for the shadow rays of two bounces back,
+// which used the same parity.
 template <uint32_t FEAT>
 int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, const PixelBuffers& px,
                     const WavefrontTuning& tune, int num_sms, cudaStream_t st, const SideStream* side,
@@ -610,31 +611,33 @@ int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, co
         ++launches;
         int q = 0;
         for (uint32_t depth = 0; depth <= P.max_bounces; ++depth) {
+            const int par = int(depth & 1u);
             cudaMemsetAsync(w.counters + C_FETCH, 0, C_ZEROED * sizeof(uint32_t), st);
             timer.begin(0, st);
             k_wf_extend<SingleCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
             timer.end();
-            if (side && depth > 0) cudaStreamWaitEvent(st, side->join, 0);
             k_wf_scatter<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
-            // The next queue and the shadow queue start empty.
+            // The next queue and this parity's shadow list start empty.
             cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
-            cudaMemsetAsync(w.counters + C_SHADOW, 0, 2 * sizeof(uint32_t), st);
+            if (side && depth >= 2) cudaStreamWaitEvent(st, side->join[par], 0);
+            cudaMemsetAsync(w.counters + C_SHADOW + 2 * par, 0, 2 * sizeof(uint32_t), st);
             timer.begin(1, st);
-            k_wf_shade<FEAT, SingleCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q);
+            k_wf_shade<FEAT, SingleCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q, par);
             timer.end();
-            k_wf_compact<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
+            k_wf_compact<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q, par);
             if (side) {
                 cudaEventRecord(side->fork, st);
                 cudaStreamWaitEvent(shadow_st, side->fork, 0);
             }
             timer.begin(2, shadow_st);
-            k_wf_shadow<SingleCtx><<<grid_trav, WF_BLOCK, 0, shadow_st>>>(ctx, w, tune.steps);
+            k_wf_shadow<SingleCtx><<<grid_trav, WF_BLOCK, 0, shadow_st>>>(ctx, w, tune.steps, par);
             timer.end();
-            if (side) cudaEventRecord(side->join, shadow_st);
+            if (side) cudaEventRecord(side->join[par], shadow_st);
             launches += 5;
             q ^= 1;
         }
-        if (side) cudaStreamWaitEvent(st, side->join, 0);
+        // The side stream runs its shadow kernels in order: the last one's end is all of theirs.
+        if (side) cudaStreamWaitEvent(st, side->join[P.max_bounces & 1u], 0);
         k_wf_finalize<<<grid_shade, WF_BLOCK, 0, st>>>(P, w, px, nk, P.sample_offset == 0u && k0 == 0);
         ++launches;
     }
@@ -668,13 +671,12 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wfb_generate(const JobDesc* __rest
         PathState ps;
         path_begin(jd.params, jd.scene.seed_hash, pixel % jd.params.width, pixel / jd.params.width, k, ps);
         store_path(w, p, ps, (g.job << 21) | pixel);
+        w.shadow_sum[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         w.queue[0][p] = p;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         w.counters[C_QUEUE0] = n_paths;
         w.counters[C_QUEUE1] = 0;
-        w.counters[C_SHADOW] = 0;
-        w.counters[C_SHADOW_FETCH] = 0;
     }
 }
 
@@ -691,8 +693,8 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wfb_finalize(const JobDesc* __rest
         float4 sn = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         for (uint32_t k = 0; k < g.nk; ++k) {
             const uint32_t p = g.path_offset + k * g.pixels + pixel;
-            const float4 rr = w.s[3][p];
-            float3 c = f3(rr.x, rr.y, rr.z);
+            const float4 rr = w.s[3][p], sr = w.shadow_sum[p];
+            float3 c = f3(rr.x + sr.x, rr.y + sr.y, rr.z + sr.z);
             const float peak = maxc(c);
             if (P.firefly_clamp > 0.0f && peak > P.firefly_clamp) c *= P.firefly_clamp / peak;
             const float4 ga = w.s[5][p];
@@ -745,11 +747,12 @@ static int batch_frame(const JobDesc* d_jobs, const WaveSegment* d_segments, con
             cudaMemsetAsync(w.counters + C_FETCH, 0, C_ZEROED * sizeof(uint32_t), st);
             k_wf_extend<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
             k_wf_scatter<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
+            const int par = int(depth & 1u);
             cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
-            cudaMemsetAsync(w.counters + C_SHADOW, 0, 2 * sizeof(uint32_t), st);
-            k_wf_shade<FEAT, BatchCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q);
-            k_wf_compact<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
-            k_wf_shadow<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, tune.steps);
+            cudaMemsetAsync(w.counters + C_SHADOW + 2 * par, 0, 2 * sizeof(uint32_t), st);
+            k_wf_shade<FEAT, BatchCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q, par);
+            k_wf_compact<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q, par);
+            k_wf_shadow<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, tune.steps, par);
             launches += 5;
             q ^= 1;
         }

@@ -71,7 +71,8 @@ struct raymond {
     DevBuf upload_scratch;  // images staged for building texture arrays and the environment on the GPU
 
     // Wavefront path state (allocated on first wavefront frame).
-    DevBuf wf_state[8], wf_hit, wf_queue[2], wf_sorted, wf_sort_key, wf_shadow, wf_counters;
+    DevBuf wf_state[8], wf_hit, wf_queue[2], wf_sorted, wf_sort_key, wf_shadow, wf_shadow_list, wf_shadow_sum,
+        wf_counters;
     uint64_t wf_capacity = 0;
     uint64_t path_capacity_limit = 0;  // from the config; 0 = default
     WavefrontTuning tuning{16, 8, 8};
@@ -201,6 +202,15 @@ void rmd::set_handleless_error(const char* msg) { g_create_error = msg; }
 
 namespace {
 
+// The shadow records and lists of both bounce parities, for a pool of cap paths.
+void set_shadow_buffers(raymond* h, uint64_t cap, WavefrontState& w) {
+    w.shadow[0] = static_cast<float4*>(h->wf_shadow.ptr);
+    w.shadow[1] = w.shadow[0] + cap * 3;
+    w.shadow_list[0] = static_cast<uint32_t*>(h->wf_shadow_list.ptr);
+    w.shadow_list[1] = w.shadow_list[0] + cap;
+    w.shadow_sum = static_cast<float4*>(h->wf_shadow_sum.ptr);
+}
+
 // Paths in flight for a frame: the whole frame if it fits the limit, else
 // whole samples of it (at least one).
 int ensure_wavefront(raymond* h, const Params& P, WavefrontState& w) {
@@ -219,7 +229,9 @@ int ensure_wavefront(raymond* h, const Params& P, WavefrontState& w) {
         if (e == cudaSuccess) e = h->wf_queue[1].reserve(cap * 4);
         if (e == cudaSuccess) e = h->wf_sorted.reserve(cap * 4);
         if (e == cudaSuccess) e = h->wf_sort_key.reserve(cap * 4);
-        if (e == cudaSuccess) e = h->wf_shadow.reserve(cap * 48);
+        if (e == cudaSuccess) e = h->wf_shadow.reserve(cap * 96);
+        if (e == cudaSuccess) e = h->wf_shadow_list.reserve(cap * 8);
+        if (e == cudaSuccess) e = h->wf_shadow_sum.reserve(cap * 16);
         if (e == cudaSuccess) e = h->wf_counters.reserve(256);
         if (e != cudaSuccess) return h->cuda_fail(e, "wavefront state");
         h->wf_capacity = cap;
@@ -230,7 +242,7 @@ int ensure_wavefront(raymond* h, const Params& P, WavefrontState& w) {
     w.queue[1] = static_cast<uint32_t*>(h->wf_queue[1].ptr);
     w.sorted = static_cast<uint32_t*>(h->wf_sorted.ptr);
     w.sort_key = static_cast<uint32_t*>(h->wf_sort_key.ptr);
-    w.shadow = static_cast<float4*>(h->wf_shadow.ptr);
+    set_shadow_buffers(h, cap, w);
     w.counters = static_cast<uint32_t*>(h->wf_counters.ptr);
     w.capacity = cap;
     return RAYMOND_OK;
@@ -275,7 +287,8 @@ int raymond_create(raymond_t** out, const raymond_config* cfg) {
     cudaEventCreateWithFlags(&h->order, cudaEventDisableTiming);
     e = cudaStreamCreateWithFlags(&h->side.stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->side.fork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->side.join, cudaEventDisableTiming);
+    for (cudaEvent_t& ev : h->side.join)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
         raymond_destroy(h);
@@ -317,7 +330,7 @@ void raymond_destroy(raymond_t* h) {
                       &h->normal_maps, &h->env_map, &h->env_table, &h->accum, &h->guide_albedo, &h->guide_normal,
                       &h->light_a, &h->light_b, &h->guide_unit, &h->denoised, &h->splats, &h->display, &h->ray_scratch,
                       &h->prim_scratch, &h->t_scratch, &h->counter, &h->upload_scratch, &h->wf_hit, &h->wf_queue[0], &h->wf_queue[1],
-                      &h->wf_sorted, &h->wf_sort_key, &h->wf_shadow, &h->wf_counters, &h->photon_heads,
+                      &h->wf_sorted, &h->wf_sort_key, &h->wf_shadow, &h->wf_shadow_list, &h->wf_shadow_sum, &h->wf_counters, &h->photon_heads,
                       &h->photons, &h->wide})
         b->release();
     for (DevBuf& b : h->wf_state) b.release();
@@ -332,7 +345,8 @@ void raymond_destroy(raymond_t* h) {
     }
     if (h->order) cudaEventDestroy(h->order);
     if (h->side.fork) cudaEventDestroy(h->side.fork);
-    if (h->side.join) cudaEventDestroy(h->side.join);
+    for (cudaEvent_t ev : h->side.join)
+        if (ev) cudaEventDestroy(ev);
     if (h->side.stream) {
         cudaStreamSynchronize(h->side.stream);
         cudaStreamDestroy(h->side.stream);
@@ -914,7 +928,9 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
             if (e == cudaSuccess) e = h->wf_queue[1].reserve(pool * 4);
             if (e == cudaSuccess) e = h->wf_sorted.reserve(pool * 4);
             if (e == cudaSuccess) e = h->wf_sort_key.reserve(pool * 4);
-            if (e == cudaSuccess) e = h->wf_shadow.reserve(pool * 48);
+            if (e == cudaSuccess) e = h->wf_shadow.reserve(pool * 96);
+            if (e == cudaSuccess) e = h->wf_shadow_list.reserve(pool * 8);
+            if (e == cudaSuccess) e = h->wf_shadow_sum.reserve(pool * 16);
             if (e == cudaSuccess) e = h->wf_counters.reserve(256 * raymond::kBatchGroups);
             if (e != cudaSuccess) return h->cuda_fail(e, "batch path pool");
             h->wf_capacity = pool;
@@ -969,7 +985,7 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
     w.queue[1] = static_cast<uint32_t*>(h->wf_queue[1].ptr);
     w.sorted = static_cast<uint32_t*>(h->wf_sorted.ptr);
     w.sort_key = static_cast<uint32_t*>(h->wf_sort_key.ptr);
-    w.shadow = static_cast<float4*>(h->wf_shadow.ptr);
+    set_shadow_buffers(h, h->wf_capacity, w);
     w.counters = static_cast<uint32_t*>(h->wf_counters.ptr);
     w.capacity = h->wf_capacity;
     const JobDesc* d_jobs = static_cast<const JobDesc*>(h->b_jobs.ptr);
@@ -989,7 +1005,11 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
             wg.queue[1] += base;
             wg.sorted += base;
             wg.sort_key += base;
-            wg.shadow += base * 3;
+            wg.shadow[0] += base * 3;
+            wg.shadow[1] += base * 3;
+            wg.shadow_list[0] += base;
+            wg.shadow_list[1] += base;
+            wg.shadow_sum += base;
             wg.counters += 64 * g;
             wg.capacity = h->b_group_cap;
             cudaStream_t sg = h->b_group_stream[g];
