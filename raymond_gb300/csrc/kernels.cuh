@@ -87,12 +87,42 @@ struct WavePlan {
 };
 
 // Launch shape of the wavefront kernels (chosen by the tuner).
-// A second stream and the two events that fork work onto it from a frame's
-// stream and join it back.
+// A second stream and the events that fork work onto it from a frame's
+// stream and join it back (one join per bounce parity).
 struct SideStream {
     cudaStream_t stream;
     cudaEvent_t fork, join[2];
 };
+
+// The streams a wavefront frame runs on beside its own: its paths split
+// into up to kGroups groups of whole samples, each group's bounces on its
+// own stream and its shadow rays on that group's side stream.
+struct FrameStreams {
+    static constexpr int kGroups = 2;
+    cudaStream_t group[kGroups];
+    SideStream side[kGroups];
+    cudaEvent_t fork, join[kGroups];
+};
+
+// Paths [base, base + capacity) of a pool as a pool of their own, numbered
+// from 0, with the counters of group g (64 words a group).
+inline WavefrontState pool_slice(const WavefrontState& w, uint64_t base, uint32_t g, uint64_t capacity) {
+    WavefrontState s = w;
+    for (int k = 0; k < 8; ++k) s.s[k] += base;
+    s.hit += base;
+    s.queue[0] += base;
+    s.queue[1] += base;
+    s.sorted += base;
+    s.sort_key += base;
+    s.shadow[0] += base * 3;
+    s.shadow[1] += base * 3;
+    s.shadow_list[0] += base;
+    s.shadow_list[1] += base;
+    s.shadow_sum += base;
+    s.counters += 64 * g;
+    s.capacity = capacity;
+    return s;
+}
 
 struct WavefrontTuning {
     int steps;                    // traversal steps between lane refills
@@ -110,7 +140,7 @@ int launch_megakernel(const Scene& s, const Params& P, uint32_t features, const 
                       cudaStream_t st);
 int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,
                      const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st,
-                     const SideStream* side, StageEvents* events);
+                     const FrameStreams* streams, StageEvents* events);
 int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments, const WavePlan* waves,
                            uint32_t n_waves, uint32_t max_bounces, uint32_t features, const WavefrontState& w,
                            const WavefrontTuning& tune, int num_sms, cudaStream_t st);

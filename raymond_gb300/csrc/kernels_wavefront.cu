@@ -583,61 +583,92 @@ struct StageTimer {
     }
 };
 
-// With a side stream, each bounce's shadow rays trace on it while the next
-// bounce extends, sorts, shades and compacts on st: the shadow kernel reads
-// only its parity's list, records and counters and adds to the paths'
-// shadow sums, which nothing else on st touches until the frame's sums, and
-// each kernel's tail, where its last rays or paths leave most of the GPU
-// idle, is filled by the other stream's blocks. A bounce waits, before it
-// resets its parity's shadow list, for the shadow rays of two bounces back,
-// which used the same parity.
+// One group's paths through every bounce, on stream st. With a side
+// stream, each bounce's shadow rays trace on it while the next bounce
+// extends, sorts, shades and compacts on st: the shadow kernel reads only
+// its parity's list, records and counters and adds to the paths' shadow
+// sums, which nothing else on st touches until the frame's sums, and each
+// kernel's tail, where its last rays or paths leave most of the GPU idle,
+// is filled by the other stream's blocks. A bounce waits, before it resets
+// its parity's shadow list, for the shadow rays of two bounces back, which
+// used the same parity. Returns with st waiting for the last shadow rays.
 template <uint32_t FEAT>
-int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, const PixelBuffers& px,
+int wavefront_group(const SingleCtx& ctx, const WavefrontState& w, uint32_t first_sample, uint32_t n,
                     const WavefrontTuning& tune, int num_sms, cudaStream_t st, const SideStream* side,
-                    StageEvents* events) {
-    StageTimer timer{events, st};
+                    StageTimer& timer) {
+    const Params& P = ctx.P;
     const cudaStream_t shadow_st = side ? side->stream : st;
-    const SingleCtx ctx{s, P};
-    const uint32_t pixels = P.width * P.height;
-    const uint32_t batch = uint32_t(w.capacity / pixels) > 0 ? uint32_t(w.capacity / pixels) : 1u;
     const int grid_trav = num_sms * tune.traversal_blocks_per_sm;
     const int grid_shade = num_sms * tune.shade_blocks_per_sm;
     const int grid_tiles = num_sms * 4;
+    k_wf_generate<FEAT><<<grid_shade, WF_BLOCK, 0, st>>>(P, w, ctx.s.seed_hash, first_sample, n);
+    int launches = 1;
+    int q = 0;
+    for (uint32_t depth = 0; depth <= P.max_bounces; ++depth) {
+        const int par = int(depth & 1u);
+        cudaMemsetAsync(w.counters + C_FETCH, 0, C_ZEROED * sizeof(uint32_t), st);
+        timer.begin(0, st);
+        k_wf_extend<SingleCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
+        timer.end();
+        k_wf_scatter<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
+        // The next queue and this parity's shadow list start empty.
+        cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
+        if (side && depth >= 2) cudaStreamWaitEvent(st, side->join[par], 0);
+        cudaMemsetAsync(w.counters + C_SHADOW + 2 * par, 0, 2 * sizeof(uint32_t), st);
+        timer.begin(1, st);
+        k_wf_shade<FEAT, SingleCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q, par);
+        timer.end();
+        k_wf_compact<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q, par);
+        if (side) {
+            cudaEventRecord(side->fork, st);
+            cudaStreamWaitEvent(shadow_st, side->fork, 0);
+        }
+        timer.begin(2, shadow_st);
+        k_wf_shadow<SingleCtx><<<grid_trav, WF_BLOCK, 0, shadow_st>>>(ctx, w, tune.steps, par);
+        timer.end();
+        if (side) cudaEventRecord(side->join[par], shadow_st);
+        launches += 5;
+        q ^= 1;
+    }
+    // The side stream runs its shadow kernels in order: the last one's end is all of theirs.
+    if (side) cudaStreamWaitEvent(st, side->join[P.max_bounces & 1u], 0);
+    return launches;
+}
+
+// A frame: its samples a pool's worth at a time; each pool's paths, with
+// streams, as up to FrameStreams::kGroups groups of whole samples, each on
+// its own stream, so one group's extension fills the GPU beside another's
+// shading. Paths do not depend on one another, so the groups change
+// nothing but the order the GPU runs them in.
+template <uint32_t FEAT>
+int wavefront_frame(const Scene& s, const Params& P, const WavefrontState& w, const PixelBuffers& px,
+                    const WavefrontTuning& tune, int num_sms, cudaStream_t st, const FrameStreams* fs,
+                    StageEvents* events) {
+    StageTimer timer{events, st};
+    const SingleCtx ctx{s, P};
+    const uint32_t pixels = P.width * P.height;
+    const uint32_t batch = uint32_t(w.capacity / pixels) > 0 ? uint32_t(w.capacity / pixels) : 1u;
+    const int grid_shade = num_sms * tune.shade_blocks_per_sm;
     int launches = 0;
     for (uint32_t k0 = 0; k0 < P.samples_per_frame; k0 += batch) {
         const uint32_t nk = (P.samples_per_frame - k0) < batch ? (P.samples_per_frame - k0) : batch;
-        const uint32_t n = nk * pixels;
-        k_wf_generate<FEAT><<<grid_shade, WF_BLOCK, 0, st>>>(P, w, s.seed_hash, k0, n);
-        ++launches;
-        int q = 0;
-        for (uint32_t depth = 0; depth <= P.max_bounces; ++depth) {
-            const int par = int(depth & 1u);
-            cudaMemsetAsync(w.counters + C_FETCH, 0, C_ZEROED * sizeof(uint32_t), st);
-            timer.begin(0, st);
-            k_wf_extend<SingleCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
-            timer.end();
-            k_wf_scatter<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
-            // The next queue and this parity's shadow list start empty.
-            cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
-            if (side && depth >= 2) cudaStreamWaitEvent(st, side->join[par], 0);
-            cudaMemsetAsync(w.counters + C_SHADOW + 2 * par, 0, 2 * sizeof(uint32_t), st);
-            timer.begin(1, st);
-            k_wf_shade<FEAT, SingleCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q, par);
-            timer.end();
-            k_wf_compact<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q, par);
-            if (side) {
-                cudaEventRecord(side->fork, st);
-                cudaStreamWaitEvent(shadow_st, side->fork, 0);
+        const uint32_t groups = fs ? (nk < uint32_t(FrameStreams::kGroups) ? nk : uint32_t(FrameStreams::kGroups)) : 1u;
+        if (groups == 1) {
+            launches += wavefront_group<FEAT>(ctx, w, k0, nk * pixels, tune, num_sms, st, fs ? &fs->side[0] : nullptr,
+                                              timer);
+        } else {
+            cudaEventRecord(fs->fork, st);
+            for (uint32_t g = 0; g < groups; ++g) {
+                const uint32_t first = g * nk / groups, end = (g + 1) * nk / groups;
+                const WavefrontState wg =
+                    pool_slice(w, uint64_t(first) * pixels, g, uint64_t(end - first) * pixels);
+                cudaStreamWaitEvent(fs->group[g], fs->fork, 0);
+                launches += wavefront_group<FEAT>(ctx, wg, k0 + first, (end - first) * pixels, tune, num_sms,
+                                                  fs->group[g], &fs->side[g], timer);
+                cudaEventRecord(fs->join[g], fs->group[g]);
+                cudaStreamWaitEvent(st, fs->join[g], 0);
             }
-            timer.begin(2, shadow_st);
-            k_wf_shadow<SingleCtx><<<grid_trav, WF_BLOCK, 0, shadow_st>>>(ctx, w, tune.steps, par);
-            timer.end();
-            if (side) cudaEventRecord(side->join[par], shadow_st);
-            launches += 5;
-            q ^= 1;
         }
-        // The side stream runs its shadow kernels in order: the last one's end is all of theirs.
-        if (side) cudaStreamWaitEvent(st, side->join[P.max_bounces & 1u], 0);
         k_wf_finalize<<<grid_shade, WF_BLOCK, 0, st>>>(P, w, px, nk, P.sample_offset == 0u && k0 == 0);
         ++launches;
     }
@@ -782,12 +813,12 @@ cudaError_t upload_srgb_table_wavefront() { return upload_srgb_table_here(); }
 
 int launch_wavefront(const Scene& s, const Params& P, uint32_t features, const WavefrontState& w,
                      const PixelBuffers& px, const WavefrontTuning& tune, int num_sms, cudaStream_t st,
-                     const SideStream* side, StageEvents* events) {
+                     const FrameStreams* streams, StageEvents* events) {
     switch (features & 15u) {
-        case 0: return wavefront_frame<0>(s, P, w, px, tune, num_sms, st, side, events);
-        case F_VOLUMES: return wavefront_frame<F_VOLUMES>(s, P, w, px, tune, num_sms, st, side, events);
-        case F_DISPERSION: return wavefront_frame<F_DISPERSION>(s, P, w, px, tune, num_sms, st, side, events);
-        default: return wavefront_frame<15u>(s, P, w, px, tune, num_sms, st, side, events);
+        case 0: return wavefront_frame<0>(s, P, w, px, tune, num_sms, st, streams, events);
+        case F_VOLUMES: return wavefront_frame<F_VOLUMES>(s, P, w, px, tune, num_sms, st, streams, events);
+        case F_DISPERSION: return wavefront_frame<F_DISPERSION>(s, P, w, px, tune, num_sms, st, streams, events);
+        default: return wavefront_frame<15u>(s, P, w, px, tune, num_sms, st, streams, events);
     }
 }
 

@@ -119,7 +119,7 @@ struct raymond {
     std::vector<cudaEvent_t> stage_begin, stage_end;
     std::vector<int> stage_kind;
     StageEvents stage{};
-    SideStream side{};  // a wavefront frame's shadow rays trace on side.stream
+    FrameStreams frame{};  // a wavefront frame's groups and their shadow rays
 
     int fail(int code, const char* fmt, ...) {
         char buf[512];
@@ -232,7 +232,7 @@ int ensure_wavefront(raymond* h, const Params& P, WavefrontState& w) {
         if (e == cudaSuccess) e = h->wf_shadow.reserve(cap * 96);
         if (e == cudaSuccess) e = h->wf_shadow_list.reserve(cap * 8);
         if (e == cudaSuccess) e = h->wf_shadow_sum.reserve(cap * 16);
-        if (e == cudaSuccess) e = h->wf_counters.reserve(256);
+        if (e == cudaSuccess) e = h->wf_counters.reserve(256 * FrameStreams::kGroups);
         if (e != cudaSuccess) return h->cuda_fail(e, "wavefront state");
         h->wf_capacity = cap;
     }
@@ -285,10 +285,16 @@ int raymond_create(raymond_t** out, const raymond_config* cfg) {
     }
     for (cudaEvent_t& ev : h->ev) cudaEventCreate(&ev);
     cudaEventCreateWithFlags(&h->order, cudaEventDisableTiming);
-    e = cudaStreamCreateWithFlags(&h->side.stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->side.fork, cudaEventDisableTiming);
-    for (cudaEvent_t& ev : h->side.join)
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    e = cudaEventCreateWithFlags(&h->frame.fork, cudaEventDisableTiming);
+    for (int g = 0; g < FrameStreams::kGroups; ++g) {
+        SideStream& sd = h->frame.side[g];
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->frame.group[g], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->frame.join[g], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sd.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sd.fork, cudaEventDisableTiming);
+        for (cudaEvent_t& ev : sd.join)
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) {
         g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
         raymond_destroy(h);
@@ -344,12 +350,15 @@ void raymond_destroy(raymond_t* h) {
         if (h->b_group_stream[g]) cudaStreamDestroy(h->b_group_stream[g]);
     }
     if (h->order) cudaEventDestroy(h->order);
-    if (h->side.fork) cudaEventDestroy(h->side.fork);
-    for (cudaEvent_t ev : h->side.join)
-        if (ev) cudaEventDestroy(ev);
-    if (h->side.stream) {
-        cudaStreamSynchronize(h->side.stream);
-        cudaStreamDestroy(h->side.stream);
+    if (h->frame.fork) cudaEventDestroy(h->frame.fork);
+    for (int g = 0; g < FrameStreams::kGroups; ++g) {
+        const SideStream& sd = h->frame.side[g];
+        if (h->frame.join[g]) cudaEventDestroy(h->frame.join[g]);
+        if (h->frame.group[g]) cudaStreamDestroy(h->frame.group[g]);
+        if (sd.fork) cudaEventDestroy(sd.fork);
+        for (cudaEvent_t ev : sd.join)
+            if (ev) cudaEventDestroy(ev);
+        if (sd.stream) cudaStreamDestroy(sd.stream);
     }
     if (h->b_staging) cudaFreeHost(h->b_staging);
     for (DevBuf* b : {&h->b_jobs, &h->b_segments, &h->b_jobpix}) b->release();
@@ -780,7 +789,7 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
     cudaEventRecord(h->ev[0], h->stream);
     h->stage.count = 0;
     if (wavefront)
-        launches += launch_wavefront(s, P, features, w, px, h->tuning, h->num_sms, h->stream, &h->side, &h->stage);
+        launches += launch_wavefront(s, P, features, w, px, h->tuning, h->num_sms, h->stream, &h->frame, &h->stage);
     else
         launches += launch_megakernel(s, P, features, px, h->num_sms, h->stream);
     cudaEventRecord(h->ev[1], h->stream);
@@ -997,21 +1006,7 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
         cudaEventRecord(h->b_fork, h->stream);
         for (uint32_t g = 0; g < groups; ++g) {
             // The group's slice of the pool, with its own counters.
-            const uint64_t base = h->b_group_cap * g;
-            WavefrontState wg = w;
-            for (int k = 0; k < 8; ++k) wg.s[k] += base;
-            wg.hit += base;
-            wg.queue[0] += base;
-            wg.queue[1] += base;
-            wg.sorted += base;
-            wg.sort_key += base;
-            wg.shadow[0] += base * 3;
-            wg.shadow[1] += base * 3;
-            wg.shadow_list[0] += base;
-            wg.shadow_list[1] += base;
-            wg.shadow_sum += base;
-            wg.counters += 64 * g;
-            wg.capacity = h->b_group_cap;
+            const WavefrontState wg = pool_slice(w, h->b_group_cap * g, g, h->b_group_cap);
             cudaStream_t sg = h->b_group_stream[g];
             cudaStreamWaitEvent(sg, h->b_fork, 0);
             launches += launch_wavefront_batch(d_jobs, d_segs, h->b_waves.data() + h->b_group_first[g],
