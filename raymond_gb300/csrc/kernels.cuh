@@ -160,6 +160,7 @@ int launch_environment(const float* rgb, uint32_t W, uint32_t H, uint32_t cw, ui
                        uint16_t* halves, float* table, double* rows, int num_sms, cudaStream_t st);
 int launch_denoise(const Params& P, const PixelBuffers& px, unsigned* status, cudaStream_t st);
 int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st);
+int launch_average(const float4* sums, float4* out, uint32_t n, float samples, int num_sms, cudaStream_t st);
 // Fill each kernel unit's sRGB decode table on the current device.
 cudaError_t upload_srgb_table_trace();
 cudaError_t upload_srgb_table_wavefront();

@@ -425,6 +425,24 @@ int launch_tonemap(const Params& P, const PixelBuffers& px, cudaStream_t st) {
     return 1;
 }
 
+namespace {
+// readPixels' average: each sum divided by the sample count, correctly
+// rounded (IEEE division, as the host's), before the image leaves the GPU.
+__global__ void k_average(const float4* __restrict__ sums, float4* __restrict__ out, uint32_t n, float samples) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 s = sums[i];
+        out[i] = make_float4(__fdiv_rn(s.x, samples), __fdiv_rn(s.y, samples), __fdiv_rn(s.z, samples),
+                             __fdiv_rn(s.w, samples));
+    }
+}
+}  // namespace
+
+int launch_average(const float4* sums, float4* out, uint32_t n, float samples, int num_sms, cudaStream_t st) {
+    const uint32_t blocks = std::min<uint32_t>((n + 255u) / 256u, uint32_t(num_sms) * 8u);
+    k_average<<<blocks ? blocks : 1u, 256, 0, st>>>(sums, out, n, samples);
+    return 1;
+}
+
 
 // ---- batched frames: the same passes over many jobs' images in one launch ----
 namespace {

@@ -1085,15 +1085,19 @@ int raymond_read_pixels(raymond_t* h, float* out_rgba, uint64_t bytes, int denoi
     const uint64_t need = uint64_t(h->width) * h->height * 16;
     if (!out_rgba || bytes < need) return h->fail(RAYMOND_EINVAL, "The output needs %llu bytes.", (unsigned long long)need);
     cudaSetDevice(h->device);
-    cudaError_t e = cudaMemcpyAsync(out_rgba, denoised ? h->denoised.ptr : h->accum.ptr, need, cudaMemcpyDeviceToHost,
-                                    h->stream);
+    const void* from = h->denoised.ptr;
+    cudaError_t e = cudaSuccess;
+    if (!denoised) {
+        // The average, divided on the GPU into scratch.
+        e = h->prim_scratch.reserve(need);
+        if (e != cudaSuccess) return h->cuda_fail(e, "read pixels");
+        launch_average(static_cast<const float4*>(h->accum.ptr), static_cast<float4*>(h->prim_scratch.ptr),
+                       uint32_t(need / 16), float(samples), h->num_sms, h->stream);
+        from = h->prim_scratch.ptr;
+    }
+    e = cudaMemcpyAsync(out_rgba, from, need, cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return h->cuda_fail(e, "read pixels");
-    if (!denoised) {
-        const float inv = float(samples);
-        const size_t n = size_t(need / 4);
-        for (size_t i = 0; i < n; ++i) out_rgba[i] /= inv;
-    }
     return RAYMOND_OK;
 }
 
