@@ -142,9 +142,20 @@ struct Traversal {
     uint32_t first, count, sp;
 };
 
+// Which tree a traversal kernel walks: fixed when a single frame launches it
+// (the kernel then holds one traversal loop and its registers), or looked up
+// per ray when a batch's jobs may differ.
+enum { TREE_ANY = 0, TREE_BINARY = 2, TREE_WIDE = 4 };
+
+template <int TREE>
+__device__ __forceinline__ bool walks_wide(const Scene& s) {
+    return TREE == TREE_WIDE || (TREE == TREE_ANY && s.wide != nullptr);
+}
+
 // Starts a ray; returns false if it misses the root box (then it is done).
 // Over the wide tree, `first` holds the reference being visited (the root
 // node first; its children's boxes are tested in the first step).
+template <int TREE>
 __device__ __forceinline__ bool trav_begin(const Scene& s, Traversal& tr, float3 o, float3 d, float t_max) {
     tr.o = o;
     tr.d = d;
@@ -153,7 +164,7 @@ __device__ __forceinline__ bool trav_begin(const Scene& s, Traversal& tr, float3
     tr.u = tr.v = 0.0f;
     tr.prim = NONE;
     tr.sp = 0;
-    if (s.wide) {
+    if (walks_wide<TREE>(s)) {
         tr.first = 0;
         tr.count = 0;
         return true;
@@ -211,10 +222,10 @@ __device__ __forceinline__ bool trav_step_wide(const Scene& s, Traversal& tr, Wi
 }
 
 // One node visit; returns false when the ray is finished.
-template <bool ANY_HIT>
+template <bool ANY_HIT, int TREE>
 __device__ __forceinline__ bool trav_step(const Scene& s, Traversal& tr, TraversalStack<STACK_SHARED>& st,
                                           WideStack<WIDE_STACK_SHARED>& wst) {
-    if (s.wide) return trav_step_wide<ANY_HIT>(s, tr, wst);
+    if (walks_wide<TREE>(s)) return trav_step_wide<ANY_HIT>(s, tr, wst);
     bool have = false;
     if (tr.count > 0) {
         for (uint32_t i = tr.first; i < tr.first + tr.count; ++i) {
@@ -256,7 +267,7 @@ __device__ __forceinline__ bool trav_step(const Scene& s, Traversal& tr, Travers
 }
 
 // ---- extend: closest hits for every path in the queue ----
-template <typename Ctx>
+template <typename Ctx, int TREE>
 __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Ctx ctx, WavefrontState w, int q, int steps) {
     __shared__ uint32_t stack[STACK_SHARED * WF_BLOCK];
     TraversalStack<STACK_SHARED> st;
@@ -291,7 +302,7 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Ctx ctx, WavefrontState 
                     path = queue[idx];
                     job = ctx.job_of_path(w, path);
                     const float4 a = w.s[0][path], b = w.s[1][path];
-                    active = trav_begin(ctx.scene(job), tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), INF);
+                    active = trav_begin<TREE>(ctx.scene(job), tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), INF);
                     if (!active) w.hit[path] = make_float4(INF, __uint_as_float(NONE), 0.0f, 0.0f);
                     missed = !active;
                 } else {
@@ -302,15 +313,17 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_extend(Ctx ctx, WavefrontState 
         bucket_count(w, missed, path, 0u);  // rays that miss the scene's box: key 0
         missed = false;
         if (!__any_sync(FULL, active || !exhausted)) return;
-        if (active) {
-            const Scene& sc = ctx.scene(job);
-            for (int k = 0; k < steps && active; ++k) {
-                if (!trav_step<false>(sc, tr, st, wst)) {
-                    w.hit[path] = make_float4(tr.t, __uint_as_float(tr.prim), tr.u, tr.v);
-                    active = false;
-                    finished = true;
-                }
+        // A round of `steps` node visits, cut short once no lane holds a ray.
+        // (Refilling as soon as 5, 13 or 21 of the 32 lanes had finished
+        // was slower: the refills' loads cost more than the idle lanes.)
+        const Scene& sc = ctx.scene(job);
+        for (int k = 0; k < steps; ++k) {
+            if (active && !trav_step<false, TREE>(sc, tr, st, wst)) {
+                w.hit[path] = make_float4(tr.t, __uint_as_float(tr.prim), tr.u, tr.v);
+                active = false;
+                finished = true;
             }
+            if (!__any_sync(FULL, active)) break;
         }
     }
 }
@@ -465,7 +478,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_wf_compact(WavefrontState w, i
 }
 
 // ---- shadow: any-hit occlusion; unoccluded rays add their light ----
-template <typename Ctx>
+template <typename Ctx, int TREE>
 __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState w, int steps, int par) {
     __shared__ uint32_t stack[STACK_SHARED * WF_BLOCK];
     TraversalStack<STACK_SHARED> st;
@@ -495,7 +508,7 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState 
                     rec = list[idx];  // the list holds paths; each path's ray sits at its slot
                     const float4 a = shadow[size_t(rec) * 3], b = shadow[size_t(rec) * 3 + 1];
                     job = __float_as_uint(shadow[size_t(rec) * 3 + 2].w);
-                    active = trav_begin(ctx.scene(job), tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w);
+                    active = trav_begin<TREE>(ctx.scene(job), tr, f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w);
                     if (!active) {
                         // Misses the scene's box: unoccluded.
                         const float4 c = shadow[size_t(rec) * 3 + 2];
@@ -508,18 +521,17 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shadow(Ctx ctx, WavefrontState 
             }
         }
         if (!__any_sync(FULL, active || !exhausted)) return;
-        if (active) {
-            const Scene& sc = ctx.scene(job);
-            for (int k = 0; k < steps && active; ++k) {
-                if (!trav_step<true>(sc, tr, st, wst)) {
-                    active = false;
-                    if (tr.prim == NONE) {
-                        const float4 c = shadow[size_t(rec) * 3 + 2];
-                        const float4 r = w.shadow_sum[rec];
-                        w.shadow_sum[rec] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
-                    }
+        const Scene& sc = ctx.scene(job);
+        for (int k = 0; k < steps; ++k) {
+            if (active && !trav_step<true, TREE>(sc, tr, st, wst)) {
+                active = false;
+                if (tr.prim == NONE) {
+                    const float4 c = shadow[size_t(rec) * 3 + 2];
+                    const float4 r = w.shadow_sum[rec];
+                    w.shadow_sum[rec] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
                 }
             }
+            if (!__any_sync(FULL, active)) break;
         }
     }
 }
@@ -598,6 +610,7 @@ int wavefront_group(const SingleCtx& ctx, const WavefrontState& w, uint32_t firs
                     StageTimer& timer) {
     const Params& P = ctx.P;
     const cudaStream_t shadow_st = side ? side->stream : st;
+    const bool wide = ctx.s.wide != nullptr;
     const int grid_trav = num_sms * tune.traversal_blocks_per_sm;
     const int grid_shade = num_sms * tune.shade_blocks_per_sm;
     const int grid_tiles = num_sms * 4;
@@ -608,7 +621,10 @@ int wavefront_group(const SingleCtx& ctx, const WavefrontState& w, uint32_t firs
         const int par = int(depth & 1u);
         cudaMemsetAsync(w.counters + C_FETCH, 0, C_ZEROED * sizeof(uint32_t), st);
         timer.begin(0, st);
-        k_wf_extend<SingleCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
+        if (wide)
+            k_wf_extend<SingleCtx, TREE_WIDE><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
+        else
+            k_wf_extend<SingleCtx, TREE_BINARY><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
         timer.end();
         k_wf_scatter<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
         // The next queue and this parity's shadow list start empty.
@@ -624,7 +640,10 @@ int wavefront_group(const SingleCtx& ctx, const WavefrontState& w, uint32_t firs
             cudaStreamWaitEvent(shadow_st, side->fork, 0);
         }
         timer.begin(2, shadow_st);
-        k_wf_shadow<SingleCtx><<<grid_trav, WF_BLOCK, 0, shadow_st>>>(ctx, w, tune.steps, par);
+        if (wide)
+            k_wf_shadow<SingleCtx, TREE_WIDE><<<grid_trav, WF_BLOCK, 0, shadow_st>>>(ctx, w, tune.steps, par);
+        else
+            k_wf_shadow<SingleCtx, TREE_BINARY><<<grid_trav, WF_BLOCK, 0, shadow_st>>>(ctx, w, tune.steps, par);
         timer.end();
         if (side) cudaEventRecord(side->join[par], shadow_st);
         launches += 5;
@@ -776,14 +795,14 @@ static int batch_frame(const JobDesc* d_jobs, const WaveSegment* d_segments, con
         int q = 0;
         for (uint32_t depth = 0; depth <= max_bounces; ++depth) {
             cudaMemsetAsync(w.counters + C_FETCH, 0, C_ZEROED * sizeof(uint32_t), st);
-            k_wf_extend<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
+            k_wf_extend<BatchCtx, TREE_ANY><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, q, tune.steps);
             k_wf_scatter<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q);
             const int par = int(depth & 1u);
             cudaMemsetAsync(w.counters + C_QUEUE0 + (q ^ 1), 0, sizeof(uint32_t), st);
             cudaMemsetAsync(w.counters + C_SHADOW + 2 * par, 0, 2 * sizeof(uint32_t), st);
             k_wf_shade<FEAT, BatchCtx><<<grid_shade, WF_BLOCK, 0, st>>>(ctx, w, q, par);
             k_wf_compact<<<grid_tiles, TILE_THREADS, 0, st>>>(w, q, par);
-            k_wf_shadow<BatchCtx><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, tune.steps, par);
+            k_wf_shadow<BatchCtx, TREE_ANY><<<grid_trav, WF_BLOCK, 0, st>>>(ctx, w, tune.steps, par);
             launches += 5;
             q ^= 1;
         }
