@@ -34,6 +34,21 @@ __device__ __forceinline__ void store_path(const WavefrontState& w, uint32_t p, 
     w.s[6][p] = ps.g_normal;
     reinterpret_cast<uint4*>(w.s[7])[p] = make_uint4(ps.rng.state, ps.rng.seed, ps.rng.index, pixel);
 }
+// A bounce's shading reads all but the normal guide (s[6]: only written,
+// once, when the path takes its guides) and writes back s[0..5], plus s[6]
+// in the bounce that sets the guides: the sample stream's key, index and
+// pixel (s[7]) never change after generation, and a camera path's stream
+// is Sobol, so its PCG state stays as generated.
+__device__ __forceinline__ void store_bounce(const WavefrontState& w, uint32_t p, const PathState& ps,
+                                             bool guides_set) {
+    w.s[0][p] = make_float4(ps.o.x, ps.o.y, ps.o.z, ps.last_pdf);
+    w.s[1][p] = make_float4(ps.d.x, ps.d.y, ps.d.z, ps.travelled);
+    w.s[2][p] = make_float4(ps.throughput.x, ps.throughput.y, ps.throughput.z, ps.wavelength);
+    w.s[3][p] = make_float4(ps.result.x, ps.result.y, ps.result.z, ps.spectrum_u);
+    w.s[4][p] = make_float4(ps.last_p.x, ps.last_p.y, ps.last_p.z, __uint_as_float((ps.depth << 16) | ps.flags));
+    w.s[5][p] = make_float4(ps.g_albedo.x, ps.g_albedo.y, ps.g_albedo.z, __uint_as_float(ps.rng.dim));
+    if (guides_set) w.s[6][p] = ps.g_normal;
+}
 __device__ __forceinline__ uint32_t load_path(const WavefrontState& w, uint32_t p, PathState& ps) {
     const float4 a = w.s[0][p], b = w.s[1][p], c = w.s[2][p], d = w.s[3][p], e = w.s[4][p], f = w.s[5][p];
     ps.o = f3(a.x, a.y, a.z);
@@ -50,7 +65,7 @@ __device__ __forceinline__ uint32_t load_path(const WavefrontState& w, uint32_t 
     ps.flags = df & 0xffffu;
     ps.g_albedo = f3(f.x, f.y, f.z);
     ps.rng.dim = __float_as_uint(f.w);
-    ps.g_normal = w.s[6][p];
+    ps.g_normal = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const uint4 r = reinterpret_cast<const uint4*>(w.s[7])[p];
     ps.rng.state = r.x;
     ps.rng.seed = r.y;
@@ -420,11 +435,12 @@ __global__ void __launch_bounds__(WF_BLOCK) k_wf_shade(Ctx ctx, WavefrontState w
         sh.valid = false;
         PathState ps;
         const uint32_t word = load_path(w, path, ps);
+        const bool guided = (ps.flags & PF_GUIDED) != 0u;
         const uint32_t job = ctx.job_of(word);
         const float4 hv = w.hit[path];
         const Hit hit{hv.x, __float_as_uint(hv.y), hv.z, hv.w};
         const bool more = path_step<FEAT>(ctx.scene(job), ctx.params(job), ps, hit, sh);
-        store_path(w, path, ps, word);
+        store_bounce(w, path, ps, !guided && (ps.flags & PF_GUIDED) != 0u);
         w.sort_key[path] = (more ? 1u : 0u) | (sh.valid ? 2u : 0u);
         if (sh.valid) {
             shadow[size_t(path) * 3 + 0] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.reach);
