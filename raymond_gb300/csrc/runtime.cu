@@ -856,7 +856,9 @@ int raymond_render_batch(raymond_t* h, const raymond_job* jobs, uint32_t n, uint
     // Path pool: the whole frame if memory allows, else waves of whole samples.
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
-    const uint64_t per_path = 8 * 16 + 16 + 8 + 48;
+    // state records, hit, two queues, shading order and key, shadow rays and
+    // lists of both parities, shadow sum
+    const uint64_t per_path = 8 * 16 + 16 + 4 * 4 + 2 * 48 + 2 * 4 + 16;
     uint64_t cap = uint64_t(double(free_b) * 0.5) / per_path;
     if (h->path_capacity_limit) cap = std::min<uint64_t>(cap, h->path_capacity_limit);
     cap = std::min<uint64_t>(cap, total_paths);
