@@ -47,6 +47,7 @@ struct CausticBuffers {
     uint32_t* splats;
     uint32_t* heads;
     float4* photons;
+    float4* gathered;  // per pixel: the photon map's gather term of the frame
     uint32_t table, capacity, photons_per_frame;
 };
 
@@ -146,8 +147,10 @@ int launch_wavefront_batch(const JobDesc* d_jobs, const WaveSegment* d_segments,
                            const WavefrontTuning& tune, int num_sms, cudaStream_t st);
 int launch_image_batch(const JobDesc* d_jobs, const JobPixels* d_pix, uint32_t n_jobs, uint32_t total_pixels,
                        int num_sms, cudaStream_t st);
-int launch_caustics(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb,
-                    const PixelBuffers& px, int num_sms, cudaStream_t st);
+int launch_caustic_light(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb, int num_sms,
+                         cudaStream_t st);
+int launch_caustic_resolve(const Params& P, const CausticBuffers& cb, const PixelBuffers& px, int num_sms,
+                           cudaStream_t st);
 // status: a device word set non-zero if a staged tile's wait runs out (null:
 // every pass reads through L2).
 int launch_light_trace_alone(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb, int num_sms,

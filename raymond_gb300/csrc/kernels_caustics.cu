@@ -213,7 +213,9 @@ __global__ void __launch_bounds__(CAUSTIC_BLOCK) k_light_trace(Scene s, Params P
     }
 }
 
-// resolve_splats (src/shaders.mjs:1819-1831).
+// resolve_splats (src/shaders.mjs:1819-1831), then the photon map's gather
+// term of the pixel (k_photon_gather's output), added in that order as the
+// reference's passes add them.
 __global__ void k_resolve_splats(Params P, CausticBuffers cb, float4* __restrict__ accum) {
     const uint32_t n = P.width * P.height;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -223,7 +225,9 @@ __global__ void k_resolve_splats(Params P, CausticBuffers cb, float4* __restrict
         const float l = luminance(f3(r, g, b));
         const float k = float(P.samples_per_frame);
         const float4 a = accum[i];
-        accum[i] = make_float4(a.x + r * k, a.y + g * k, a.z + b * k, a.w + l * l * k);
+        const float4 s = make_float4(a.x + r * k, a.y + g * k, a.z + b * k, a.w + l * l * k);
+        const float4 t = cb.gathered[i];
+        accum[i] = make_float4(s.x + t.x, s.y + t.y, s.z + t.z, s.w + t.w);
     }
 }
 
@@ -260,10 +264,13 @@ __device__ float3 gather(const Params& P, const CausticBuffers& cb, const Surfac
     return sum / (PI * r2);
 }
 
-// photon_gather (src/shaders.mjs:1577-1626).
+// photon_gather (src/shaders.mjs:1577-1626): each pixel's term (its light
+// times the frame's samples, and luminance² likewise; zero where the camera
+// ray finds nothing to gather) written to out, for k_resolve_splats to add
+// once the camera paths' sums are in.
 template <uint32_t FEAT>
 __global__ void __launch_bounds__(CAUSTIC_BLOCK) k_photon_gather(Scene s, Params P, CausticBuffers cb,
-                                                                 float4* __restrict__ accum) {
+                                                                 float4* __restrict__ out) {
     __shared__ uint32_t stack[STACK_SHARED * CAUSTIC_BLOCK];
     uint32_t* col = stack + threadIdx.x;
     const uint32_t n = P.width * P.height;
@@ -274,6 +281,7 @@ __global__ void __launch_bounds__(CAUSTIC_BLOCK) k_photon_gather(Scene s, Params
         float3 o, d;
         camera_ray(P, make_float2(float(index % P.width) + jx, float(index / P.width) + jy), true, rng, o, d);
         float3 throughput = f3(1.0f);
+        float4 term = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         for (uint32_t depth = 0; depth < P.max_bounces; ++depth) {
             const Hit hit = trace_ray<false>(s, o, d, INF, col, CAUSTIC_BLOCK);
             if (hit.prim == NONE) break;
@@ -287,9 +295,8 @@ __global__ void __launch_bounds__(CAUSTIC_BLOCK) k_photon_gather(Scene s, Params
                     if (finite3(light)) {
                         const float l = luminance(light);
                         const float k = float(P.samples_per_frame);
-                        const float4 a = accum[index];
-                        accum[index] = make_float4(a.x + light.x * k, a.y + light.y * k, a.z + light.z * k,
-                                                   a.w + l * l * k);
+                        term = make_float4(__fmul_rn(light.x, k), __fmul_rn(light.y, k), __fmul_rn(light.z, k),
+                                           __fmul_rn(l * l, k));
                     }
                 }
                 break;
@@ -300,6 +307,7 @@ __global__ void __launch_bounds__(CAUSTIC_BLOCK) k_photon_gather(Scene s, Params
             o = offset_origin(sf, bs.wi);
             d = bs.wi;
         }
+        out[index] = term;
     }
 }
 
@@ -332,15 +340,16 @@ int gather_alone(const Scene& s, const Params& P, const CausticBuffers& cb, uint
     return 2;
 }
 
+// A frame's light tracing and gathering need nothing of its camera paths,
+// so they run on a stream of their own beside them; only the resolve waits
+// for the camera paths' sums.
 template <uint32_t FEAT>
-int caustics_frame(const Scene& s, const Params& P, const CausticBuffers& cb, const PixelBuffers& px, int num_sms,
-                   cudaStream_t st) {
+int caustics_light(const Scene& s, const Params& P, const CausticBuffers& cb, int num_sms, cudaStream_t st) {
     cudaMemsetAsync(cb.heads, 0, (size_t(cb.table) + 1) * sizeof(uint32_t), st);
     const int grid = num_sms * 8;
     k_light_trace<FEAT><<<grid, CAUSTIC_BLOCK, 0, st>>>(s, P, cb);
-    k_resolve_splats<<<grid, 256, 0, st>>>(P, cb, px.accum);
-    k_photon_gather<FEAT><<<grid, CAUSTIC_BLOCK, 0, st>>>(s, P, cb, px.accum);
-    return 3;
+    k_photon_gather<FEAT><<<grid, CAUSTIC_BLOCK, 0, st>>>(s, P, cb, cb.gathered);
+    return 2;
 }
 
 }  // namespace
@@ -365,13 +374,19 @@ int launch_gather_alone(const Scene& s, const Params& P, uint32_t features, cons
     }
 }
 
-int launch_caustics(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb,
-                    const PixelBuffers& px, int num_sms, cudaStream_t st) {
+int launch_caustic_light(const Scene& s, const Params& P, uint32_t features, const CausticBuffers& cb, int num_sms,
+                         cudaStream_t st) {
     switch (features & 15u) {
-        case 0: return caustics_frame<0>(s, P, cb, px, num_sms, st);
-        case F_DISPERSION: return caustics_frame<F_DISPERSION>(s, P, cb, px, num_sms, st);
-        default: return caustics_frame<15u>(s, P, cb, px, num_sms, st);
+        case 0: return caustics_light<0>(s, P, cb, num_sms, st);
+        case F_DISPERSION: return caustics_light<F_DISPERSION>(s, P, cb, num_sms, st);
+        default: return caustics_light<15u>(s, P, cb, num_sms, st);
     }
+}
+
+int launch_caustic_resolve(const Params& P, const CausticBuffers& cb, const PixelBuffers& px, int num_sms,
+                           cudaStream_t st) {
+    k_resolve_splats<<<num_sms * 8, 256, 0, st>>>(P, cb, px.accum);
+    return 1;
 }
 
 }  // namespace rmd

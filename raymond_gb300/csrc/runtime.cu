@@ -67,7 +67,7 @@ struct raymond {
     uint64_t capacity = 0;
 
     // Scratch for host-pointer trace calls, and the work counter.
-    DevBuf ray_scratch, prim_scratch, t_scratch, counter;
+    DevBuf ray_scratch, prim_scratch, t_scratch, counter, gathered;
     DevBuf upload_scratch;  // images staged for building texture arrays and the environment on the GPU
 
     // Wavefront path state (allocated on first wavefront frame).
@@ -120,6 +120,7 @@ struct raymond {
     std::vector<int> stage_kind;
     StageEvents stage{};
     FrameStreams frame{};  // a wavefront frame's groups and their shadow rays
+    SideStream caustic{};  // a frame's light tracing and photon gathering
 
     int fail(int code, const char* fmt, ...) {
         char buf[512];
@@ -286,6 +287,10 @@ int raymond_create(raymond_t** out, const raymond_config* cfg) {
     for (cudaEvent_t& ev : h->ev) cudaEventCreate(&ev);
     cudaEventCreateWithFlags(&h->order, cudaEventDisableTiming);
     e = cudaEventCreateWithFlags(&h->frame.fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->caustic.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->caustic.fork, cudaEventDisableTiming);
+    for (cudaEvent_t& ev : h->caustic.join)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     for (int g = 0; g < FrameStreams::kGroups; ++g) {
         SideStream& sd = h->frame.side[g];
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->frame.group[g], cudaStreamNonBlocking);
@@ -335,7 +340,7 @@ void raymond_destroy(raymond_t* h) {
     for (DevBuf* b : {&h->prims, &h->nodes, &h->materials, &h->attributes, &h->lights, &h->emitters, &h->textures,
                       &h->normal_maps, &h->env_map, &h->env_table, &h->accum, &h->guide_albedo, &h->guide_normal,
                       &h->light_a, &h->light_b, &h->guide_unit, &h->denoised, &h->splats, &h->display, &h->ray_scratch,
-                      &h->prim_scratch, &h->t_scratch, &h->counter, &h->upload_scratch, &h->wf_hit, &h->wf_queue[0], &h->wf_queue[1],
+                      &h->prim_scratch, &h->t_scratch, &h->counter, &h->gathered, &h->upload_scratch, &h->wf_hit, &h->wf_queue[0], &h->wf_queue[1],
                       &h->wf_sorted, &h->wf_sort_key, &h->wf_shadow, &h->wf_shadow_list, &h->wf_shadow_sum, &h->wf_counters, &h->photon_heads,
                       &h->photons, &h->wide})
         b->release();
@@ -351,6 +356,10 @@ void raymond_destroy(raymond_t* h) {
     }
     if (h->order) cudaEventDestroy(h->order);
     if (h->frame.fork) cudaEventDestroy(h->frame.fork);
+    if (h->caustic.fork) cudaEventDestroy(h->caustic.fork);
+    for (cudaEvent_t ev : h->caustic.join)
+        if (ev) cudaEventDestroy(ev);
+    if (h->caustic.stream) cudaStreamDestroy(h->caustic.stream);
     for (int g = 0; g < FrameStreams::kGroups; ++g) {
         const SideStream& sd = h->frame.side[g];
         if (h->frame.join[g]) cudaEventDestroy(h->frame.join[g]);
@@ -660,6 +669,9 @@ static int caustic_buffers(raymond_t* h, Params& P, CausticBuffers& cb) {
         h->photon_table = table;
         h->photon_capacity_alloc = h->photon_capacity;
     }
+    if (cudaError_t e = h->gathered.reserve(size_t(P.width) * P.height * 16); e != cudaSuccess)
+        return h->cuda_fail(e, "gather terms");
+    cb.gathered = static_cast<float4*>(h->gathered.ptr);
     cb.splats = static_cast<uint32_t*>(h->splats.ptr);
     cb.heads = static_cast<uint32_t*>(h->photon_heads.ptr);
     cb.photons = static_cast<float4*>(h->photons.ptr);
@@ -788,12 +800,23 @@ int raymond_render(raymond_t* h, const void* params208, uint32_t features, uint3
     int launches = 0;
     cudaEventRecord(h->ev[0], h->stream);
     h->stage.count = 0;
+    if (P.caustics != 0u) {
+        // Light tracing and the gather beside the camera paths (they read
+        // nothing of them); the resolve below waits for both.
+        cudaEventRecord(h->caustic.fork, h->stream);
+        cudaStreamWaitEvent(h->caustic.stream, h->caustic.fork, 0);
+        launches += launch_caustic_light(s, P, features, cb, h->num_sms, h->caustic.stream);
+        cudaEventRecord(h->caustic.join[0], h->caustic.stream);
+    }
     if (wavefront)
         launches += launch_wavefront(s, P, features, w, px, h->tuning, h->num_sms, h->stream, &h->frame, &h->stage);
     else
         launches += launch_megakernel(s, P, features, px, h->num_sms, h->stream);
     cudaEventRecord(h->ev[1], h->stream);
-    if (P.caustics != 0u) launches += launch_caustics(s, P, features, cb, px, h->num_sms, h->stream);
+    if (P.caustics != 0u) {
+        cudaStreamWaitEvent(h->stream, h->caustic.join[0], 0);
+        launches += launch_caustic_resolve(P, cb, px, h->num_sms, h->stream);
+    }
     cudaEventRecord(h->ev[2], h->stream);
     if (P.denoise != 0u) launches += launch_denoise(P, px, h->status_word(), h->stream);
     cudaEventRecord(h->ev[3], h->stream);
