@@ -1,7 +1,9 @@
-"""The wavefront path (extend / shade / shadow kernels over queues in HBM)
-against the one-kernel path: the same bounce step on the same sample
-streams, with the light of each shadow ray added in the same order, so
-their accumulated sums agree to the last bits."""
+"""The wavefront path (extend / shade / shadow kernels over queues in HBM,
+a frame's samples in two groups on their own streams, shadow rays on side
+streams) against the one-kernel path: the same bounce step on the same
+sample streams. The wavefront sums a path's shadow-ray light apart from its
+own radiance and adds the two at the frame's end, so the accumulated sums
+agree to float rounding."""
 
 import numpy as np
 import pytest
