@@ -382,6 +382,28 @@ def measure_denoiser(scene, camera, local, steps, warmup, width=1920, height=108
         "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "frames/s", "cores": 1, "kind": "port",
                          "sample": "oracle network forward on a 32x32 crop, scaled by pixels"},
         "l2": "flushed between steps (512 MB write)",
+        "training": training_note(),
+    }
+
+
+def training_note():
+    """How the shipped weights were trained, against the configured data set
+    (2,000 crops of 256² rendered at 1–8 spp with 16,384-spp targets): read
+    from the training report that sits beside the weights."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "raymond_gb300", "weights", "denoiser_unet.json")
+    try:
+        with open(path) as f:
+            rep = json.load(f)
+    except (OSError, ValueError):
+        return None
+    views, size, target = int(rep["views"]), int(rep["size"]), int(rep["target_spp"])
+    noisy = [int(s) for s in rep["noisy_spp"]]
+    return {
+        "views": views, "crop_px": size, "target_spp": target, "input_spp": noisy, "adam_steps": int(rep["steps"]),
+        "paths": views * size * size * (target + sum(noisy)),
+        "configured": "2,000 crops of 256x256 at 1-8 spp with 16,384-spp targets",
+        "configured_paths": 2000 * 256 * 256 * (16384 + 8),
+        "note": "a reduced data set (about 1/7 of the configured paths), with inputs up to 512 spp",
     }
 
 
@@ -397,7 +419,8 @@ def run_denoise(args, local):
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": d["ms_per_frame"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
         "data": "synthetic (seeded mulberry32 scene, rendered at 4 spp)",
-        "config": {"workload": d["workload"], "l2": d["l2"], "weights": "raymond_gb300/weights/denoiser_unet.npz"},
+        "config": {"workload": d["workload"], "l2": d["l2"], "weights": "raymond_gb300/weights/denoiser_unet.npz",
+                   "training": d["training"]},
         "e2e": d["e2e"], "gpu_launches": d["launches_per_frame"] * args.steps, "roofline": d["roofline"],
         "cpu_baseline": d["cpu_baseline"], "clocks": clock_info,
     }
