@@ -8,8 +8,9 @@ sun); one frame's light tracing (splat sums and photons, matched by light
 path) and the photon map's gather on identical photon lists, on the
 reference's caustic fixtures and on the water-caustics scene at 1M light
 paths, a 4M-photon map and r = 0.01; and the 16-seed unbiasedness test on
-a small scene of the sphere field's kind. No unexplained difference is
-allowed anywhere.
+a small scene of the sphere field's kind; and the jobs of one batched
+frame, each against the oracle. No unexplained difference is allowed
+anywhere.
 
 Reference: src/shaders.mjs:133-212 (streams), 714-871 (BSDFs),
 1148-1166 (camera_ray), 1436-1831 (splat, photon map, light_trace,
@@ -130,6 +131,46 @@ def test_sphere_field_crop_matches_oracle_per_pixel(gpu, sphere_field, crop, fla
 def sphere_field():
     scene, camera, _ = scenes.sphere_field()
     return scene, camera
+
+
+# Jobs of one batched frame: (case, size, spp, crop or None, share that must agree outright).
+BATCH_CASES = [("cornell", 64, 8, None, 0.99), ("mixed_metal_plastic_glass", 48, 8, None, 0.99),
+               ("dispersive_glass", 48, 8, None, 0.99), ("environment", 48, 4, None, 0.99),
+               ("sphere_field", 1024, 4, (480, 480), 0.85)]
+
+
+def test_batched_jobs_match_oracle_per_pixel(gpu, sphere_field):
+    """One batched frame of several scenes (raymond_render_batch: one path
+    pool in groups, one CUDA graph), each job's image against the oracle on
+    its own parameters, every difference classified: the batch is checked
+    against the oracle itself, not only against single frames."""
+    from raymond_gb300 import BatchRenderer
+
+    jobs = []
+    for name, size, spp, crop, share in BATCH_CASES:
+        scene, camera = sphere_field if name == "sphere_field" else IMAGE_CASES[name][0]()
+        r = Renderer.create(Canvas(size, size), seed=0)
+        r.scene, r.camera = scene, camera
+        r.maxBounces, r.samplesPerFrame, r.fireflyClamp, r.denoise = 8, spp, 0, False
+        r.flags = WF
+        jobs.append((name, scene, r, crop, share))
+    batch = BatchRenderer(graph=True)
+    batch.render([j[2] for j in jobs])
+    batch.sync()
+    for name, scene, r, crop, share in jobs:
+        got = r.readGuides()[0]
+        if crop is None:
+            ref, runs = oracle_frame(scene, r.params)
+        else:
+            x0, y0 = crop
+            ref, runs = oracle_frame(scene, r.params, region=(x0, y0, 64, 64))
+            got = got[y0:y0 + 64, x0:x0 + 64]
+        c = classify_pixels(got, ref, runs)
+        assert c["unexplained"] == 0, (name, c)
+        assert c["agree"] >= share * c["n"], (name, c)
+    for j in jobs:
+        j[2].dispose()
+    batch.dispose()
 
 
 # ---- light transport ----
