@@ -400,6 +400,7 @@ def training_note():
     noisy = [int(s) for s in rep["noisy_spp"]]
     return {
         "views": views, "crop_px": size, "target_spp": target, "input_spp": noisy, "adam_steps": int(rep["steps"]),
+        "field_spheres": rep.get("field_spheres"), "field_mesh_frequency": rep.get("field_frequency"),
         "paths": views * size * size * (target + sum(noisy)),
         "configured": "2,000 crops of 256x256 at 1-8 spp with 16,384-spp targets",
         "configured_paths": 2000 * 256 * 256 * (16384 + 8),

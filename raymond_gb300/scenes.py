@@ -277,20 +277,21 @@ def water_caustics(seed: int = 3, segments: int = 255):
 
 # ------------------------------------------------- denoiser training views ----
 
-def training_views(count: int, seed: int = 7):
-    """`count` seeded views for the learned denoiser, alternating small
-    sphere-field variants (C2's generator with 300–3,000 spheres and a
-    2k–60k-triangle centre mesh, seen from a random orbit) and water
-    caustics variants (C3's generator with a random camera). Returns a
-    list of (scene, camera, info)."""
+def training_views(count: int, seed: int = 7, spheres=(300, 3000), frequency=(10, 55)):
+    """`count` seeded views for the learned denoiser, alternating
+    sphere-field variants (C2's generator with spheres[0]–spheres[1]
+    spheres and a centre mesh of frequency[0]–frequency[1], 20·f²
+    triangles, seen from a random orbit) and water caustics variants (C3's
+    generator with a random camera). Returns a list of (scene, camera,
+    info)."""
     rnd = mulberry32(seed)
     out = []
     for i in range(count):
         scene_seed = int(rnd() * 2147483647.0)
         if i % 2 == 0:
-            spheres = int(300 + 2700 * rnd())
-            freq = int(10 + 45 * rnd())
-            scene, camera, info = sphere_field(seed=scene_seed, spheres=spheres, frequency=freq)
+            n_spheres = int(spheres[0] + (spheres[1] - spheres[0]) * rnd())
+            freq = int(frequency[0] + (frequency[1] - frequency[0]) * rnd())
+            scene, camera, info = sphere_field(seed=scene_seed, spheres=n_spheres, frequency=freq)
             az = 2.0 * math.pi * rnd()
             dist = 6.0 + 10.0 * rnd()
             elev = 0.5 + 5.0 * rnd()

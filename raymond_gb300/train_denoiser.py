@@ -20,6 +20,7 @@ import argparse
 import json
 import math
 import os
+import shlex
 import sys
 import time
 
@@ -210,6 +211,8 @@ def main(argv=None):
     ap.add_argument("--noisy-spp", default=",".join(str(v) for v in NOISY_SPP),
                     help="sample counts of the noisy inputs (increasing)")
     ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--field-spheres", default="300,3000", help="sphere-field views: spheres, min,max")
+    ap.add_argument("--field-frequency", default="10,55", help="sphere-field views: centre-mesh frequency, min,max")
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     ap.add_argument("--report", default=None)
     args = ap.parse_args(argv)
@@ -219,7 +222,10 @@ def main(argv=None):
         print(msg, flush=True)
 
     t0 = time.time()
-    views = scenes.training_views(args.views + args.holdout, seed=args.seed)
+    field_spheres = tuple(int(v) for v in args.field_spheres.split(","))
+    field_frequency = tuple(int(v) for v in args.field_frequency.split(","))
+    views = scenes.training_views(args.views + args.holdout, seed=args.seed, spheres=field_spheres,
+                                  frequency=field_frequency)
     train_views, held = views[:args.views], views[args.views:]
     log(f"{len(train_views)} training views, {len(held)} held out; {args.size}² at {args.target_spp} spp")
     targets, inputs = build_dataset(train_views, args.size, args.target_spp, log)
@@ -254,10 +260,11 @@ def main(argv=None):
             net.dispose()
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     best[1].save(args.out)
-    report = {"command": "python -m raymond_gb300.train_denoiser " + " ".join(argv if argv is not None else sys.argv[1:]),
+    report = {"command": "python -m raymond_gb300.train_denoiser " + shlex.join(argv if argv is not None else sys.argv[1:]),
               "views": args.views, "holdout": args.holdout, "size": args.size, "target_spp": args.target_spp,
               "noisy_spp": list(NOISY_SPP), "steps": args.steps, "batch": args.batch, "crop": args.crop,
-              "lr": args.lr, "seed": args.seed, "seconds_data": t_data, "variants": variants,
+              "lr": args.lr, "seed": args.seed, "field_spheres": list(field_spheres),
+              "field_frequency": list(field_frequency), "seconds_data": t_data, "variants": variants,
               "eval_spp": eval_spp,
               "chosen": {"w_log": best[2]["w_log"], "w_rel": best[2]["w_rel"], "rel_eps": best[2]["rel_eps"]},
               "weights": os.path.basename(args.out)}
