@@ -336,7 +336,15 @@ int raymond_create(raymond_t** out, const raymond_config* cfg) {
 void raymond_destroy(raymond_t* h) {
     if (!h) return;
     cudaSetDevice(h->device);
+    // Every stream that may still run the handle's kernels, before its memory goes.
     cudaStreamSynchronize(h->stream);
+    for (int g = 0; g < FrameStreams::kGroups; ++g) {
+        if (h->frame.group[g]) cudaStreamSynchronize(h->frame.group[g]);
+        if (h->frame.side[g].stream) cudaStreamSynchronize(h->frame.side[g].stream);
+    }
+    if (h->caustic.stream) cudaStreamSynchronize(h->caustic.stream);
+    for (cudaStream_t sg : h->b_group_stream)
+        if (sg) cudaStreamSynchronize(sg);
     for (DevBuf* b : {&h->prims, &h->nodes, &h->materials, &h->attributes, &h->lights, &h->emitters, &h->textures,
                       &h->normal_maps, &h->env_map, &h->env_table, &h->accum, &h->guide_albedo, &h->guide_normal,
                       &h->light_a, &h->light_b, &h->guide_unit, &h->denoised, &h->splats, &h->display, &h->ray_scratch,
