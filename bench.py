@@ -33,6 +33,7 @@ slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import math
 import os
@@ -775,21 +776,26 @@ def time_to_rmse(scene, camera, local, size, spp, bounces, threshold=0.01, refer
         the running average, the curve)."""
         views, elapsed, curve = None, 0.0, []
         shown = raw = None
-        while r.samples < max_spp and (shown is None or raw is None):
-            torch.cuda.synchronize()
-            t = time.perf_counter()
-            r.render()
-            r._sync()
-            elapsed += time.perf_counter() - t
-            if views is None:
-                views = (view(r, display), view(r, "accum"))
-            e_raw = rmse(views[1] / r.samples)
-            e = e_raw if display == "accum" else rmse(views[0])
-            curve.append((r.samples, round(elapsed, 4), round(e, 5), round(e_raw, 5)))
-            if shown is None and e <= threshold:
-                shown = (r.samples, elapsed)
-            if raw is None and e_raw <= threshold:
-                raw = (r.samples, elapsed)
+        gc.collect()
+        gc.disable()  # no collector pause inside a timed frame
+        try:
+            while r.samples < max_spp and (shown is None or raw is None):
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                r.render()
+                r._sync()
+                elapsed += time.perf_counter() - t
+                if views is None:
+                    views = (view(r, display), view(r, "accum"))
+                e_raw = rmse(views[1] / r.samples)
+                e = e_raw if display == "accum" else rmse(views[0])
+                curve.append((r.samples, round(elapsed, 4), round(e, 5), round(e_raw, 5)))
+                if shown is None and e <= threshold:
+                    shown = (r.samples, elapsed)
+                if raw is None and e_raw <= threshold:
+                    raw = (r.samples, elapsed)
+        finally:
+            gc.enable()
         return shown, raw, curve
 
     def summary(reached, curve):

@@ -195,6 +195,45 @@ def _train_loop(net, targets, inputs, steps, batch, crop, lr, rng, levels, log, 
     return losses, time.time() - t0
 
 
+def choose_tau(net, targets, inputs, eval_spp, taus, log):
+    """Held-out scores (mean learned/noisy error ratio over eval_spp) for each
+    display guard τ, and the best τ."""
+    scores = {}
+    for tau in (float(v) for v in taus.split(",")):
+        net.blend = tau
+        ratios = []
+        for spp in eval_spp:
+            mean, _ = evaluate(net, targets, inputs, spp)
+            ratios.append(mean["learned"] / mean["noisy"])
+        scores[str(tau)] = {"score": float(np.mean(ratios)), "ratios": dict(zip(map(str, eval_spp), ratios))}
+        log(f"tau {tau}: {scores[str(tau)]}")
+    best = min(scores, key=lambda k: scores[k]["score"])
+    return scores, float(best)
+
+
+def tune_only(args, argv, log):
+    """Held-out evaluation of saved weights at each --tau, the best τ saved
+    with them (the held-out views are the training run's: the same seeded
+    list, after its --views)."""
+    field_spheres = tuple(int(v) for v in args.field_spheres.split(","))
+    field_frequency = tuple(int(v) for v in args.field_frequency.split(","))
+    views = scenes.training_views(args.views + args.holdout, seed=args.seed, spheres=field_spheres,
+                                  frequency=field_frequency)
+    h_targets, h_inputs = build_dataset(views[args.views:], args.size, args.target_spp, log)
+    eval_spp = [int(v) for v in args.eval_spp.split(",")]
+    net = Denoiser(weights=args.weights)
+    scores, tau = choose_tau(net, h_targets, h_inputs, eval_spp, args.tau or str(net.blend), log)
+    net.blend = tau
+    net.save(args.out)
+    net.dispose()
+    report = {"command": "python -m raymond_gb300.train_denoiser " + shlex.join(argv if argv is not None else sys.argv[1:]),
+              "tau_scores": scores, "tau": tau}
+    if args.report:
+        with open(args.report, "w") as f:
+            json.dump(report, f, indent=1)
+    return report
+
+
 def main(argv=None):
     global NOISY_SPP
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
@@ -215,12 +254,19 @@ def main(argv=None):
     ap.add_argument("--field-frequency", default="10,55", help="sphere-field views: centre-mesh frequency, min,max")
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     ap.add_argument("--report", default=None)
+    ap.add_argument("--tau", default=None,
+                    help="display guards τ to try on the held-out views after training (comma-separated); "
+                         "the one with the lowest mean learned/noisy error ratio is saved with the weights")
+    ap.add_argument("--weights", default=None,
+                    help="skip training: load these weights and only evaluate (and choose τ) on the held-out views")
     args = ap.parse_args(argv)
     NOISY_SPP = tuple(int(v) for v in args.noisy_spp.split(","))
 
     def log(msg):
         print(msg, flush=True)
 
+    if args.weights:
+        return tune_only(args, argv, log)
     t0 = time.time()
     field_spheres = tuple(int(v) for v in args.field_spheres.split(","))
     field_frequency = tuple(int(v) for v in args.field_frequency.split(","))
@@ -258,6 +304,9 @@ def main(argv=None):
             best = (score, net, result)
         else:
             net.dispose()
+    if args.tau:
+        best[2]["tau_scores"], tau = choose_tau(best[1], h_targets, h_inputs, eval_spp, args.tau, log)
+        best[1].blend = tau
     os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
     best[1].save(args.out)
     report = {"command": "python -m raymond_gb300.train_denoiser " + shlex.join(argv if argv is not None else sys.argv[1:]),
