@@ -86,3 +86,29 @@ def test_reference_arm_maps_no_product_library(workload):
     assert r.returncode == 0, r.stderr[-2000:]
     marker = [ln for ln in r.stdout.splitlines() if ln.startswith("MAPS")]
     assert marker == ["MAPS False True"], r.stdout[-2000:]
+
+
+def test_denoiser_lines_report_the_training_set():
+    """The learned-denoiser lines carry how the shipped weights were trained,
+    read from the report beside them, against the configured data set."""
+    import bench
+
+    note = bench.training_note()
+    assert note is not None
+    assert note["views"] > 0 and note["target_spp"] == 16384 and note["adam_steps"] > 0
+    assert note["paths"] < note["configured_paths"]
+    assert note["field_spheres"] and note["field_spheres"][0] <= note["field_spheres"][1]
+
+
+def test_training_views_follow_the_density_options():
+    """Sphere-field training views draw their sphere count and mesh frequency
+    from the given ranges; the defaults keep the original sequence."""
+    from raymond_gb300 import scenes
+
+    dense = scenes.training_views(6, seed=3, spheres=(3000, 3100), frequency=(20, 22))
+    fields = [info for _, _, info in dense if "spheres" in info]
+    assert fields and all(3000 <= f["spheres"] < 3100 for f in fields)
+    assert all(f["triangles"] in (20 * 20 * 20, 20 * 21 * 21) for f in fields)
+    default = scenes.training_views(4, seed=99)
+    again = scenes.training_views(4, seed=99, spheres=(300, 3000), frequency=(10, 55))
+    assert [v[2] for v in default] == [v[2] for v in again]
